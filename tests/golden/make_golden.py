@@ -1,0 +1,204 @@
+"""Generate the golden fixtures in this folder from the XLuminA reference source.
+
+Run in a container that holds the reference checkout (read-only is fine):
+
+    python tests/golden/make_golden.py /path/to/XLuminA
+
+The reference is pure Python on jax; jax is not installable here, so
+``jax_numpy_standin.install()`` first registers a numpy-backed stand-in for the
+jax calls the reference makes (float64 / complex128 throughout, as the
+reference forces ``jax_enable_x64``).  The reference's own functions then run
+unchanged on small seeded inputs and their outputs are written as ``.npz``
+fixtures.  The fixtures travel with the repository; the tests never need the
+reference checkout.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _save(name, **arrays):
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", path)
+
+
+def main(ref_root):
+    sys.path.insert(0, HERE)
+    import jax_numpy_standin
+
+    jax_numpy_standin.install()
+    sys.path.insert(0, ref_root)
+    import contextlib
+    import io
+
+    from xlumina import loss_functions as lf
+    from xlumina import optical_elements as oe
+    from xlumina import toolbox as tb
+    from xlumina.vectorized_optics import PolarizedLightSource, VectorizedLight
+    from xlumina.wave_optics import LightSource, ScalarLight
+
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    rng = np.random.default_rng(1234)
+
+    with quiet:
+        # 1. scalar RS, square grid, SLM-modulated Gaussian, z > 0 and z < 0.
+        x, y = tb.space(150.0, 64)
+        wl = 0.65
+        src = LightSource(x, y, wl)
+        src.gaussian_beam(w0=(40.0, 40.0), E0=1)
+        phase = rng.uniform(-np.pi, np.pi, (64, 64))
+        mod, _ = oe.SLM(src, phase, 64)
+        out_p, qf_p = mod.RS_propagation(3000.0)
+        out_n, qf_n = mod.RS_propagation(-2500.0)
+        _save("rs_square", x=x, y=y, wavelength=wl, phase=phase, source=src.field,
+              field_in=mod.field, z_pos=3000.0, out_pos=out_p.field, qf_pos=qf_p,
+              z_neg=-2500.0, out_neg=out_n.field, qf_neg=qf_n)
+
+        # 2. scalar RS of a complex random input on another grid (the reference's
+        # build_grid only supports nx == ny: it reuses the x sign pattern for y).
+        x = np.linspace(-150.0, 150.0, 48)
+        y = np.linspace(-150.0, 150.0, 48)
+        f_in = rng.standard_normal((48, 48)) + 1j * rng.standard_normal((48, 48))
+        light = ScalarLight(x, y, 0.532)
+        light.field = f_in
+        out, qf = light.RS_propagation(1800.0)
+        _save("rs_complex", x=x, y=y, wavelength=0.532, field_in=f_in, z=1800.0, out=out.field, qf=qf)
+
+        # 3. scalar RS, odd N.
+        x, y = tb.space(120.0, 63)
+        f_in = rng.standard_normal((63, 63)) + 1j * rng.standard_normal((63, 63))
+        light = ScalarLight(x, y, 0.633)
+        light.field = f_in
+        out, qf = light.RS_propagation(2200.0)
+        _save("rs_odd", x=x, y=y, wavelength=0.633, field_in=f_in, z=2200.0, out=out.field, qf=qf)
+
+        # 4. VRS behind a per-pixel LCD and a per-pixel linear polarizer.
+        x, y = tb.space(160.0, 64)
+        wl = 0.633
+        pls = PolarizedLightSource(x, y, wl)
+        pls.gaussian_beam(w0=(50.0, 50.0), jones_vector=(1, 0.5))
+        eta = rng.uniform(0, 2 * np.pi, (64, 64))
+        theta = rng.uniform(0, 2 * np.pi, (64, 64))
+        alpha = rng.uniform(0, np.pi) * np.ones((64, 64))
+        l1 = oe.LCD(pls, eta, theta)
+        l2 = oe.linear_polarizer(l1, alpha)
+        vout, vqf = l2.VRS_propagation(2500.0)
+        _save("vrs", x=x, y=y, wavelength=wl, Ex0=pls.Ex, Ey0=pls.Ey, eta=eta, theta=theta, alpha=alpha,
+              lcd_Ex=l1.Ex, lcd_Ey=l1.Ey, lcd_Ez=l1.Ez, lp_Ex=l2.Ex, lp_Ey=l2.Ey, lp_Ez=l2.Ez,
+              z=2500.0, Ex=vout.Ex, Ey=vout.Ey, Ez=vout.Ez, qf=vqf)
+
+        # 5. scalar CZT with the default output grid, and to a non-square ROI.
+        x, y = tb.space(150.0, 64)
+        wl = 0.532
+        src = LightSource(x, y, wl)
+        src.gaussian_beam(w0=(45.0, 45.0), E0=1)
+        ph = rng.uniform(-np.pi, np.pi, (64, 64))
+        mod, _ = oe.SLM(src, ph, 64)
+        c_def = mod.CZT(4000.0)
+        xo = np.linspace(-40.0, 40.0, 48)
+        yo = np.linspace(-30.0, 30.0, 40)
+        c_roi = mod.CZT(4000.0, xo, yo)
+        _save("czt", x=x, y=y, wavelength=wl, field_in=mod.field, z=4000.0, out_default=c_def.field,
+              xout=xo, yout=yo, out_roi=c_roi.field)
+
+        # 6. vectorial CZT.
+        x, y = tb.space(150.0, 64)
+        Ex = rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64))
+        Ey = rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64))
+        vl = VectorizedLight(x, y, 0.65)
+        vl.Ex, vl.Ey = Ex, Ey
+        xo = np.linspace(-60.0, 60.0, 32)
+        yo = np.linspace(-50.0, 50.0, 40)
+        vc = vl.VCZT(3500.0, xo, yo)
+        _save("vczt", x=x, y=y, wavelength=0.65, Ex_in=Ex, Ey_in=Ey, z=3500.0, xout=xo, yout=yo,
+              Ex=vc.Ex, Ey=vc.Ey, Ez=vc.Ez)
+
+        # 7. high-NA objective lens and VCZT through it.
+        x, y = tb.space(1500.0, 64)
+        wl = 0.65
+        radius = 1800.0
+        f = radius / 0.9
+        pls = PolarizedLightSource(x, y, wl)
+        pls.gaussian_beam(w0=(1200.0, 1200.0), jones_vector=(1, 0.3))
+        a_ph = rng.uniform(0, 2 * np.pi, (64, 64))
+        p_ph = rng.uniform(0, 2 * np.pi, (64, 64))
+        mod = oe.sSLM(pls, a_ph, p_ph)
+        lens_out, smax = oe.high_NA_objective_lens(mod, radius, f)
+        xo, yo = tb.space(1.0, 32)
+        foc = oe.VCZT_objective_lens(mod, radius, f, xo, yo)
+        _save("high_na", x=x, y=y, wavelength=wl, radius=radius, f=f, Ex_in=mod.Ex, Ey_in=mod.Ey,
+              lens_out=lens_out, sin_theta_max=smax, xout=xo, yout=yo, Ex=foc.Ex, Ey=foc.Ey, Ez=foc.Ez)
+
+        # 8. masks and sources.
+        x, y = tb.space(150.0, 48)
+        wl = 0.633
+        g = LightSource(x, y, wl)
+        g.gaussian_beam(w0=(40.0, 55.0), E0=1.5, center=(10.0, -5.0), z_w0=(300.0, 200.0), alpha=0.3)
+        pw = LightSource(x, y, wl)
+        pw.plane_wave(A=2.0, theta=0.01, phi=0.7, z0=3.0)
+        pg = PolarizedLightSource(x, y, wl)
+        pg.gaussian_beam(w0=(40.0, 40.0), jones_vector=(1, 1j), center=(3.0, 4.0))
+        al = rng.uniform(0, 2 * np.pi, (48, 48))
+        phi = rng.uniform(0, 2 * np.pi, (48, 48))
+        A1 = rng.uniform(0, 1, (48, 48))
+        A2 = rng.uniform(0, 1, (48, 48))
+        s1 = oe.sSLM(pg, al, phi)
+        s2 = oe.sSLM_with_amplitude(pg, al, phi, A1, A2)
+        l_sc, lmask = oe.lens(g, (120.0, 100.0), (2000.0, 2500.0))
+        vl = VectorizedLight(x, y, wl)
+        vl.Ex, vl.Ey, vl.Ez = pg.Ex, pg.Ey, pg.Ex * 0.1
+        l_v, _ = oe.lens(vl, (120.0, 120.0), (3000.0, 3000.0))
+        lcd_s = oe.LCD(vl, 1.1, 0.4)
+        _save("masks", x=x, y=y, wavelength=wl, gauss=g.field, plane=pw.field, pol_Ex=pg.Ex, pol_Ey=pg.Ey,
+              pol_Ez=pg.Ez, alpha=al, phi=phi, A1=A1, A2=A2, sslm_Ex=s1.Ex, sslm_Ey=s1.Ey,
+              sslma_Ex=s2.Ex, sslma_Ey=s2.Ey, lens_scalar=l_sc.field, lens_mask=lmask,
+              vin_Ez=vl.Ez, lens_vec_Ex=l_v.Ex, lens_vec_Ey=l_v.Ey, lens_vec_Ez=l_v.Ez,
+              lcd_scalar_Ex=lcd_s.Ex, lcd_scalar_Ey=lcd_s.Ey, lcd_scalar_Ez=lcd_s.Ez)
+
+        # 9. losses.
+        a = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        b = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        I = np.abs(rng.standard_normal((40, 40))) ** 3
+        _save("losses", a=a, b=b, mse_intensity=lf.MSE_Intensity(a, b), I=I,
+              small_area=lf.small_area_hybrid(I))
+
+        # 10. building block: sSLM -> VRS -> LCD.
+        x, y = tb.space(150.0, 48)
+        pg = PolarizedLightSource(x, y, 0.633)
+        pg.gaussian_beam(w0=(40.0, 40.0), jones_vector=(1, 0))
+        al = rng.uniform(0, 2 * np.pi, (48, 48))
+        phi = rng.uniform(0, 2 * np.pi, (48, 48))
+        bb = oe.building_block(pg, al, phi, 2000.0, np.pi / 2, np.pi / 4)
+        _save("building_block", x=x, y=y, wavelength=0.633, Ex_in=pg.Ex, Ey_in=pg.Ey, alpha=al, phi=phi,
+              z=2000.0, eta=np.pi / 2, theta=np.pi / 4, Ex=bb.Ex, Ey=bb.Ey, Ez=bb.Ez)
+
+        # 11. a 4f-style table: SLM -> RS -> lens -> CZT(ROI) -> SLM -> CZT, intensity + MSE.
+        x, y = tb.space(200.0, 64)
+        wl = 0.532
+        f4 = 6000.0
+        src = LightSource(x, y, wl)
+        src.gaussian_beam(w0=(80.0, 80.0), E0=1)
+        p1 = rng.uniform(-np.pi, np.pi, (64, 64))
+        l1, _ = oe.SLM(src, p1, 64)
+        l2, _ = l1.RS_propagation(f4)
+        l3, _ = oe.lens(l2, (200.0, 200.0), (f4, f4))
+        xo, yo = tb.space(60.0, 32)
+        l4 = l3.CZT(f4, xo, yo)
+        p2 = rng.uniform(-np.pi, np.pi, (32, 32))
+        l5, _ = oe.SLM(l4, p2, 32)
+        l6 = l5.CZT(f4)
+        I = np.abs(l6.field) ** 2
+        target = (rng.uniform(0, 1, (32, 32)) < 0.1).astype(np.float64)
+        _save("four_f", x=x, y=y, wavelength=wl, f=f4, source=src.field, phase1=p1, xout=xo, yout=yo,
+              phase2=p2, after_rs=l2.field, after_lens=l3.field, after_czt1=l4.field, out=l6.field,
+              intensity=I, target=target)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

@@ -1,0 +1,124 @@
+"""Pin the FP64 oracle to the golden fixtures produced by the reference's own source.
+
+These run on CPU only.  The bar is rounding-level agreement (rel-L2 <= 1e-10):
+both sides compute in float64 / complex128 with the same formulas and layouts.
+"""
+import numpy as np
+import pytest
+
+from oracle import xlumina_ref as ref
+from tests.conftest import golden, rel_l2
+
+TOL = 1e-10
+
+
+def test_rs_square_both_signs_of_z():
+    g = golden("rs_square")
+    field = ref.slm(ref.gaussian_beam(g["x"], g["y"], g["wavelength"], (40.0, 40.0)), g["phase"])[0]
+    assert rel_l2(field, g["field_in"]) < 1e-13
+    for tag in ("pos", "neg"):
+        out = ref.rs_propagate(g["field_in"], g["x"], g["y"], g["wavelength"], float(g[f"z_{tag}"]))
+        assert rel_l2(out, g[f"out_{tag}"]) < TOL
+        qf = ref.rs_quality_factor(g["x"], g["y"], g["wavelength"], float(g[f"z_{tag}"]))
+        assert qf == pytest.approx(float(g[f"qf_{tag}"]), rel=1e-12)
+
+
+@pytest.mark.parametrize("case", ["rs_complex", "rs_odd"])
+def test_rs_random_fields(case):
+    g = golden(case)
+    out = ref.rs_propagate(g["field_in"], g["x"], g["y"], g["wavelength"], float(g["z"]))
+    assert rel_l2(out, g["out"]) < TOL
+
+
+def test_vrs_behind_lcd_and_polarizer():
+    g = golden("vrs")
+    Ex0, Ey0 = ref.polarized_gaussian_beam(g["x"], g["y"], g["wavelength"], (50.0, 50.0), (1, 0.5))
+    assert rel_l2(Ex0, g["Ex0"]) < 1e-13 and rel_l2(Ey0, g["Ey0"]) < 1e-13
+    Ex1, Ey1 = ref.lcd(g["Ex0"], g["Ey0"], g["eta"], g["theta"])
+    assert rel_l2(Ex1, g["lcd_Ex"]) < 1e-13 and rel_l2(Ey1, g["lcd_Ey"]) < 1e-13
+    Ex2, Ey2 = ref.linear_polarizer(Ex1, Ey1, g["alpha"])
+    assert rel_l2(Ex2, g["lp_Ex"]) < 1e-13 and rel_l2(Ey2, g["lp_Ey"]) < 1e-13
+    assert np.all(g["lp_Ez"] == 0)
+    out = ref.vrs_propagate(g["lp_Ex"], g["lp_Ey"], g["x"], g["y"], g["wavelength"], float(g["z"]))
+    for o, key in zip(out, ("Ex", "Ey", "Ez")):
+        assert rel_l2(o, g[key]) < TOL
+
+
+def test_czt_default_and_roi():
+    g = golden("czt")
+    out = ref.czt(g["field_in"], g["x"], g["y"], g["wavelength"], float(g["z"]))
+    assert rel_l2(out, g["out_default"]) < TOL
+    out = ref.czt(g["field_in"], g["x"], g["y"], g["wavelength"], float(g["z"]), g["xout"], g["yout"])
+    assert out.shape == (len(g["yout"]), len(g["xout"]))
+    assert rel_l2(out, g["out_roi"]) < TOL
+
+
+def test_vczt():
+    g = golden("vczt")
+    out = ref.vczt(g["Ex_in"], g["Ey_in"], g["x"], g["y"], g["wavelength"], float(g["z"]), g["xout"], g["yout"])
+    for o, key in zip(out, ("Ex", "Ey", "Ez")):
+        assert rel_l2(o, g[key]) < TOL
+
+
+def test_high_na_lens_and_focus():
+    g = golden("high_na")
+    E, s = ref.high_na_lens(g["Ex_in"], g["Ey_in"], g["x"], g["y"], float(g["radius"]), float(g["f"]))
+    assert s == pytest.approx(float(g["sin_theta_max"]), rel=1e-14)
+    assert rel_l2(E, g["lens_out"]) < 1e-13
+    out = ref.vczt_objective_lens(g["Ex_in"], g["Ey_in"], g["x"], g["y"], g["wavelength"],
+                                  float(g["radius"]), float(g["f"]), g["xout"], g["yout"])
+    for o, key in zip(out, ("Ex", "Ey", "Ez")):
+        assert rel_l2(o, g[key]) < TOL
+
+
+def test_masks_and_sources():
+    g = golden("masks")
+    x, y, wl = g["x"], g["y"], g["wavelength"]
+    gb = ref.gaussian_beam(x, y, wl, (40.0, 55.0), 1.5, (10.0, -5.0), (300.0, 200.0), 0.3)
+    assert rel_l2(gb, g["gauss"]) < 1e-13
+    assert rel_l2(ref.plane_wave(x, y, wl, 2.0, 0.01, 0.7, 3.0), g["plane"]) < 1e-13
+    Ex, Ey = ref.polarized_gaussian_beam(x, y, wl, (40.0, 40.0), (1, 1j), (3.0, 4.0))
+    assert rel_l2(Ex, g["pol_Ex"]) < 1e-13 and rel_l2(Ey, g["pol_Ey"]) < 1e-13
+    ox, oy = ref.sslm(g["pol_Ex"], g["pol_Ey"], g["alpha"], g["phi"])
+    assert rel_l2(ox, g["sslm_Ex"]) < 1e-13 and rel_l2(oy, g["sslm_Ey"]) < 1e-13
+    ox, oy = ref.sslm(g["pol_Ex"], g["pol_Ey"], g["alpha"], g["phi"], g["A1"], g["A2"])
+    assert rel_l2(ox, g["sslma_Ex"]) < 1e-13 and rel_l2(oy, g["sslma_Ey"]) < 1e-13
+    m = ref.lens_mask(x, y, wl, (120.0, 100.0), (2000.0, 2500.0))
+    assert rel_l2(m, g["lens_mask"]) < 1e-13
+    assert rel_l2(g["gauss"] * m, g["lens_scalar"]) < 1e-13
+    mv = ref.lens_mask(x, y, wl, (120.0, 120.0), (3000.0, 3000.0))
+    assert rel_l2(g["pol_Ex"] * mv, g["lens_vec_Ex"]) < 1e-13
+    assert np.all(g["lens_vec_Ez"] == 0)
+    lx, ly = ref.lcd(g["pol_Ex"], g["pol_Ey"], 1.1, 0.4)
+    assert rel_l2(lx, g["lcd_scalar_Ex"]) < 1e-13 and rel_l2(ly, g["lcd_scalar_Ey"]) < 1e-13
+    assert np.array_equal(g["lcd_scalar_Ez"], g["vin_Ez"])
+
+
+def test_losses():
+    g = golden("losses")
+    assert ref.mse_intensity(g["a"], g["b"]) == pytest.approx(float(g["mse_intensity"]), rel=1e-13)
+    assert ref.small_area_hybrid(g["I"]) == pytest.approx(float(g["small_area"]), rel=1e-13)
+
+
+def test_building_block_chain():
+    g = golden("building_block")
+    Ex, Ey = ref.sslm(g["Ex_in"], g["Ey_in"], g["alpha"], g["phi"])
+    Ex, Ey, Ez = ref.vrs_propagate(Ex, Ey, g["x"], g["y"], g["wavelength"], float(g["z"]))
+    Ex, Ey = ref.lcd(Ex, Ey, float(g["eta"]), float(g["theta"]))
+    for o, key in zip((Ex, Ey, Ez), ("Ex", "Ey", "Ez")):
+        assert rel_l2(o, g[key]) < TOL
+
+
+def test_four_f_chain():
+    g = golden("four_f")
+    x, y, wl, f = g["x"], g["y"], g["wavelength"], float(g["f"])
+    u = ref.slm(g["source"], g["phase1"])[0]
+    u = ref.rs_propagate(u, x, y, wl, f)
+    assert rel_l2(u, g["after_rs"]) < TOL
+    u = u * ref.lens_mask(x, y, wl, (200.0, 200.0), (f, f))
+    assert rel_l2(u, g["after_lens"]) < TOL
+    u = ref.czt(u, x, y, wl, f, g["xout"], g["yout"])
+    assert rel_l2(u, g["after_czt1"]) < TOL
+    u = ref.slm(u, g["phase2"])[0]
+    u = ref.czt(u, g["xout"], g["yout"], wl, f)
+    assert rel_l2(u, g["out"]) < TOL
