@@ -1,0 +1,314 @@
+"""Benchmark: vectorial RS (VRS) propagation of 2048 x 2048 fields on one GB300.
+
+Workload: 2048^2 grid over a 4 mm window (space(2 mm, 2048)), 633 nm; a
+radially polarised source (Ex = x/w e^{-rho^2/w^2}, Ey = y/w e^{-rho^2/w^2},
+w = 1 mm) behind a per-pixel LCD retarder (eta, theta uniform in [0, 2 pi))
+and a linear polarizer at one random angle; Ez derived; z drawn from
+{1, 5, 10, 20} cm.  One step propagates a batch of B fields (default 8).
+
+Arms:
+  default            libxlgb kernels; `value` = fields/s with inputs resident in
+                     HBM; `e2e` = the same through the public API with pinned
+                     host buffers copied in and the propagated fields copied out.
+  --impl reference   the FP64 CPU restatement of the reference algorithm (the
+                     reference itself is pure jax, which is not installable on
+                     these machines) on all host cores, one field per step.
+
+Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 2048
+HALF_WIDTH = 2000.0          # um, space(2 mm, 2048)
+WAVELENGTH = 0.633           # um
+WAIST = 1000.0               # um
+Z_SET = (1e4, 5e4, 1e5, 2e5)  # um
+METRIC = "2048² VRS fields/s"
+WORKLOAD = ("VRS 2048x2048 complex64, 4 mm window, 633 nm, radially polarised source w=1 mm, "
+            "per-pixel LCD (eta, theta) + linear polarizer fused, Ez derived, z in {1,5,10,20} cm")
+
+
+def make_inputs(batch, seed=1000):
+    """Seeded synthetic inputs for `batch` fields (float64 host arrays)."""
+    x = np.linspace(-HALF_WIDTH, HALF_WIDTH, N)
+    X, Y = np.meshgrid(x, x)
+    g = np.exp(-(X ** 2 + Y ** 2) / WAIST ** 2)
+    Ex = (X / WAIST) * g
+    Ey = (Y / WAIST) * g
+    rng = np.random.default_rng(seed)
+    eta = rng.uniform(0, 2 * np.pi, (batch, N, N)).astype(np.float32)
+    theta = rng.uniform(0, 2 * np.pi, (batch, N, N)).astype(np.float32)
+    alpha = float(rng.uniform(0, np.pi))
+    zs = [Z_SET[i % len(Z_SET)] for i in range(batch)]
+    return x, Ex, Ey, eta, theta, alpha, zs
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
+    """One field of the workload through the FP64 CPU restatement."""
+    ax, ay = ref.lcd(Ex, Ey, eta.astype(np.float64), theta.astype(np.float64))
+    ax, ay = ref.linear_polarizer(ax, ay, alpha)
+    return ref.vrs_propagate(ax, ay, x, x, WAVELENGTH, z)
+
+
+def run_reference(args):
+    from oracle import xlumina_ref as ref
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    x, Ex, Ey, eta, theta, alpha, zs = make_inputs(1)
+    for _ in range(args.warmup):
+        cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, zs[0])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, Z_SET[i % len(Z_SET)])
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    cores = ref.WORKERS
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "fields/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "batch": 1},
+            "cpu_baseline": {"value": v, "unit": "fields/s", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} fields, one per step, scipy.fft with {cores} workers"},
+            "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def cpu_baseline_sample(seconds=20.0):
+    from oracle import xlumina_ref as ref
+    x, Ex, Ey, eta, theta, alpha, zs = make_inputs(1)
+    cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, zs[0])  # warm-up (FFT plans, page-in)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, Z_SET[n % len(Z_SET)])
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt > seconds or n >= 8:
+            break
+    return {"value": n / dt, "unit": "fields/s", "cores": ref.WORKERS, "kind": "port",
+            "sample": f"{n} fields of the same workload (FP64 numpy/scipy restatement, "
+                      f"scipy.fft workers={ref.WORKERS})"}
+
+
+def run_gpu(args):
+    import torch
+
+    from xlumina_gb300 import engine
+    from xlumina_gb300 import optical_elements as oe
+    from xlumina_gb300 import vectorized_optics as vo
+
+    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
+        print(json.dumps({"error": "this benchmark runs on one GPU only (--gpus 1)"}))
+        sys.exit(2)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    B = args.batch
+    x, Ex, Ey, eta, theta, alpha, zs = make_inputs(B)
+    Ex_d = torch.as_tensor(Ex, dtype=torch.complex64, device=dev).expand(B, N, N).contiguous()
+    Ey_d = torch.as_tensor(Ey, dtype=torch.complex64, device=dev).expand(B, N, N).contiguous()
+    eta_d = torch.as_tensor(eta, device=dev)
+    theta_d = torch.as_tensor(theta, device=dev)
+    pre = [engine.op_lcd(eta_d, theta_d), engine.op_lp(alpha)]
+    call = engine.RsCall([Ex_d, Ey_d], x, x, WAVELENGTH, zs, vector=True, pre=pre)
+    stream = torch.cuda.current_stream()
+
+    # warm-up (transfer spectra are built here, once per distinct z)
+    for _ in range(args.warmup):
+        for s in range(3):
+            call.stage(s)
+    torch.cuda.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            for s in range(3):
+                call.stage(s)
+                ev[k][s + 1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    total_ms = t_start.elapsed_time(t_end)
+    stage_ms = [sum(ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps)) / args.steps
+                for s in range(3)]
+    value = B * args.steps / (total_ms / 1e3)
+
+    # roofline: algorithmic bytes per launch (B fields), per stage
+    n2 = N * N
+    alg = [72 * n2 * B, 128 * n2 * B, 72 * n2 * B]
+    names = ["rs_rows_fwd", "rs_cols_conv", "rs_rows_inv"]
+    dom = int(np.argmax(stage_ms))
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
+    pipe_gbs = sum(alg) / (sum(stage_ms) / 1e3) / 1e9
+
+    # plain path: one public-API call per field, no batching
+    src = vo.VectorizedLight(x, x, WAVELENGTH)
+    src.Ex = Ex_d[0]
+    src.Ey = Ey_d[0]
+    for _ in range(2):
+        oe.linear_polarizer(oe.LCD(src, eta_d[0], theta_d[0]), alpha).VRS_propagation(zs[0])
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    nplain = 2 * B
+    for i in range(nplain):
+        light = oe.linear_polarizer(oe.LCD(src, eta_d[i % B], theta_d[i % B]), alpha)
+        out, _ = light.VRS_propagation(zs[i % B])
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain = nplain / (p0.elapsed_time(p1) / 1e3)
+
+    # end to end through the public API: pinned host in, fields out
+    h_Ex = torch.as_tensor(np.broadcast_to(Ex, (B, N, N)).astype(np.complex64)).pin_memory()
+    h_Ey = torch.as_tensor(np.broadcast_to(Ey, (B, N, N)).astype(np.complex64)).pin_memory()
+    h_eta = torch.as_tensor(eta).pin_memory()
+    h_theta = torch.as_tensor(theta).pin_memory()
+    h_out = [torch.empty((B, N, N), dtype=torch.complex64).pin_memory() for _ in range(3)]
+    zarr = np.asarray(zs)
+
+    def e2e_step():
+        light = vo.VectorizedLight(x, x, WAVELENGTH)
+        light.Ex = h_Ex.to(dev, non_blocking=True)
+        light.Ey = h_Ey.to(dev, non_blocking=True)
+        e_ = h_eta.to(dev, non_blocking=True)
+        t_ = h_theta.to(dev, non_blocking=True)
+        out, _ = oe.linear_polarizer(oe.LCD(light, e_, t_), alpha).VRS_propagation(zarr)
+        for h, d in zip(h_out, (out.Ex, out.Ey, out.Ez)):
+            h.copy_(d, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    q0 = torch.cuda.Event(enable_timing=True)
+    q1 = torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        e2e_step()
+    q1.record(stream)
+    torch.cuda.synchronize()
+    e2e = B * ke / (q0.elapsed_time(q1) / 1e3)
+    h2d = (h_Ex.numel() + h_Ey.numel()) * 8 + (h_eta.numel() + h_theta.numel()) * 4
+    d2h = sum(h.numel() for h in h_out) * 8
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch": B, "fields_per_step": B,
+                   "l2": "inputs larger than L2 (%.2f GB of fields and masks per step)" %
+                         ((Ex_d.numel() + Ey_d.numel()) * 8 / 1e9 + (eta_d.numel() + theta_d.numel()) * 4 / 1e9)},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                     "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
+        "stages_ms": dict(zip(names, stage_ms)),
+        "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
+        "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
+        "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+        "spectrum_builds": engine.SPECTRA.builds,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--impl", default="xlgb", choices=["xlgb", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

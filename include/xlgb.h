@@ -1,0 +1,141 @@
+/*
+ * xlgb.h -- C ABI of libxlgb, the GB300 (sm_103a) light-propagation library
+ * behind the xlumina_gb300 Python package.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * handle (cudaStream_t passed as void*), launches on that stream and returns
+ * without synchronising.  Complex fields are complex64: interleaved
+ * (re, im) float32 pairs, row-major planes of ny rows by nx columns.  The
+ * library allocates no device memory: callers pass every output and
+ * workspace buffer, sized with the *_bytes() helpers.
+ *
+ * Return value: XL_OK (0) or a negative XL_E* code; xl_last_error() gives a
+ * one-line description of the most recent failure on the calling thread.
+ *
+ * The reference (XLuminA, pure Python on jax) has no native interface: each
+ * entry point below replaces a jitted jax function of its Python API, cited
+ * next to the declaration as file:line inside the XLuminA repository.
+ */
+#ifndef XLGB_H_
+#define XLGB_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XL_OK 0
+#define XL_EINVAL (-1)
+#define XL_ENOMEM (-2)
+#define XL_ETIMEOUT (-3)
+#define XL_ECUDA (-4)
+#define XL_EUNSUPPORTED (-5)
+
+#define XL_MAX_OPS 8
+#define XL_MAX_FFT 8192   /* longest FFT any kernel runs (RS transfer spectrum: 2Q) */
+#define XL_MAX_SIDE 4096  /* longest field side (Q <= 4096) */
+
+/* Per-pixel operations fused into the first / last pass of a propagator
+ * (or run alone by xl_apply_ops).  Parameter i is a per-pixel float32 plane
+ * when bit i of pmask is set (ptr[i], batch stride pbstride elements),
+ * otherwise the scalar sval[i]. */
+enum {
+  XL_OP_NONE = 0,
+  XL_OP_PHASE = 1,     /* scalar SLM, optical_elements.py:76-103: e0 *= exp(i p0) */
+  XL_OP_SSLM = 2,      /* sSLM, optical_elements.py:186-222: e0 *= exp(i p0), e1 *= exp(i p1) */
+  XL_OP_SSLM_AMP = 3,  /* sSLM_with_amplitude, :224-264: also *= p2, p3 */
+  XL_OP_LCD = 4,       /* LCD retarder (eta=p0, theta=p1), :266-305, Ez kept */
+  XL_OP_LP = 5,        /* linear_polarizer (alpha=p0), :307-332, Ez zeroed */
+  XL_OP_SEPMASK = 6,   /* separable mask colfac[col]*rowfac[row] with FP64 pupil test
+                          (thin lens, :678-703); sval[0] != 0 zeroes Ez (vector lens) */
+  XL_OP_CMUL = 7,      /* multiply all components by a complex64 plane ptr[0] */
+  XL_OP_HIGHNA = 8     /* high-NA objective lens, optical_elements.py:515-594: ptr[0], ptr[1]
+                          float64 x, y; dval[0] radius, dval[1] focal length, dval[2]
+                          sin(theta_max); Ez derived from Ex, Ey, output (Ex, Ey, Ez) */
+};
+
+typedef struct {
+  int kind;
+  int pmask;
+  const void* ptr[4];
+  float sval[4];
+  long long pbstride;
+  double dval[4];
+} XlOp;
+
+typedef struct {
+  int nops;
+  XlOp ops[XL_MAX_OPS];
+} XlProg;
+
+const char* xl_last_error(void);
+int xl_version(void);
+
+/* Upload the twiddle tables to the current device.  Called once per device
+ * before the first launch (every entry point calls it lazily as well). */
+int xl_init(void);
+
+/* ---- Rayleigh-Sommerfeld (RS / VRS) ----------------------------------- */
+
+/* Bytes of one transfer spectrum for an ny x nx field: (2Q)^2 complex64,
+ * Q = next power of two >= max(ny, nx). */
+size_t xl_rs_spectrum_bytes(int ny, int nx);
+/* Bytes of workspace xl_rs_transfer_spectrum needs. */
+size_t xl_rs_spectrum_work_bytes(int ny, int nx);
+
+/* Transfer spectrum of the RS impulse response, wave_optics.py:291-297 and
+ * the fft2(H) of :288.  offx / offy: device float64 arrays of length 2Q
+ * holding the impulse-response offsets in wrapped order (entry d mod 2Q
+ * holds the offset of index distance d, |d| <= n-1, built from the
+ * reference's reflect-padded grid, :265-279); scale multiplies the spectrum
+ * (dx*dy / (2Q)^2 for a propagator).  Output in the layout
+ * xl_rs_propagate reads. */
+int xl_rs_transfer_spectrum(void* stream, int ny, int nx, const double* offx, const double* offy,
+                            double z, double wavelength, double scale, void* spectrum, void* work);
+
+typedef struct {
+  int batch;          /* fields in this call */
+  int comps_in;       /* 1: scalar field; 2: (Ex, Ey) */
+  int comps_out;      /* 1: scalar; 3: (Ex, Ey, Ez), Ez derived from Ex, Ey (VRS) */
+  int ny, nx;
+  const void* in[3];  /* complex64 input planes per component */
+  long long in_bstride;
+  void* out[3];       /* complex64 output planes per component */
+  long long out_bstride;
+  const double* x;    /* device coordinates, nx (VRS Ez derivation) */
+  const double* y;    /* device coordinates, ny */
+  const double* z;    /* device, one distance per batch entry (VRS Ez derivation) */
+  const void* spectrum;        /* stacked transfer spectra */
+  long long spectrum_stride;   /* complex64 elements between spectra */
+  const int* spectrum_index;   /* device, spectrum used by each batch entry; NULL: entry 0 */
+  void* work;                  /* >= xl_rs_work_bytes(batch, comps_out, ny, nx) */
+  XlProg pre;                  /* fused before the first pass */
+  XlProg post;                 /* fused after the last pass */
+} XlRsArgs;
+
+size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx);
+
+/* RS / VRS propagation: RS_propagation_jit, wave_optics.py:281-289, and
+ * VRS_propagation_jit, vectorized_optics.py:364-373, with the VRS Ez of
+ * vectorized_optics.py:258-261.  Output = crop(ifft2(fft2(pad(E)) * S)),
+ * S the transfer spectrum (its scale includes dx*dy / (2Q)^2). */
+int xl_rs_propagate(void* stream, const XlRsArgs* args);
+
+/* One pass of xl_rs_propagate, for callers that time or overlap the passes:
+ * stage 0 = prologue + row spectra, 1 = column convolution (in place),
+ * 2 = inverse rows + crop + epilogue.  Running 0, 1, 2 in order on one stream
+ * equals xl_rs_propagate. */
+int xl_rs_stage(void* stream, const XlRsArgs* args, int stage);
+
+/* ---- Elementwise ------------------------------------------------------ */
+
+/* Apply a Jones program to batch x comps planes (out may alias in). */
+int xl_apply_ops(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
+                 long long in_bstride, void* const* out, long long out_bstride, const XlProg* prog);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XLGB_H_ */

@@ -1,0 +1,64 @@
+// CPU harness for the device FFT engine: runs the T threads of one FFT group
+// in sequence, pass by pass, with the same shared-memory exchange the kernels
+// use.  Built by tests/test_fft_core_cpu.py with g++ and called through ctypes.
+#include <cmath>
+#include <vector>
+#include "../../xlumina_gb300/csrc/fft_core.cuh"
+
+using namespace xl;
+
+struct Regs { float2 v[16]; };
+
+template <int LOGN, int DIR, int P>
+static void emu(std::vector<Regs>& V, float2* sm, const float2* tw) {
+  using S = FftShape<LOGN>;
+  for (int j = 0; j < S::T; ++j) fft_pass<LOGN, P, DIR>(V[j].v, j, sm, tw);
+  if constexpr (P < S::NPASS - 1) {
+    for (int j = 0; j < S::T; ++j) fft_gather<LOGN>(V[j].v, j, sm);
+    emu<LOGN, DIR, P + 1>(V, sm, tw);
+  }
+}
+
+template <int LOGN, int DIR>
+static void run(const float* in, float* out) {
+  using S = FftShape<LOGN>;
+  std::vector<float2> tw(S::N), sm(S::SMEM);
+  for (int q = 0; q < S::N; ++q) {
+    double a = 2.0 * M_PI * q / S::N;
+    tw[q] = make_float2((float)std::cos(a), (float)-std::sin(a));
+  }
+  std::vector<Regs> V(S::T);
+  for (int j = 0; j < S::T; ++j)
+    for (int m = 0; m < 16; ++m) {
+      int n = j + m * S::T;
+      V[j].v[m] = make_float2(in[2 * n], in[2 * n + 1]);
+    }
+  emu<LOGN, DIR, 0>(V, sm.data(), tw.data());
+  for (int j = 0; j < S::T; ++j)
+    for (int m = 0; m < 16; ++m) {
+      int n = j + m * S::T;
+      out[2 * n] = V[j].v[m].x;
+      out[2 * n + 1] = V[j].v[m].y;
+    }
+}
+
+template <int DIR>
+static int dispatch(int logn, const float* in, float* out) {
+  switch (logn) {
+    case 4: run<4, DIR>(in, out); return 0;
+    case 5: run<5, DIR>(in, out); return 0;
+    case 6: run<6, DIR>(in, out); return 0;
+    case 7: run<7, DIR>(in, out); return 0;
+    case 8: run<8, DIR>(in, out); return 0;
+    case 9: run<9, DIR>(in, out); return 0;
+    case 10: run<10, DIR>(in, out); return 0;
+    case 11: run<11, DIR>(in, out); return 0;
+    case 12: run<12, DIR>(in, out); return 0;
+    case 13: run<13, DIR>(in, out); return 0;
+  }
+  return -1;
+}
+
+extern "C" int fft_core_check(int logn, int dir, const float* in, float* out) {
+  return dir < 0 ? dispatch<-1>(logn, in, out) : dispatch<1>(logn, in, out);
+}

@@ -1,0 +1,95 @@
+"""CPU checks of the C ABI library and of the host-side planning code.
+
+No kernel runs here: the library must load and export every entry point that
+include/xlgb.h declares, the ctypes mirrors must have the C layout, and the
+host geometry must match the reference's formulas.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import xlumina_ref as ref
+from tests.conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "xlgb.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(xl_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from xlumina_gb300 import _build, _lib
+    _build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from xlumina_gb300 import _lib
+    names = _declared()
+    assert "xl_rs_propagate" in names and "xl_last_error" in names
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} declared in xlgb.h but not bound in _lib"
+
+
+def test_ctypes_layouts():
+    from xlumina_gb300 import _lib
+    assert ctypes.sizeof(_lib.XlOp) == 96
+    assert _lib.XlOp.dval.offset == 64
+    assert ctypes.sizeof(_lib.XlProg) == 8 + 8 * 96
+    assert _lib.XlRsArgs.inp.offset == 24
+    assert _lib.XlRsArgs.pre.offset % 8 == 0
+
+
+def test_size_helpers(lib):
+    assert lib.xl_rs_spectrum_bytes(2048, 2048) == 4096 * 4096 * 8
+    assert lib.xl_rs_spectrum_bytes(1000, 1000) == 2048 * 2048 * 8
+    assert lib.xl_rs_work_bytes(8, 3, 2048, 2048) == 8 * 3 * 2048 * 4096 * 8
+    assert lib.xl_rs_spectrum_bytes(1, 10) == 0
+    assert lib.xl_rs_spectrum_bytes(8192, 8192) == 0
+
+
+def test_argument_errors_without_gpu(lib):
+    from xlumina_gb300 import _lib
+    a = _lib.XlRsArgs()
+    a.batch, a.comps_in, a.comps_out, a.ny, a.nx = 1, 2, 2, 64, 64
+    assert lib.xl_rs_propagate(None, ctypes.byref(a)) == _lib.XL_EINVAL
+    assert b"comps_in/comps_out" in lib.xl_last_error()
+    assert lib.xl_rs_stage(None, ctypes.byref(a), 7) == _lib.XL_EINVAL
+    rc = lib.xl_rs_transfer_spectrum(None, 64, 64, None, None, 1.0, 0.5, 1.0, None, None)
+    assert rc == _lib.XL_EINVAL
+
+
+def test_wrapped_offsets_match_reference_grid():
+    from xlumina_gb300 import engine
+    for n in (5, 8, 63, 64):
+        x, _ = ref.space(100.0, n)
+        ext = ref.rs_offset_axis(x)
+        P = 2 << engine.rs_logq(n, n)
+        w = engine.rs_wrapped_offsets(x, P)
+        for d in range(-(n - 1), n):
+            assert w[d % P] == ext[d + n - 1]
+        assert np.isnan(w).sum() == P - (2 * n - 1)
+
+
+def test_quality_factor_and_lens_factors():
+    from xlumina_gb300 import engine
+    x, y = ref.space(150.0, 48)
+    assert engine.quality_factor(x, y, 0.633, 2e3) == ref.rs_quality_factor(x, y, 0.633, 2e3)
+    cf, rf, tc, tr = engine.lens_factors(x, y, 0.633, (120.0, 100.0), (2000.0, 2500.0))
+    m = np.where((tc[None, :] + tr[:, None]) < 1, 1, 0) * (rf[:, None] * cf[None, :])
+    assert np.max(np.abs(m - ref.lens_mask(x, y, 0.633, (120.0, 100.0), (2000.0, 2500.0)))) < 1e-12
+
+
+def test_cuda_required_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from xlumina_gb300 import wave_optics
+    with pytest.raises(RuntimeError, match="CUDA"):
+        wave_optics.ScalarLight(np.linspace(-1, 1, 8), np.linspace(-1, 1, 8), 0.5).field

@@ -1,0 +1,92 @@
+"""ctypes binding of libxlgb.so (declarations mirror ``include/xlgb.h``).
+
+The library is the only compute path: if it is missing or fails to load,
+every propagator raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from ._build import LIB
+
+XL_OK = 0
+XL_EINVAL = -1
+XL_ENOMEM = -2
+XL_ETIMEOUT = -3
+XL_ECUDA = -4
+XL_EUNSUPPORTED = -5
+XL_MAX_OPS = 8
+XL_MAX_SIDE = 4096
+
+OP_NONE, OP_PHASE, OP_SSLM, OP_SSLM_AMP, OP_LCD, OP_LP, OP_SEPMASK, OP_CMUL, OP_HIGHNA = range(9)
+
+
+class XlOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("pmask", ctypes.c_int), ("ptr", ctypes.c_void_p * 4),
+                ("sval", ctypes.c_float * 4), ("pbstride", ctypes.c_longlong), ("dval", ctypes.c_double * 4)]
+
+
+class XlProg(ctypes.Structure):
+    _fields_ = [("nops", ctypes.c_int), ("ops", XlOp * XL_MAX_OPS)]
+
+
+class XlRsArgs(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("comps_in", ctypes.c_int), ("comps_out", ctypes.c_int),
+                ("ny", ctypes.c_int), ("nx", ctypes.c_int),
+                ("inp", ctypes.c_void_p * 3), ("in_bstride", ctypes.c_longlong),
+                ("out", ctypes.c_void_p * 3), ("out_bstride", ctypes.c_longlong),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("spectrum", ctypes.c_void_p), ("spectrum_stride", ctypes.c_longlong),
+                ("spectrum_index", ctypes.c_void_p), ("work", ctypes.c_void_p),
+                ("pre", XlProg), ("post", XlProg)]
+
+
+# name -> (restype, argtypes); every symbol include/xlgb.h declares.
+SIGNATURES = {
+    "xl_last_error": (ctypes.c_char_p, []),
+    "xl_version": (ctypes.c_int, []),
+    "xl_init": (ctypes.c_int, []),
+    "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "xl_rs_spectrum_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "xl_rs_transfer_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_rs_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "xl_rs_propagate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
+    "xl_rs_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs), ctypes.c_int]),
+    "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                    ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                    ctypes.POINTER(XlProg)]),
+}
+
+_lib = None
+
+
+class XlError(RuntimeError):
+    """A libxlgb entry point returned an error code."""
+
+
+def load(path: str = LIB):
+    """Load libxlgb.so and declare its entry points (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"libxlgb.so not found at {path}: build it with `python -m xlumina_gb300._build` "
+            "(nvcc, sm_103a); there is no fallback compute path")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != XL_OK:
+        msg = _lib.xl_last_error().decode() if _lib is not None else ""
+        raise XlError(f"{what or 'libxlgb'} failed with code {rc}: {msg}")

@@ -1,0 +1,69 @@
+// Library-wide C ABI pieces: error reporting, version, per-device set-up.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+
+namespace xl {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  set_error("%s: CUDA error %d (%s)", where, (int)e, cudaGetErrorString(e));
+  return XL_ECUDA;
+}
+
+static std::mutex g_init_mu;
+static bool g_init_dev[256];
+
+// Twiddle tables for S = 1, 2, 4, ..., XL_MAX_FFT at offset S: e^{-2 pi i q / S},
+// computed in float64 and rounded once.
+static const std::vector<float2>& host_twiddles() {
+  static std::vector<float2> t;
+  if (t.empty()) {
+    t.assign(2 * XL_MAX_FFT, make_float2(0.f, 0.f));
+    for (int s = 1; s <= XL_MAX_FFT; s <<= 1)
+      for (int q = 0; q < s; ++q) {
+        const double a = 2.0 * M_PI * (double)q / (double)s;
+        t[s + q] = make_float2((float)cos(a), (float)-sin(a));
+      }
+  }
+  return t;
+}
+
+int ensure_init() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 256) {
+    set_error("device index %d out of range", dev);
+    return XL_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (g_init_dev[dev]) return XL_OK;
+  const float2* h = host_twiddles().data();
+  if ((e = rs_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (rs)");
+  if ((e = czt_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (czt)");
+  if ((e = elem_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (elem)");
+  g_init_dev[dev] = true;
+  return XL_OK;
+}
+
+}  // namespace xl
+
+extern "C" const char* xl_last_error(void) { return xl::g_err; }
+
+extern "C" int xl_version(void) { return 100; }
+
+extern "C" int xl_init(void) { return xl::ensure_init(); }

@@ -1,0 +1,40 @@
+// Host-side helpers shared by the translation units of libxlgb.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include "xl_types.h"
+
+namespace xl {
+
+// Thread-local last-error string (defined in capi.cu).
+void set_error(const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* where);
+int ensure_init();  // uploads twiddle tables to the current device once
+
+inline int ilog2_ceil(long long v) {
+  int l = 0;
+  while ((1LL << l) < v) ++l;
+  return l;
+}
+
+// Allow a kernel more than 48 KB of dynamic shared memory (once per device).
+template <typename K>
+inline cudaError_t allow_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+#define XL_CHECK_LAUNCH(where)                                  \
+  do {                                                          \
+    cudaError_t _e = cudaGetLastError();                        \
+    if (_e != cudaSuccess) return ::xl::cuda_fail(_e, where);   \
+  } while (0)
+
+// Per-translation-unit twiddle upload hooks (each TU has its own table copy).
+cudaError_t rs_upload_twiddles(const float2* host);
+cudaError_t czt_upload_twiddles(const float2* host);
+cudaError_t elem_upload_twiddles(const float2* host);
+
+}  // namespace xl

@@ -1,0 +1,509 @@
+// Rayleigh-Sommerfeld propagation (scalar RS and vectorial VRS) for sm_103a.
+//
+// The reference (wave_optics.py:281-289) zero-pads the N x N field to
+// (2N-1)^2, multiplies fft2(U) by fft2(H) and crops [N-1:, N-1:].  Here the
+// same linear convolution runs on a P = 2Q grid (Q = next power of two >= N),
+// which gives the identical result because the impulse response is placed
+// at wrapped offsets, and the transform is split into Q-point halves:
+//
+//   row pass (rs_rows_fwd):  for each of the N input rows, the P-point
+//       spectrum of the zero-padded row as two Q-point FFTs (even and odd
+//       frequencies; the odd half of the input is pre-twiddled by w_P^n).
+//       The Jones program and the VRS Ez derivation run in this pass.
+//   column pass (rs_cols_conv): for each of the 2Q spectrum columns, the same
+//       split along y, a multiply by the transfer spectrum, the inverse split,
+//       and only the N output rows that survive the crop are written back.
+//   inverse row pass (rs_rows_inv): inverse split along x, crop to N
+//       columns, optional fused epilogue program, store.
+//
+// Intermediate data per component: N rows x 2Q complex64 (one buffer, the
+// column pass works in place).  Transfer spectra are built once per
+// (z, wavelength, grid) by rs_hhat_rows / rs_hhat_cols and stored
+// column-major for the column pass: S[(col*2 + parity)*Q + k].
+#include <math.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace xl {
+
+template <int LOGQ> struct RsCfg {
+  using S = FftShape<LOGQ>;
+  static constexpr int Q = S::N;
+  static constexpr int P = 2 * Q;
+  static constexpr int T = S::T;
+  static constexpr int XS = S::SMEM;  // exchange buffer slots
+  static constexpr int RPC = (256 / (2 * T)) > 1 ? (256 / (2 * T)) : 1;  // rows per CTA
+  static constexpr int WC = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));  // conv tile width
+  static constexpr int WH = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));   // spectrum-build tile
+  static constexpr int ROW_THREADS = 2 * RPC * T;
+  static constexpr int CONV_THREADS = 2 * WC * T;
+  static constexpr int HCOL_THREADS = 2 * WH * T;
+};
+
+// ---------------------------------------------------------------------------
+// Transfer spectrum, step 1: rows of the wrapped impulse response -> P-point
+// row spectra, written in parity-split order (even frequencies, then odd).
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_hhat_rows(int ny, int nx, const double* __restrict__ offx,
+                             const double* __restrict__ offy, double z, double inv_lambda, float k,
+                             float2* __restrict__ out) {
+  using C = RsCfg<LOGQ>;
+  extern __shared__ float2 smem[];
+  float2* row = smem;                         // RPC x P
+  float2* xch = smem + C::RPC * C::P;         // 2 RPC x XS
+  const int tid = threadIdx.x;
+  const int slot = tid / (2 * C::T);
+  const int par = (tid / C::T) & 1;
+  const int j = tid % C::T;
+  const int i0 = blockIdx.x * C::RPC;
+
+  for (int idx = tid; idx < C::RPC * C::P; idx += blockDim.x) {
+    const int s = idx / C::P, col = idx % C::P, i = i0 + s;
+    const bool vy = (i < ny) || (i > C::P - ny);
+    const bool vx = (col < nx) || (col > C::P - nx);
+    float2 h = make_float2(0.f, 0.f);
+    if (i < C::P && vy && vx) h = rs_kernel_value(offx[col], offy[i], z, inv_lambda, k);
+    row[idx] = h;
+  }
+  __syncthreads();
+
+  const float2* twQ = tw_table(LOGQ);
+  const float2* twP = tw_table(LOGQ + 1);
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int n = j + m * C::T;
+    const float2 a = row[slot * C::P + n], b = row[slot * C::P + n + C::Q];
+    v[m] = par ? cmul(csub(a, b), twP[n]) : cadd(a, b);
+  }
+  block_fft<LOGQ, -1>(v, j, xch + (2 * slot + par) * C::XS, twQ);
+  const int i = i0 + slot;
+  if (i < C::P) {
+    float2* dst = out + (long long)i * C::P + par * C::Q;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) dst[j + m * C::T] = v[m];
+  }
+}
+
+// Transfer spectrum, step 2: P-point column transforms of the row spectra,
+// stored column-major in parity-split order, times `scale`.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS) rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
+  using C = RsCfg<LOGQ>;
+  constexpr int W = C::WH, PITCH = C::WH + 1;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;                  // P x PITCH
+  float2* xch = smem + C::P * PITCH;    // 2W x XS
+  const int tid = threadIdx.x;
+  const int w = tid / (2 * C::T);
+  const int par = (tid / C::T) & 1;
+  const int j = tid % C::T;
+  const int c0 = blockIdx.x * W;
+
+  for (int idx = tid; idx < C::P * W; idx += blockDim.x) {
+    const int r = idx / W, ww = idx % W;
+    tile[r * PITCH + ww] = in[(long long)r * C::P + c0 + ww];
+  }
+  __syncthreads();
+  const float2* twQ = tw_table(LOGQ);
+  const float2* twP = tw_table(LOGQ + 1);
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int n = j + m * C::T;
+    const float2 a = tile[n * PITCH + w], b = tile[(n + C::Q) * PITCH + w];
+    v[m] = par ? cmul(csub(a, b), twP[n]) : cadd(a, b);
+  }
+  block_fft<LOGQ, -1>(v, j, xch + (2 * w + par) * C::XS, twQ);
+  float2* dst = out + ((long long)(c0 + w) * 2 + par) * C::Q;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) dst[j + m * C::T] = cscale(v[m], scale);
+}
+
+// ---------------------------------------------------------------------------
+struct RsLaunch {
+  int B, cin, cout, ny, nx;
+  const float2* in[3];
+  long long ibs;
+  float2* out[3];
+  long long obs;
+  const double* x;
+  const double* y;
+  const double* z;
+  const float2* spec;
+  long long sstride;
+  const int* sidx;
+  float2* work;
+  XlProg pre, post;
+};
+
+// Row pass: prologue (Jones program, VRS Ez) + parity-split row spectra.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_rows_fwd(const RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  extern __shared__ float2 smem[];
+  const int nc = p.cout;
+  float2* stage = smem;                          // RPC x nc x Q
+  float2* xch = smem + C::RPC * nc * C::Q;       // 2 RPC x XS
+  const int tid = threadIdx.x;
+  const int slot = tid / (2 * C::T);
+  const int par = (tid / C::T) & 1;
+  const int j = tid % C::T;
+  const int b = blockIdx.y;
+  const int r0 = blockIdx.x * C::RPC;
+  const float zb = p.z ? (float)p.z[b] : 0.f;
+
+  for (int idx = tid; idx < C::RPC * p.nx; idx += blockDim.x) {
+    const int s = idx / p.nx, n = idx % p.nx, r = r0 + s;
+    if (r >= p.ny) continue;
+    const long long off = (long long)b * p.ibs + (long long)r * p.nx + n;
+    float2 e[3];
+    e[0] = p.in[0][off];
+    e[1] = p.cin > 1 ? p.in[1][off] : make_float2(0.f, 0.f);
+    e[2] = make_float2(0.f, 0.f);
+    PixelCtx px{r, n, (long long)r * p.nx + n, b};
+    apply_prog(p.pre, e, px);
+    if (nc == 3) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
+      const float X = (float)p.x[n], Y = (float)p.y[r];
+      const float rr = sqrtf(X * X + Y * Y + zb * zb);
+      e[2] = cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr));
+    }
+    for (int c = 0; c < nc; ++c) stage[(s * nc + c) * C::Q + n] = e[c];
+  }
+  __syncthreads();
+
+  const float2* twQ = tw_table(LOGQ);
+  const float2* twP = tw_table(LOGQ + 1);
+  const int r = r0 + slot;
+  for (int c = 0; c < nc; ++c) {
+    float2 v[16];
+    const float2* src = stage + (slot * nc + c) * C::Q;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int n = j + m * C::T;
+      float2 a = (n < p.nx && r < p.ny) ? src[n] : make_float2(0.f, 0.f);
+      v[m] = par ? cmul(a, twP[n]) : a;
+    }
+    block_fft<LOGQ, -1>(v, j, xch + (2 * slot + par) * C::XS, twQ);
+    if (r < p.ny) {
+      float2* dst = p.work + (((long long)b * nc + c) * p.ny + r) * C::P + par * C::Q;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dst[j + m * C::T] = v[m];
+    }
+  }
+}
+
+// Column pass: y-split spectra, times the transfer spectrum, inverse, crop.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  constexpr int W = C::WC, PITCH = C::WC + 1;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;                   // Q x PITCH
+  float2* xch = smem + C::Q * PITCH;     // 2W x XS
+  const int tid = threadIdx.x;
+  const int w = tid / (2 * C::T);
+  const int par = (tid / C::T) & 1;
+  const int j = tid % C::T;
+  const int b = blockIdx.y;
+  const int c0 = blockIdx.x * W;
+  const int col = c0 + w;
+  const int nc = p.cout;
+  const float2* twQ = tw_table(LOGQ);
+  const float2* twP = tw_table(LOGQ + 1);
+  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride +
+                       ((long long)col * 2 + par) * C::Q;
+
+  for (int c = 0; c < nc; ++c) {
+    float2* plane = p.work + ((long long)b * nc + c) * p.ny * C::P;
+    for (int idx = tid; idx < p.ny * W; idx += blockDim.x) {
+      const int r = idx / W, ww = idx % W;
+      tile[r * PITCH + ww] = plane[(long long)r * C::P + c0 + ww];
+    }
+    __syncthreads();
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int n = j + m * C::T;
+      const float2 a = n < p.ny ? tile[n * PITCH + w] : make_float2(0.f, 0.f);
+      v[m] = par ? cmul(a, twP[n]) : a;
+    }
+    float2* xb = xch + (2 * w + par) * C::XS;
+    block_fft<LOGQ, -1>(v, j, xb, twQ);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], spec[j + m * C::T]);
+    block_fft<LOGQ, 1>(v, j, xb, twQ);
+    if (par) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * C::T;
+        xb[smpad(n)] = cmulc(v[m], twP[n]);
+      }
+    }
+    __syncthreads();
+    if (!par) {
+      const float2* xo = xch + (2 * w + 1) * C::XS;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * C::T;
+        if (n < p.ny) tile[n * PITCH + w] = cadd(v[m], xo[smpad(n)]);
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < p.ny * W; idx += blockDim.x) {
+      const int r = idx / W, ww = idx % W;
+      plane[(long long)r * C::P + c0 + ww] = tile[r * PITCH + ww];
+    }
+    __syncthreads();
+  }
+}
+
+// Inverse row pass: x-split inverse, crop to nx columns, epilogue, store.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_rows_inv(const RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  extern __shared__ float2 smem[];
+  const int nc = p.cout;
+  float2* xch = smem;                              // 2 RPC x XS
+  float2* stage = smem + 2 * C::RPC * C::XS;       // RPC x nc x Q (epilogue only)
+  const bool epi = p.post.nops > 0;
+  const int tid = threadIdx.x;
+  const int slot = tid / (2 * C::T);
+  const int par = (tid / C::T) & 1;
+  const int j = tid % C::T;
+  const int b = blockIdx.y;
+  const int r0 = blockIdx.x * C::RPC;
+  const int r = r0 + slot;
+  const float2* twQ = tw_table(LOGQ);
+  const float2* twP = tw_table(LOGQ + 1);
+
+  for (int c = 0; c < nc; ++c) {
+    float2 v[16];
+    const float2* src = p.work + (((long long)b * nc + c) * p.ny + (r < p.ny ? r : 0)) * C::P +
+                        par * C::Q;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = src[j + m * C::T];
+    float2* xb = xch + (2 * slot + par) * C::XS;
+    block_fft<LOGQ, 1>(v, j, xb, twQ);
+    if (par) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * C::T;
+        xb[smpad(n)] = cmulc(v[m], twP[n]);
+      }
+    }
+    __syncthreads();
+    if (!par && r < p.ny) {
+      const float2* xo = xch + (2 * slot + 1) * C::XS;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * C::T;
+        if (n < p.nx) {
+          const float2 o = cadd(v[m], xo[smpad(n)]);
+          if (epi) stage[(slot * nc + c) * C::Q + n] = o;
+          else p.out[c][(long long)b * p.obs + (long long)r * p.nx + n] = o;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (epi) {
+    for (int idx = tid; idx < C::RPC * p.nx; idx += blockDim.x) {
+      const int s = idx / p.nx, n = idx % p.nx, rr = r0 + s;
+      if (rr >= p.ny) continue;
+      float2 e[3] = {stage[(s * nc) * C::Q + n], make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      for (int c = 1; c < nc; ++c) e[c] = stage[(s * nc + c) * C::Q + n];
+      PixelCtx px{rr, n, (long long)rr * p.nx + n, b};
+      apply_prog(p.post, e, px);
+      for (int c = 0; c < nc; ++c) p.out[c][(long long)b * p.obs + (long long)rr * p.nx + n] = e[c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+static int rs_logq(int ny, int nx) {
+  const int n = ny > nx ? ny : nx;
+  int l = ilog2_ceil(n);
+  return l < 4 ? 4 : l;
+}
+
+template <int LOGQ>
+static int launch_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy,
+                           double z, double wavelength, double scale, float2* spec, float2* work) {
+  using C = RsCfg<LOGQ>;
+  const size_t sm1 = (size_t)(C::RPC * C::P + 2 * C::RPC * C::XS) * sizeof(float2);
+  cudaError_t e = allow_smem(rs_hhat_rows<LOGQ>, sm1);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
+  const float k = (float)(2.0 * M_PI / wavelength);
+  rs_hhat_rows<LOGQ><<<(C::P + C::RPC - 1) / C::RPC, 2 * C::RPC * C::T, sm1, st>>>(
+      ny, nx, offx, offy, z, 1.0 / wavelength, k, work);
+  XL_CHECK_LAUNCH("rs_hhat_rows");
+  const size_t sm2 = (size_t)(C::P * (C::WH + 1) + 2 * C::WH * C::XS) * sizeof(float2);
+  e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_cols smem");
+  rs_hhat_cols<LOGQ><<<C::P / C::WH, 2 * C::WH * C::T, sm2, st>>>(work, (float)scale, spec);
+  XL_CHECK_LAUNCH("rs_hhat_cols");
+  return XL_OK;
+}
+
+template <int LOGQ>
+static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
+  using C = RsCfg<LOGQ>;
+  const dim3 g_rows((p.ny + C::RPC - 1) / C::RPC, p.B);
+  cudaError_t e;
+  if (stage == 0) {
+    const size_t sm = (size_t)(C::RPC * p.cout * C::Q + 2 * C::RPC * C::XS) * sizeof(float2);
+    if ((e = allow_smem(rs_rows_fwd<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_fwd smem");
+    rs_rows_fwd<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
+    XL_CHECK_LAUNCH("rs_rows_fwd");
+  } else if (stage == 1) {
+    const size_t sm = (size_t)(C::Q * (C::WC + 1) + 2 * C::WC * C::XS) * sizeof(float2);
+    if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
+    rs_cols_conv<LOGQ><<<dim3(C::P / C::WC, p.B), C::CONV_THREADS, sm, st>>>(p);
+    XL_CHECK_LAUNCH("rs_cols_conv");
+  } else {
+    const size_t sm =
+        (size_t)(2 * C::RPC * C::XS + (p.post.nops ? C::RPC * p.cout * C::Q : 0)) * sizeof(float2);
+    if ((e = allow_smem(rs_rows_inv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_inv smem");
+    rs_rows_inv<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
+    XL_CHECK_LAUNCH("rs_rows_inv");
+  }
+  return XL_OK;
+}
+
+template <int LOGQ>
+static int launch_propagate(cudaStream_t st, const RsLaunch& p, int stage) {
+  if (stage >= 0) return launch_stage<LOGQ>(st, p, stage);
+  for (int s = 0; s < 3; ++s)
+    if (int rc = launch_stage<LOGQ>(st, p, s)) return rc;
+  return XL_OK;
+}
+
+#define XL_RS_DISPATCH(LOGQ_VAR, CALL)          \
+  switch (LOGQ_VAR) {                           \
+    case 4: return CALL(4);                     \
+    case 5: return CALL(5);                     \
+    case 6: return CALL(6);                     \
+    case 7: return CALL(7);                     \
+    case 8: return CALL(8);                     \
+    case 9: return CALL(9);                     \
+    case 10: return CALL(10);                   \
+    case 11: return CALL(11);                   \
+    case 12: return CALL(12);                   \
+    default: break;                             \
+  }
+
+cudaError_t rs_upload_twiddles(const float2* host) {
+  return cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
+}
+
+}  // namespace xl
+
+using namespace xl;
+
+extern "C" size_t xl_rs_spectrum_bytes(int ny, int nx) {
+  if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE) return 0;
+  const size_t P = (size_t)2 << rs_logq(ny, nx);
+  return P * P * sizeof(float2);
+}
+
+extern "C" size_t xl_rs_spectrum_work_bytes(int ny, int nx) { return xl_rs_spectrum_bytes(ny, nx); }
+
+extern "C" size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx) {
+  if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE || batch < 1 || comps < 1) return 0;
+  const size_t P = (size_t)2 << rs_logq(ny, nx);
+  return (size_t)batch * comps * ny * P * sizeof(float2);
+}
+
+extern "C" int xl_rs_transfer_spectrum(void* stream, int ny, int nx, const double* offx,
+                                       const double* offy, double z, double wavelength,
+                                       double scale, void* spectrum, void* work) {
+  if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE) {
+    set_error("xl_rs_transfer_spectrum: field side out of range (2..%d): %d x %d", XL_MAX_SIDE, ny, nx);
+    return XL_EINVAL;
+  }
+  if (!offx || !offy || !spectrum || !work) {
+    set_error("xl_rs_transfer_spectrum: null pointer argument");
+    return XL_EINVAL;
+  }
+  if (!(z != 0.0) || !(wavelength > 0.0)) {
+    set_error("xl_rs_transfer_spectrum: need z != 0 and wavelength > 0 (got z=%g, wavelength=%g)", z,
+              wavelength);
+    return XL_EINVAL;
+  }
+  if (int rc = ensure_init()) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int lq = rs_logq(ny, nx);
+#define CALL(L) launch_spectrum<L>(st, ny, nx, offx, offy, z, wavelength, scale, (float2*)spectrum, \
+                                   (float2*)work)
+  XL_RS_DISPATCH(lq, CALL)
+#undef CALL
+  set_error("xl_rs_transfer_spectrum: unsupported size");
+  return XL_EUNSUPPORTED;
+}
+
+static int rs_run(void* stream, const XlRsArgs* a, int stage) {
+  if (!a) {
+    set_error("xl_rs_propagate: null args");
+    return XL_EINVAL;
+  }
+  if (a->ny < 2 || a->nx < 2 || a->ny > XL_MAX_SIDE || a->nx > XL_MAX_SIDE || a->batch < 1) {
+    set_error("xl_rs_propagate: bad shape batch=%d ny=%d nx=%d", a->batch, a->ny, a->nx);
+    return XL_EINVAL;
+  }
+  const bool scalar = a->comps_in == 1 && a->comps_out == 1;
+  const bool vector = a->comps_in == 2 && a->comps_out == 3;
+  if (!scalar && !vector) {
+    set_error("xl_rs_propagate: comps_in/comps_out must be 1/1 (RS) or 2/3 (VRS), got %d/%d",
+              a->comps_in, a->comps_out);
+    return XL_EINVAL;
+  }
+  for (int c = 0; c < a->comps_in; ++c)
+    if (!a->in[c]) { set_error("xl_rs_propagate: null input plane %d", c); return XL_EINVAL; }
+  for (int c = 0; c < a->comps_out; ++c)
+    if (!a->out[c]) { set_error("xl_rs_propagate: null output plane %d", c); return XL_EINVAL; }
+  if (!a->spectrum || !a->work) {
+    set_error("xl_rs_propagate: null spectrum or workspace");
+    return XL_EINVAL;
+  }
+  if (vector && (!a->x || !a->y || !a->z)) {
+    set_error("xl_rs_propagate: VRS needs x, y and z arrays");
+    return XL_EINVAL;
+  }
+  if (a->pre.nops < 0 || a->pre.nops > XL_MAX_OPS || a->post.nops < 0 || a->post.nops > XL_MAX_OPS) {
+    set_error("xl_rs_propagate: op program too long");
+    return XL_EINVAL;
+  }
+  if (int rc = ensure_init()) return rc;
+  RsLaunch p;
+  p.B = a->batch; p.cin = a->comps_in; p.cout = a->comps_out; p.ny = a->ny; p.nx = a->nx;
+  for (int c = 0; c < 3; ++c) {
+    p.in[c] = (const float2*)a->in[c];
+    p.out[c] = (float2*)a->out[c];
+  }
+  p.ibs = a->in_bstride; p.obs = a->out_bstride;
+  p.x = a->x; p.y = a->y; p.z = a->z;
+  p.spec = (const float2*)a->spectrum; p.sstride = a->spectrum_stride; p.sidx = a->spectrum_index;
+  p.work = (float2*)a->work;
+  p.pre = a->pre; p.post = a->post;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int lq = rs_logq(a->ny, a->nx);
+#define CALL(L) launch_propagate<L>(st, p, stage)
+  XL_RS_DISPATCH(lq, CALL)
+#undef CALL
+  set_error("xl_rs_propagate: unsupported size");
+  return XL_EUNSUPPORTED;
+}
+
+extern "C" int xl_rs_propagate(void* stream, const XlRsArgs* a) { return rs_run(stream, a, -1); }
+
+extern "C" int xl_rs_stage(void* stream, const XlRsArgs* a, int stage) {
+  if (stage < 0 || stage > 2) {
+    set_error("xl_rs_stage: stage must be 0, 1 or 2 (got %d)", stage);
+    return XL_EINVAL;
+  }
+  return rs_run(stream, a, stage);
+}

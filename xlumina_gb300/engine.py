@@ -1,0 +1,437 @@
+"""Host side of the propagation path: geometry planning, caches, and the calls
+into libxlgb.
+
+Everything here either prepares small float64 host data (offset grids, chirp
+vectors, separable mask factors), manages device buffers owned by torch, or
+launches a libxlgb entry point on the current torch stream.  No field data is
+computed on the host.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes
+import math
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_LOCK = threading.Lock()
+
+
+# ----------------------------------------------------------------- device --
+
+def lib():
+    return _lib.load()
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("xlumina_gb300 needs a CUDA device (sm_103a); there is no CPU path")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_handle() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def as_field(a, dev=None) -> torch.Tensor:
+    """complex64, contiguous, on the CUDA device."""
+    dev = dev or device()
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=dev)
+        if t.dtype != torch.complex64:
+            t = t.to(torch.complex64)
+        return t.contiguous()
+    return torch.as_tensor(np.asarray(a), device=dev).to(torch.complex64).contiguous()
+
+
+def as_real_param(a, dev=None):
+    """A mask parameter: python float for scalars, else a float32 contiguous CUDA tensor."""
+    if isinstance(a, (int, float, np.floating, np.integer)):
+        return float(a)
+    if isinstance(a, torch.Tensor):
+        if a.dim() == 0:
+            return float(a.item())
+        return a.to(device=dev or device(), dtype=torch.float32).contiguous()
+    arr = np.asarray(a)
+    if arr.ndim == 0:
+        return float(arr)
+    return torch.as_tensor(arr, device=dev or device()).to(torch.float32).contiguous()
+
+
+def as_grid(a) -> np.ndarray:
+    if isinstance(a, torch.Tensor):
+        a = a.detach().cpu().numpy()
+    return np.asarray(a, dtype=np.float64)
+
+
+_grid_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def device_grid(a: np.ndarray) -> torch.Tensor:
+    """float64 copy of a coordinate array on the device (cached by value)."""
+    key = (a.tobytes(), torch.cuda.current_device())
+    with _LOCK:
+        t = _grid_cache.get(key)
+        if t is not None:
+            _grid_cache.move_to_end(key)
+            return t
+    t = torch.as_tensor(a, dtype=torch.float64, device=device())
+    with _LOCK:
+        _grid_cache[key] = t
+        while len(_grid_cache) > 64:
+            _grid_cache.popitem(last=False)
+    return t
+
+
+# ------------------------------------------------------------- geometry --
+
+def rs_logq(ny: int, nx: int) -> int:
+    """Q = 2^logq is the half transform length: the smallest power of two >= the field side."""
+    n = max(ny, nx)
+    return max(4, int(math.ceil(math.log2(n))))
+
+
+def rs_offset_axis(x: np.ndarray) -> np.ndarray:
+    """The reference's 2N-1 impulse-response offsets (wave_optics.py:265-279):
+    ``x[0] - x[N-1-j]`` for j < N, then ``x[m] - x[0]``."""
+    return np.concatenate([x[0] - x[::-1], x[1:] - x[0]])
+
+
+def rs_wrapped_offsets(x: np.ndarray, P: int) -> np.ndarray:
+    """Offsets in wrapped order for a P-point circular convolution: entry d mod P
+    holds the offset of index distance d, |d| <= N-1; other entries are NaN."""
+    n = len(x)
+    ext = rs_offset_axis(x)
+    out = np.full(P, np.nan)
+    d = np.arange(-(n - 1), n)
+    out[d % P] = ext[d + n - 1]
+    return out
+
+
+def quality_factor(x, y, wavelength, z):
+    """wave_optics.py:187-191 / vectorized_optics.py:264-270."""
+    dx = x[1] - x[0]
+    dy = y[1] - y[0]
+    dr_real = np.sqrt(dx ** 2 + dy ** 2)
+    rmax = np.sqrt((x ** 2).max() + (y ** 2).max())
+    dr_ideal = np.sqrt(wavelength ** 2 + rmax ** 2 + 2 * wavelength * np.sqrt(rmax ** 2 + z ** 2)) - rmax
+    return dr_ideal / dr_real
+
+
+# --------------------------------------------------------- Jones program --
+
+class JonesOp:
+    """One per-pixel operation of a fused program (see XL_OP_* in xlgb.h)."""
+
+    __slots__ = ("kind", "params", "ptrs", "sval", "dval", "keep")
+
+    def __init__(self, kind, params=(), ptrs=(), sval=(), dval=(), keep=()):
+        self.kind = kind
+        self.params = list(params)   # floats or float32 tensors, parameter slots 0..3
+        self.ptrs = list(ptrs)       # raw device tensors for pointer slots (SEPMASK / CMUL / HIGHNA)
+        self.sval = list(sval)
+        self.dval = list(dval)
+        self.keep = list(keep)
+
+    def fill(self, op: _lib.XlOp, ny: int, nx: int) -> None:
+        op.kind = self.kind
+        pmask = 0
+        pbstride = 0
+        for i, p in enumerate(self.params):
+            if isinstance(p, torch.Tensor):
+                if p.shape[-2:] != (ny, nx):
+                    raise ValueError(f"mask parameter has shape {tuple(p.shape)}, field is {(ny, nx)}")
+                pmask |= 1 << i
+                op.ptr[i] = p.data_ptr()
+                if p.dim() == 3 and p.shape[0] > 1:
+                    pbstride = ny * nx
+            else:
+                op.sval[i] = float(p)
+        for i, t in enumerate(self.ptrs):
+            op.ptr[i] = 0 if t is None else t.data_ptr()
+            if t is not None and t.dim() == 3 and t.shape[0] > 1:
+                pbstride = ny * nx
+        for i, s in enumerate(self.sval):
+            op.sval[i] = float(s)
+        for i, d in enumerate(self.dval):
+            op.dval[i] = float(d)
+        op.pmask = pmask
+        op.pbstride = pbstride
+
+
+def fill_prog(prog: _lib.XlProg, ops, ny, nx) -> None:
+    ops = list(ops or ())
+    if len(ops) > _lib.XL_MAX_OPS:
+        raise ValueError(f"at most {_lib.XL_MAX_OPS} fused operations per pass")
+    prog.nops = len(ops)
+    for i, o in enumerate(ops):
+        o.fill(prog.ops[i], ny, nx)
+
+
+def op_phase(phase):
+    return JonesOp(_lib.OP_PHASE, [as_real_param(phase)])
+
+
+def op_sslm(alpha, phi):
+    return JonesOp(_lib.OP_SSLM, [as_real_param(alpha), as_real_param(phi)])
+
+
+def op_sslm_amp(alpha, phi, a1, a2):
+    return JonesOp(_lib.OP_SSLM_AMP, [as_real_param(alpha), as_real_param(phi), as_real_param(a1),
+                                      as_real_param(a2)])
+
+
+def op_lcd(eta, theta):
+    return JonesOp(_lib.OP_LCD, [as_real_param(eta), as_real_param(theta)])
+
+
+def op_lp(alpha):
+    return JonesOp(_lib.OP_LP, [as_real_param(alpha)])
+
+
+def lens_factors(x, y, wavelength, radius, focal):
+    """Separable factors of optical_elements.py:678-703 (float64 on the host):
+    colfac = exp(-ik x^2/2fx), rowfac = exp(-ik y^2/2fy), pupil terms x^2/rx^2, y^2/ry^2."""
+    k = 2 * np.pi / wavelength
+    fx, fy = focal
+    rx, ry = radius
+    colfac = np.exp(-1j * k * (x ** 2 / (2 * fx)))
+    rowfac = np.exp(-1j * k * (y ** 2 / (2 * fy)))
+    return colfac, rowfac, x ** 2 / rx ** 2, y ** 2 / ry ** 2
+
+
+def op_lens(x, y, wavelength, radius, focal, vector):
+    colfac, rowfac, tc, tr = lens_factors(x, y, wavelength, radius, focal)
+    dev = device()
+    c = torch.as_tensor(colfac, device=dev).to(torch.complex64)
+    r = torch.as_tensor(rowfac, device=dev).to(torch.complex64)
+    tct = torch.as_tensor(tc, device=dev, dtype=torch.float64)
+    trt = torch.as_tensor(tr, device=dev, dtype=torch.float64)
+    return JonesOp(_lib.OP_SEPMASK, ptrs=[c, r, tct, trt], sval=[1.0 if vector else 0.0])
+
+
+def op_high_na(x, y, radius, f):
+    """optical_elements.py:515-594 as one per-pixel op (returns the op and sin(theta_max))."""
+    s_max = radius / np.sqrt(radius ** 2 + f ** 2)
+    op = JonesOp(_lib.OP_HIGHNA, ptrs=[device_grid(x), device_grid(y)], dval=[radius, f, s_max])
+    return op, s_max
+
+
+def op_cmul(mask: torch.Tensor):
+    return JonesOp(_lib.OP_CMUL, ptrs=[as_field(mask)])
+
+
+def apply_ops(comps, ops, ny, nx):
+    """Materialise a Jones program on 1..3 component planes; returns new tensors."""
+    L = lib()
+    comps = [as_field(c) for c in comps]
+    lead = comps[0].shape[:-2]
+    B = int(np.prod(lead)) if len(lead) else 1
+    outs = [torch.empty_like(comps[0]) for _ in comps]
+    prog = _lib.XlProg()
+    fill_prog(prog, ops, ny, nx)
+    inp = (ctypes.c_void_p * 3)(*[c.data_ptr() for c in comps] + [0] * (3 - len(comps)))
+    out = (ctypes.c_void_p * 3)(*[o.data_ptr() for o in outs] + [0] * (3 - len(outs)))
+    _lib.check(L.xl_apply_ops(stream_handle(), B, len(comps), ny, nx, inp, ny * nx, out, ny * nx,
+                              ctypes.byref(prog)), "xl_apply_ops")
+    return outs
+
+
+# ------------------------------------------------------ RS transfer spectra --
+
+class SpectrumCache:
+    """Transfer spectra keyed by (grid, z, wavelength); LRU, bounded in bytes.
+
+    A spectrum depends only on the geometry, never on field data; the
+    reference recomputes it on every call (wave_optics.py:285-288)."""
+
+    def __init__(self, max_bytes=8 << 30):
+        self.max_bytes = max_bytes
+        self._d: "collections.OrderedDict" = collections.OrderedDict()
+        self._bytes = 0
+        self.builds = 0
+
+    @staticmethod
+    def key(x, y, z, wavelength):
+        return (x.tobytes(), y.tobytes(), float(z), float(wavelength), torch.cuda.current_device())
+
+    def get(self, x, y, z, wavelength):
+        k = self.key(x, y, z, wavelength)
+        with _LOCK:
+            s = self._d.get(k)
+            if s is not None:
+                self._d.move_to_end(k)
+                return s
+        s = build_rs_spectrum(x, y, z, wavelength)
+        nb = s.numel() * 8
+        with _LOCK:
+            self._d[k] = s
+            self._bytes += nb
+            self.builds += 1
+            while self._bytes > self.max_bytes and len(self._d) > 1:
+                _, old = self._d.popitem(last=False)
+                self._bytes -= old.numel() * 8
+        return s
+
+    def clear(self):
+        with _LOCK:
+            self._d.clear()
+            self._bytes = 0
+
+
+SPECTRA = SpectrumCache()
+
+
+def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
+    L = lib()
+    ny, nx = len(y), len(x)
+    lq = rs_logq(ny, nx)
+    P = 2 << lq
+    dev = device()
+    offx = torch.as_tensor(rs_wrapped_offsets(x, P), device=dev)
+    offy = torch.as_tensor(rs_wrapped_offsets(y, P), device=dev)
+    spec = torch.empty(P * P, dtype=torch.complex64, device=dev)
+    work = torch.empty(P * P, dtype=torch.complex64, device=dev)
+    dx = x[1] - x[0]
+    dy = y[1] - y[0]
+    scale = dx * dy / float(P * P)
+    _lib.check(L.xl_rs_transfer_spectrum(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(), float(z),
+                                         float(wavelength), scale, spec.data_ptr(), work.data_ptr()),
+               "xl_rs_transfer_spectrum")
+    return spec
+
+
+class RsCall:
+    """One prepared RS / VRS launch: arguments, outputs and the buffers they point at.
+
+    ``comps`` are complex64 CUDA tensors of shape (ny, nx) or (B, ny, nx);
+    ``z`` is a float or a sequence of B floats (one transfer spectrum per
+    distinct value, from the cache)."""
+
+    def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None):
+        L = lib()
+        x = as_grid(x)
+        y = as_grid(y)
+        ny, nx = len(y), len(x)
+        comps = [as_field(c) for c in comps]
+        lead = comps[0].shape[:-2]
+        if comps[0].shape[-2:] != (ny, nx):
+            raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid ({ny}, {nx})")
+        if len(comps) != (2 if vector else 1):
+            raise ValueError("RS takes one field, VRS takes (Ex, Ey)")
+        B = int(np.prod(lead)) if len(lead) else 1
+        zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
+        uniq = sorted(set(zs))
+        specs = [SPECTRA.get(x, y, zz, wavelength) for zz in uniq]
+        dev = comps[0].device
+        if len(specs) == 1:
+            spec, sidx, sstride = specs[0], None, 0
+        else:
+            spec = torch.stack(specs)
+            sstride = specs[0].numel()
+            sidx = torch.as_tensor([uniq.index(v) for v in zs], dtype=torch.int32, device=dev)
+        cout = 3 if vector else 1
+        if work is None:
+            work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
+        if outs is None:
+            outs = [torch.empty(comps[0].shape, dtype=torch.complex64, device=dev) for _ in range(cout)]
+        zt = torch.as_tensor(zs, dtype=torch.float64, device=dev) if vector else None
+        a = _lib.XlRsArgs()
+        a.batch = B
+        a.comps_in = len(comps)
+        a.comps_out = cout
+        a.ny, a.nx = ny, nx
+        for i, c in enumerate(comps):
+            a.inp[i] = c.data_ptr()
+        for i, o in enumerate(outs):
+            a.out[i] = o.data_ptr()
+        a.in_bstride = ny * nx
+        a.out_bstride = ny * nx
+        if vector:
+            a.x = device_grid(x).data_ptr()
+            a.y = device_grid(y).data_ptr()
+            a.z = zt.data_ptr()
+        a.spectrum = spec.data_ptr()
+        a.spectrum_stride = sstride
+        a.spectrum_index = _ptr(sidx)
+        a.work = work.data_ptr()
+        fill_prog(a.pre, pre, ny, nx)
+        fill_prog(a.post, post, ny, nx)
+        self.args = a
+        self.outs = outs
+        self.batch, self.ny, self.nx, self.comps = B, ny, nx, cout
+        self._keep = (comps, spec, sidx, work, zt, list(pre or ()), list(post or ()))
+
+    def run(self):
+        _lib.check(lib().xl_rs_propagate(stream_handle(), ctypes.byref(self.args)), "xl_rs_propagate")
+        return self.outs
+
+    def stage(self, s: int):
+        _lib.check(lib().xl_rs_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_rs_stage")
+
+
+def rs_propagate(comps, x, y, wavelength, z, vector: bool, pre=(), post=()):
+    """Scalar RS (comps = [field]) or VRS (comps = [Ex, Ey]); returns 1 or 3 tensors."""
+    return RsCall(comps, x, y, wavelength, z, vector, pre, post).run()
+
+
+# ---------------------------------------------------------------- sources --
+
+def _mesh64(x, y):
+    dev = device()
+    return torch.meshgrid(torch.as_tensor(x, device=dev), torch.as_tensor(y, device=dev), indexing="xy")
+
+
+def gaussian_field(x, y, wavelength, w0, E0=1.0, center=(0, 0), z_w0=(0, 0), alpha=0.0):
+    """wave_optics.py:468-523 evaluated on the device in float64, returned as complex64.
+    (The reference tests z_w0x for both radii of curvature, :503-510; kept.)"""
+    k = 2 * np.pi / wavelength
+    w0x, w0y = w0
+    x0, y0 = center
+    zx, zy = z_w0
+    Rlx = k * w0x ** 2 / 2
+    Rly = k * w0y ** 2 / 2
+    gx = np.arctan2(zx, Rlx)
+    gy = np.arctan2(zy, Rly)
+    wx = w0x * np.sqrt(1 + (zx / Rlx) ** 2)
+    wy = w0y * np.sqrt(1 + (zy / Rly) ** 2)
+    Rx = 1e12 if zx == 0 else zx * (1 + (Rlx / zx) ** 2)
+    Ry = 1e12 if zx == 0 else zy * (1 + (Rly / zy) ** 2)
+    X, Y = _mesh64(x, y)
+    xr = X * np.cos(alpha) + Y * np.sin(alpha)
+    yr = -X * np.sin(alpha) + Y * np.cos(alpha)
+    ph = -((k * zx + k * X ** 2 / (2 * Rx) - gx) + (k * zy + k * Y ** 2 / (2 * Ry) - gy))
+    amp = E0 * (w0x / wx) * (w0y / wy) * torch.exp(-(xr - x0) ** 2 / wx ** 2 - (yr - y0) ** 2 / wy ** 2)
+    return torch.polar(amp, ph).to(torch.complex64)
+
+
+def plane_wave_field(x, y, wavelength, A=1.0, theta=0.0, phi=0.0, z0=0.0):
+    """wave_optics.py:525-542 on the device (float64, returned as complex64)."""
+    k = 2 * np.pi / wavelength
+    X, Y = _mesh64(x, y)
+    ph = k * (X * np.sin(theta) * np.cos(phi) + Y * np.sin(theta) * np.sin(phi) + z0 * np.cos(theta))
+    return torch.polar(torch.full_like(ph, float(A)), ph).to(torch.complex64)
+
+
+# -------------------------------------------------------------------- CZT --
+
+def czt_grid(z, wavelength, xin, yin, xout, yout):
+    """wave_optics.py:299-331: Dm = lambda z / dx and the frequency limits."""
+    dx = xin[1] - xin[0]
+    dy = yin[1] - yin[0]
+    Dm = wavelength * z / dx
+    return dict(nx=len(xout), ny=len(yout), dx=dx, dy=dy, Dm=Dm,
+                fy1=yout[0] + Dm / 2, fy2=yout[-1] + Dm / 2,
+                fx1=xout[0] + Dm / 2, fx2=xout[-1] + Dm / 2)
+
+
+def czt_propagate(comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None):
+    raise NotImplementedError("chirp-z propagation kernels are not built yet")

@@ -1,0 +1,67 @@
+"""Loss functions of the optimisation tables (reference: xlumina/loss_functions.py)."""
+from __future__ import annotations
+
+import torch
+
+
+def _t(a):
+    return a if isinstance(a, torch.Tensor) else torch.as_tensor(a)
+
+
+def small_area_hybrid(detected_intensity):
+    """loss_functions.py:24-40: area above 0.7*max over the enclosed normalised intensity."""
+    I = _t(detected_intensity)
+    In = I / (torch.sum(I) + 1e-08)
+    mask = (In > 0.7 * torch.max(In)).to(In.dtype)
+    return torch.sum(mask) / (torch.sum(mask * In) + 1e-08)
+
+
+def vectorized_loss_hybrid(detected_intensities):
+    """loss_functions.py:42-50."""
+    return torch.stack([small_area_hybrid(i) for i in _t(detected_intensities)])
+
+
+def MSE_Intensity(input_light, target_light):
+    """loss_functions.py:137-149: sum((|a|^2 - |b|^2)^2) / num_pix."""
+    a, b = _t(input_light), _t(target_light)
+    n = a.shape[-1] * a.shape[-2]
+    return torch.sum((torch.abs(a) ** 2 - torch.abs(b) ** 2) ** 2, dim=(-2, -1)) / n
+
+
+def MSE_Amplitude(input_light, target_light):
+    """loss_functions.py:109-121."""
+    a, b = _t(input_light), _t(target_light)
+    n = a.shape[-1] * a.shape[-2]
+    return torch.sum((torch.abs(a) - torch.abs(b)) ** 2, dim=(-2, -1)) / n
+
+
+def MSE_Phase(input_light, target_light):
+    """loss_functions.py:123-135."""
+    a, b = _t(input_light), _t(target_light)
+    n = a.shape[-1] * a.shape[-2]
+    return torch.sum((torch.angle(a) - torch.angle(b)) ** 2, dim=(-2, -1)) / n
+
+
+def mean_batch_MSE_Intensity(optimized, target):
+    """loss_functions.py:52-59."""
+    mse = MSE_Intensity(optimized, target)
+    return torch.mean(mse), mse
+
+
+def _stack(light):
+    return torch.stack([light.Ex, light.Ey, light.Ez])
+
+
+def vMSE_Amplitude(input_light, target_light):
+    """loss_functions.py:61-75."""
+    return MSE_Amplitude(_stack(input_light), _stack(target_light))
+
+
+def vMSE_Phase(input_light, target_light):
+    """loss_functions.py:77-91."""
+    return MSE_Phase(_stack(input_light), _stack(target_light))
+
+
+def vMSE_Intensity(input_light, target_light):
+    """loss_functions.py:93-107."""
+    return MSE_Intensity(_stack(input_light), _stack(target_light))
