@@ -128,6 +128,20 @@ int xl_rs_propagate(void* stream, const XlRsArgs* args);
  * equals xl_rs_propagate. */
 int xl_rs_stage(void* stream, const XlRsArgs* args, int stage);
 
+/* Allocation-free variant of xl_rs_propagate, for callers that cannot call
+ * cudaMalloc (a host that reserves all device memory for its own pool, or a
+ * hardware-driving loop that cannot take cudaMalloc's implicit
+ * synchronisation).  No counterpart in the reference.  args->work is
+ * ignored: the workspace is a fixed device array of
+ * XL_RS_NOALLOC_MAX_WORK_BYTES inside the library, held on every GPU that
+ * loads it until exit.  Calls needing more scratch than that
+ * (xl_rs_work_bytes) fail with XL_EINVAL.  The first call on a device looks
+ * up the array's address (and uploads the twiddle tables if no other entry
+ * point has); make that first call before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU race. */
+#define XL_RS_NOALLOC_MAX_WORK_BYTES (64ull << 20)
+int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* args);
+
 /* ---- Elementwise ------------------------------------------------------ */
 
 /* Apply a Jones program to batch x comps planes (out may alias in). */

@@ -18,6 +18,7 @@ XL_ECUDA = -4
 XL_EUNSUPPORTED = -5
 XL_MAX_OPS = 8
 XL_MAX_SIDE = 4096
+XL_RS_NOALLOC_MAX_WORK_BYTES = 64 << 20
 
 OP_NONE, OP_PHASE, OP_SSLM, OP_SSLM_AMP, OP_LCD, OP_LP, OP_SEPMASK, OP_CMUL, OP_HIGHNA = range(9)
 
@@ -55,6 +56,7 @@ SIGNATURES = {
     "xl_rs_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_rs_propagate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
     "xl_rs_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs), ctypes.c_int]),
+    "xl_rs_propagate_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

@@ -22,6 +22,8 @@
 // column-major for the column pass: S[(col*2 + parity)*Q + k].
 #include <math.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -506,4 +508,74 @@ extern "C" int xl_rs_stage(void* stream, const XlRsArgs* a, int stage) {
     return XL_EINVAL;
   }
   return rs_run(stream, a, stage);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free RS / VRS.
+//
+// Some callers of this library cannot call cudaMalloc.  Two examples: a host
+// program that reserves all device memory for its own pool at start-up (a
+// later cudaMalloc fails or fragments the pool), and a loop that drives
+// optical hardware frame by frame, which cannot take the implicit device
+// synchronisation and unbounded latency that cudaMalloc / cudaFree can cause.
+// xl_rs_propagate_noalloc serves them.  It runs exactly the passes of
+// xl_rs_propagate, but its workspace is the fixed device array below, so the
+// caller passes only inputs (fields, transfer spectrum, coordinates) and
+// outputs, and the call allocates no device memory.
+//
+// The array holds XL_RS_NOALLOC_MAX_WORK_BYTES on every GPU that loads the
+// library, until the process exits.  All calls share it and it keeps the last
+// call's contents; nothing in it needs clearing, because the first pass writes
+// every element the later passes read.  Calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on the array.
+static __device__ __align__(256) float2 g_rs_noalloc_scratch[XL_RS_NOALLOC_MAX_WORK_BYTES / sizeof(float2)];
+
+static std::mutex g_noalloc_mu;
+static float2* g_noalloc_ptr[256];
+
+// Device address of the scratch array for the current device.  The array's
+// name in host code is only a stand-in for the symbol, so the address is
+// looked up once per device, with that device current.
+static int noalloc_scratch(float2** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= 256) {
+    set_error("xl_rs_propagate_noalloc: device index %d out of range", dev);
+    return XL_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_rs_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = (float2*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return XL_OK;
+}
+
+extern "C" int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* a) {
+  if (!a) {
+    set_error("xl_rs_propagate_noalloc: null args");
+    return XL_EINVAL;
+  }
+  const size_t need = xl_rs_work_bytes(a->batch, a->comps_out, a->ny, a->nx);
+  if (need == 0) {
+    set_error("xl_rs_propagate_noalloc: bad shape batch=%d comps_out=%d ny=%d nx=%d", a->batch,
+              a->comps_out, a->ny, a->nx);
+    return XL_EINVAL;
+  }
+  if (need > (size_t)XL_RS_NOALLOC_MAX_WORK_BYTES) {
+    set_error("xl_rs_propagate_noalloc: this call needs %zu bytes of scratch, the fixed limit is %llu "
+              "(e.g. one 1024x1024 VRS field or one 2048x2048 scalar field); use xl_rs_propagate with a "
+              "caller workspace for larger work",
+              need, (unsigned long long)XL_RS_NOALLOC_MAX_WORK_BYTES);
+    return XL_EINVAL;
+  }
+  float2* scratch = nullptr;
+  if (int rc = noalloc_scratch(&scratch)) return rc;
+  XlRsArgs b = *a;
+  b.work = scratch;
+  return rs_run(stream, &b, -1);
 }
