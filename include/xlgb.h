@@ -142,6 +142,52 @@ int xl_rs_stage(void* stream, const XlRsArgs* args, int stage);
 #define XL_RS_NOALLOC_MAX_WORK_BYTES (64ull << 20)
 int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* args);
 
+/* ---- Chirp-z (CZT / VCZT / high-NA focus) ----------------------------- */
+
+enum {
+  XL_CZT_SCALAR = 0,  /* CZT_jit, wave_optics.py:333-357: F * field -> B_y B_x -> F0 * cte */
+  XL_CZT_VECTOR = 1,  /* VCZT, vectorized_optics.py:321-384: Ez = (Ex X/r + Ey Y/r) z/r, then as scalar */
+  XL_CZT_PLAIN = 2    /* CZT_for_high_NA_jit, wave_optics.py:359-371: no transfer functions, * cte */
+};
+
+typedef struct {
+  int batch, comps_in, comps_out, mode;
+  int ny, nx;            /* input plane */
+  int my, mx;            /* output plane */
+  int log2_lx, log2_ly;  /* Bluestein lengths (>= nx + mx, >= ny + my) */
+  const void* in[3];
+  long long in_bstride;
+  void* out[3];
+  long long out_bstride;
+  const double* x;       /* device float64 coordinates: nx, ny, mx, my */
+  const double* y;
+  const double* xout;
+  const double* yout;
+  double z, wavelength;
+  double cte_re, cte_im; /* constant output factor */
+  /* complex64 chirp data per axis (wave_optics.py:385-460, float64 on the host):
+   * pre[n] = A^-n h[m-1+n] (m values); g = fft(1/h[:m+M], L) in parity-split
+   * order (even entries, then odd); post[l] = h[m-1+l] e^{-i 2 pi l_f (1/2 - m/2)/Dm} / L */
+  const void* pre_x;
+  const void* g_x;
+  const void* post_x;
+  const void* pre_y;
+  const void* g_y;
+  const void* post_y;
+  void* work;            /* >= xl_czt_work_bytes(batch, comps_out, ny, mx) */
+  XlProg pre;            /* fused before the first pass (masks, XL_OP_HIGHNA) */
+} XlCztArgs;
+
+size_t xl_czt_work_bytes(int batch, int comps, int ny, int mx);
+
+/* Chirp-z propagation: CZT (wave_optics.py:233-263), VCZT
+ * (vectorized_optics.py:321-361) and VCZT_objective_lens's focus
+ * (optical_elements.py:600-638 with XL_OP_HIGHNA in args->pre). */
+int xl_czt(void* stream, const XlCztArgs* args);
+
+/* One pass of xl_czt: 0 = prologue + x transform, 1 = y transform + epilogue. */
+int xl_czt_stage(void* stream, const XlCztArgs* args, int stage);
+
 /* ---- Elementwise ------------------------------------------------------ */
 
 /* Apply a Jones program to batch x comps planes (out may alias in). */

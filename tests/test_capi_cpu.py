@@ -93,3 +93,32 @@ def test_cuda_required_without_gpu():
     from xlumina_gb300 import wave_optics
     with pytest.raises(RuntimeError, match="CUDA"):
         wave_optics.ScalarLight(np.linspace(-1, 1, 8), np.linspace(-1, 1, 8), 0.5).field
+
+
+def test_bluestein_plan_matches_oracle_chirps():
+    from xlumina_gb300 import engine
+    for m, M, f1, f2, Dm in [(64, 48, -40.0, 40.0, 800.0), (2048, 1024, -1.0, 1.0, 3.4), (63, 3, 5.0, 6.0, 90.0)]:
+        L, pre, g, post = engine.bluestein_plan(m, f1, f2, Dm, M)
+        Lr, pre_r, g_r, post_r = ref.bluestein_vectors(m, f1, f2, Dm, M)
+        assert L == max(Lr, 32)
+        assert np.allclose(pre, pre_r, rtol=0, atol=1e-12)
+        assert np.allclose(post * L, post_r, rtol=0, atol=1e-12)
+        if L == Lr:
+            assert np.allclose(np.concatenate([g_r[0::2], g_r[1::2]]), g, rtol=0, atol=1e-9)
+
+
+def test_bluestein_rejects_power_of_two_window():
+    from xlumina_gb300 import engine
+    with pytest.raises(ValueError, match="power of two"):
+        engine.bluestein_plan(1024, -1.0, 1.0, 10.0, 1025)
+
+
+def test_czt_argument_errors(lib):
+    from xlumina_gb300 import _lib
+    a = _lib.XlCztArgs()
+    a.batch, a.comps_in, a.comps_out, a.mode, a.ny, a.nx, a.my, a.mx = 1, 2, 2, _lib.XL_CZT_VECTOR, 64, 64, 32, 32
+    assert lib.xl_czt(None, ctypes.byref(a)) == _lib.XL_EINVAL
+    a.comps_out = 3
+    a.log2_lx, a.log2_ly = 6, 7   # 64 < 64 + 32
+    assert lib.xl_czt(None, ctypes.byref(a)) == _lib.XL_EINVAL
+    assert b"Bluestein" in lib.xl_last_error()

@@ -43,6 +43,23 @@ class XlRsArgs(ctypes.Structure):
                 ("pre", XlProg), ("post", XlProg)]
 
 
+XL_CZT_SCALAR, XL_CZT_VECTOR, XL_CZT_PLAIN = 0, 1, 2
+
+
+class XlCztArgs(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("comps_in", ctypes.c_int), ("comps_out", ctypes.c_int),
+                ("mode", ctypes.c_int), ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("my", ctypes.c_int),
+                ("mx", ctypes.c_int), ("log2_lx", ctypes.c_int), ("log2_ly", ctypes.c_int),
+                ("inp", ctypes.c_void_p * 3), ("in_bstride", ctypes.c_longlong),
+                ("out", ctypes.c_void_p * 3), ("out_bstride", ctypes.c_longlong),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("xout", ctypes.c_void_p),
+                ("yout", ctypes.c_void_p), ("z", ctypes.c_double), ("wavelength", ctypes.c_double),
+                ("cte_re", ctypes.c_double), ("cte_im", ctypes.c_double),
+                ("pre_x", ctypes.c_void_p), ("g_x", ctypes.c_void_p), ("post_x", ctypes.c_void_p),
+                ("pre_y", ctypes.c_void_p), ("g_y", ctypes.c_void_p), ("post_y", ctypes.c_void_p),
+                ("work", ctypes.c_void_p), ("pre", XlProg)]
+
+
 # name -> (restype, argtypes); every symbol include/xlgb.h declares.
 SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
@@ -57,6 +74,9 @@ SIGNATURES = {
     "xl_rs_propagate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
     "xl_rs_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs), ctypes.c_int]),
     "xl_rs_propagate_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
+    "xl_czt_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "xl_czt": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs)]),
+    "xl_czt_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs), ctypes.c_int]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

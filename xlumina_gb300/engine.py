@@ -433,5 +433,118 @@ def czt_grid(z, wavelength, xin, yin, xout, yout):
                 fx1=xout[0] + Dm / 2, fx2=xout[-1] + Dm / 2)
 
 
+def bluestein_plan(m, f1, f2, Dm, M):
+    """Chirp data of wave_optics.py:385-460 for an m-point input and M outputs, float64.
+
+    Returns (L, pre, g_split, post): L the transform length; pre[n] = A^-n
+    h[m-1+n]; g = fft(1/h[:m+M], L) reordered even entries then odd entries;
+    post[l] = h[m-1+l] exp(-i 2 pi l_f (1/2 - m/2) / Dm) / L, where
+    h[q] = W^((q-m+1)^2/2) with the complex power's principal branch.
+    """
+    if M < 2:
+        raise ValueError("chirp-z needs at least 2 output samples per axis")
+    D1 = f1 + (M * Dm + f2 - f1) / (2 * M)
+    D2 = f2 + (M * Dm + f2 - f1) / (2 * M)
+    mp = m + M - 1
+    L = int(2 ** int(np.ceil(np.log2(mp))))
+    if L == mp:
+        raise ValueError(f"m + M - 1 = {mp} is a power of two: the reference's Bluestein output slice "
+                         "(wave_optics.py:446) is one sample short for this size")
+    A = np.exp(1j * 2 * np.pi * D1 / Dm)
+    W = np.exp(-1j * 2 * np.pi * (D2 - D1) / (M * Dm))
+    q = np.arange(-m + 1, max(M - 1, m - 1) + 1)
+    h = W ** (q ** 2 / 2)
+    Lk = max(L, 32)
+    g = np.fft.fft(1 / h[:mp + 1], Lk)
+    pre = A ** (-np.arange(m)) * h[m - 1:2 * m - 1]
+    lf = np.linspace(0, M - 1, M) / M * (D2 - D1) + D1
+    post = h[m - 1:mp] * np.exp(-1j * 2 * np.pi * lf * (-m / 2 + 0.5) / Dm) / Lk
+    return Lk, pre, np.concatenate([g[0::2], g[1::2]]), post
+
+
+_chirp_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def device_chirps(m, f1, f2, Dm, M):
+    key = (int(m), float(f1), float(f2), float(Dm), int(M), torch.cuda.current_device())
+    with _LOCK:
+        v = _chirp_cache.get(key)
+        if v is not None:
+            _chirp_cache.move_to_end(key)
+            return v
+    L, pre, g, post = bluestein_plan(m, f1, f2, Dm, M)
+    dev = device()
+    v = (L,) + tuple(torch.as_tensor(a, device=dev).to(torch.complex64) for a in (pre, g, post))
+    with _LOCK:
+        _chirp_cache[key] = v
+        while len(_chirp_cache) > 64:
+            _chirp_cache.popitem(last=False)
+    return v
+
+
+class CztCall:
+    """One prepared chirp-z launch (scalar CZT, VCZT, or the high-NA focus).
+
+    mode "scalar": wave_optics.py:233-263; "vczt": vectorized_optics.py:321-361;
+    "high_na": optical_elements.py:600-638 (the lens op must be in ``pre``,
+    ``lens`` = (radius, f, sin_theta_max))."""
+
+    def __init__(self, comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None, outs=None):
+        L = lib()
+        x, y, xout, yout = (as_grid(a) for a in (x, y, xout, yout))
+        ny, nx, my, mx = len(y), len(x), len(yout), len(xout)
+        comps = [as_field(c) for c in comps]
+        if comps[0].shape[-2:] != (ny, nx):
+            raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid ({ny}, {nx})")
+        lead = comps[0].shape[:-2]
+        B = int(np.prod(lead)) if len(lead) else 1
+        dev = comps[0].device
+        if mode == "high_na":
+            r, f, s_max = lens
+            Dm = f * wavelength * (nx - 1) / (2 * r)
+            cmode, cin, cout = _lib.XL_CZT_PLAIN, len(comps), 3
+            cte = -(1j * s_max ** 2 / (f * wavelength))
+            zz = 0.0
+        else:
+            Dm = wavelength * z / (x[1] - x[0])
+            cmode = _lib.XL_CZT_SCALAR if mode == "scalar" else _lib.XL_CZT_VECTOR
+            cin, cout = (1, 1) if mode == "scalar" else (2, 3)
+            cte = z * (x[1] - x[0]) * (y[1] - y[0]) * wavelength
+            zz = float(z)
+        Lx, prex, gx, postx = device_chirps(nx, xout[0] + Dm / 2, xout[-1] + Dm / 2, Dm, mx)
+        Ly, prey, gy, posty = device_chirps(ny, yout[0] + Dm / 2, yout[-1] + Dm / 2, Dm, my)
+        work = torch.empty(L.xl_czt_work_bytes(B, cout, ny, mx) // 8, dtype=torch.complex64, device=dev)
+        if outs is None:
+            outs = [torch.empty(tuple(lead) + (my, mx), dtype=torch.complex64, device=dev) for _ in range(cout)]
+        a = _lib.XlCztArgs()
+        a.batch, a.comps_in, a.comps_out, a.mode = B, cin, cout, cmode
+        a.ny, a.nx, a.my, a.mx = ny, nx, my, mx
+        a.log2_lx, a.log2_ly = int(Lx).bit_length() - 1, int(Ly).bit_length() - 1
+        for i, c in enumerate(comps):
+            a.inp[i] = c.data_ptr()
+        for i, o in enumerate(outs):
+            a.out[i] = o.data_ptr()
+        a.in_bstride, a.out_bstride = ny * nx, my * mx
+        gx_, gy_, gxo, gyo = (device_grid(v) for v in (x, y, xout, yout))
+        a.x, a.y, a.xout, a.yout = gx_.data_ptr(), gy_.data_ptr(), gxo.data_ptr(), gyo.data_ptr()
+        a.z, a.wavelength = zz, float(wavelength)
+        a.cte_re, a.cte_im = complex(cte).real, complex(cte).imag
+        a.pre_x, a.g_x, a.post_x = prex.data_ptr(), gx.data_ptr(), postx.data_ptr()
+        a.pre_y, a.g_y, a.post_y = prey.data_ptr(), gy.data_ptr(), posty.data_ptr()
+        a.work = work.data_ptr()
+        fill_prog(a.pre, pre, ny, nx)
+        self.args = a
+        self.outs = outs
+        self._keep = (comps, work, prex, gx, postx, prey, gy, posty, gx_, gy_, gxo, gyo, list(pre or ()))
+
+    def run(self):
+        _lib.check(lib().xl_czt(stream_handle(), ctypes.byref(self.args)), "xl_czt")
+        return self.outs
+
+    def stage(self, s: int):
+        _lib.check(lib().xl_czt_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_czt_stage")
+
+
 def czt_propagate(comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None):
-    raise NotImplementedError("chirp-z propagation kernels are not built yet")
+    """Scalar CZT, VCZT or the high-NA focus; returns 1 or 3 output tensors."""
+    return CztCall(comps, x, y, wavelength, z, xout, yout, mode, pre, lens).run()
