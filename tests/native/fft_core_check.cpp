@@ -19,6 +19,18 @@ static void emu(std::vector<Regs>& V, float2* sm, const float2* tw) {
   }
 }
 
+template <int LOGN, int DIR, int P>
+static void emu_s(std::vector<Regs>& V, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN>;
+  for (int j = 0; j < S::T; ++j) fft_pass_s<LOGN, P, DIR>(V[j].v, j, sm, stw);
+  if constexpr (P < S::NPASS - 1) {
+    for (int j = 0; j < S::T; ++j) fft_gather<LOGN>(V[j].v, j, sm);
+    emu_s<LOGN, DIR, P + 1>(V, sm, stw);
+  }
+}
+
+static int g_use_stw = 0;
+
 template <int LOGN, int DIR>
 static void run(const float* in, float* out) {
   using S = FftShape<LOGN>;
@@ -33,7 +45,13 @@ static void run(const float* in, float* out) {
       int n = j + m * S::T;
       V[j].v[m] = make_float2(in[2 * n], in[2 * n + 1]);
     }
-  emu<LOGN, DIR, 0>(V, sm.data(), tw.data());
+  if (g_use_stw) {
+    std::vector<float2> stw(FftTw<LOGN>::SIZE);
+    for (int i = 0; i < FftTw<LOGN>::SIZE; ++i) stw[i] = pass_twiddle_entry<LOGN>(i, tw.data());
+    emu_s<LOGN, DIR, 0>(V, sm.data(), stw.data());
+  } else {
+    emu<LOGN, DIR, 0>(V, sm.data(), tw.data());
+  }
   for (int j = 0; j < S::T; ++j)
     for (int m = 0; m < 16; ++m) {
       int n = j + m * S::T;
@@ -57,6 +75,13 @@ static int dispatch(int logn, const float* in, float* out) {
     case 13: run<13, DIR>(in, out); return 0;
   }
   return -1;
+}
+
+extern "C" int fft_core_check_stw(int logn, int dir, const float* in, float* out) {
+  g_use_stw = 1;
+  int rc = dir < 0 ? dispatch<-1>(logn, in, out) : dispatch<1>(logn, in, out);
+  g_use_stw = 0;
+  return rc;
 }
 
 extern "C" int fft_core_check(int logn, int dir, const float* in, float* out) {

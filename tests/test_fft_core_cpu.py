@@ -16,17 +16,20 @@ def fftlib(tmp_path_factory):
     subprocess.check_call(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", src, "-o", str(out)])
     lib = ctypes.CDLL(str(out))
     lib.fft_core_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.fft_core_check_stw.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     return lib
 
 
 @pytest.mark.parametrize("logn", range(4, 14))
 @pytest.mark.parametrize("direction", [-1, 1])
-def test_block_fft_matches_numpy(fftlib, logn, direction):
+@pytest.mark.parametrize("tables", ["global", "shared"])
+def test_block_fft_matches_numpy(fftlib, logn, direction, tables):
     n = 1 << logn
     rng = np.random.default_rng(logn * 7 + (direction > 0))
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
     out = np.empty_like(x)
-    assert fftlib.fft_core_check(logn, direction, x.ctypes.data, out.ctypes.data) == 0
+    fn = fftlib.fft_core_check if tables == "global" else fftlib.fft_core_check_stw
+    assert fn(logn, direction, x.ctypes.data, out.ctypes.data) == 0
     ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
     err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
     assert err < 2e-7 * logn, err

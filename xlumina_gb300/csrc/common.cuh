@@ -83,9 +83,11 @@ __device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const P
     }
     case XL_OP_LCD: {  // general retarder with delta = 0 (eta, theta); Ez unchanged
       float sh, ch, s2, c2;
-      sincosf(0.5f * op_param(op, 0, px), &sh, &ch);
       float st, ct;
-      sincosf(op_param(op, 1, px), &st, &ct);
+      if (op.pmask & 1) sincosf(0.5f * op_param(op, 0, px), &sh, &ch);
+      else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
+      if (op.pmask & 2) sincosf(op_param(op, 1, px), &st, &ct);
+      else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
       // a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2)
       c2 = ct * ct - st * st;
       s2 = 2.f * st * ct;
@@ -99,7 +101,8 @@ __device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const P
     }
     case XL_OP_LP: {  // linear polarizer at alpha; Ez set to zero
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
+      if (op.pmask & 1) sincosf(op_param(op, 0, px), &s, &c);
+      else { c = op.sval[2]; s = op.sval[3]; }   // scalar alpha: cos, sin from the host
       const float2 x = e[0], y = e[1];
       e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
       e[1] = cadd(cscale(x, c * s), cscale(y, s * s));

@@ -21,12 +21,16 @@ __global__ void apply_ops_kernel(const ElemLaunch p) {
        i += (long long)gridDim.x * blockDim.x) {
     float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     const long long off = (long long)b * p.ibs + i;
-    for (int c = 0; c < p.C; ++c) e[c] = p.in[c][off];
+    e[0] = p.in[0][off];
+    if (p.C > 1) e[1] = p.in[1][off];
+    if (p.C > 2) e[2] = p.in[2][off];
     const int row = (int)(i / p.nx), col = (int)(i % p.nx);
     PixelCtx px{row, col, i, b};
     apply_prog(p.prog, e, px);
     const long long o = (long long)b * p.obs + i;
-    for (int c = 0; c < p.C; ++c) p.out[c][o] = e[c];
+    p.out[0][o] = e[0];
+    if (p.C > 1) p.out[1][o] = e[1];
+    if (p.C > 2) p.out[2][o] = e[2];
   }
 }
 

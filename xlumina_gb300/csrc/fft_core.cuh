@@ -154,6 +154,12 @@ template <int LOGN> struct FftShape {
   static constexpr int NPASS = NFULL + (REM ? 1 : 0);
   static constexpr int SMEM = N + N / 16;  // padded float2 slots per exchange buffer
   template <int P> static constexpr int radix() { return P < NFULL ? 16 : (1 << REM); }
+  static constexpr int radix_rt(int P) { return P < NFULL ? 16 : (1 << REM); }
+  static constexpr int stride_rt(int P) {
+    int ns = 1;
+    for (int q = 0; q < P; ++q) ns *= (q < NFULL ? 16 : (1 << REM));
+    return ns;
+  }
   template <int P> static constexpr int stride() {
     int ns = 1;
     for (int q = 0; q < P; ++q) ns *= (q < NFULL ? 16 : (1 << REM));
@@ -204,7 +210,85 @@ template <int LOGN> XL_HD void fft_gather(float2 (&v)[16], int j, const float2* 
   for (int m = 0; m < 16; ++m) v[m] = sm[smpad(j + m * S::T)];
 }
 
+// ---- per-pass twiddle tables (shared memory) ----
+// Pass P >= 1 (radix R, stride NS) keeps e^{-2 pi i (i k) / (NS R)} at
+// [off<P>() + (i-1) NS + k], i = 1..R-1, k = 0..NS-1: consecutive threads
+// (consecutive k) read consecutive slots, so the reads are conflict-free.
+template <int LOGN> struct FftTw {
+  using S = FftShape<LOGN>;
+  template <int P> static constexpr int off() {
+    int o = 0;
+    for (int q = 1; q < P; ++q) o += (S::radix_rt(q) - 1) * S::stride_rt(q);
+    return o;
+  }
+  static constexpr int SIZE = off<S::NPASS>() > 0 ? off<S::NPASS>() : 1;
+};
+
+// Fill one slot of the pass tables from the size-N table twN[q] = e^{-2 pi i q/N}.
+template <int LOGN> XL_HD float2 pass_twiddle_entry(int idx, const float2* twN) {
+  using S = FftShape<LOGN>;
+  int base = 0;
+  for (int q = 1; q < S::NPASS; ++q) {
+    const int R = S::radix_rt(q), NS = S::stride_rt(q);
+    const int sz = (R - 1) * NS;
+    if (idx < base + sz) {
+      const int i = (idx - base) / NS + 1, k = (idx - base) % NS;
+      return twN[i * k * (S::N / (NS * R))];
+    }
+    base += sz;
+  }
+  return make_float2(1.f, 0.f);
+}
+
+// Stockham pass with twiddles from the shared pass tables.
+template <int LOGN, int P, int DIR>
+XL_HD void fft_pass_s(float2 (&v)[16], int j, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN>;
+  constexpr int R = S::template radix<P>();
+  constexpr int NS = S::template stride<P>();
+  constexpr bool LAST = (P == S::NPASS - 1);
+  constexpr int BPT = 16 / R;
+  constexpr int OFF = FftTw<LOGN>::template off<P>();
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = j + t * S::T;
+    const int k = b & (NS - 1);
+    float2 x[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) x[i] = v[t + i * BPT];
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int i = 1; i < R; ++i) {
+        const float2 w = stw[OFF + (i - 1) * NS + k];
+        x[i] = DIR < 0 ? cmul(x[i], w) : cmulc(x[i], w);
+      }
+    }
+    dftR<R, DIR>(x);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[t + i * BPT] = x[i];
+    } else {
+      const int base = (b / NS) * (NS * R) + k;
+#pragma unroll
+      for (int i = 0; i < R; ++i) sm[smpad(base + i * NS)] = x[i];
+    }
+  }
+}
+
 #if defined(__CUDACC__)
+// Whole FFT for a thread group, twiddles from the shared pass tables.
+template <int LOGN, int DIR, int P = 0>
+__device__ __forceinline__ void block_fft_s(float2 (&v)[16], int j, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN>;
+  fft_pass_s<LOGN, P, DIR>(v, j, sm, stw);
+  if constexpr (P < S::NPASS - 1) {
+    __syncthreads();
+    fft_gather<LOGN>(v, j, sm);
+    __syncthreads();
+    block_fft_s<LOGN, DIR, P + 1>(v, j, sm, stw);
+  }
+}
+
 // Whole FFT for a thread group.  Every thread of the CTA must call this the
 // same number of times (it uses __syncthreads between passes).
 template <int LOGN, int DIR, int P = 0>

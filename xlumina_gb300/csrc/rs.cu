@@ -34,33 +34,59 @@ template <int LOGQ> struct RsCfg {
   static constexpr int Q = S::N;
   static constexpr int P = 2 * Q;
   static constexpr int T = S::T;
-  static constexpr int XS = S::SMEM;  // exchange buffer slots
-  static constexpr int RPC = (256 / (2 * T)) > 1 ? (256 / (2 * T)) : 1;  // rows per CTA
-  static constexpr int WC = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));  // conv tile width
-  static constexpr int WH = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));   // spectrum-build tile
-  static constexpr int ROW_THREADS = 2 * RPC * T;
-  static constexpr int CONV_THREADS = 2 * WC * T;
+  static constexpr int XS = S::SMEM;            // exchange buffer slots
+  static constexpr int TW = FftTw<LOGQ>::SIZE;  // pass-twiddle slots
+  // Column-block width of the blocked intermediate and spectrum layouts:
+  // element (row r, column col) of a plane with ny rows lives at
+  // ((col / W) * ny + r) * W + col % W, so W adjacent columns of one row are
+  // contiguous and a column tile is one contiguous block.
+  static constexpr int W = LOGQ >= 12 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
+  static constexpr int RPC = (128 / T) > 1 ? (128 / T) : 1;  // rows per CTA, one group per row
+  static constexpr int ROW_THREADS = RPC * T;
+  static constexpr int CONV_THREADS = W * T;
+  // per-group padding of the column-pass shared buffers: with W groups
+  // interleaved in every warp, unpadded buffers would start on the same bank
+  static constexpr int CPAD = W >= 8 ? 0 : 4;
+  static constexpr int CXS = XS + CPAD;
+  static constexpr int CYS = Q + CPAD;
+  // one-time spectrum build
+  static constexpr int HRPC = (256 / (2 * T)) > 1 ? (256 / (2 * T)) : 1;
+  static constexpr int HROW_THREADS = 2 * HRPC * T;
+  static constexpr int WH = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));
   static constexpr int HCOL_THREADS = 2 * WH * T;
 };
 
+template <int LOGQ>
+__device__ __forceinline__ long long blk(int r, int col, int ny) {
+  constexpr int W = RsCfg<LOGQ>::W;
+  return ((long long)(col / W) * ny + r) * W + (col % W);
+}
+
+template <int LOGQ>
+__device__ __forceinline__ void fill_pass_twiddles(float2* stw) {
+  const float2* twQ = tw_table(LOGQ);
+  for (int idx = threadIdx.x; idx < RsCfg<LOGQ>::TW; idx += blockDim.x)
+    stw[idx] = pass_twiddle_entry<LOGQ>(idx, twQ);
+}
+
 // ---------------------------------------------------------------------------
 // Transfer spectrum, step 1: rows of the wrapped impulse response -> P-point
-// row spectra, written in parity-split order (even frequencies, then odd).
+// row spectra, written row-major in parity-split order (even, then odd).
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_hhat_rows(int ny, int nx, const double* __restrict__ offx,
-                             const double* __restrict__ offy, double z, double inv_lambda, float k,
-                             float2* __restrict__ out) {
+__global__ void __launch_bounds__(RsCfg<LOGQ>::HROW_THREADS)
+    rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double z,
+                 double inv_lambda, float k, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
-  float2* row = smem;                         // RPC x P
-  float2* xch = smem + C::RPC * C::P;         // 2 RPC x XS
+  float2* row = smem;                         // HRPC x P
+  float2* xch = smem + C::HRPC * C::P;        // 2 HRPC x XS
   const int tid = threadIdx.x;
   const int slot = tid / (2 * C::T);
   const int par = (tid / C::T) & 1;
   const int j = tid % C::T;
-  const int i0 = blockIdx.x * C::RPC;
+  const int i0 = blockIdx.x * C::HRPC;
 
-  for (int idx = tid; idx < C::RPC * C::P; idx += blockDim.x) {
+  for (int idx = tid; idx < C::HRPC * C::P; idx += blockDim.x) {
     const int s = idx / C::P, col = idx % C::P, i = i0 + s;
     const bool vy = (i < ny) || (i > C::P - ny);
     const bool vx = (col < nx) || (col > C::P - nx);
@@ -89,22 +115,24 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_hhat_rows(int ny,
 }
 
 // Transfer spectrum, step 2: P-point column transforms of the row spectra,
-// stored column-major in parity-split order, times `scale`.
+// times `scale`, stored in the blocked spectrum layout
+// S[((tile*2 + parity)*Q + k)*W + w] for spectrum column tile*W + w.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS) rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
+__global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS)
+    rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
-  constexpr int W = C::WH, PITCH = C::WH + 1;
+  constexpr int WH = C::WH, PITCH = C::WH + 1;
   extern __shared__ float2 smem[];
   float2* tile = smem;                  // P x PITCH
-  float2* xch = smem + C::P * PITCH;    // 2W x XS
+  float2* xch = smem + C::P * PITCH;    // 2 WH x XS
   const int tid = threadIdx.x;
   const int w = tid / (2 * C::T);
   const int par = (tid / C::T) & 1;
   const int j = tid % C::T;
-  const int c0 = blockIdx.x * W;
+  const int c0 = blockIdx.x * WH;
 
-  for (int idx = tid; idx < C::P * W; idx += blockDim.x) {
-    const int r = idx / W, ww = idx % W;
+  for (int idx = tid; idx < C::P * WH; idx += blockDim.x) {
+    const int r = idx / WH, ww = idx % WH;
     tile[r * PITCH + ww] = in[(long long)r * C::P + c0 + ww];
   }
   __syncthreads();
@@ -118,9 +146,10 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS) rs_hhat_cols(const 
     v[m] = par ? cmul(csub(a, b), twP[n]) : cadd(a, b);
   }
   block_fft<LOGQ, -1>(v, j, xch + (2 * w + par) * C::XS, twQ);
-  float2* dst = out + ((long long)(c0 + w) * 2 + par) * C::Q;
+  const int col = c0 + w;
+  float2* dst = out + ((long long)(col / C::W) * 2 + par) * C::Q * C::W + (col % C::W);
 #pragma unroll
-  for (int m = 0; m < 16; ++m) dst[j + m * C::T] = cscale(v[m], scale);
+  for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * C::W] = cscale(v[m], scale);
 }
 
 // ---------------------------------------------------------------------------
@@ -140,21 +169,24 @@ struct RsLaunch {
   XlProg pre, post;
 };
 
-// Row pass: prologue (Jones program, VRS Ez) + parity-split row spectra.
+// Row pass: prologue (Jones program; VRS Ez derived at load) and, per
+// component, the even- and odd-frequency Q-point row spectra, stored in the
+// blocked layout.  One thread group per row.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_rows_fwd(const RsLaunch p) {
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::ROW_THREADS)
+    rs_rows_fwd(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
-  const int nc = p.cout;
-  float2* stage = smem;                          // RPC x nc x Q
-  float2* xch = smem + C::RPC * nc * C::Q;       // 2 RPC x XS
+  const int ns = p.cin;                            // staged components
+  float2* stage = smem;                            // RPC x ns x nx
+  float2* xch = stage + C::RPC * ns * p.nx;        // RPC x XS
+  float2* stw = xch + C::RPC * C::XS;              // TW
   const int tid = threadIdx.x;
-  const int slot = tid / (2 * C::T);
-  const int par = (tid / C::T) & 1;
+  const int slot = tid / C::T;
   const int j = tid % C::T;
   const int b = blockIdx.y;
   const int r0 = blockIdx.x * C::RPC;
-  const float zb = p.z ? (float)p.z[b] : 0.f;
+  fill_pass_twiddles<LOGQ>(stw);
 
   for (int idx = tid; idx < C::RPC * p.nx; idx += blockDim.x) {
     const int s = idx / p.nx, n = idx % p.nx, r = r0 + s;
@@ -166,159 +198,166 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_rows_fwd(const Rs
     e[2] = make_float2(0.f, 0.f);
     PixelCtx px{r, n, (long long)r * p.nx + n, b};
     apply_prog(p.pre, e, px);
-    if (nc == 3) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
-      const float X = (float)p.x[n], Y = (float)p.y[r];
-      const float rr = sqrtf(X * X + Y * Y + zb * zb);
-      e[2] = cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr));
-    }
-    for (int c = 0; c < nc; ++c) stage[(s * nc + c) * C::Q + n] = e[c];
+    stage[(s * ns) * p.nx + n] = e[0];
+    if (ns > 1) stage[(s * ns + 1) * p.nx + n] = e[1];
   }
   __syncthreads();
 
-  const float2* twQ = tw_table(LOGQ);
   const float2* twP = tw_table(LOGQ + 1);
   const int r = r0 + slot;
-  for (int c = 0; c < nc; ++c) {
-    float2 v[16];
-    const float2* src = stage + (slot * nc + c) * C::Q;
+  const bool live = r < p.ny;
+  const float zb = p.z ? (float)p.z[b] : 0.f;
+  const float Y = (live && p.cout == 3) ? (float)p.y[r] : 0.f;
+  const float2* st = stage + slot * ns * p.nx;
+  float2* xb = xch + slot * C::XS;
+  for (int c = 0; c < p.cout; ++c) {
+    float2* plane = p.work + ((long long)b * p.cout + c) * p.ny * C::P;
+    for (int par = 0; par < 2; ++par) {
+      float2 v[16];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      const int n = j + m * C::T;
-      float2 a = (n < p.nx && r < p.ny) ? src[n] : make_float2(0.f, 0.f);
-      v[m] = par ? cmul(a, twP[n]) : a;
-    }
-    block_fft<LOGQ, -1>(v, j, xch + (2 * slot + par) * C::XS, twQ);
-    if (r < p.ny) {
-      float2* dst = p.work + (((long long)b * nc + c) * p.ny + r) * C::P + par * C::Q;
+      for (int m = 0; m < 16; ++m) {
+        const int n = j + m * C::T;
+        float2 a = make_float2(0.f, 0.f);
+        if (live && n < p.nx) {
+          if (c < ns) {
+            a = st[c * p.nx + n];
+          } else {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
+            const float X = (float)p.x[n];
+            const float inv = rsqrtf(X * X + Y * Y + zb * zb);
+            a = cadd(cscale(st[n], X * inv), cscale(st[p.nx + n], Y * inv));
+          }
+        }
+        v[m] = par ? cmul(a, twP[n]) : a;
+      }
+      block_fft_s<LOGQ, -1>(v, j, xb, stw);
+      if (live) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) dst[j + m * C::T] = v[m];
+        for (int m = 0; m < 16; ++m) plane[blk<LOGQ>(r, par * C::Q + j + m * C::T, p.ny)] = v[m];
+      }
     }
   }
 }
 
-// Column pass: y-split spectra, times the transfer spectrum, inverse, crop.
+// Column pass, in place on one tile of W spectrum columns: for each column,
+// even chain FFT -> x S_even -> IFFT and odd chain (pre-twiddled) likewise,
+// combined in registers; only the ny rows that survive the crop are kept.
+// Lanes interleave the W columns so every warp access is 256 contiguous bytes.
 template <int LOGQ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
-  constexpr int W = C::WC, PITCH = C::WC + 1;
+  constexpr int W = C::W, LPW = 32 / W;
   extern __shared__ float2 smem[];
-  float2* tile = smem;                   // Q x PITCH
-  float2* xch = smem + C::Q * PITCH;     // 2W x XS
+  float2* xch = smem;                // W x CXS
+  float2* stw = smem + W * C::CXS;   // TW
+  float2* yb = stw + C::TW;          // W x CYS: even-chain result, held across the odd chain
   const int tid = threadIdx.x;
-  const int w = tid / (2 * C::T);
-  const int par = (tid / C::T) & 1;
-  const int j = tid % C::T;
+  const int lane = tid & 31;
+  const int w = lane % W;
+  const int j = (tid >> 5) * LPW + lane / W;
+  const int t = blockIdx.x;
   const int b = blockIdx.y;
-  const int c0 = blockIdx.x * W;
-  const int col = c0 + w;
-  const int nc = p.cout;
-  const float2* twQ = tw_table(LOGQ);
+  fill_pass_twiddles<LOGQ>(stw);
+  __syncthreads();
   const float2* twP = tw_table(LOGQ + 1);
-  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride +
-                       ((long long)col * 2 + par) * C::Q;
+  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * 2 * C::Q * W + w;
+  float2* xb = xch + w * C::CXS;
+  float2* y0 = yb + w * C::CYS;
 
-  for (int c = 0; c < nc; ++c) {
-    float2* plane = p.work + ((long long)b * nc + c) * p.ny * C::P;
-    for (int idx = tid; idx < p.ny * W; idx += blockDim.x) {
-      const int r = idx / W, ww = idx % W;
-      tile[r * PITCH + ww] = plane[(long long)r * C::P + c0 + ww];
-    }
-    __syncthreads();
-    float2 v[16];
+  for (int c = 0; c < p.cout; ++c) {
+    float2* tileA = p.work + ((long long)b * p.cout + c) * p.ny * C::P + (long long)t * p.ny * W + w;
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      const int n = j + m * C::T;
-      const float2 a = n < p.ny ? tile[n * PITCH + w] : make_float2(0.f, 0.f);
-      v[m] = par ? cmul(a, twP[n]) : a;
-    }
-    float2* xb = xch + (2 * w + par) * C::XS;
-    block_fft<LOGQ, -1>(v, j, xb, twQ);
-#pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], spec[j + m * C::T]);
-    block_fft<LOGQ, 1>(v, j, xb, twQ);
-    if (par) {
+    for (int par = 0; par < 2; ++par) {
+      float2 v[16];
 #pragma unroll
       for (int m = 0; m < 16; ++m) {
         const int n = j + m * C::T;
-        xb[smpad(n)] = cmulc(v[m], twP[n]);
+        const float2 a = n < p.ny ? tileA[(long long)n * W] : make_float2(0.f, 0.f);
+        v[m] = par ? cmul(a, twP[n]) : a;
       }
-    }
-    __syncthreads();
-    if (!par) {
-      const float2* xo = xch + (2 * w + 1) * C::XS;
+      block_fft_s<LOGQ, -1>(v, j, xb, stw);
+      const float2* sp = spec + (long long)par * C::Q * W;
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
-        const int n = j + m * C::T;
-        if (n < p.ny) tile[n * PITCH + w] = cadd(v[m], xo[smpad(n)]);
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], sp[(long long)(j + m * C::T) * W]);
+      block_fft_s<LOGQ, 1>(v, j, xb, stw);
+      if (par == 0) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) y0[j + m * C::T] = v[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          const int n = j + m * C::T;
+          if (n < p.ny) tileA[(long long)n * W] = cadd(y0[n], cmulc(v[m], twP[n]));
+        }
       }
     }
-    __syncthreads();
-    for (int idx = tid; idx < p.ny * W; idx += blockDim.x) {
-      const int r = idx / W, ww = idx % W;
-      plane[(long long)r * C::P + c0 + ww] = tile[r * PITCH + ww];
-    }
-    __syncthreads();
   }
 }
 
-// Inverse row pass: x-split inverse, crop to nx columns, epilogue, store.
+// Inverse row pass: inverse of both parity halves, combined in registers,
+// cropped to nx columns; optional fused epilogue program; store.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS) rs_rows_inv(const RsLaunch p) {
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::ROW_THREADS)
+    rs_rows_inv(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
   const int nc = p.cout;
-  float2* xch = smem;                              // 2 RPC x XS
-  float2* stage = smem + 2 * C::RPC * C::XS;       // RPC x nc x Q (epilogue only)
   const bool epi = p.post.nops > 0;
+  float2* xch = smem;                           // RPC x XS
+  float2* stw = xch + C::RPC * C::XS;           // TW
+  float2* yb = stw + C::TW;                     // RPC x Q: even-half result
+  float2* stage = yb + C::RPC * C::Q;           // RPC x nc x nx (epilogue only)
   const int tid = threadIdx.x;
-  const int slot = tid / (2 * C::T);
-  const int par = (tid / C::T) & 1;
+  const int slot = tid / C::T;
   const int j = tid % C::T;
   const int b = blockIdx.y;
   const int r0 = blockIdx.x * C::RPC;
   const int r = r0 + slot;
-  const float2* twQ = tw_table(LOGQ);
+  const bool live = r < p.ny;
+  const int rr = live ? r : 0;
+  fill_pass_twiddles<LOGQ>(stw);
+  __syncthreads();
   const float2* twP = tw_table(LOGQ + 1);
+  float2* xb = xch + slot * C::XS;
+  float2* y0 = yb + slot * C::Q;
 
   for (int c = 0; c < nc; ++c) {
-    float2 v[16];
-    const float2* src = p.work + (((long long)b * nc + c) * p.ny + (r < p.ny ? r : 0)) * C::P +
-                        par * C::Q;
+    const float2* plane = p.work + ((long long)b * nc + c) * p.ny * C::P;
 #pragma unroll
-    for (int m = 0; m < 16; ++m) v[m] = src[j + m * C::T];
-    float2* xb = xch + (2 * slot + par) * C::XS;
-    block_fft<LOGQ, 1>(v, j, xb, twQ);
-    if (par) {
+    for (int par = 0; par < 2; ++par) {
+      float2 v[16];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
-        const int n = j + m * C::T;
-        xb[smpad(n)] = cmulc(v[m], twP[n]);
-      }
-    }
-    __syncthreads();
-    if (!par && r < p.ny) {
-      const float2* xo = xch + (2 * slot + 1) * C::XS;
+      for (int m = 0; m < 16; ++m) v[m] = plane[blk<LOGQ>(rr, par * C::Q + j + m * C::T, p.ny)];
+      block_fft_s<LOGQ, 1>(v, j, xb, stw);
+      if (par == 0) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
-        const int n = j + m * C::T;
-        if (n < p.nx) {
-          const float2 o = cadd(v[m], xo[smpad(n)]);
-          if (epi) stage[(slot * nc + c) * C::Q + n] = o;
-          else p.out[c][(long long)b * p.obs + (long long)r * p.nx + n] = o;
+        for (int m = 0; m < 16; ++m) y0[j + m * C::T] = v[m];
+      } else if (live) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          const int n = j + m * C::T;
+          if (n < p.nx) {
+            const float2 o = cadd(y0[n], cmulc(v[m], twP[n]));
+            if (epi) stage[(slot * nc + c) * p.nx + n] = o;
+            else p.out[c][(long long)b * p.obs + (long long)r * p.nx + n] = o;
+          }
         }
       }
     }
-    __syncthreads();
   }
   if (epi) {
+    __syncthreads();
     for (int idx = tid; idx < C::RPC * p.nx; idx += blockDim.x) {
-      const int s = idx / p.nx, n = idx % p.nx, rr = r0 + s;
-      if (rr >= p.ny) continue;
-      float2 e[3] = {stage[(s * nc) * C::Q + n], make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-      for (int c = 1; c < nc; ++c) e[c] = stage[(s * nc + c) * C::Q + n];
-      PixelCtx px{rr, n, (long long)rr * p.nx + n, b};
+      const int s = idx / p.nx, n = idx % p.nx, ro = r0 + s;
+      if (ro >= p.ny) continue;
+      const float2 zero = make_float2(0.f, 0.f);
+      float2 e[3] = {stage[(s * nc) * p.nx + n], nc > 1 ? stage[(s * nc + 1) * p.nx + n] : zero,
+                     nc > 2 ? stage[(s * nc + 2) * p.nx + n] : zero};
+      PixelCtx px{ro, n, (long long)ro * p.nx + n, b};
       apply_prog(p.post, e, px);
-      for (int c = 0; c < nc; ++c) p.out[c][(long long)b * p.obs + (long long)rr * p.nx + n] = e[c];
+      const long long o = (long long)b * p.obs + (long long)ro * p.nx + n;
+      p.out[0][o] = e[0];
+      if (nc > 1) p.out[1][o] = e[1];
+      if (nc > 2) p.out[2][o] = e[2];
     }
   }
 }
@@ -336,17 +375,17 @@ template <int LOGQ>
 static int launch_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy,
                            double z, double wavelength, double scale, float2* spec, float2* work) {
   using C = RsCfg<LOGQ>;
-  const size_t sm1 = (size_t)(C::RPC * C::P + 2 * C::RPC * C::XS) * sizeof(float2);
+  const size_t sm1 = (size_t)(C::HRPC * C::P + 2 * C::HRPC * C::XS) * sizeof(float2);
   cudaError_t e = allow_smem(rs_hhat_rows<LOGQ>, sm1);
   if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
   const float k = (float)(2.0 * M_PI / wavelength);
-  rs_hhat_rows<LOGQ><<<(C::P + C::RPC - 1) / C::RPC, 2 * C::RPC * C::T, sm1, st>>>(
+  rs_hhat_rows<LOGQ><<<(C::P + C::HRPC - 1) / C::HRPC, C::HROW_THREADS, sm1, st>>>(
       ny, nx, offx, offy, z, 1.0 / wavelength, k, work);
   XL_CHECK_LAUNCH("rs_hhat_rows");
   const size_t sm2 = (size_t)(C::P * (C::WH + 1) + 2 * C::WH * C::XS) * sizeof(float2);
   e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
   if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_cols smem");
-  rs_hhat_cols<LOGQ><<<C::P / C::WH, 2 * C::WH * C::T, sm2, st>>>(work, (float)scale, spec);
+  rs_hhat_cols<LOGQ><<<C::P / C::WH, C::HCOL_THREADS, sm2, st>>>(work, (float)scale, spec);
   XL_CHECK_LAUNCH("rs_hhat_cols");
   return XL_OK;
 }
@@ -357,18 +396,18 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   const dim3 g_rows((p.ny + C::RPC - 1) / C::RPC, p.B);
   cudaError_t e;
   if (stage == 0) {
-    const size_t sm = (size_t)(C::RPC * p.cout * C::Q + 2 * C::RPC * C::XS) * sizeof(float2);
+    const size_t sm = (size_t)(C::RPC * p.cin * p.nx + C::RPC * C::XS + C::TW) * sizeof(float2);
     if ((e = allow_smem(rs_rows_fwd<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_fwd smem");
     rs_rows_fwd<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_rows_fwd");
   } else if (stage == 1) {
-    const size_t sm = (size_t)(C::Q * (C::WC + 1) + 2 * C::WC * C::XS) * sizeof(float2);
+    const size_t sm = (size_t)(C::W * C::CXS + C::TW + C::W * C::CYS) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
-    rs_cols_conv<LOGQ><<<dim3(C::P / C::WC, p.B), C::CONV_THREADS, sm, st>>>(p);
+    rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::CONV_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
   } else {
-    const size_t sm =
-        (size_t)(2 * C::RPC * C::XS + (p.post.nops ? C::RPC * p.cout * C::Q : 0)) * sizeof(float2);
+    const size_t sm = (size_t)(C::RPC * C::XS + C::TW + C::RPC * C::Q +
+                               (p.post.nops ? C::RPC * p.cout * p.nx : 0)) * sizeof(float2);
     if ((e = allow_smem(rs_rows_inv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_inv smem");
     rs_rows_inv<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_rows_inv");

@@ -190,11 +190,20 @@ def op_sslm_amp(alpha, phi, a1, a2):
 
 
 def op_lcd(eta, theta):
-    return JonesOp(_lib.OP_LCD, [as_real_param(eta), as_real_param(theta)])
+    e, t = as_real_param(eta), as_real_param(theta)
+    dv = [0.0, 0.0, 0.0, 0.0]
+    if not isinstance(e, torch.Tensor):
+        dv[0], dv[1] = math.cos(0.5 * e), math.sin(0.5 * e)
+    if not isinstance(t, torch.Tensor):
+        dv[2], dv[3] = math.cos(t), math.sin(t)
+    return JonesOp(_lib.OP_LCD, [e, t], dval=dv)
 
 
 def op_lp(alpha):
-    return JonesOp(_lib.OP_LP, [as_real_param(alpha)])
+    a = as_real_param(alpha)
+    sv = [] if isinstance(a, torch.Tensor) else [a, 0.0, math.cos(a), math.sin(a)]
+    op = JonesOp(_lib.OP_LP, [a], sval=sv)
+    return op
 
 
 def lens_factors(x, y, wavelength, radius, focal):
