@@ -112,6 +112,11 @@ typedef struct {
   void* work;                  /* >= xl_rs_work_bytes(batch, comps_out, ny, nx) */
   XlProg pre;                  /* fused before the first pass */
   XlProg post;                 /* fused after the last pass */
+  int adjoint;                 /* 1: adjoint propagation (conjugate spectrum).  Scalar: 1 -> 1.
+                                  VRS: comps_in = comps_out = 3 gradients (Ex, Ey, Ez) in; the Ez
+                                  gradient is folded back into Ex, Ey with the weights X/r, Y/r of
+                                  the forward Ez derivation; outputs out[0], out[1].  pre/post must
+                                  be empty. */
 } XlRsArgs;
 
 size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx);
@@ -176,6 +181,12 @@ typedef struct {
   const void* post_y;
   void* work;            /* >= xl_czt_work_bytes(batch, comps_out, ny, mx) */
   XlProg pre;            /* fused before the first pass (masks, XL_OP_HIGHNA) */
+  int adjoint;           /* 1: conjugate transpose of the forward chirp-z.  The input plane
+                            (ny, nx, x, y) is the forward's output grid and the output plane
+                            (my, mx, xout, yout) its input grid; chirp vectors are the adjoint
+                            ones (pre' = conj(post) L, g' = conj(g), post' = conj(pre) / L);
+                            z, wavelength and cte as for the forward.  VCZT: 3 gradients in,
+                            the Ez gradient folded into out[0], out[1]. */
 } XlCztArgs;
 
 size_t xl_czt_work_bytes(int batch, int comps, int ny, int mx);
@@ -193,6 +204,19 @@ int xl_czt_stage(void* stream, const XlCztArgs* args, int stage);
 /* Apply a Jones program to batch x comps planes (out may alias in). */
 int xl_apply_ops(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
                  long long in_bstride, void* const* out, long long out_bstride, const XlProg* prog);
+
+/* Backward of a Jones program: the gradients jax.grad takes through the masks
+ * of optical_elements.py:76-332, :515-594 and :678-703.  `in` holds the
+ * program's input planes and `gout` the gradient of its output (torch
+ * convention for complex tensors, 2 dL/d conj(y)); `gin` receives the
+ * gradient of the input (in[1], in[2] may be NULL for planes that are zero,
+ * e.g. the Ez a propagator derives itself).  pgrad[op*4 + i] (XL_MAX_OPS*4 entries, NULL skips)
+ * receives dL/dp for parameter i of op: a float32 plane for a per-pixel
+ * parameter (summed over the batch when the parameter is shared by it), or
+ * one float64 accumulator that the call adds into for a scalar parameter. */
+int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
+                    long long in_bstride, const void* const* gout, long long gout_bstride,
+                    void* const* gin, long long gin_bstride, const XlProg* prog, void* const* pgrad);
 
 #ifdef __cplusplus
 }

@@ -122,3 +122,64 @@ def test_four_f_chain():
     u = ref.slm(u, g["phase2"])[0]
     u = ref.czt(u, g["xout"], g["yout"], wl, f)
     assert rel_l2(u, g["out"]) < TOL
+
+
+# ---- the torch restatement (gradient oracle) is pinned to the numpy oracle ----
+
+def test_torch_restatement_matches_numpy_oracle():
+    import torch
+    from oracle import torch_ref as tr
+    g = golden("four_f")
+    x, y, wl, f = g["x"], g["y"], g["wavelength"], float(g["f"])
+    u = tr.slm(torch.as_tensor(g["source"]), torch.as_tensor(g["phase1"]))
+    u = tr.rs_propagate(u, x, y, wl, f)
+    assert rel_l2(u.numpy(), g["after_rs"]) < TOL
+    u = tr.lens(u, x, y, wl, (200.0, 200.0), (f, f))
+    u = tr.czt(u, x, y, wl, f, g["xout"], g["yout"])
+    assert rel_l2(u.numpy(), g["after_czt1"]) < TOL
+    h = golden("high_na")
+    out = tr.vczt_objective_lens(torch.as_tensor(h["Ex_in"]), torch.as_tensor(h["Ey_in"]), h["x"], h["y"],
+                                 h["wavelength"], float(h["radius"]), float(h["f"]), h["xout"], h["yout"])
+    for o, key in zip(out, ("Ex", "Ey", "Ez")):
+        assert rel_l2(o.numpy(), h[key]) < TOL
+    v = golden("vrs")
+    Ex, Ey = tr.lcd(torch.as_tensor(v["Ex0"]), torch.as_tensor(v["Ey0"]), v["eta"], v["theta"])
+    Ex, Ey = tr.linear_polarizer(Ex, Ey, v["alpha"])
+    out = tr.vrs_propagate(Ex, Ey, v["x"], v["y"], v["wavelength"], float(v["z"]))
+    for o, key in zip(out, ("Ex", "Ey", "Ez")):
+        assert rel_l2(o.numpy(), v[key]) < TOL
+
+
+def test_torch_restatement_gradients_match_finite_differences():
+    """Central differences in float64 on a few mask parameters of a 4f-style chain."""
+    import torch
+    from oracle import torch_ref as tr
+    n = 24
+    x, y = ref.space(120.0, n)
+    rng = np.random.default_rng(11)
+    src = torch.as_tensor(ref.gaussian_beam(x, y, 0.6, (50.0, 50.0)))
+    w = torch.as_tensor(rng.uniform(0, 1, (16, 16)))
+    xo, yo = ref.space(40.0, 16)
+
+    def loss(ph, eta):
+        u = tr.slm(src, ph)
+        u = tr.rs_propagate(u, x, y, 0.6, 3000.0)
+        ex, ey = tr.lcd(u, 0.3 * u, eta, 0.7)
+        u = tr.czt(ex + ey, x, y, 0.6, 3000.0, xo, yo)
+        return torch.sum(w * torch.abs(u) ** 2)
+
+    ph = torch.as_tensor(rng.uniform(-np.pi, np.pi, (n, n)), dtype=torch.float64).requires_grad_(True)
+    eta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (n, n)), dtype=torch.float64).requires_grad_(True)
+    L = loss(ph, eta)
+    L.backward()
+    h = 1e-6
+    for (i, j) in [(3, 4), (12, 12), (20, 7)]:
+        for t, gt in ((ph, ph.grad), (eta, eta.grad)):
+            with torch.no_grad():
+                t[i, j] += h
+                lp = loss(ph, eta).item()
+                t[i, j] -= 2 * h
+                lm = loss(ph, eta).item()
+                t[i, j] += h
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - gt[i, j].item()) <= 1e-6 * max(1.0, abs(fd)) + 1e-9 * abs(L.item())

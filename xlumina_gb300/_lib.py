@@ -40,7 +40,7 @@ class XlRsArgs(ctypes.Structure):
                 ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
                 ("spectrum", ctypes.c_void_p), ("spectrum_stride", ctypes.c_longlong),
                 ("spectrum_index", ctypes.c_void_p), ("work", ctypes.c_void_p),
-                ("pre", XlProg), ("post", XlProg)]
+                ("pre", XlProg), ("post", XlProg), ("adjoint", ctypes.c_int)]
 
 
 XL_CZT_SCALAR, XL_CZT_VECTOR, XL_CZT_PLAIN = 0, 1, 2
@@ -57,7 +57,7 @@ class XlCztArgs(ctypes.Structure):
                 ("cte_re", ctypes.c_double), ("cte_im", ctypes.c_double),
                 ("pre_x", ctypes.c_void_p), ("g_x", ctypes.c_void_p), ("post_x", ctypes.c_void_p),
                 ("pre_y", ctypes.c_void_p), ("g_y", ctypes.c_void_p), ("post_y", ctypes.c_void_p),
-                ("work", ctypes.c_void_p), ("pre", XlProg)]
+                ("work", ctypes.c_void_p), ("pre", XlProg), ("adjoint", ctypes.c_int)]
 
 
 # name -> (restype, argtypes); every symbol include/xlgb.h declares.
@@ -77,6 +77,11 @@ SIGNATURES = {
     "xl_czt_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_czt": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs)]),
     "xl_czt_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs), ctypes.c_int]),
+    "xl_ops_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                       ctypes.POINTER(XlProg), ctypes.POINTER(ctypes.c_void_p)]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

@@ -1,0 +1,144 @@
+"""Differentiation of the propagation path through hand-written adjoints.
+
+Each propagator call becomes one ``torch.autograd.Function`` that runs the
+fused forward kernels (Jones program + propagator), and whose backward runs:
+
+* the adjoint propagator on the output gradients: conjugate transfer spectrum
+  for RS / VRS, conjugate-transpose chirp-z for CZT / VCZT / the high-NA
+  focus, with the Ez derivation folded back in;
+* then ``xl_ops_backward`` for the Jones program, which gives the gradient of
+  the input field and of every trainable mask parameter.
+
+This replaces ``jax.grad`` through RS_propagation_jit / CZT_jit and the masks
+(e.g. experiments/four_f_optimizer.py:43, experiments/hybrid_optimizer.py:60).
+Gradients follow torch's convention for complex tensors.  Distances z,
+wavelengths and lens geometry are not differentiable here.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import engine
+
+
+def _trainable(ops):
+    """(op index, slot, tensor) for every parameter tensor that requires grad."""
+    out = []
+    for k, o in enumerate(ops):
+        for q, p in enumerate(o.params):
+            if isinstance(p, torch.Tensor) and p.requires_grad:
+                out.append((k, q, p))
+    return out
+
+
+def needs_grad(base, ops) -> bool:
+    if not torch.is_grad_enabled():
+        return False
+    if any(isinstance(b, torch.Tensor) and b.requires_grad for b in base):
+        return True
+    return bool(_trainable(ops))
+
+
+class RsPlan:
+    """RS (one component) or VRS ((Ex, Ey) -> (Ex, Ey, Ez)) with a fused Jones prologue."""
+
+    def __init__(self, x, y, wavelength, z, vector, ops):
+        self.x, self.y, self.wavelength, self.z, self.vector = x, y, wavelength, z, vector
+        self.ops = list(ops or ())
+        self.ny, self.nx = len(y), len(x)
+
+    def forward(self, base):
+        return engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector,
+                             pre=self.ops).run()
+
+    def adjoint(self, grads):
+        return engine.RsCall(list(grads), self.x, self.y, self.wavelength, self.z, self.vector,
+                             adjoint=True).run()
+
+
+class CztPlan:
+    """CZT (one component), VCZT, or the high-NA focus (lens op inside ``ops``)."""
+
+    def __init__(self, x, y, wavelength, z, xout, yout, mode, ops, lens=None):
+        self.x, self.y, self.wavelength, self.z = x, y, wavelength, z
+        self.xout, self.yout, self.mode, self.lens = xout, yout, mode, lens
+        self.ops = list(ops or ())
+        self.ny, self.nx = len(y), len(x)
+
+    @property
+    def vector(self):
+        return self.mode != "scalar"
+
+    def forward(self, base):
+        return engine.CztCall(list(base), self.x, self.y, self.wavelength, self.z, self.xout, self.yout,
+                              self.mode, pre=self.ops, lens=self.lens).run()
+
+    def adjoint(self, grads):
+        return engine.CztCall(list(grads), self.x, self.y, self.wavelength, self.z, self.xout, self.yout,
+                              self.mode, lens=self.lens, adjoint=True).run()
+
+
+class _Fused(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan, n_base, n_out, *tensors):
+        base = tensors[:n_base]
+        ctx.plan = plan
+        ctx.n_base = n_base
+        ctx.save_for_backward(*base)
+        outs = plan.forward(base)
+        return tuple(outs[:n_out])
+
+    @staticmethod
+    def backward(ctx, *gouts):
+        plan = ctx.plan
+        base = ctx.saved_tensors
+        ref = next((g for g in gouts if g is not None), None)
+        gouts = [g if g is not None else torch.zeros_like(ref) for g in gouts]
+        gouts = [g.to(torch.complex64).contiguous() for g in gouts]
+        gprog = plan.adjoint(gouts)           # gradient of the Jones program's output
+        trainable = _trainable(plan.ops)
+        if plan.ops:
+            nb = len(gprog)
+            b = list(base) + [None] * (nb - len(base))
+            gin, pgrads = engine.ops_backward(b[:nb], gprog, plan.ops, plan.ny, plan.nx)
+        else:
+            gin, pgrads = gprog, {}
+        gbase = []
+        for i, t in enumerate(base):
+            gbase.append(gin[i] if (t.requires_grad and i < len(gin)) else None)
+        gparams = [pgrads.get((k, q)) for (k, q, _) in trainable]
+        return (None, None, None, *gbase, *gparams)
+
+
+def fused_propagate(plan, base, n_out):
+    """Run ``plan`` through autograd; ``base`` are the input planes."""
+    params = [p for (_, _, p) in _trainable(plan.ops)]
+    return list(_Fused.apply(plan, len(base), n_out, *base, *params))
+
+
+class _Ops(torch.autograd.Function):
+    """A Jones program materialised on its own (a light's component is read)."""
+
+    @staticmethod
+    def forward(ctx, ops, ny, nx, n_base, *tensors):
+        base = tensors[:n_base]
+        ctx.ops, ctx.ny, ctx.nx = ops, ny, nx
+        ctx.save_for_backward(*base)
+        return tuple(engine.apply_ops(list(base), ops, ny, nx))
+
+    @staticmethod
+    def backward(ctx, *gouts):
+        base = ctx.saved_tensors
+        ref = next((g for g in gouts if g is not None), None)
+        gouts = [(g if g is not None else torch.zeros_like(ref)).to(torch.complex64).contiguous() for g in gouts]
+        gin, pgrads = engine.ops_backward(list(base), gouts, ctx.ops, ctx.ny, ctx.nx)
+        trainable = _trainable(ctx.ops)
+        gbase = [gin[i] if base[i].requires_grad else None for i in range(len(base))]
+        return (None, None, None, None, *gbase, *[pgrads.get((k, q)) for (k, q, _) in trainable])
+
+
+def apply_ops(base, ops, ny, nx):
+    if needs_grad(base, ops):
+        params = [p for (_, _, p) in _trainable(ops)]
+        return list(_Ops.apply(list(ops), ny, nx, len(base), *base, *params))
+    return engine.apply_ops(base, ops, ny, nx)

@@ -170,4 +170,133 @@ __device__ __forceinline__ void apply_prog(const XlProg& prog, float2 (&e)[3], c
   for (int i = 0; i < prog.nops; ++i) apply_op(prog.ops[i], e, px);
 }
 
+// ---- backward of one op ----
+// e: the op's input (Ex, Ey, Ez); g: on entry the gradient of the op's output,
+// on exit the gradient of its input (torch convention for complex tensors:
+// g = 2 dL/d conj(y)).  pg[i] += dL/dp_i for the op's real parameters, where
+// dL/dp = Re(sum_c g_c conj(dy_c/dp)).
+__device__ __forceinline__ float re_gconj(float2 g, float2 d) { return g.x * d.x + g.y * d.y; }
+
+__device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
+                                             const PixelCtx& px, float (&pg)[4]) {
+  switch (op.kind) {
+    case XL_OP_PHASE: {
+      float s, c;
+      sincosf(op_param(op, 0, px), &s, &c);
+      const float2 ph = make_float2(c, s);
+      const float2 y = cmul(e[0], ph);
+      pg[0] += re_gconj(g[0], make_float2(-y.y, y.x));   // dy/dphi = i y
+      g[0] = cmulc(g[0], ph);
+      break;
+    }
+    case XL_OP_SSLM:
+    case XL_OP_SSLM_AMP: {
+      const bool amp = op.kind == XL_OP_SSLM_AMP;
+      float s, c;
+      sincosf(op_param(op, 0, px), &s, &c);
+      const float2 p0 = make_float2(c, s);
+      sincosf(op_param(op, 1, px), &s, &c);
+      const float2 p1 = make_float2(c, s);
+      const float a1 = amp ? op_param(op, 2, px) : 1.f, a2 = amp ? op_param(op, 3, px) : 1.f;
+      const float2 u0 = cmul(e[0], p0), u1 = cmul(e[1], p1);   // before the amplitudes
+      pg[0] += a1 * re_gconj(g[0], make_float2(-u0.y, u0.x));
+      pg[1] += a2 * re_gconj(g[1], make_float2(-u1.y, u1.x));
+      if (amp) {
+        pg[2] += re_gconj(g[0], u0);
+        pg[3] += re_gconj(g[1], u1);
+      }
+      g[0] = cscale(cmulc(g[0], p0), a1);
+      g[1] = cscale(cmulc(g[1], p1), a2);
+      break;
+    }
+    case XL_OP_LCD: {
+      float sh, ch, st, ct;
+      if (op.pmask & 1) sincosf(0.5f * op_param(op, 0, px), &sh, &ch);
+      else { ch = op.dval[0]; sh = op.dval[1]; }
+      if (op.pmask & 2) sincosf(op_param(op, 1, px), &st, &ct);
+      else { ct = op.dval[2]; st = op.dval[3]; }
+      const float c2 = ct * ct - st * st, s2 = 2.f * st * ct;
+      const float2 a = make_float2(ch, -sh * c2), bb = make_float2(0.f, -sh * s2), d = make_float2(ch, sh * c2);
+      // derivatives of the matrix entries
+      const float2 a_e = make_float2(-0.5f * sh, -0.5f * ch * c2), b_e = make_float2(0.f, -0.5f * ch * s2);
+      const float2 d_e = make_float2(-0.5f * sh, 0.5f * ch * c2);
+      const float2 a_t = make_float2(0.f, 2.f * sh * s2), b_t = make_float2(0.f, -2.f * sh * c2);
+      const float2 d_t = make_float2(0.f, -2.f * sh * s2);
+      const float2 x = e[0], y = e[1];
+      pg[0] += re_gconj(g[0], cadd(cmul(a_e, x), cmul(b_e, y))) + re_gconj(g[1], cadd(cmul(b_e, x), cmul(d_e, y)));
+      pg[1] += re_gconj(g[0], cadd(cmul(a_t, x), cmul(b_t, y))) + re_gconj(g[1], cadd(cmul(b_t, x), cmul(d_t, y)));
+      const float2 g0 = g[0], g1 = g[1];   // J symmetric: J^H g = conj(J) g
+      g[0] = cadd(cmul(cconj(a), g0), cmul(cconj(bb), g1));
+      g[1] = cadd(cmul(cconj(bb), g0), cmul(cconj(d), g1));
+      break;
+    }
+    case XL_OP_LP: {
+      float s, c;
+      if (op.pmask & 1) sincosf(op_param(op, 0, px), &s, &c);
+      else { c = op.sval[2]; s = op.sval[3]; }
+      const float2 x = e[0], y = e[1];
+      const float dcs = c * c - s * s, tcs = 2.f * c * s;
+      pg[0] += re_gconj(g[0], cadd(cscale(x, -tcs), cscale(y, dcs))) +
+               re_gconj(g[1], cadd(cscale(x, dcs), cscale(y, tcs)));
+      const float2 g0 = g[0], g1 = g[1];
+      g[0] = cadd(cscale(g0, c * c), cscale(g1, c * s));
+      g[1] = cadd(cscale(g0, c * s), cscale(g1, s * s));
+      g[2] = make_float2(0.f, 0.f);
+      break;
+    }
+    case XL_OP_SEPMASK: {
+      const float2 fc = ((const float2*)op.ptr[0])[px.col];
+      const float2 fr = ((const float2*)op.ptr[1])[px.row];
+      float2 m = cmul(fc, fr);
+      if (op.ptr[2]) {
+        const double tc = ((const double*)op.ptr[2])[px.col];
+        const double tr = ((const double*)op.ptr[3])[px.row];
+        if (!(tc + tr < 1.0)) m = make_float2(0.f, 0.f);
+      }
+      g[0] = cmulc(g[0], m);
+      g[1] = cmulc(g[1], m);
+      g[2] = op.sval[0] != 0.f ? make_float2(0.f, 0.f) : cmulc(g[2], m);
+      break;
+    }
+    case XL_OP_CMUL: {
+      const float2 m = ((const float2*)op.ptr[0])[(long long)px.batch * op.pbstride + px.pix];
+      g[0] = cmulc(g[0], m);
+      g[1] = cmulc(g[1], m);
+      g[2] = cmulc(g[2], m);
+      break;
+    }
+    case XL_OP_HIGHNA: {
+      const double Xd = ((const double*)op.ptr[0])[px.col];
+      const double Yd = ((const double*)op.ptr[1])[px.row];
+      const double rad = op.dval[0];
+      const double q = (Xd * Xd + Yd * Yd) / (rad * rad);
+      const float smax = (float)op.dval[2];
+      const float G = q < 1.0 ? 1.f / sqrtf(fabsf(1.f - (float)q * smax * smax)) : 0.f;
+      const float X = (float)Xd, Y = (float)Yd;
+      const float rho = sqrtf(X * X + Y * Y);
+      const float th = rho / (float)op.dval[1];
+      const float phi = atan2f(Y, X);
+      float st, ct, sp, cp;
+      sincosf(th, &st, &ct);
+      sincosf(phi, &sp, &cp);
+      const float w = sqrtf(fabsf(ct)) * G;
+      const float ux = X / rho, uy = Y / rho;
+      // rows of RL; the input Ez' = ux Ex + uy Ey
+      const float r00 = ct * cp * cp + sp * sp, r01 = ct * cp * sp - sp * cp, r02 = -cp * st;
+      const float r10 = sp * ct * cp - cp * sp, r11 = ct * sp * sp + cp * cp, r12 = -sp * st;
+      const float r20 = st * cp, r21 = st * sp, r22 = ct;
+      const float k00 = w * (r00 + r02 * ux), k01 = w * (r01 + r02 * uy);
+      const float k10 = w * (r10 + r12 * ux), k11 = w * (r11 + r12 * uy);
+      const float k20 = w * (r20 + r22 * ux), k21 = w * (r21 + r22 * uy);
+      const float2 g0 = g[0], g1 = g[1], g2 = g[2];
+      g[0] = cadd(cadd(cscale(g0, k00), cscale(g1, k10)), cscale(g2, k20));
+      g[1] = cadd(cadd(cscale(g0, k01), cscale(g1, k11)), cscale(g2, k21));
+      g[2] = make_float2(0.f, 0.f);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
 }  // namespace xl

@@ -24,8 +24,10 @@
 namespace xl {
 
 struct CztLaunch {
-  int B, cin, cout, ny, nx, my, mx;  // input ny x nx, output my x mx
+  int B, cin, cout, ny, nx, my, mx;  // input plane ny x nx, output plane my x mx
   int mode;                          // XL_CZT_SCALAR / XL_CZT_VECTOR / XL_CZT_PLAIN
+  int adjoint;                       // transpose-conjugate of the forward transform
+  int ioff_x, ooff_x, ioff_y, ooff_y;  // where the input / output lines sit in the length-L line
   const float2* in[3];
   long long ibs;
   float2* out[3];
@@ -80,18 +82,19 @@ __device__ __forceinline__ void bluestein_chain(float2 (&v)[16], int j, int par,
   }
 }
 
-// Chain input for parity `par` from a line src[0..m) (zero beyond m), times pre[n].
+// Chain input for parity `par`: the length-L line holds src[i] * pre[i] at
+// position off + i (i < m) and zeros elsewhere; a_par[n] = (x[n] +- x[n+Q]) w_L^(par n).
 template <int LOGQ>
 __device__ __forceinline__ void bluestein_load(float2 (&v)[16], int j, int par, const float2* src,
-                                               int stride, int m, const float2* __restrict__ pre) {
+                                               int stride, int m, int off, const float2* __restrict__ pre) {
   using C = CztCfg<LOGQ>;
   const float2* twL = tw_table(LOGQ + 1);
 #pragma unroll
   for (int mm = 0; mm < 16; ++mm) {
     const int n = j + mm * C::T;
-    float2 a = n < m ? cmul(src[n * stride], pre[n]) : make_float2(0.f, 0.f);
-    const int n2 = n + C::Q;
-    const float2 b = n2 < m ? cmul(src[n2 * stride], pre[n2]) : make_float2(0.f, 0.f);
+    const int i1 = n - off, i2 = n + C::Q - off;
+    const float2 a = (i1 >= 0 && i1 < m) ? cmul(src[i1 * stride], pre[i1]) : make_float2(0.f, 0.f);
+    const float2 b = (i2 >= 0 && i2 < m) ? cmul(src[i2 * stride], pre[i2]) : make_float2(0.f, 0.f);
     v[mm] = par ? cmul(csub(a, b), twL[n]) : cadd(a, b);
   }
 }
@@ -120,18 +123,25 @@ __global__ void __launch_bounds__(CztCfg<LOGQ>::ROW_THREADS) czt_rows(const CztL
     e[0] = p.in[0][off];
     e[1] = p.cin > 1 ? p.in[1][off] : make_float2(0.f, 0.f);
     e[2] = make_float2(0.f, 0.f);
+    if (p.cin > 2) e[2] = p.in[2][off];
     PixelCtx px{r, n, (long long)r * p.nx + n, b};
     apply_prog(p.pre, e, px);
     if (p.mode != XL_CZT_PLAIN) {
-      if (p.mode == XL_CZT_VECTOR) {  // vectorized_optics.py:340-344
+      if (p.mode == XL_CZT_VECTOR && !p.adjoint) {  // vectorized_optics.py:340-344
         const float X = (float)p.x[n], Y = (float)p.y[r];
         const float rr = sqrtf(X * X + Y * Y + zf * zf);
         e[2] = cscale(cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr)), zf / rr);
       }
-      const float2 F = rs_kernel_value(p.x[n], p.y[r], p.z, p.inv_lambda, p.k);  // wave_optics.py:341
-      for (int c = 0; c < nc; ++c) e[c] = cmul(e[c], F);
+      // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
+      float2 F = rs_kernel_value(p.x[n], p.y[r], p.z, p.inv_lambda, p.k);
+      if (p.adjoint) F = cconj(F);
+      e[0] = cmul(e[0], F);
+      e[1] = cmul(e[1], F);
+      e[2] = cmul(e[2], F);
     }
-    for (int c = 0; c < nc; ++c) stage[(s * nc + c) * p.nx + n] = e[c];
+    stage[(s * nc) * p.nx + n] = e[0];
+    if (nc > 1) stage[(s * nc + 1) * p.nx + n] = e[1];
+    if (nc > 2) stage[(s * nc + 2) * p.nx + n] = e[2];
   }
   __syncthreads();
 
@@ -141,13 +151,14 @@ __global__ void __launch_bounds__(CztCfg<LOGQ>::ROW_THREADS) czt_rows(const CztL
   const float2* xo = xch + (2 * slot + 1) * C::XS;
   for (int c = 0; c < nc; ++c) {
     float2 v[16];
-    bluestein_load<LOGQ>(v, j, par, stage + (slot * nc + c) * p.nx, 1, r < p.ny ? p.nx : 0, p.pre_x);
+    bluestein_load<LOGQ>(v, j, par, stage + (slot * nc + c) * p.nx, 1, r < p.ny ? p.nx : 0, p.ioff_x,
+                         p.pre_x);
     bluestein_chain<LOGQ>(v, j, par, xb, p.g_x);
     __syncthreads();
     if (r < p.ny) {
       float2* dst = p.work + (((long long)b * nc + c) * p.ny + r) * p.mx;
       for (int o = par * C::T + j; o < p.mx; o += 2 * C::T) {
-        const int n2 = p.nx + o;
+        const int n2 = p.ooff_x + o;
         const int i = n2 & (C::Q - 1);
         const float2 t = (n2 >> LOGQ) & 1 ? csub(xe[smpad(i)], xo[smpad(i)]) : cadd(xe[smpad(i)], xo[smpad(i)]);
         dst[o] = cmul(t, p.post_x[o]);
@@ -183,7 +194,7 @@ __global__ void __launch_bounds__(CztCfg<LOGQ>::COL_THREADS) czt_cols(const CztL
     }
     __syncthreads();
     float2 v[16];
-    bluestein_load<LOGQ>(v, j, par, tile + w, PITCH, p.ny, p.pre_y);
+    bluestein_load<LOGQ>(v, j, par, tile + w, PITCH, p.ny, p.ioff_y, p.pre_y);
     bluestein_chain<LOGQ>(v, j, par, xb, p.g_y);
     __syncthreads();
     // combine: output rows o in [0, my) of the W columns, into the tile
@@ -191,20 +202,34 @@ __global__ void __launch_bounds__(CztCfg<LOGQ>::COL_THREADS) czt_cols(const CztL
       const int o = idx / W, ww = idx % W;
       const float2* e0 = xch + (2 * ww) * C::XS;
       const float2* e1 = xch + (2 * ww + 1) * C::XS;
-      const int n2 = p.ny + o;
+      const int n2 = p.ooff_y + o;
       const int i = n2 & (C::Q - 1);
       float2 t = (n2 >> LOGQ) & 1 ? csub(e0[smpad(i)], e1[smpad(i)]) : cadd(e0[smpad(i)], e1[smpad(i)]);
       t = cmul(t, p.post_y[o]);
       const int col = c0 + ww;
-      if (p.mode != XL_CZT_PLAIN && col < p.mx) {  // wave_optics.py:340, 355: F0 * U
-        t = cmul(t, rs_kernel_value(p.xo[col], p.yo[o], p.z, p.inv_lambda, p.k));
+      if (p.mode != XL_CZT_PLAIN && col < p.mx) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
+        const float2 F = rs_kernel_value(p.xo[col], p.yo[o], p.z, p.inv_lambda, p.k);
+        t = p.adjoint ? cmulc(t, F) : cmul(t, F);
       }
       tile[o * PITCH + ww] = cmul(t, p.cte);
     }
     __syncthreads();
+    const bool fold = p.adjoint && p.mode == XL_CZT_VECTOR;
     for (int idx = tid; idx < p.my * W; idx += blockDim.x) {
       const int o = idx / W, ww = idx % W;
-      if (c0 + ww < p.mx) p.out[c][(long long)b * p.obs + (long long)o * p.mx + c0 + ww] = tile[o * PITCH + ww];
+      const int col = c0 + ww;
+      if (col >= p.mx) continue;
+      const long long pix = (long long)b * p.obs + (long long)o * p.mx + col;
+      if (fold && c == 2) {  // adjoint of Ez = (Ex X/r + Ey Y/r) z/r, vectorized_optics.py:341-344
+        const float zf = (float)p.z;
+        const float X = (float)p.xo[col], Y = (float)p.yo[o];
+        const float r2 = X * X + Y * Y + zf * zf;
+        const float2 gz = tile[o * PITCH + ww];
+        p.out[0][pix] = cadd(p.out[0][pix], cscale(gz, X * zf / r2));
+        p.out[1][pix] = cadd(p.out[1][pix], cscale(gz, Y * zf / r2));
+      } else {
+        p.out[c][pix] = tile[o * PITCH + ww];
+      }
     }
     __syncthreads();
   }
@@ -293,7 +318,8 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
     return XL_EINVAL;
   }
   const bool ok_modes = (a->mode == XL_CZT_SCALAR && a->comps_in == 1 && a->comps_out == 1) ||
-                        (a->mode == XL_CZT_VECTOR && a->comps_in == 2 && a->comps_out == 3) ||
+                        (a->mode == XL_CZT_VECTOR && !a->adjoint && a->comps_in == 2 && a->comps_out == 3) ||
+                        (a->mode == XL_CZT_VECTOR && a->adjoint && a->comps_in == 3 && a->comps_out == 3) ||
                         (a->mode == XL_CZT_PLAIN && a->comps_in >= 1 && a->comps_in <= 3 &&
                          a->comps_out >= a->comps_in && a->comps_out <= 3);
   if (!ok_modes) {
@@ -317,16 +343,23 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
   }
   for (int c = 0; c < a->comps_in; ++c)
     if (!a->in[c]) { set_error("xl_czt: null input plane %d", c); return XL_EINVAL; }
-  for (int c = 0; c < a->comps_out; ++c)
+  const int nout = (a->adjoint && a->mode == XL_CZT_VECTOR) ? 2 : a->comps_out;
+  for (int c = 0; c < nout; ++c)
     if (!a->out[c]) { set_error("xl_czt: null output plane %d", c); return XL_EINVAL; }
-  if (a->pre.nops < 0 || a->pre.nops > XL_MAX_OPS) {
-    set_error("xl_czt: op program too long");
+  if (a->pre.nops < 0 || a->pre.nops > XL_MAX_OPS || (a->adjoint && a->pre.nops)) {
+    set_error("xl_czt: op program too long (or given to the adjoint)");
     return XL_EINVAL;
   }
   if (int rc = ensure_init()) return rc;
   CztLaunch p;
   p.B = a->batch; p.cin = a->comps_in; p.cout = a->comps_out;
   p.ny = a->ny; p.nx = a->nx; p.my = a->my; p.mx = a->mx; p.mode = a->mode;
+  p.adjoint = a->adjoint ? 1 : 0;
+  // forward: the input line starts at 0 and the output window at m; the adjoint swaps them
+  p.ioff_x = p.adjoint ? a->mx : 0;
+  p.ooff_x = p.adjoint ? 0 : a->nx;
+  p.ioff_y = p.adjoint ? a->my : 0;
+  p.ooff_y = p.adjoint ? 0 : a->ny;
   for (int c = 0; c < 3; ++c) {
     p.in[c] = (const float2*)a->in[c];
     p.out[c] = (float2*)a->out[c];
@@ -336,7 +369,7 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
   p.z = a->z;
   p.inv_lambda = a->wavelength > 0 ? 1.0 / a->wavelength : 0.0;
   p.k = a->wavelength > 0 ? (float)(2.0 * M_PI / a->wavelength) : 0.f;
-  p.cte = make_float2((float)a->cte_re, (float)a->cte_im);
+  p.cte = make_float2((float)a->cte_re, (float)(a->adjoint ? -a->cte_im : a->cte_im));
   p.pre_x = (const float2*)a->pre_x; p.g_x = (const float2*)a->g_x; p.post_x = (const float2*)a->post_x;
   p.pre_y = (const float2*)a->pre_y; p.g_y = (const float2*)a->g_y; p.post_y = (const float2*)a->post_y;
   p.work = (float2*)a->work;

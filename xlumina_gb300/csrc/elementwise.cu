@@ -34,6 +34,95 @@ __global__ void apply_ops_kernel(const ElemLaunch p) {
   }
 }
 
+struct OpsBwdLaunch {
+  int B, C, ny, nx;
+  const float2* in[3];
+  long long ibs;
+  const float2* gout[3];
+  long long gbs;
+  float2* gin[3];
+  long long ginbs;
+  XlProg prog;
+  void* pgrad[XL_MAX_OPS * 4];
+};
+
+// One thread per pixel, looping over the batch so that gradients of
+// parameters shared by the batch are summed in a fixed order.
+__global__ void __launch_bounds__(256) ops_backward_kernel(const OpsBwdLaunch p) {
+  const long long npix = (long long)p.ny * p.nx;
+  const int K = p.prog.nops;
+  float sacc[XL_MAX_OPS * 4];
+  for (int q = 0; q < XL_MAX_OPS * 4; ++q) sacc[q] = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int row = (int)(i / p.nx), col = (int)(i % p.nx);
+    float pacc[XL_MAX_OPS * 4];   // shared per-pixel parameters, summed over the batch
+    for (int q = 0; q < XL_MAX_OPS * 4; ++q) pacc[q] = 0.f;
+    for (int b = 0; b < p.B; ++b) {
+      PixelCtx px{row, col, i, b};
+      float2 st[XL_MAX_OPS][3];
+      float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      const long long off = (long long)b * p.ibs + i;
+      e[0] = p.in[0][off];
+      if (p.C > 1 && p.in[1]) e[1] = p.in[1][off];
+      if (p.C > 2 && p.in[2]) e[2] = p.in[2][off];
+      for (int k = 0; k < K; ++k) {
+        st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
+        apply_op(p.prog.ops[k], e, px);
+      }
+      float2 g[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      const long long go = (long long)b * p.gbs + i;
+      g[0] = p.gout[0][go];
+      if (p.C > 1) g[1] = p.gout[1][go];
+      if (p.C > 2) g[2] = p.gout[2][go];
+      for (int k = K - 1; k >= 0; --k) {
+        const XlOp& op = p.prog.ops[k];
+        float pg[4] = {0.f, 0.f, 0.f, 0.f};
+        const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
+        apply_op_bwd(op, ek, g, px, pg);
+        for (int q = 0; q < 4; ++q) {
+          void* dst = p.pgrad[k * 4 + q];
+          if (!dst) continue;
+          if (op.pmask & (1 << q)) {
+            if (op.pbstride) ((float*)dst)[(long long)b * op.pbstride + i] = pg[q];
+            else pacc[k * 4 + q] += pg[q];
+          } else {
+            sacc[k * 4 + q] += pg[q];
+          }
+        }
+      }
+      const long long gi = (long long)b * p.ginbs + i;
+      if (p.gin[0]) p.gin[0][gi] = g[0];
+      if (p.C > 1 && p.gin[1]) p.gin[1][gi] = g[1];
+      if (p.C > 2 && p.gin[2]) p.gin[2][gi] = g[2];
+    }
+    for (int k = 0; k < K; ++k)
+      for (int q = 0; q < 4; ++q) {
+        const XlOp& op = p.prog.ops[k];
+        if (p.pgrad[k * 4 + q] && (op.pmask & (1 << q)) && !op.pbstride)
+          ((float*)p.pgrad[k * 4 + q])[i] = pacc[k * 4 + q];
+      }
+  }
+  // scalar parameters: block reduction, one float64 atomic per block and slot
+  __shared__ float red[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < K; ++k)
+    for (int q = 0; q < 4; ++q) {
+      const XlOp& op = p.prog.ops[k];
+      if (!p.pgrad[k * 4 + q] || (op.pmask & (1 << q))) continue;
+      float v = sacc[k * 4 + q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][0] = v;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][0];
+        atomicAdd((double*)p.pgrad[k * 4 + q], t);
+      }
+      __syncthreads();
+    }
+}
+
 cudaError_t elem_upload_twiddles(const float2* host) {
   return cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
 }
@@ -41,6 +130,40 @@ cudaError_t elem_upload_twiddles(const float2* host) {
 }  // namespace xl
 
 using namespace xl;
+
+extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
+                               long long in_bstride, const void* const* gout, long long gout_bstride,
+                               void* const* gin, long long gin_bstride, const XlProg* prog,
+                               void* const* pgrad) {
+  if (batch < 1 || comps < 1 || comps > 3 || ny < 1 || nx < 1 || !in || !gout || !gin || !prog) {
+    set_error("xl_ops_backward: bad arguments");
+    return XL_EINVAL;
+  }
+  if (prog->nops < 0 || prog->nops > XL_MAX_OPS) {
+    set_error("xl_ops_backward: op program too long");
+    return XL_EINVAL;
+  }
+  OpsBwdLaunch p;
+  p.B = batch; p.C = comps; p.ny = ny; p.nx = nx;
+  p.ibs = in_bstride; p.gbs = gout_bstride; p.ginbs = gin_bstride;
+  for (int c = 0; c < 3; ++c) {
+    p.in[c] = c < comps ? (const float2*)in[c] : nullptr;
+    p.gout[c] = c < comps ? (const float2*)gout[c] : nullptr;
+    p.gin[c] = c < comps ? (float2*)gin[c] : nullptr;
+    if (c < comps && ((!p.in[c] && c == 0) || !p.gout[c])) {
+      set_error("xl_ops_backward: null plane %d", c);
+      return XL_EINVAL;
+    }
+  }
+  p.prog = *prog;
+  for (int q = 0; q < XL_MAX_OPS * 4; ++q) p.pgrad[q] = pgrad ? pgrad[q] : nullptr;
+  const long long npix = (long long)ny * nx;
+  int blocks = (int)((npix + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  ops_backward_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(p);
+  XL_CHECK_LAUNCH("ops_backward_kernel");
+  return XL_OK;
+}
 
 extern "C" int xl_apply_ops(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
                             long long in_bstride, void* const* out, long long out_bstride,

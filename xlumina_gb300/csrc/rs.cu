@@ -167,6 +167,7 @@ struct RsLaunch {
   const int* sidx;
   float2* work;
   XlProg pre, post;
+  int adjoint;
 };
 
 // Row pass: prologue (Jones program; VRS Ez derived at load) and, per
@@ -195,11 +196,12 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
     float2 e[3];
     e[0] = p.in[0][off];
     e[1] = p.cin > 1 ? p.in[1][off] : make_float2(0.f, 0.f);
-    e[2] = make_float2(0.f, 0.f);
+    e[2] = p.cin > 2 ? p.in[2][off] : make_float2(0.f, 0.f);
     PixelCtx px{r, n, (long long)r * p.nx + n, b};
     apply_prog(p.pre, e, px);
     stage[(s * ns) * p.nx + n] = e[0];
     if (ns > 1) stage[(s * ns + 1) * p.nx + n] = e[1];
+    if (ns > 2) stage[(s * ns + 2) * p.nx + n] = e[2];
   }
   __syncthreads();
 
@@ -276,8 +278,13 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const 
       }
       block_fft_s<LOGQ, -1>(v, j, xb, stw);
       const float2* sp = spec + (long long)par * C::Q * W;
+      if (p.adjoint) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], sp[(long long)(j + m * C::T) * W]);
+        for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], sp[(long long)(j + m * C::T) * W]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], sp[(long long)(j + m * C::T) * W]);
+      }
       block_fft_s<LOGQ, 1>(v, j, xb, stw);
       if (par == 0) {
 #pragma unroll
@@ -301,7 +308,8 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
   const int nc = p.cout;
-  const bool epi = p.post.nops > 0;
+  const bool fold = p.adjoint && nc == 3;      // VRS adjoint: Ez gradient folded into Ex, Ey
+  const bool epi = p.post.nops > 0 || fold;
   float2* xch = smem;                           // RPC x XS
   float2* stw = xch + C::RPC * C::XS;           // TW
   float2* yb = stw + C::TW;                     // RPC x Q: even-half result
@@ -352,9 +360,17 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
       const float2 zero = make_float2(0.f, 0.f);
       float2 e[3] = {stage[(s * nc) * p.nx + n], nc > 1 ? stage[(s * nc + 1) * p.nx + n] : zero,
                      nc > 2 ? stage[(s * nc + 2) * p.nx + n] : zero};
+      const long long o = (long long)b * p.obs + (long long)ro * p.nx + n;
+      if (fold) {  // adjoint of Ez = Ex X/r + Ey Y/r (vectorized_optics.py:258-261)
+        const float zb = (float)p.z[b];
+        const float X = (float)p.x[n], Y = (float)p.y[ro];
+        const float inv = rsqrtf(X * X + Y * Y + zb * zb);
+        p.out[0][o] = cadd(e[0], cscale(e[2], X * inv));
+        p.out[1][o] = cadd(e[1], cscale(e[2], Y * inv));
+        continue;
+      }
       PixelCtx px{ro, n, (long long)ro * p.nx + n, b};
       apply_prog(p.post, e, px);
-      const long long o = (long long)b * p.obs + (long long)ro * p.nx + n;
       p.out[0][o] = e[0];
       if (nc > 1) p.out[1][o] = e[1];
       if (nc > 2) p.out[2][o] = e[2];
@@ -406,8 +422,9 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::CONV_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
   } else {
+    const bool stage_out = p.post.nops || (p.adjoint && p.cout == 3);
     const size_t sm = (size_t)(C::RPC * C::XS + C::TW + C::RPC * C::Q +
-                               (p.post.nops ? C::RPC * p.cout * p.nx : 0)) * sizeof(float2);
+                               (stage_out ? C::RPC * p.cout * p.nx : 0)) * sizeof(float2);
     if ((e = allow_smem(rs_rows_inv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_inv smem");
     rs_rows_inv<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_rows_inv");
@@ -496,15 +513,21 @@ static int rs_run(void* stream, const XlRsArgs* a, int stage) {
     return XL_EINVAL;
   }
   const bool scalar = a->comps_in == 1 && a->comps_out == 1;
-  const bool vector = a->comps_in == 2 && a->comps_out == 3;
+  const bool vector = a->adjoint ? (a->comps_in == 3 && a->comps_out == 3)
+                                 : (a->comps_in == 2 && a->comps_out == 3);
   if (!scalar && !vector) {
-    set_error("xl_rs_propagate: comps_in/comps_out must be 1/1 (RS) or 2/3 (VRS), got %d/%d",
-              a->comps_in, a->comps_out);
+    set_error("xl_rs_propagate: comps_in/comps_out must be 1/1 (RS), 2/3 (VRS) or 3/3 (VRS adjoint), "
+              "got %d/%d (adjoint=%d)", a->comps_in, a->comps_out, a->adjoint);
     return XL_EINVAL;
   }
+  if (a->adjoint && (a->pre.nops || a->post.nops)) {
+    set_error("xl_rs_propagate: the adjoint takes no fused programs");
+    return XL_EINVAL;
+  }
+  const int nout = (a->adjoint && vector) ? 2 : a->comps_out;
   for (int c = 0; c < a->comps_in; ++c)
     if (!a->in[c]) { set_error("xl_rs_propagate: null input plane %d", c); return XL_EINVAL; }
-  for (int c = 0; c < a->comps_out; ++c)
+  for (int c = 0; c < nout; ++c)
     if (!a->out[c]) { set_error("xl_rs_propagate: null output plane %d", c); return XL_EINVAL; }
   if (!a->spectrum || !a->work) {
     set_error("xl_rs_propagate: null spectrum or workspace");
@@ -530,6 +553,7 @@ static int rs_run(void* stream, const XlRsArgs* a, int stage) {
   p.spec = (const float2*)a->spectrum; p.sstride = a->spectrum_stride; p.sidx = a->spectrum_index;
   p.work = (float2*)a->work;
   p.pre = a->pre; p.post = a->post;
+  p.adjoint = a->adjoint ? 1 : 0;
   cudaStream_t st = (cudaStream_t)stream;
   const int lq = rs_logq(a->ny, a->nx);
 #define CALL(L) launch_propagate<L>(st, p, stage)

@@ -57,7 +57,7 @@ def as_real_param(a, dev=None):
     if isinstance(a, (int, float, np.floating, np.integer)):
         return float(a)
     if isinstance(a, torch.Tensor):
-        if a.dim() == 0:
+        if a.dim() == 0 and not a.requires_grad:
             return float(a.item())
         return a.to(device=dev or device(), dtype=torch.float32).contiguous()
     arr = np.asarray(a)
@@ -146,6 +146,9 @@ class JonesOp:
         pmask = 0
         pbstride = 0
         for i, p in enumerate(self.params):
+            if isinstance(p, torch.Tensor) and p.dim() < 2:
+                raise ValueError("a mask parameter must be a scalar or an (ny, nx) plane; a 0-d tensor "
+                                 "that requires grad must be expanded to the plane by the caller")
             if isinstance(p, torch.Tensor):
                 if p.shape[-2:] != (ny, nx):
                     raise ValueError(f"mask parameter has shape {tuple(p.shape)}, field is {(ny, nx)}")
@@ -254,6 +257,40 @@ def apply_ops(comps, ops, ny, nx):
     return outs
 
 
+def ops_backward(base, gout, ops, ny, nx, want_input=True):
+    """Backward of a Jones program.  ``base``: the program's input planes (None
+    for a plane that is zero); ``gout``: gradients of its output planes.
+    Returns (input gradients, {(op, slot): parameter gradient})."""
+    L = lib()
+    C = len(gout)
+    ref = next(t for t in gout if t is not None)
+    lead = ref.shape[:-2]
+    B = int(np.prod(lead)) if len(lead) else 1
+    dev = ref.device
+    gin = [torch.empty_like(ref) if (want_input and i < len(base) and base[i] is not None) else None
+           for i in range(C)]
+    pgrad = (ctypes.c_void_p * (_lib.XL_MAX_OPS * 4))()
+    grads = {}
+    for k, o in enumerate(ops):
+        for q, p in enumerate(o.params):
+            if isinstance(p, torch.Tensor):
+                if not p.requires_grad:
+                    continue
+                t = torch.empty(p.shape, dtype=torch.float32, device=dev)
+            else:
+                continue
+            grads[(k, q)] = t
+            pgrad[k * 4 + q] = t.data_ptr()
+    prog = _lib.XlProg()
+    fill_prog(prog, ops, ny, nx)
+    inp = (ctypes.c_void_p * 3)(*[(b.data_ptr() if b is not None else 0) for b in base] + [0] * (3 - len(base)))
+    go = (ctypes.c_void_p * 3)(*[g.data_ptr() for g in gout] + [0] * (3 - C))
+    gi = (ctypes.c_void_p * 3)(*[(g.data_ptr() if g is not None else 0) for g in gin] + [0] * (3 - C))
+    _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ny * nx, go, ny * nx, gi, ny * nx,
+                                 ctypes.byref(prog), pgrad), "xl_ops_backward")
+    return gin, grads
+
+
 # ------------------------------------------------------ RS transfer spectra --
 
 class SpectrumCache:
@@ -325,7 +362,8 @@ class RsCall:
     ``z`` is a float or a sequence of B floats (one transfer spectrum per
     distinct value, from the cache)."""
 
-    def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None):
+    def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None,
+                 adjoint=False):
         L = lib()
         x = as_grid(x)
         y = as_grid(y)
@@ -334,8 +372,8 @@ class RsCall:
         lead = comps[0].shape[:-2]
         if comps[0].shape[-2:] != (ny, nx):
             raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid ({ny}, {nx})")
-        if len(comps) != (2 if vector else 1):
-            raise ValueError("RS takes one field, VRS takes (Ex, Ey)")
+        if len(comps) != (1 if not vector else (3 if adjoint else 2)):
+            raise ValueError("RS takes one field, VRS takes (Ex, Ey) (adjoint: three gradients)")
         B = int(np.prod(lead)) if len(lead) else 1
         zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
         uniq = sorted(set(zs))
@@ -351,7 +389,8 @@ class RsCall:
         if work is None:
             work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
-            outs = [torch.empty(comps[0].shape, dtype=torch.complex64, device=dev) for _ in range(cout)]
+            nout = 2 if (adjoint and vector) else cout
+            outs = [torch.empty(comps[0].shape, dtype=torch.complex64, device=dev) for _ in range(nout)]
         zt = torch.as_tensor(zs, dtype=torch.float64, device=dev) if vector else None
         a = _lib.XlRsArgs()
         a.batch = B
@@ -374,6 +413,7 @@ class RsCall:
         a.work = work.data_ptr()
         fill_prog(a.pre, pre, ny, nx)
         fill_prog(a.post, post, ny, nx)
+        a.adjoint = 1 if adjoint else 0
         self.args = a
         self.outs = outs
         self.batch, self.ny, self.nx, self.comps = B, ny, nx, cout
@@ -474,14 +514,17 @@ def bluestein_plan(m, f1, f2, Dm, M):
 _chirp_cache: "collections.OrderedDict" = collections.OrderedDict()
 
 
-def device_chirps(m, f1, f2, Dm, M):
-    key = (int(m), float(f1), float(f2), float(Dm), int(M), torch.cuda.current_device())
+def device_chirps(m, f1, f2, Dm, M, adjoint=False):
+    """Chirp vectors on the device; the adjoint set is (conj(post) L, conj(g), conj(pre) / L)."""
+    key = (int(m), float(f1), float(f2), float(Dm), int(M), bool(adjoint), torch.cuda.current_device())
     with _LOCK:
         v = _chirp_cache.get(key)
         if v is not None:
             _chirp_cache.move_to_end(key)
             return v
     L, pre, g, post = bluestein_plan(m, f1, f2, Dm, M)
+    if adjoint:
+        pre, g, post = np.conj(post) * L, np.conj(g), np.conj(pre) / L
     dev = device()
     v = (L,) + tuple(torch.as_tensor(a, device=dev).to(torch.complex64) for a in (pre, g, post))
     with _LOCK:
@@ -498,36 +541,42 @@ class CztCall:
     "high_na": optical_elements.py:600-638 (the lens op must be in ``pre``,
     ``lens`` = (radius, f, sin_theta_max))."""
 
-    def __init__(self, comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None, outs=None):
+    def __init__(self, comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None, outs=None,
+                 adjoint=False):
         L = lib()
         x, y, xout, yout = (as_grid(a) for a in (x, y, xout, yout))
         ny, nx, my, mx = len(y), len(x), len(yout), len(xout)
         comps = [as_field(c) for c in comps]
-        if comps[0].shape[-2:] != (ny, nx):
-            raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid ({ny}, {nx})")
+        if comps[0].shape[-2:] != ((my, mx) if adjoint else (ny, nx)):
+            raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid")
         lead = comps[0].shape[:-2]
         B = int(np.prod(lead)) if len(lead) else 1
         dev = comps[0].device
         if mode == "high_na":
             r, f, s_max = lens
             Dm = f * wavelength * (nx - 1) / (2 * r)
-            cmode, cin, cout = _lib.XL_CZT_PLAIN, len(comps), 3
+            cmode, cin, cout = _lib.XL_CZT_PLAIN, (3 if adjoint else len(comps)), 3
             cte = -(1j * s_max ** 2 / (f * wavelength))
             zz = 0.0
         else:
             Dm = wavelength * z / (x[1] - x[0])
             cmode = _lib.XL_CZT_SCALAR if mode == "scalar" else _lib.XL_CZT_VECTOR
-            cin, cout = (1, 1) if mode == "scalar" else (2, 3)
+            cin, cout = (1, 1) if mode == "scalar" else ((3 if adjoint else 2), 3)
             cte = z * (x[1] - x[0]) * (y[1] - y[0]) * wavelength
             zz = float(z)
-        Lx, prex, gx, postx = device_chirps(nx, xout[0] + Dm / 2, xout[-1] + Dm / 2, Dm, mx)
-        Ly, prey, gy, posty = device_chirps(ny, yout[0] + Dm / 2, yout[-1] + Dm / 2, Dm, my)
+        Lx, prex, gx, postx = device_chirps(nx, xout[0] + Dm / 2, xout[-1] + Dm / 2, Dm, mx, adjoint)
+        Ly, prey, gy, posty = device_chirps(ny, yout[0] + Dm / 2, yout[-1] + Dm / 2, Dm, my, adjoint)
+        if adjoint:   # the call reads the forward's output plane and writes its input plane
+            x, y, xout, yout = xout, yout, x, y
+            ny, nx, my, mx = my, mx, ny, nx
         work = torch.empty(L.xl_czt_work_bytes(B, cout, ny, mx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
-            outs = [torch.empty(tuple(lead) + (my, mx), dtype=torch.complex64, device=dev) for _ in range(cout)]
+            nout = 2 if (adjoint and cmode == _lib.XL_CZT_VECTOR) else cout
+            outs = [torch.empty(tuple(lead) + (my, mx), dtype=torch.complex64, device=dev) for _ in range(nout)]
         a = _lib.XlCztArgs()
         a.batch, a.comps_in, a.comps_out, a.mode = B, cin, cout, cmode
         a.ny, a.nx, a.my, a.mx = ny, nx, my, mx
+        a.adjoint = 1 if adjoint else 0
         a.log2_lx, a.log2_ly = int(Lx).bit_length() - 1, int(Ly).bit_length() - 1
         for i, c in enumerate(comps):
             a.inp[i] = c.data_ptr()

@@ -13,7 +13,7 @@ import time
 import numpy as np
 import torch
 
-from . import cm, engine, um  # noqa: F401  (units re-exported as in the reference)
+from . import autograd, cm, engine, um  # noqa: F401  (units re-exported as in the reference)
 from .toolbox import build_LCD_cell, rotate_mask  # noqa: F401
 from .vectorized_optics import VectorizedLight
 from .wave_optics import ScalarLight, _report
@@ -124,7 +124,7 @@ def high_NA_objective_lens(input_field, radius, f):
     op, s_max = engine.op_high_na(input_field.x, input_field.y, radius, f)
     E = input_field._base()
     ny, nx = len(input_field.y), len(input_field.x)
-    out = engine.apply_ops(E, input_field._ops + [op], ny, nx)
+    out = autograd.apply_ops(E, input_field._ops + [op], ny, nx)
     return torch.stack(out), s_max
 
 
@@ -143,8 +143,14 @@ def VCZT_objective_lens(input_field, r, f, xout, yout):
     yout = engine.as_grid(yout)
     op, s_max = engine.op_high_na(input_field.x, input_field.y, r, f)
     E = input_field._base(2)
-    outs = engine.czt_propagate(E, input_field.x, input_field.y, input_field.wavelength, None, xout, yout,
-                                mode="high_na", pre=input_field._ops + [op], lens=(r, f, s_max))
+    ops = input_field._ops + [op]
+    if autograd.needs_grad(E, ops):
+        plan = autograd.CztPlan(input_field.x, input_field.y, input_field.wavelength, None, xout, yout,
+                                "high_na", ops, lens=(r, f, s_max))
+        outs = autograd.fused_propagate(plan, E, 3)
+    else:
+        outs = engine.czt_propagate(E, input_field.x, input_field.y, input_field.wavelength, None, xout, yout,
+                                    mode="high_na", pre=ops, lens=(r, f, s_max))
     _report("VCZT through objective lens", tic)
     return VectorizedLight._wrap(xout, yout, input_field.wavelength, outs)
 

@@ -12,7 +12,7 @@ import time
 import numpy as np
 import torch
 
-from . import engine
+from . import autograd, engine
 from .wave_optics import _Grid, _report
 
 
@@ -49,7 +49,7 @@ class VectorizedLight(_Grid):
         if self._ops:
             E = self._base()
             ny, nx = E[0].shape[-2:]
-            self._E = engine.apply_ops(E, self._ops, ny, nx)
+            self._E = autograd.apply_ops(E, self._ops, ny, nx)
             self._ops = []
         for i in range(3):
             if self._E[i] is None:
@@ -81,7 +81,11 @@ class VectorizedLight(_Grid):
         tic = time.perf_counter()
         qf = engine.quality_factor(self.x, self.y, self.wavelength, z)
         E = self._base(2)
-        Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, z, vector=True, pre=self._ops)
+        if autograd.needs_grad(E, self._ops):
+            plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, True, self._ops)
+            Ex, Ey, Ez = autograd.fused_propagate(plan, E, 3)
+        else:
+            Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, z, vector=True, pre=self._ops)
         _report("VRS", tic)
         return VectorizedLight._wrap(self.x, self.y, self.wavelength, [Ex, Ey, Ez]), qf
 
@@ -104,8 +108,12 @@ class VectorizedLight(_Grid):
         xout = self.x if xout is None else engine.as_grid(xout)
         yout = self.y if yout is None else engine.as_grid(yout)
         E = self._base(2)
-        outs = engine.czt_propagate(E, self.x, self.y, self.wavelength, z, xout, yout, mode="vczt",
-                                    pre=self._ops)
+        if autograd.needs_grad(E, self._ops):
+            plan = autograd.CztPlan(self.x, self.y, self.wavelength, z, xout, yout, "vczt", self._ops)
+            outs = autograd.fused_propagate(plan, E, 3)
+        else:
+            outs = engine.czt_propagate(E, self.x, self.y, self.wavelength, z, xout, yout, mode="vczt",
+                                        pre=self._ops)
         _report("VCZT", tic)
         return VectorizedLight._wrap(xout, yout, self.wavelength, outs)
 

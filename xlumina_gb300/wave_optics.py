@@ -14,7 +14,7 @@ import time
 import numpy as np
 import torch
 
-from . import engine
+from . import autograd, engine
 
 _PRINT_TIMES = os.environ.get("XL_PRINT_TIMES", "0") not in ("", "0")
 
@@ -81,7 +81,7 @@ class ScalarLight(_Grid):
             self._field = torch.zeros((len(self.x), len(self.y)), dtype=torch.complex64, device=engine.device())
         if self._ops:
             ny, nx = self._field.shape[-2:]
-            self._field = engine.apply_ops([self._field], self._ops, ny, nx)[0]
+            self._field = autograd.apply_ops([self._field], self._ops, ny, nx)[0]
             self._ops = []
         return self._field
 
@@ -136,8 +136,12 @@ class ScalarLight(_Grid):
         """wave_optics.py:173-196: returns (ScalarLight, quality_factor)."""
         tic = time.perf_counter()
         qf = engine.quality_factor(self.x, self.y, self.wavelength, z)
-        out = engine.rs_propagate([self._base()], self.x, self.y, self.wavelength, z, vector=False,
-                                  pre=self._ops)[0]
+        base = [self._base()]
+        if autograd.needs_grad(base, self._ops):
+            plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, False, self._ops)
+            out = autograd.fused_propagate(plan, base, 1)[0]
+        else:
+            out = engine.rs_propagate(base, self.x, self.y, self.wavelength, z, vector=False, pre=self._ops)[0]
         _report("RS", tic)
         return ScalarLight._wrap(self.x, self.y, self.wavelength, out), qf
 
@@ -159,8 +163,13 @@ class ScalarLight(_Grid):
         tic = time.perf_counter()
         xout = self.x if xout is None else engine.as_grid(xout)
         yout = self.y if yout is None else engine.as_grid(yout)
-        out = engine.czt_propagate([self._base()], self.x, self.y, self.wavelength, z, xout, yout,
-                                   mode="scalar", pre=self._ops)[0]
+        base = [self._base()]
+        if autograd.needs_grad(base, self._ops):
+            plan = autograd.CztPlan(self.x, self.y, self.wavelength, z, xout, yout, "scalar", self._ops)
+            out = autograd.fused_propagate(plan, base, 1)[0]
+        else:
+            out = engine.czt_propagate(base, self.x, self.y, self.wavelength, z, xout, yout,
+                                       mode="scalar", pre=self._ops)[0]
         _report("CZT", tic)
         return ScalarLight._wrap(xout, yout, self.wavelength, out)
 
