@@ -287,9 +287,138 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "spectrum_builds": engine.SPECTRA.builds,
     }
+    if not args.no_fwd_bwd:
+        del call, Ex_d, Ey_d, eta_d, theta_d, h_Ex, h_Ey, h_eta, h_theta, h_out
+        torch.cuda.empty_cache()
+        line["fwd_bwd"] = run_fwd_bwd()
+    if not args.no_serving:
+        line["serving"] = run_serving(args.serve_requests)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
     print(json.dumps(line))
+
+
+def _time_steps(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / 1e3 / steps
+
+
+def run_fwd_bwd(steps=10, warmup=3):
+    """fwd+bwd optimisation steps through the hand-written adjoints: the batched
+    form (one step over the whole batch) and the plain form (one table per call)."""
+    import torch
+
+    from xlumina_gb300.tables import FourFTable, HighNATable
+    out = {}
+    t4 = FourFTable()
+    dt = _time_steps(t4.step, steps, warmup)
+    single = lambda i=[0]: t4.step(t4.inputs[i[0] % t4.B:i[0] % t4.B + 1], t4.target[i[0] % t4.B:i[0] % t4.B + 1])  # noqa: E731
+    dt1 = _time_steps(single, t4.B, 2)
+    out["four_f"] = {"workload": "4f table 16 x 1024^2 (SLM1 -> RS 25 cm -> lens -> CZT 512^2 ROI -> SLM2 -> CZT), "
+                                 "532 nm, normalised intensity MSE, AdamW",
+                     "steps_per_s": 1.0 / dt, "tables_per_s": t4.B / dt, "plain_tables_per_s": 1.0 / dt1,
+                     "batch": t4.B}
+    del t4
+    torch.cuda.empty_cache()
+    th = HighNATable()
+    dt = _time_steps(th.step, max(2, steps // 2), 2)
+    out["high_na"] = {"workload": "high-NA table 32 x 2048^2 -> 1024^2 focal ROI (2 um), 650 nm, NA 0.9, f 3 mm, "
+                                  "LCD + sSLM, Ez spot loss, AdamW", "steps_per_s": 1.0 / dt,
+                      "tables_per_s": th.B / dt, "batch": th.B}
+    del th
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_serving(n_req=10000, seed=4000):
+    """Poisson stream of mixed requests (sizes 256..2048 with weights .4/.3/.2/.1; RS, VRS, CZT
+    or an SLM-phase gradient; z uniform in [1, 20] cm) through the continuous-batching server,
+    against the plain path (one call per request, in order)."""
+    import threading
+
+    import torch
+
+    from xlumina_gb300 import toolbox
+    from xlumina_gb300.serving import Request, Server, run_batch
+    rng = np.random.default_rng(seed)
+    sizes = np.array([256, 512, 1024, 2048])
+    kinds = ["rs", "vrs", "czt", "grad"]
+    pool = {}
+    for n in sizes:
+        g = torch.Generator(device="cuda").manual_seed(int(n))
+        f = lambda: torch.randn((int(n), int(n)), dtype=torch.complex64, device="cuda", generator=g)  # noqa: E731
+        x, y = toolbox.space(2000.0 * n / 2048, int(n))
+        xo, yo = toolbox.space(200.0 * n / 2048, int(n) // 2)
+        pool[int(n)] = dict(f=[f(), f()], x=x, y=y, xo=xo, yo=yo,
+                            ph=torch.rand((int(n), int(n)), device="cuda", generator=g) * 6.2832 - 3.1416,
+                            tgt=torch.rand((int(n), int(n)), device="cuda", generator=g))
+
+    def make(i):
+        n = int(rng.choice(sizes, p=[0.4, 0.3, 0.2, 0.1]))
+        k = kinds[int(rng.integers(4))]
+        z = float(rng.uniform(1e4, 2e5))
+        p = pool[n]
+        if k == "czt":
+            return Request(k, [p["f"][0]], p["x"], p["y"], 0.633, z, xout=p["xo"], yout=p["yo"])
+        if k == "grad":
+            return Request(k, [p["f"][0]], p["x"], p["y"], 0.633, z, phase=p["ph"], target=p["tgt"])
+        return Request(k, p["f"][:1 if k == "rs" else 2], p["x"], p["y"], 0.633, z)
+
+    # plain path: one call per request, each waited for
+    n_plain = min(600, n_req)
+    plain_reqs = [make(i) for i in range(n_plain)]
+    for r in plain_reqs[:20]:
+        run_batch([r])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat = []
+    for r in plain_reqs:
+        t1 = time.perf_counter()
+        run_batch([r])
+        torch.cuda.synchronize()
+        lat.append(time.perf_counter() - t1)
+    plain_rate = n_plain / (time.perf_counter() - t0)
+
+    rate = 0.8 * plain_rate * 1.5   # offered load: above the plain path's capacity, inside the batched one
+    reqs = [make(i) for i in range(n_req)]
+    gaps = rng.exponential(1.0 / rate, n_req)
+    srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2)
+    futs = [None] * n_req
+
+    def client():
+        t = time.perf_counter()
+        for i, r in enumerate(reqs):
+            t += gaps[i]
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            futs[i] = srv.submit(r)
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    for f in futs:
+        f.result(timeout=600)
+    wall = time.perf_counter() - t0
+    srv.close()
+    st = srv.stats()
+    return {"workload": "10,000 Poisson requests, sizes 256/512/1024/2048 (.4/.3/.2/.1), RS/VRS/CZT/grad, "
+                        "z U[1,20] cm, HBM budget 150 GB",
+            "requests": n_req, "offered_req_per_s": rate, "served_req_per_s": n_req / wall,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_batch": st["mean_batch"],
+            "plain_req_per_s": plain_rate, "plain_p50_ms": float(np.percentile(np.asarray(lat) * 1e3, 50)),
+            "plain_p99_ms": float(np.percentile(np.asarray(lat) * 1e3, 99))}
 
 
 def main():
@@ -300,6 +429,9 @@ def main():
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--impl", default="xlgb", choices=["xlgb", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fwd-bwd", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -196,3 +196,40 @@ def test_adjoint_dot_product_identity(mods):
     lhs = sum(dot(a, b) for a, b in zip(Au, ws))
     rhs = dot(ux, Ahw[0]) + dot(uy, Ahw[1])
     assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+
+
+def test_prebuilt_tables_step(mods):
+    torch, tr, wo, vo, oe, lf = mods
+    from xlumina_gb300.tables import FourFTable, HighNATable
+    t4 = FourFTable(n=128, roi_n=64, batch=4, half_width=400.0, f=2.0e4, roi_half_width=150.0, waist=300.0)
+    p0 = t4.phase1.detach().clone()
+    l0 = t4.step().item()
+    l1 = t4.step().item()
+    assert np.isfinite(l0) and np.isfinite(l1)
+    assert not torch.equal(p0, t4.phase1.detach())
+    th = HighNATable(n=128, roi_n=64, batch=3, half_width=1500.0, f=2000.0, waist=1200.0)
+    a0 = th.alpha.detach().clone()
+    assert np.isfinite(th.step().item())
+    assert not torch.equal(a0, th.alpha.detach())
+
+
+def test_broadcast_batch_inputs_match_materialised(mods):
+    torch, tr, wo, vo, oe, lf = mods
+    from xlumina_gb300 import engine
+    n = 128
+    x, y = ref.space(300.0, n)
+    rng = np.random.default_rng(8)
+    e = torch.as_tensor((rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64),
+                        device="cuda")
+    a = torch.as_tensor(rng.uniform(0, 6, (3, n, n)).astype(np.float32), device="cuda")
+    ops = [engine.op_sslm(a, a)]
+    xo, yo = ref.space(100.0, 64)
+    b1 = engine.rs_propagate([e.expand(3, n, n), e.expand(3, n, n)], x, y, 0.6, [1e4, 2e4, 3e4], True, pre=ops)
+    b2 = engine.rs_propagate([e.expand(3, n, n).contiguous(), e.expand(3, n, n).contiguous()], x, y, 0.6,
+                             [1e4, 2e4, 3e4], True, pre=ops)
+    for u, v in zip(b1, b2):
+        assert torch.equal(u, v)
+    c1 = engine.czt_propagate([e.expand(3, n, n), e.expand(3, n, n)], x, y, 0.6, 2e4, xo, yo, "vczt", pre=ops)
+    c2 = engine.czt_propagate([e.expand(3, n, n).contiguous()] * 2, x, y, 0.6, 2e4, xo, yo, "vczt", pre=ops)
+    for u, v in zip(c1, c2):
+        assert torch.equal(u, v)

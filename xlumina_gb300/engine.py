@@ -52,6 +52,21 @@ def as_field(a, dev=None) -> torch.Tensor:
     return torch.as_tensor(np.asarray(a), device=dev).to(torch.complex64).contiguous()
 
 
+def batch_planes(comps, ny, nx):
+    """Component planes for a launch: (tensors, batch, batch stride in elements).
+
+    A batch of fields that is one plane broadcast along the batch (an
+    ``expand``-ed view, stride 0) is passed without copying, with batch stride 0.
+    """
+    comps = [c if isinstance(c, torch.Tensor) else as_field(c) for c in comps]
+    lead = comps[0].shape[:-2]
+    B = int(np.prod(lead)) if len(lead) else 1
+    if B > 1 and all(c.dim() == 3 and c.stride(0) == 0 and c.dtype == torch.complex64 and c.is_cuda and
+                     c[0].is_contiguous() for c in comps):
+        return [c[0] for c in comps], B, 0
+    return [as_field(c) for c in comps], B, ny * nx
+
+
 def as_real_param(a, dev=None):
     """A mask parameter: python float for scalars, else a float32 contiguous CUDA tensor."""
     if isinstance(a, (int, float, np.floating, np.integer)):
@@ -244,15 +259,14 @@ def op_cmul(mask: torch.Tensor):
 def apply_ops(comps, ops, ny, nx):
     """Materialise a Jones program on 1..3 component planes; returns new tensors."""
     L = lib()
-    comps = [as_field(c) for c in comps]
     lead = comps[0].shape[:-2]
-    B = int(np.prod(lead)) if len(lead) else 1
-    outs = [torch.empty_like(comps[0]) for _ in comps]
+    comps, B, ibs = batch_planes(comps, ny, nx)
+    outs = [torch.empty(tuple(lead) + (ny, nx), dtype=torch.complex64, device=comps[0].device) for _ in comps]
     prog = _lib.XlProg()
     fill_prog(prog, ops, ny, nx)
     inp = (ctypes.c_void_p * 3)(*[c.data_ptr() for c in comps] + [0] * (3 - len(comps)))
     out = (ctypes.c_void_p * 3)(*[o.data_ptr() for o in outs] + [0] * (3 - len(outs)))
-    _lib.check(L.xl_apply_ops(stream_handle(), B, len(comps), ny, nx, inp, ny * nx, out, ny * nx,
+    _lib.check(L.xl_apply_ops(stream_handle(), B, len(comps), ny, nx, inp, ibs, out, ny * nx,
                               ctypes.byref(prog)), "xl_apply_ops")
     return outs
 
@@ -267,6 +281,10 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
     lead = ref.shape[:-2]
     B = int(np.prod(lead)) if len(lead) else 1
     dev = ref.device
+    present = [b for b in base if b is not None]
+    planes, _, ibs = batch_planes(present, ny, nx) if present else ([], B, ny * nx)
+    it = iter(planes)
+    base = [next(it) if b is not None else None for b in base]
     gin = [torch.empty_like(ref) if (want_input and i < len(base) and base[i] is not None) else None
            for i in range(C)]
     pgrad = (ctypes.c_void_p * (_lib.XL_MAX_OPS * 4))()
@@ -286,7 +304,7 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
     inp = (ctypes.c_void_p * 3)(*[(b.data_ptr() if b is not None else 0) for b in base] + [0] * (3 - len(base)))
     go = (ctypes.c_void_p * 3)(*[g.data_ptr() for g in gout] + [0] * (3 - C))
     gi = (ctypes.c_void_p * 3)(*[(g.data_ptr() if g is not None else 0) for g in gin] + [0] * (3 - C))
-    _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ny * nx, go, ny * nx, gi, ny * nx,
+    _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ibs, go, ny * nx, gi, ny * nx,
                                  ctypes.byref(prog), pgrad), "xl_ops_backward")
     return gin, grads
 
@@ -352,6 +370,8 @@ def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
     _lib.check(L.xl_rs_transfer_spectrum(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(), float(z),
                                          float(wavelength), scale, spec.data_ptr(), work.data_ptr()),
                "xl_rs_transfer_spectrum")
+    # cached spectra are shared by every stream: finish the build before handing it out
+    torch.cuda.current_stream().synchronize()
     return spec
 
 
@@ -368,13 +388,12 @@ class RsCall:
         x = as_grid(x)
         y = as_grid(y)
         ny, nx = len(y), len(x)
-        comps = [as_field(c) for c in comps]
-        lead = comps[0].shape[:-2]
         if comps[0].shape[-2:] != (ny, nx):
             raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid ({ny}, {nx})")
         if len(comps) != (1 if not vector else (3 if adjoint else 2)):
             raise ValueError("RS takes one field, VRS takes (Ex, Ey) (adjoint: three gradients)")
-        B = int(np.prod(lead)) if len(lead) else 1
+        lead = comps[0].shape[:-2]
+        comps, B, ibs = batch_planes(comps, ny, nx)
         zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
         uniq = sorted(set(zs))
         specs = [SPECTRA.get(x, y, zz, wavelength) for zz in uniq]
@@ -390,7 +409,7 @@ class RsCall:
             work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
             nout = 2 if (adjoint and vector) else cout
-            outs = [torch.empty(comps[0].shape, dtype=torch.complex64, device=dev) for _ in range(nout)]
+            outs = [torch.empty(tuple(lead) + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(nout)]
         zt = torch.as_tensor(zs, dtype=torch.float64, device=dev) if vector else None
         a = _lib.XlRsArgs()
         a.batch = B
@@ -401,7 +420,7 @@ class RsCall:
             a.inp[i] = c.data_ptr()
         for i, o in enumerate(outs):
             a.out[i] = o.data_ptr()
-        a.in_bstride = ny * nx
+        a.in_bstride = ibs
         a.out_bstride = ny * nx
         if vector:
             a.x = device_grid(x).data_ptr()
@@ -546,11 +565,10 @@ class CztCall:
         L = lib()
         x, y, xout, yout = (as_grid(a) for a in (x, y, xout, yout))
         ny, nx, my, mx = len(y), len(x), len(yout), len(xout)
-        comps = [as_field(c) for c in comps]
         if comps[0].shape[-2:] != ((my, mx) if adjoint else (ny, nx)):
             raise ValueError(f"field shape {tuple(comps[0].shape)} does not match the grid")
         lead = comps[0].shape[:-2]
-        B = int(np.prod(lead)) if len(lead) else 1
+        comps, B, ibs = batch_planes(comps, *comps[0].shape[-2:])
         dev = comps[0].device
         if mode == "high_na":
             r, f, s_max = lens
@@ -582,7 +600,7 @@ class CztCall:
             a.inp[i] = c.data_ptr()
         for i, o in enumerate(outs):
             a.out[i] = o.data_ptr()
-        a.in_bstride, a.out_bstride = ny * nx, my * mx
+        a.in_bstride, a.out_bstride = (ibs if ibs == 0 else ny * nx), my * mx
         gx_, gy_, gxo, gyo = (device_grid(v) for v in (x, y, xout, yout))
         a.x, a.y, a.xout, a.yout = gx_.data_ptr(), gy_.data_ptr(), gxo.data_ptr(), gyo.data_ptr()
         a.z, a.wavelength = zz, float(wavelength)

@@ -1,0 +1,112 @@
+"""Prebuilt optimisation tables on the propagation path (one fwd+bwd step each).
+
+* ``FourFTable``: SLM1 -> RS(f) -> thin lens(f) -> CZT to an ROI -> SLM2 -> CZT,
+  matched to target intensities with the normalised intensity MSE; a batch of
+  input masks shares the SLM parameters (the structure of
+  experiments/four_f_optical_table.py:36-127, with the table's propagators).
+* ``HighNATable``: LCD + sSLM -> VCZT through a high-NA objective lens, with an
+  Ez-weighted focal-spot loss (small_area_hybrid, loss_functions.py:24-40);
+  one set of sSLM phases per batch entry (the sharp-focus table of
+  experiments/hybrid_sharp_optical_table.py).
+
+Both are built only from the public API (``wave_optics``, ``vectorized_optics``,
+``optical_elements``), so a step runs the fused kernels forward and the
+hand-written adjoints backward.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import optical_elements as oe
+from . import toolbox
+from .vectorized_optics import VectorizedLight
+from .wave_optics import LightSource
+
+
+class FourFTable:
+    def __init__(self, n=1024, roi_n=512, batch=16, wavelength=0.532, half_width=1500.0, f=2.5e5,
+                 roi_half_width=1000.0, waist=1200.0, seed=2000, device="cuda"):
+        self.n, self.m, self.B, self.f = n, roi_n, batch, f
+        self.x, self.y = toolbox.space(half_width, n)
+        self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
+        self.wavelength = wavelength
+        self.lens_r = (half_width, half_width)
+        rng = np.random.default_rng(seed)
+        src = LightSource(self.x, self.y, wavelength)
+        src.gaussian_beam(w0=(waist, waist), E0=1)
+        masks = (rng.uniform(0, 1, (batch, n, n)) > 0.5).astype(np.float32)
+        self.inputs = src.field[None] * torch.as_tensor(masks, device=device)
+        tgt = (rng.uniform(0, 1, (batch, roi_n, roi_n)) < 0.1).astype(np.float32)
+        tgt /= tgt.sum(axis=(-2, -1), keepdims=True)
+        self.target = torch.as_tensor(tgt, device=device)
+        self.phase1 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (n, n)).astype(np.float32),
+                                      device=device).requires_grad_(True)
+        self.phase2 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32),
+                                      device=device).requires_grad_(True)
+        self.opt = torch.optim.AdamW([self.phase1, self.phase2], lr=0.05)
+
+    def loss(self, inputs=None, target=None):
+        inputs = self.inputs if inputs is None else inputs
+        target = self.target if target is None else target
+        light = LightSource(self.x, self.y, self.wavelength)
+        light.field = inputs
+        l1, _ = oe.SLM(light, self.phase1, self.n)
+        l2, _ = l1.RS_propagation(self.f)
+        l3, _ = oe.lens(l2, self.lens_r, (self.f, self.f))
+        l4 = l3.CZT(self.f, self.xo, self.yo)
+        l5, _ = oe.SLM(l4, self.phase2, self.m)
+        I = torch.abs(l5.CZT(self.f).field) ** 2
+        I = I / torch.sum(I, dim=(-2, -1), keepdim=True)
+        return torch.mean(torch.sum((I - target) ** 2, dim=(-2, -1)) / (self.m * self.m))
+
+    def step(self, inputs=None, target=None):
+        self.opt.zero_grad(set_to_none=True)
+        L = self.loss(inputs, target)
+        L.backward()
+        self.opt.step()
+        return L
+
+
+def small_area_hybrid_batched(I):
+    """loss_functions.py:24-40 for each leading-batch entry, then the mean."""
+    In = I / (torch.sum(I, dim=(-2, -1), keepdim=True) + 1e-08)
+    mx = torch.amax(In, dim=(-2, -1), keepdim=True)
+    mask = (In > 0.7 * mx).to(In.dtype)
+    return torch.mean(torch.sum(mask, dim=(-2, -1)) / (torch.sum(mask * In, dim=(-2, -1)) + 1e-08))
+
+
+class HighNATable:
+    def __init__(self, n=2048, roi_n=1024, batch=32, wavelength=0.650, half_width=2700.0, na=0.9,
+                 f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda"):
+        self.n, self.m, self.B = n, roi_n, batch
+        self.x, self.y = toolbox.space(half_width, n)
+        self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
+        self.wavelength, self.f, self.r = wavelength, f, na * f
+        rng = np.random.default_rng(seed)
+        src = LightSource(self.x, self.y, wavelength)
+        src.gaussian_beam(w0=(waist, waist), E0=1)
+        self.Ex = src.field
+        self.Ey = torch.zeros_like(src.field)
+        self.eta = torch.full((n, n), float(rng.uniform(0, 2 * np.pi)), device=device).requires_grad_(True)
+        self.theta = torch.full((n, n), float(rng.uniform(0, 2 * np.pi)), device=device).requires_grad_(True)
+        self.alpha = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
+                                     device=device).requires_grad_(True)
+        self.phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
+                                   device=device).requires_grad_(True)
+        self.opt = torch.optim.AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05)
+
+    def loss(self):
+        light = VectorizedLight(self.x, self.y, self.wavelength)
+        light.Ex = self.Ex.expand(self.B, self.n, self.n)
+        light.Ey = self.Ey.expand(self.B, self.n, self.n)
+        focus = oe.VCZT_objective_lens(oe.sSLM(oe.LCD(light, self.eta, self.theta), self.alpha, self.phi),
+                                       self.r, self.f, self.xo, self.yo)
+        return small_area_hybrid_batched(torch.abs(focus.Ez) ** 2)
+
+    def step(self):
+        self.opt.zero_grad(set_to_none=True)
+        L = self.loss()
+        L.backward()
+        self.opt.step()
+        return L
