@@ -7,57 +7,65 @@
 
 using namespace xl;
 
-struct Regs { float2 v[16]; };
+template <int E> struct Regs { float2 v[E]; };
 
-template <int LOGN, int DIR, int P>
-static void emu(std::vector<Regs>& V, float2* sm, const float2* tw) {
-  using S = FftShape<LOGN>;
-  for (int j = 0; j < S::T; ++j) fft_pass<LOGN, P, DIR>(V[j].v, j, sm, tw);
+template <int LOGN, int E, int DIR, int P>
+static void emu(std::vector<Regs<E>>& V, float2* sm, const float2* tw) {
+  using S = FftShape<LOGN, E>;
+  for (int j = 0; j < S::T; ++j) fft_pass<LOGN, E, P, DIR>(V[j].v, j, sm, tw);
   if constexpr (P < S::NPASS - 1) {
-    for (int j = 0; j < S::T; ++j) fft_gather<LOGN>(V[j].v, j, sm);
-    emu<LOGN, DIR, P + 1>(V, sm, tw);
+    for (int j = 0; j < S::T; ++j) fft_gather<LOGN, E>(V[j].v, j, sm);
+    emu<LOGN, E, DIR, P + 1>(V, sm, tw);
   }
 }
 
-template <int LOGN, int DIR, int P>
-static void emu_s(std::vector<Regs>& V, float2* sm, const float2* stw) {
-  using S = FftShape<LOGN>;
-  for (int j = 0; j < S::T; ++j) fft_pass_s<LOGN, P, DIR>(V[j].v, j, sm, stw);
+template <int LOGN, int E, int DIR, int P>
+static void emu_s(std::vector<Regs<E>>& V, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN, E>;
+  for (int j = 0; j < S::T; ++j) fft_pass_s<LOGN, E, P, DIR>(V[j].v, j, sm, stw);
   if constexpr (P < S::NPASS - 1) {
-    for (int j = 0; j < S::T; ++j) fft_gather<LOGN>(V[j].v, j, sm);
-    emu_s<LOGN, DIR, P + 1>(V, sm, stw);
+    for (int j = 0; j < S::T; ++j) fft_gather<LOGN, E>(V[j].v, j, sm);
+    emu_s<LOGN, E, DIR, P + 1>(V, sm, stw);
   }
 }
 
 static int g_use_stw = 0;
 
-template <int LOGN, int DIR>
-static void run(const float* in, float* out) {
-  using S = FftShape<LOGN>;
+static int g_e = 16;
+
+template <int LOGN, int E, int DIR>
+static void run_e(const float* in, float* out) {
+  using S = FftShape<LOGN, E>;
   std::vector<float2> tw(S::N), sm(S::SMEM);
   for (int q = 0; q < S::N; ++q) {
     double a = 2.0 * M_PI * q / S::N;
     tw[q] = make_float2((float)std::cos(a), (float)-std::sin(a));
   }
-  std::vector<Regs> V(S::T);
+  std::vector<Regs<E>> V(S::T);
   for (int j = 0; j < S::T; ++j)
-    for (int m = 0; m < 16; ++m) {
+    for (int m = 0; m < E; ++m) {
       int n = j + m * S::T;
       V[j].v[m] = make_float2(in[2 * n], in[2 * n + 1]);
     }
   if (g_use_stw) {
-    std::vector<float2> stw(FftTw<LOGN>::SIZE);
-    for (int i = 0; i < FftTw<LOGN>::SIZE; ++i) stw[i] = pass_twiddle_entry<LOGN>(i, tw.data());
-    emu_s<LOGN, DIR, 0>(V, sm.data(), stw.data());
+    std::vector<float2> stw(FftTw<LOGN, E>::SIZE);
+    for (int i = 0; i < FftTw<LOGN, E>::SIZE; ++i) stw[i] = pass_twiddle_entry<LOGN, E>(i, tw.data());
+    emu_s<LOGN, E, DIR, 0>(V, sm.data(), stw.data());
   } else {
-    emu<LOGN, DIR, 0>(V, sm.data(), tw.data());
+    emu<LOGN, E, DIR, 0>(V, sm.data(), tw.data());
   }
   for (int j = 0; j < S::T; ++j)
-    for (int m = 0; m < 16; ++m) {
+    for (int m = 0; m < E; ++m) {
       int n = j + m * S::T;
       out[2 * n] = V[j].v[m].x;
       out[2 * n + 1] = V[j].v[m].y;
     }
+}
+
+template <int LOGN, int DIR>
+static void run(const float* in, float* out) {
+  if (g_e == 8) run_e<LOGN, 8, DIR>(in, out);
+  else run_e<LOGN, 16, DIR>(in, out);
 }
 
 template <int DIR>
@@ -76,6 +84,8 @@ static int dispatch(int logn, const float* in, float* out) {
   }
   return -1;
 }
+
+extern "C" void fft_core_set_e(int e) { g_e = e; }
 
 extern "C" int fft_core_check_stw(int logn, int dir, const float* in, float* out) {
   g_use_stw = 1;

@@ -23,11 +23,13 @@ def fftlib(tmp_path_factory):
 @pytest.mark.parametrize("logn", range(4, 14))
 @pytest.mark.parametrize("direction", [-1, 1])
 @pytest.mark.parametrize("tables", ["global", "shared"])
-def test_block_fft_matches_numpy(fftlib, logn, direction, tables):
+@pytest.mark.parametrize("elems", [16, 8])
+def test_block_fft_matches_numpy(fftlib, logn, direction, tables, elems):
     n = 1 << logn
     rng = np.random.default_rng(logn * 7 + (direction > 0))
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
     out = np.empty_like(x)
+    fftlib.fft_core_set_e(elems)
     fn = fftlib.fft_core_check if tables == "global" else fftlib.fft_core_check_stw
     assert fn(logn, direction, x.ctypes.data, out.ctypes.data) == 0
     ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n

@@ -69,11 +69,11 @@ __device__ __forceinline__ void bluestein_chain(float2 (&v)[16], int j, int par,
   using C = CztCfg<LOGQ>;
   const float2* twQ = tw_table(LOGQ);
   const float2* twL = tw_table(LOGQ + 1);
-  block_fft<LOGQ, -1>(v, j, xb, twQ);
+  block_fft<LOGQ, 16, -1>(v, j, xb, twQ);
   const float2* gp = g + par * C::Q;
 #pragma unroll
   for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], gp[j + m * C::T]);
-  block_fft<LOGQ, 1>(v, j, xb, twQ);
+  block_fft<LOGQ, 16, 1>(v, j, xb, twQ);
   // block_fft ends with all gathers done; the buffer may be overwritten.
 #pragma unroll
   for (int m = 0; m < 16; ++m) {

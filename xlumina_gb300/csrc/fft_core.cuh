@@ -2,8 +2,9 @@
 // radix-2/4/8 pass), shared by every propagation kernel of the library.
 //
 // Layout contract: an FFT of length N = 2^LOGN is computed by a group of
-// T = N/16 threads; thread j holds v[m] = x[j + m*T] (m = 0..15) on entry and
-// X[j + m*T] on exit, so loads and stores of whole lines are coalesced.
+// T = N/E threads (E = 16 or 8 elements per thread); thread j holds
+// v[m] = x[j + m*T] (m < E) on entry and X[j + m*T] on exit, so loads and
+// stores of whole lines are coalesced.
 // Between passes the group exchanges data through a padded shared-memory
 // buffer of N + N/16 float2 (one pad slot every 16 elements keeps the
 // stride-16 writes of the first pass free of bank conflicts).
@@ -144,39 +145,38 @@ template <int R, int DIR> XL_HD void dftR(float2* a) {
 
 XL_HD int smpad(int i) { return i + (i >> 4); }
 
-template <int LOGN> struct FftShape {
+// FFT of length N = 2^LOGN by a group of T = N/E threads, E elements each.
+// Passes: radix E while possible, then one radix 2^(LOGN mod log2 E).
+template <int LOGN, int E = 16> struct FftShape {
+  static_assert(E == 8 || E == 16, "8 or 16 elements per thread");
   static_assert(LOGN >= 4 && LOGN <= 13, "FFT length 16..8192");
+  static constexpr int LE = E == 16 ? 4 : 3;
   static constexpr int N = 1 << LOGN;
-  static constexpr int E = 16;          // elements per thread
   static constexpr int T = N / E;       // threads per FFT
-  static constexpr int NFULL = LOGN / 4;
-  static constexpr int REM = LOGN % 4;
+  static constexpr int NFULL = LOGN / LE;
+  static constexpr int REM = LOGN % LE;
   static constexpr int NPASS = NFULL + (REM ? 1 : 0);
   static constexpr int SMEM = N + N / 16;  // padded float2 slots per exchange buffer
-  template <int P> static constexpr int radix() { return P < NFULL ? 16 : (1 << REM); }
-  static constexpr int radix_rt(int P) { return P < NFULL ? 16 : (1 << REM); }
+  template <int P> static constexpr int radix() { return P < NFULL ? E : (1 << REM); }
+  static constexpr int radix_rt(int P) { return P < NFULL ? E : (1 << REM); }
   static constexpr int stride_rt(int P) {
     int ns = 1;
-    for (int q = 0; q < P; ++q) ns *= (q < NFULL ? 16 : (1 << REM));
+    for (int q = 0; q < P; ++q) ns *= (q < NFULL ? E : (1 << REM));
     return ns;
   }
-  template <int P> static constexpr int stride() {
-    int ns = 1;
-    for (int q = 0; q < P; ++q) ns *= (q < NFULL ? 16 : (1 << REM));
-    return ns;
-  }
+  template <int P> static constexpr int stride() { return stride_rt(P); }
 };
 
-// Twiddle table lookup: tw points at the size-N table, tw[q] = e^{-2 pi i q / N}.
-// One Stockham pass for thread j.  Input layout v[m] = x[j + m T].
-// LAST: outputs stay in v (natural order, same layout); otherwise written to sm.
-template <int LOGN, int P, int DIR>
-XL_HD void fft_pass(float2 (&v)[16], int j, float2* sm, const float2* tw) {
-  using S = FftShape<LOGN>;
+// One Stockham pass for thread j.  Input layout v[m] = x[j + m T]; tw is the
+// size-N table tw[q] = e^{-2 pi i q / N}.  The last pass leaves its outputs
+// in v in natural order (same layout); the others write them to sm.
+template <int LOGN, int E, int P, int DIR>
+XL_HD void fft_pass(float2 (&v)[E], int j, float2* sm, const float2* tw) {
+  using S = FftShape<LOGN, E>;
   constexpr int R = S::template radix<P>();
   constexpr int NS = S::template stride<P>();
   constexpr bool LAST = (P == S::NPASS - 1);
-  constexpr int BPT = 16 / R;
+  constexpr int BPT = E / R;
   constexpr int TWS = S::N / (NS * R);
 #pragma unroll
   for (int t = 0; t < BPT; ++t) {
@@ -204,18 +204,18 @@ XL_HD void fft_pass(float2 (&v)[16], int j, float2* sm, const float2* tw) {
   }
 }
 
-template <int LOGN> XL_HD void fft_gather(float2 (&v)[16], int j, const float2* sm) {
-  using S = FftShape<LOGN>;
+template <int LOGN, int E> XL_HD void fft_gather(float2 (&v)[E], int j, const float2* sm) {
+  using S = FftShape<LOGN, E>;
 #pragma unroll
-  for (int m = 0; m < 16; ++m) v[m] = sm[smpad(j + m * S::T)];
+  for (int m = 0; m < E; ++m) v[m] = sm[smpad(j + m * S::T)];
 }
 
 // ---- per-pass twiddle tables (shared memory) ----
 // Pass P >= 1 (radix R, stride NS) keeps e^{-2 pi i (i k) / (NS R)} at
 // [off<P>() + (i-1) NS + k], i = 1..R-1, k = 0..NS-1: consecutive threads
 // (consecutive k) read consecutive slots, so the reads are conflict-free.
-template <int LOGN> struct FftTw {
-  using S = FftShape<LOGN>;
+template <int LOGN, int E = 16> struct FftTw {
+  using S = FftShape<LOGN, E>;
   template <int P> static constexpr int off() {
     int o = 0;
     for (int q = 1; q < P; ++q) o += (S::radix_rt(q) - 1) * S::stride_rt(q);
@@ -224,9 +224,9 @@ template <int LOGN> struct FftTw {
   static constexpr int SIZE = off<S::NPASS>() > 0 ? off<S::NPASS>() : 1;
 };
 
-// Fill one slot of the pass tables from the size-N table twN[q] = e^{-2 pi i q/N}.
-template <int LOGN> XL_HD float2 pass_twiddle_entry(int idx, const float2* twN) {
-  using S = FftShape<LOGN>;
+// One slot of the pass tables from the size-N table twN[q] = e^{-2 pi i q/N}.
+template <int LOGN, int E = 16> XL_HD float2 pass_twiddle_entry(int idx, const float2* twN) {
+  using S = FftShape<LOGN, E>;
   int base = 0;
   for (int q = 1; q < S::NPASS; ++q) {
     const int R = S::radix_rt(q), NS = S::stride_rt(q);
@@ -241,14 +241,14 @@ template <int LOGN> XL_HD float2 pass_twiddle_entry(int idx, const float2* twN) 
 }
 
 // Stockham pass with twiddles from the shared pass tables.
-template <int LOGN, int P, int DIR>
-XL_HD void fft_pass_s(float2 (&v)[16], int j, float2* sm, const float2* stw) {
-  using S = FftShape<LOGN>;
+template <int LOGN, int E, int P, int DIR>
+XL_HD void fft_pass_s(float2 (&v)[E], int j, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN, E>;
   constexpr int R = S::template radix<P>();
   constexpr int NS = S::template stride<P>();
   constexpr bool LAST = (P == S::NPASS - 1);
-  constexpr int BPT = 16 / R;
-  constexpr int OFF = FftTw<LOGN>::template off<P>();
+  constexpr int BPT = E / R;
+  constexpr int OFF = FftTw<LOGN, E>::template off<P>();
 #pragma unroll
   for (int t = 0; t < BPT; ++t) {
     const int b = j + t * S::T;
@@ -276,30 +276,29 @@ XL_HD void fft_pass_s(float2 (&v)[16], int j, float2* sm, const float2* stw) {
 }
 
 #if defined(__CUDACC__)
-// Whole FFT for a thread group, twiddles from the shared pass tables.
-template <int LOGN, int DIR, int P = 0>
-__device__ __forceinline__ void block_fft_s(float2 (&v)[16], int j, float2* sm, const float2* stw) {
-  using S = FftShape<LOGN>;
-  fft_pass_s<LOGN, P, DIR>(v, j, sm, stw);
+// Whole FFT for a thread group.  Every thread of the CTA must call these the
+// same number of times (they use __syncthreads between passes).
+template <int LOGN, int E, int DIR, int P = 0>
+__device__ __forceinline__ void block_fft_s(float2 (&v)[E], int j, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN, E>;
+  fft_pass_s<LOGN, E, P, DIR>(v, j, sm, stw);
   if constexpr (P < S::NPASS - 1) {
     __syncthreads();
-    fft_gather<LOGN>(v, j, sm);
+    fft_gather<LOGN, E>(v, j, sm);
     __syncthreads();
-    block_fft_s<LOGN, DIR, P + 1>(v, j, sm, stw);
+    block_fft_s<LOGN, E, DIR, P + 1>(v, j, sm, stw);
   }
 }
 
-// Whole FFT for a thread group.  Every thread of the CTA must call this the
-// same number of times (it uses __syncthreads between passes).
-template <int LOGN, int DIR, int P = 0>
-__device__ __forceinline__ void block_fft(float2 (&v)[16], int j, float2* sm, const float2* tw) {
-  using S = FftShape<LOGN>;
-  fft_pass<LOGN, P, DIR>(v, j, sm, tw);
+template <int LOGN, int E, int DIR, int P = 0>
+__device__ __forceinline__ void block_fft(float2 (&v)[E], int j, float2* sm, const float2* tw) {
+  using S = FftShape<LOGN, E>;
+  fft_pass<LOGN, E, P, DIR>(v, j, sm, tw);
   if constexpr (P < S::NPASS - 1) {
     __syncthreads();
-    fft_gather<LOGN>(v, j, sm);
+    fft_gather<LOGN, E>(v, j, sm);
     __syncthreads();
-    block_fft<LOGN, DIR, P + 1>(v, j, sm, tw);
+    block_fft<LOGN, E, DIR, P + 1>(v, j, sm, tw);
   }
 }
 #endif

@@ -29,27 +29,41 @@
 
 namespace xl {
 
+#ifndef XL_RS_ROW_E
+#define XL_RS_ROW_E 8
+#endif
+#ifndef XL_RS_COL_E
+#define XL_RS_COL_E 16
+#endif
+
 template <int LOGQ> struct RsCfg {
-  using S = FftShape<LOGQ>;
-  static constexpr int Q = S::N;
+  static constexpr int Q = 1 << LOGQ;
   static constexpr int P = 2 * Q;
-  static constexpr int T = S::T;
-  static constexpr int XS = S::SMEM;            // exchange buffer slots
-  static constexpr int TW = FftTw<LOGQ>::SIZE;  // pass-twiddle slots
+  static constexpr int XS = Q + Q / 16;         // exchange buffer slots
+  // row passes: one group of TR threads (ER elements each) per row
+  static constexpr int ER = (Q / XL_RS_ROW_E) >= 1 ? XL_RS_ROW_E : 16;
+  static constexpr int TR = Q / ER;
+  static constexpr int TWR = FftTw<LOGQ, ER>::SIZE;
+  static constexpr int RPC = (128 / TR) > 1 ? (128 / TR) : 1;  // rows per CTA
+  static constexpr int ROW_THREADS = RPC * TR;
+  static constexpr int ROW_MINB = ((ER == 8 ? 1024 : 512) / ROW_THREADS) > 1 ? ((ER == 8 ? 1024 : 512) / ROW_THREADS) : 1;
+  // column pass: W groups of TC threads (EC elements each), one per column
+  static constexpr int EC = XL_RS_COL_E;
+  static constexpr int TC = Q / EC;
+  static constexpr int TWC = FftTw<LOGQ, EC>::SIZE;
   // Column-block width of the blocked intermediate and spectrum layouts:
   // element (row r, column col) of a plane with ny rows lives at
   // ((col / W) * ny + r) * W + col % W, so W adjacent columns of one row are
   // contiguous and a column tile is one contiguous block.
-  static constexpr int W = LOGQ >= 12 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
-  static constexpr int RPC = (128 / T) > 1 ? (128 / T) : 1;  // rows per CTA, one group per row
-  static constexpr int ROW_THREADS = RPC * T;
-  static constexpr int CONV_THREADS = W * T;
+  static constexpr int W = (LOGQ >= 12 && EC == 16) ? 2 : ((32 / TC) > 4 ? (32 / TC) : 4);
+  static constexpr int CONV_THREADS = W * TC;
   // per-group padding of the column-pass shared buffers: with W groups
   // interleaved in every warp, unpadded buffers would start on the same bank
   static constexpr int CPAD = W >= 8 ? 0 : 4;
   static constexpr int CXS = XS + CPAD;
   static constexpr int CYS = Q + CPAD;
-  // one-time spectrum build
+  // one-time spectrum build (16 elements per thread)
+  static constexpr int T = Q / 16;
   static constexpr int HRPC = (256 / (2 * T)) > 1 ? (256 / (2 * T)) : 1;
   static constexpr int HROW_THREADS = 2 * HRPC * T;
   static constexpr int WH = (256 / T) < 1 ? 1 : ((256 / T) > 32 ? 32 : (256 / T));
@@ -62,11 +76,11 @@ __device__ __forceinline__ long long blk(int r, int col, int ny) {
   return ((long long)(col / W) * ny + r) * W + (col % W);
 }
 
-template <int LOGQ>
+template <int LOGQ, int E>
 __device__ __forceinline__ void fill_pass_twiddles(float2* stw) {
   const float2* twQ = tw_table(LOGQ);
-  for (int idx = threadIdx.x; idx < RsCfg<LOGQ>::TW; idx += blockDim.x)
-    stw[idx] = pass_twiddle_entry<LOGQ>(idx, twQ);
+  for (int idx = threadIdx.x; idx < FftTw<LOGQ, E>::SIZE; idx += blockDim.x)
+    stw[idx] = pass_twiddle_entry<LOGQ, E>(idx, twQ);
 }
 
 // ---------------------------------------------------------------------------
@@ -105,7 +119,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::HROW_THREADS)
     const float2 a = row[slot * C::P + n], b = row[slot * C::P + n + C::Q];
     v[m] = par ? cmul(csub(a, b), twP[n]) : cadd(a, b);
   }
-  block_fft<LOGQ, -1>(v, j, xch + (2 * slot + par) * C::XS, twQ);
+  block_fft<LOGQ, 16, -1>(v, j, xch + (2 * slot + par) * C::XS, twQ);
   const int i = i0 + slot;
   if (i < C::P) {
     float2* dst = out + (long long)i * C::P + par * C::Q;
@@ -145,7 +159,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS)
     const float2 a = tile[n * PITCH + w], b = tile[(n + C::Q) * PITCH + w];
     v[m] = par ? cmul(csub(a, b), twP[n]) : cadd(a, b);
   }
-  block_fft<LOGQ, -1>(v, j, xch + (2 * w + par) * C::XS, twQ);
+  block_fft<LOGQ, 16, -1>(v, j, xch + (2 * w + par) * C::XS, twQ);
   const int col = c0 + w;
   float2* dst = out + ((long long)(col / C::W) * 2 + par) * C::Q * C::W + (col % C::W);
 #pragma unroll
@@ -174,20 +188,20 @@ struct RsLaunch {
 // component, the even- and odd-frequency Q-point row spectra, stored in the
 // blocked layout.  One thread group per row.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::ROW_THREADS)
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, RsCfg<LOGQ>::ROW_MINB)
     rs_rows_fwd(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
   const int ns = p.cin;                            // staged components
   float2* stage = smem;                            // RPC x ns x nx
   float2* xch = stage + C::RPC * ns * p.nx;        // RPC x XS
-  float2* stw = xch + C::RPC * C::XS;              // TW
+  float2* stw = xch + C::RPC * C::XS;              // TWR
   const int tid = threadIdx.x;
-  const int slot = tid / C::T;
-  const int j = tid % C::T;
+  const int slot = tid / C::TR;
+  const int j = tid % C::TR;
   const int b = blockIdx.y;
   const int r0 = blockIdx.x * C::RPC;
-  fill_pass_twiddles<LOGQ>(stw);
+  fill_pass_twiddles<LOGQ, C::ER>(stw);
 
   for (int idx = tid; idx < C::RPC * p.nx; idx += blockDim.x) {
     const int s = idx / p.nx, n = idx % p.nx, r = r0 + s;
@@ -215,10 +229,10 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
   for (int c = 0; c < p.cout; ++c) {
     float2* plane = p.work + ((long long)b * p.cout + c) * p.ny * C::P;
     for (int par = 0; par < 2; ++par) {
-      float2 v[16];
+      float2 v[C::ER];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
-        const int n = j + m * C::T;
+      for (int m = 0; m < C::ER; ++m) {
+        const int n = j + m * C::TR;
         float2 a = make_float2(0.f, 0.f);
         if (live && n < p.nx) {
           if (c < ns) {
@@ -231,10 +245,10 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
         }
         v[m] = par ? cmul(a, twP[n]) : a;
       }
-      block_fft_s<LOGQ, -1>(v, j, xb, stw);
+      block_fft_s<LOGQ, C::ER, -1>(v, j, xb, stw);
       if (live) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) plane[blk<LOGQ>(r, par * C::Q + j + m * C::T, p.ny)] = v[m];
+        for (int m = 0; m < C::ER; ++m) plane[blk<LOGQ>(r, par * C::Q + j + m * C::TR, p.ny)] = v[m];
       }
     }
   }
@@ -250,15 +264,15 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const 
   constexpr int W = C::W, LPW = 32 / W;
   extern __shared__ float2 smem[];
   float2* xch = smem;                // W x CXS
-  float2* stw = smem + W * C::CXS;   // TW
-  float2* yb = stw + C::TW;          // W x CYS: even-chain result, held across the odd chain
+  float2* stw = smem + W * C::CXS;   // TWC
+  float2* yb = stw + C::TWC;         // W x CYS: even-chain result, held across the odd chain
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int w = lane % W;
   const int j = (tid >> 5) * LPW + lane / W;
   const int t = blockIdx.x;
   const int b = blockIdx.y;
-  fill_pass_twiddles<LOGQ>(stw);
+  fill_pass_twiddles<LOGQ, C::EC>(stw);
   __syncthreads();
   const float2* twP = tw_table(LOGQ + 1);
   const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * 2 * C::Q * W + w;
@@ -269,30 +283,30 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const 
     float2* tileA = p.work + ((long long)b * p.cout + c) * p.ny * C::P + (long long)t * p.ny * W + w;
 #pragma unroll
     for (int par = 0; par < 2; ++par) {
-      float2 v[16];
+      float2 v[C::EC];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
-        const int n = j + m * C::T;
+      for (int m = 0; m < C::EC; ++m) {
+        const int n = j + m * C::TC;
         const float2 a = n < p.ny ? tileA[(long long)n * W] : make_float2(0.f, 0.f);
         v[m] = par ? cmul(a, twP[n]) : a;
       }
-      block_fft_s<LOGQ, -1>(v, j, xb, stw);
+      block_fft_s<LOGQ, C::EC, -1>(v, j, xb, stw);
       const float2* sp = spec + (long long)par * C::Q * W;
       if (p.adjoint) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], sp[(long long)(j + m * C::T) * W]);
+        for (int m = 0; m < C::EC; ++m) v[m] = cmulc(v[m], sp[(long long)(j + m * C::TC) * W]);
       } else {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], sp[(long long)(j + m * C::T) * W]);
+        for (int m = 0; m < C::EC; ++m) v[m] = cmul(v[m], sp[(long long)(j + m * C::TC) * W]);
       }
-      block_fft_s<LOGQ, 1>(v, j, xb, stw);
+      block_fft_s<LOGQ, C::EC, 1>(v, j, xb, stw);
       if (par == 0) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) y0[j + m * C::T] = v[m];
+        for (int m = 0; m < C::EC; ++m) y0[j + m * C::TC] = v[m];
       } else {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) {
-          const int n = j + m * C::T;
+        for (int m = 0; m < C::EC; ++m) {
+          const int n = j + m * C::TC;
           if (n < p.ny) tileA[(long long)n * W] = cadd(y0[n], cmulc(v[m], twP[n]));
         }
       }
@@ -303,7 +317,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const 
 // Inverse row pass: inverse of both parity halves, combined in registers,
 // cropped to nx columns; optional fused epilogue program; store.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::ROW_THREADS)
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, RsCfg<LOGQ>::ROW_MINB)
     rs_rows_inv(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
   extern __shared__ float2 smem[];
@@ -311,18 +325,18 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
   const bool fold = p.adjoint && nc == 3;      // VRS adjoint: Ez gradient folded into Ex, Ey
   const bool epi = p.post.nops > 0 || fold;
   float2* xch = smem;                           // RPC x XS
-  float2* stw = xch + C::RPC * C::XS;           // TW
-  float2* yb = stw + C::TW;                     // RPC x Q: even-half result
+  float2* stw = xch + C::RPC * C::XS;           // TWR
+  float2* yb = stw + C::TWR;                    // RPC x Q: even-half result
   float2* stage = yb + C::RPC * C::Q;           // RPC x nc x nx (epilogue only)
   const int tid = threadIdx.x;
-  const int slot = tid / C::T;
-  const int j = tid % C::T;
+  const int slot = tid / C::TR;
+  const int j = tid % C::TR;
   const int b = blockIdx.y;
   const int r0 = blockIdx.x * C::RPC;
   const int r = r0 + slot;
   const bool live = r < p.ny;
   const int rr = live ? r : 0;
-  fill_pass_twiddles<LOGQ>(stw);
+  fill_pass_twiddles<LOGQ, C::ER>(stw);
   __syncthreads();
   const float2* twP = tw_table(LOGQ + 1);
   float2* xb = xch + slot * C::XS;
@@ -332,17 +346,17 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, 512 / RsCfg<LOGQ>::R
     const float2* plane = p.work + ((long long)b * nc + c) * p.ny * C::P;
 #pragma unroll
     for (int par = 0; par < 2; ++par) {
-      float2 v[16];
+      float2 v[C::ER];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = plane[blk<LOGQ>(rr, par * C::Q + j + m * C::T, p.ny)];
-      block_fft_s<LOGQ, 1>(v, j, xb, stw);
+      for (int m = 0; m < C::ER; ++m) v[m] = plane[blk<LOGQ>(rr, par * C::Q + j + m * C::TR, p.ny)];
+      block_fft_s<LOGQ, C::ER, 1>(v, j, xb, stw);
       if (par == 0) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) y0[j + m * C::T] = v[m];
+        for (int m = 0; m < C::ER; ++m) y0[j + m * C::TR] = v[m];
       } else if (live) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) {
-          const int n = j + m * C::T;
+        for (int m = 0; m < C::ER; ++m) {
+          const int n = j + m * C::TR;
           if (n < p.nx) {
             const float2 o = cadd(y0[n], cmulc(v[m], twP[n]));
             if (epi) stage[(slot * nc + c) * p.nx + n] = o;
@@ -412,18 +426,18 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   const dim3 g_rows((p.ny + C::RPC - 1) / C::RPC, p.B);
   cudaError_t e;
   if (stage == 0) {
-    const size_t sm = (size_t)(C::RPC * p.cin * p.nx + C::RPC * C::XS + C::TW) * sizeof(float2);
+    const size_t sm = (size_t)(C::RPC * p.cin * p.nx + C::RPC * C::XS + C::TWR) * sizeof(float2);
     if ((e = allow_smem(rs_rows_fwd<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_fwd smem");
     rs_rows_fwd<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_rows_fwd");
   } else if (stage == 1) {
-    const size_t sm = (size_t)(C::W * C::CXS + C::TW + C::W * C::CYS) * sizeof(float2);
+    const size_t sm = (size_t)(C::W * C::CXS + C::TWC + C::W * C::CYS) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
     rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::CONV_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
   } else {
     const bool stage_out = p.post.nops || (p.adjoint && p.cout == 3);
-    const size_t sm = (size_t)(C::RPC * C::XS + C::TW + C::RPC * C::Q +
+    const size_t sm = (size_t)(C::RPC * C::XS + C::TWR + C::RPC * C::Q +
                                (stage_out ? C::RPC * p.cout * p.nx : 0)) * sizeof(float2);
     if ((e = allow_smem(rs_rows_inv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_rows_inv smem");
     rs_rows_inv<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
