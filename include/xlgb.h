@@ -52,7 +52,9 @@ enum {
   XL_OP_CMUL = 7,      /* multiply all components by a complex64 plane ptr[0] */
   XL_OP_HIGHNA = 8     /* high-NA objective lens, optical_elements.py:515-594: ptr[0], ptr[1]
                           float64 x, y; dval[0] radius, dval[1] focal length, dval[2]
-                          sin(theta_max); Ez derived from Ex, Ey, output (Ex, Ey, Ez) */
+                          sin(theta_max), dval[3] 1/radius^2; Ez derived from Ex, Ey, output
+                          (Ex, Ey, Ez).  ptr[2] (optional): the 6 coefficient planes from
+                          xl_highna_coefficients, plane stride pbstride (ny*nx) */
 };
 
 typedef struct {
@@ -71,6 +73,11 @@ typedef struct {
 
 const char* xl_last_error(void);
 int xl_version(void);
+
+/* Number of bounded waits (on TMA-copy barriers) that ran out of iterations
+ * since the last reset, on the current device; such a launch records the
+ * event and returns without hanging, its output is not valid.  Synchronous. */
+int xl_device_timeouts(unsigned int* count, int reset);
 
 /* Upload the twiddle tables to the current device.  Called once per device
  * before the first launch (every entry point calls it lazily as well). */
@@ -204,6 +211,12 @@ int xl_czt_stage(void* stream, const XlCztArgs* args, int stage);
 /* Apply a Jones program to batch x comps planes (out may alias in). */
 int xl_apply_ops(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
                  long long in_bstride, void* const* out, long long out_bstride, const XlProg* prog);
+
+/* The per-pixel coefficients of the high-NA lens (optical_elements.py:528-594)
+ * as 6 float32 planes of ny x nx: E' = K [Ex, Ey] with K = {K00, K01, K10,
+ * K11, K20, K21}; they depend on the geometry only and are cached by callers. */
+int xl_highna_coefficients(void* stream, int ny, int nx, const double* x, const double* y, double radius,
+                           double f, void* out);
 
 /* Backward of a Jones program: the gradients jax.grad takes through the masks
  * of optical_elements.py:76-332, :515-594 and :678-703.  `in` holds the

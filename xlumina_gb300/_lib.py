@@ -65,6 +65,7 @@ SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
     "xl_version": (ctypes.c_int, []),
     "xl_init": (ctypes.c_int, []),
+    "xl_device_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_spectrum_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_transfer_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
@@ -82,6 +83,8 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                        ctypes.POINTER(XlProg), ctypes.POINTER(ctypes.c_void_p)]),
+    "xl_highna_coefficients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

@@ -42,11 +42,66 @@ __device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, 
 
 // ---- fused per-pixel Jones program ----
 
+struct PixelCtx;
+__device__ __forceinline__ void highna_coeffs(const XlOp& op, const PixelCtx& px, float (&kc)[6]);
+
 struct PixelCtx {
   int row, col;  // pixel position
   long long pix; // row * ld + col inside one plane of the parameter arrays
   int batch;
 };
+
+// High-NA objective lens (optical_elements.py:528-594) as a real 3x2 matrix K
+// per pixel: E' = K [Ex, Ey], folding in Ez = Ex X/rho + Ey Y/rho (NaN at
+// rho = 0, as the reference), the rotation RL(theta, phi), sqrt|cos theta|
+// and the pupil factor G.  kc = {K00, K01, K10, K11, K20, K21}.
+__device__ __forceinline__ void highna_coeffs(const XlOp& op, const PixelCtx& px, float (&kc)[6]) {
+  if (op.ptr[2]) {  // precomputed coefficient planes (6 x ny x nx float32)
+    const float* cp = (const float*)op.ptr[2];
+    const long long plane = op.pbstride;   // ny * nx
+#pragma unroll
+    for (int q = 0; q < 6; ++q) kc[q] = __ldg(cp + q * plane + px.pix);
+    return;
+  }
+  const double Xd = ((const double*)op.ptr[0])[px.col];
+  const double Yd = ((const double*)op.ptr[1])[px.row];
+  const double rad = op.dval[0];
+  // pupil (X^2 + Y^2) / r^2 < 1, tested as X^2 + Y^2 < r^2 (equivalent for positive doubles)
+  const double rho2 = Xd * Xd + Yd * Yd;
+  const bool inside = rho2 < rad * rad;
+  const float smax = (float)op.dval[2];
+  const float q = (float)rho2 * (float)op.dval[3];   // (u^2 + v^2), dval[3] = 1 / r^2
+  const float G = inside ? 1.f / sqrtf(fabsf(1.f - q * smax * smax)) : 0.f;
+  const float X = (float)Xd, Y = (float)Yd;
+  const float rho = sqrtf(X * X + Y * Y);
+  const float th = rho / (float)op.dval[1];
+  const float phi = atan2f(Y, X);
+  float st, ct, sp, cp;
+  sincosf(th, &st, &ct);
+  sincosf(phi, &sp, &cp);
+  const float w = sqrtf(fabsf(ct)) * G;
+  const float ux = X / rho, uy = Y / rho;
+  const float r00 = ct * cp * cp + sp * sp, r01 = ct * cp * sp - sp * cp, r02 = -cp * st;
+  const float r10 = sp * ct * cp - cp * sp, r11 = ct * sp * sp + cp * cp, r12 = -sp * st;
+  const float r20 = st * cp, r21 = st * sp, r22 = ct;
+  kc[0] = w * (r00 + r02 * ux); kc[1] = w * (r01 + r02 * uy);
+  kc[2] = w * (r10 + r12 * ux); kc[3] = w * (r11 + r12 * uy);
+  kc[4] = w * (r20 + r22 * ux); kc[5] = w * (r21 + r22 * uy);
+}
+
+__device__ __forceinline__ void apply_highna(const float (&kc)[6], float2 (&e)[3]) {
+  const float2 ex = e[0], ey = e[1];
+  e[0] = cadd(cscale(ex, kc[0]), cscale(ey, kc[1]));
+  e[1] = cadd(cscale(ex, kc[2]), cscale(ey, kc[3]));
+  e[2] = cadd(cscale(ex, kc[4]), cscale(ey, kc[5]));
+}
+
+__device__ __forceinline__ void apply_highna_bwd(const float (&kc)[6], float2 (&g)[3]) {
+  const float2 g0 = g[0], g1 = g[1], g2 = g[2];
+  g[0] = cadd(cadd(cscale(g0, kc[0]), cscale(g1, kc[2])), cscale(g2, kc[4]));
+  g[1] = cadd(cadd(cscale(g0, kc[1]), cscale(g1, kc[3])), cscale(g2, kc[5]));
+  g[2] = make_float2(0.f, 0.f);
+}
 
 __device__ __forceinline__ float op_param(const XlOp& op, int i, const PixelCtx& px) {
   if (op.pmask & (1 << i)) {
@@ -135,30 +190,9 @@ __device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const P
       break;
     }
     case XL_OP_HIGHNA: {  // optical_elements.py:528-594
-      const double Xd = ((const double*)op.ptr[0])[px.col];
-      const double Yd = ((const double*)op.ptr[1])[px.row];
-      const double rad = op.dval[0];
-      const double q = (Xd * Xd + Yd * Yd) / (rad * rad);   // (u^2 + v^2), FP64 pupil test
-      const float smax = (float)op.dval[2];
-      const float G = q < 1.0 ? 1.f / sqrtf(fabsf(1.f - (float)q * smax * smax)) : 0.f;
-      const float X = (float)Xd, Y = (float)Yd;
-      const float rho = sqrtf(X * X + Y * Y);
-      const float th = rho / (float)op.dval[1];
-      const float phi = atan2f(Y, X);
-      float st, ct, sp, cp;
-      sincosf(th, &st, &ct);
-      sincosf(phi, &sp, &cp);
-      const float w = sqrtf(fabsf(ct)) * G;
-      const float2 ex = e[0], ey = e[1];
-      const float2 ez = cadd(cscale(ex, X / rho), cscale(ey, Y / rho));  // NaN at rho = 0, as the reference
-      const float2 ox = cadd(cadd(cscale(ex, ct * cp * cp + sp * sp), cscale(ey, ct * cp * sp - sp * cp)),
-                             cscale(ez, -cp * st));
-      const float2 oy = cadd(cadd(cscale(ex, sp * ct * cp - cp * sp), cscale(ey, ct * sp * sp + cp * cp)),
-                             cscale(ez, -sp * st));
-      const float2 oz = cadd(cadd(cscale(ex, st * cp), cscale(ey, st * sp)), cscale(ez, ct));
-      e[0] = cscale(ox, w);
-      e[1] = cscale(oy, w);
-      e[2] = cscale(oz, w);
+      float kc[6];
+      highna_coeffs(op, px, kc);
+      apply_highna(kc, e);
       break;
     }
     default:
@@ -266,37 +300,67 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
       break;
     }
     case XL_OP_HIGHNA: {
-      const double Xd = ((const double*)op.ptr[0])[px.col];
-      const double Yd = ((const double*)op.ptr[1])[px.row];
-      const double rad = op.dval[0];
-      const double q = (Xd * Xd + Yd * Yd) / (rad * rad);
-      const float smax = (float)op.dval[2];
-      const float G = q < 1.0 ? 1.f / sqrtf(fabsf(1.f - (float)q * smax * smax)) : 0.f;
-      const float X = (float)Xd, Y = (float)Yd;
-      const float rho = sqrtf(X * X + Y * Y);
-      const float th = rho / (float)op.dval[1];
-      const float phi = atan2f(Y, X);
-      float st, ct, sp, cp;
-      sincosf(th, &st, &ct);
-      sincosf(phi, &sp, &cp);
-      const float w = sqrtf(fabsf(ct)) * G;
-      const float ux = X / rho, uy = Y / rho;
-      // rows of RL; the input Ez' = ux Ex + uy Ey
-      const float r00 = ct * cp * cp + sp * sp, r01 = ct * cp * sp - sp * cp, r02 = -cp * st;
-      const float r10 = sp * ct * cp - cp * sp, r11 = ct * sp * sp + cp * cp, r12 = -sp * st;
-      const float r20 = st * cp, r21 = st * sp, r22 = ct;
-      const float k00 = w * (r00 + r02 * ux), k01 = w * (r01 + r02 * uy);
-      const float k10 = w * (r10 + r12 * ux), k11 = w * (r11 + r12 * uy);
-      const float k20 = w * (r20 + r22 * ux), k21 = w * (r21 + r22 * uy);
-      const float2 g0 = g[0], g1 = g[1], g2 = g[2];
-      g[0] = cadd(cadd(cscale(g0, k00), cscale(g1, k10)), cscale(g2, k20));
-      g[1] = cadd(cadd(cscale(g0, k01), cscale(g1, k11)), cscale(g2, k21));
-      g[2] = make_float2(0.f, 0.f);
+      float kc[6];
+      highna_coeffs(op, px, kc);
+      apply_highna_bwd(kc, g);
       break;
     }
     default:
       break;
   }
+}
+
+}  // namespace xl
+
+// ---- TMA bulk copies into shared memory, completed on an mbarrier ----
+namespace xl {
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* mbar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+
+// Make prior generic-proxy shared-memory accesses visible to the async proxy
+// (the TMA engine) before it overwrites the same buffer.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: arm the barrier for `bytes` and start a 1-D bulk copy
+// global -> shared (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* mbar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(mbar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `phase` of the barrier.  Returns false if the
+// iteration limit ran out (the caller records the error and skips its work).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* mbar, unsigned phase) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(mbar, phase)) return true;
+  return false;
 }
 
 }  // namespace xl

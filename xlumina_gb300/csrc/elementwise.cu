@@ -47,47 +47,75 @@ struct OpsBwdLaunch {
 };
 
 // One thread per pixel, looping over the batch so that gradients of
-// parameters shared by the batch are summed in a fixed order.
-__global__ void __launch_bounds__(256) ops_backward_kernel(const OpsBwdLaunch p) {
+// parameters shared by the batch are summed in a fixed order.  The op loops
+// are unrolled to XL_MAX_OPS so the per-op intermediates stay in registers;
+// the per-thread parameter-gradient accumulators live in shared memory,
+// [slot][thread] so that a warp's accesses fall in distinct banks.
+template <int KMAX>
+__global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p) {
+  constexpr int NS = XL_MAX_OPS * 4;
+  constexpr int NT = 128;
+  __shared__ float acc_s[NS * NT];    // scalar-parameter partial sums
+  __shared__ float acc_p[NS * NT];    // shared per-pixel parameters, summed over the batch
   const long long npix = (long long)p.ny * p.nx;
   const int K = p.prog.nops;
-  float sacc[XL_MAX_OPS * 4];
-  for (int q = 0; q < XL_MAX_OPS * 4; ++q) sacc[q] = 0.f;
+  const int tid = threadIdx.x;
+  for (int q = 0; q < NS; ++q) acc_s[q * NT + tid] = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
        i += (long long)gridDim.x * blockDim.x) {
     const int row = (int)(i / p.nx), col = (int)(i % p.nx);
-    float pacc[XL_MAX_OPS * 4];   // shared per-pixel parameters, summed over the batch
-    for (int q = 0; q < XL_MAX_OPS * 4; ++q) pacc[q] = 0.f;
+    for (int q = 0; q < 4 * K; ++q) acc_p[q * NT + tid] = 0.f;
+    // the high-NA lens depends on the pixel only: its coefficients are hoisted out of the batch loop
+    float kc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int hk = -1;
+    {
+      PixelCtx px0{row, col, i, 0};
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k)
+        if (k < K && hk < 0 && p.prog.ops[k].kind == XL_OP_HIGHNA) {
+          highna_coeffs(p.prog.ops[k], px0, kc);
+          hk = k;
+        }
+    }
     for (int b = 0; b < p.B; ++b) {
       PixelCtx px{row, col, i, b};
-      float2 st[XL_MAX_OPS][3];
+      float2 st[KMAX][3];
       float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       const long long off = (long long)b * p.ibs + i;
       e[0] = p.in[0][off];
       if (p.C > 1 && p.in[1]) e[1] = p.in[1][off];
       if (p.C > 2 && p.in[2]) e[2] = p.in[2][off];
-      for (int k = 0; k < K; ++k) {
-        st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
-        apply_op(p.prog.ops[k], e, px);
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k) {
+        if (k < K) {
+          st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
+          if (k == hk) apply_highna(kc, e);
+          else apply_op(p.prog.ops[k], e, px);
+        }
       }
       float2 g[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       const long long go = (long long)b * p.gbs + i;
       g[0] = p.gout[0][go];
       if (p.C > 1) g[1] = p.gout[1][go];
       if (p.C > 2) g[2] = p.gout[2][go];
-      for (int k = K - 1; k >= 0; --k) {
-        const XlOp& op = p.prog.ops[k];
-        float pg[4] = {0.f, 0.f, 0.f, 0.f};
-        const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
-        apply_op_bwd(op, ek, g, px, pg);
-        for (int q = 0; q < 4; ++q) {
-          void* dst = p.pgrad[k * 4 + q];
-          if (!dst) continue;
-          if (op.pmask & (1 << q)) {
-            if (op.pbstride) ((float*)dst)[(long long)b * op.pbstride + i] = pg[q];
-            else pacc[k * 4 + q] += pg[q];
-          } else {
-            sacc[k * 4 + q] += pg[q];
+#pragma unroll
+      for (int k = KMAX - 1; k >= 0; --k) {
+        if (k < K) {
+          const XlOp& op = p.prog.ops[k];
+          float pg[4] = {0.f, 0.f, 0.f, 0.f};
+          const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
+          if (k == hk) apply_highna_bwd(kc, g);
+          else apply_op_bwd(op, ek, g, px, pg);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            void* dst = p.pgrad[k * 4 + q];
+            if (!dst) continue;
+            if (op.pmask & (1 << q)) {
+              if (op.pbstride) ((float*)dst)[(long long)b * op.pbstride + i] = pg[q];
+              else acc_p[(k * 4 + q) * NT + tid] += pg[q];
+            } else {
+              acc_s[(k * 4 + q) * NT + tid] += pg[q];
+            }
           }
         }
       }
@@ -100,27 +128,39 @@ __global__ void __launch_bounds__(256) ops_backward_kernel(const OpsBwdLaunch p)
       for (int q = 0; q < 4; ++q) {
         const XlOp& op = p.prog.ops[k];
         if (p.pgrad[k * 4 + q] && (op.pmask & (1 << q)) && !op.pbstride)
-          ((float*)p.pgrad[k * 4 + q])[i] = pacc[k * 4 + q];
+          ((float*)p.pgrad[k * 4 + q])[i] = acc_p[(k * 4 + q) * NT + tid];
       }
   }
   // scalar parameters: block reduction, one float64 atomic per block and slot
-  __shared__ float red[8][32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ float red[8];
+  const int lane = tid & 31, warp = tid >> 5;
   for (int k = 0; k < K; ++k)
     for (int q = 0; q < 4; ++q) {
       const XlOp& op = p.prog.ops[k];
       if (!p.pgrad[k * 4 + q] || (op.pmask & (1 << q))) continue;
-      float v = sacc[k * 4 + q];
+      float v = acc_s[(k * 4 + q) * NT + tid];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp][0] = v;
+      if (lane == 0) red[warp] = v;
       __syncthreads();
-      if (threadIdx.x == 0) {
+      if (tid == 0) {
         double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][0];
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
         atomicAdd((double*)p.pgrad[k * 4 + q], t);
       }
       __syncthreads();
     }
+}
+
+__global__ void highna_plane_kernel(int ny, int nx, XlOp op, float* out) {
+  const long long npix = (long long)ny * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    PixelCtx px{(int)(i / nx), (int)(i % nx), i, 0};
+    float kc[6];
+    highna_coeffs(op, px, kc);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) out[q * npix + i] = kc[q];
+  }
 }
 
 cudaError_t elem_upload_twiddles(const float2* host) {
@@ -158,10 +198,33 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
   p.prog = *prog;
   for (int q = 0; q < XL_MAX_OPS * 4; ++q) p.pgrad[q] = pgrad ? pgrad[q] : nullptr;
   const long long npix = (long long)ny * nx;
+  int blocks = (int)((npix + 127) / 128);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (prog->nops <= 4) ops_backward_kernel<4><<<blocks, 128, 0, (cudaStream_t)stream>>>(p);
+  else ops_backward_kernel<XL_MAX_OPS><<<blocks, 128, 0, (cudaStream_t)stream>>>(p);
+  XL_CHECK_LAUNCH("ops_backward_kernel");
+  return XL_OK;
+}
+
+extern "C" int xl_highna_coefficients(void* stream, int ny, int nx, const double* x, const double* y,
+                                      double radius, double f, void* out) {
+  if (ny < 1 || nx < 1 || !x || !y || !out || !(radius > 0) || !(f > 0)) {
+    set_error("xl_highna_coefficients: bad arguments");
+    return XL_EINVAL;
+  }
+  XlOp op = {};
+  op.kind = XL_OP_HIGHNA;
+  op.ptr[0] = x;
+  op.ptr[1] = y;
+  op.dval[0] = radius;
+  op.dval[1] = f;
+  op.dval[2] = radius / sqrt(radius * radius + f * f);
+  op.dval[3] = 1.0 / (radius * radius);
+  const long long npix = (long long)ny * nx;
   int blocks = (int)((npix + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
-  ops_backward_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(p);
-  XL_CHECK_LAUNCH("ops_backward_kernel");
+  highna_plane_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(ny, nx, op, (float*)out);
+  XL_CHECK_LAUNCH("highna_plane_kernel");
   return XL_OK;
 }
 

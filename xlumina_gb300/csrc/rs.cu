@@ -62,6 +62,11 @@ template <int LOGQ> struct RsCfg {
   static constexpr int CPAD = W >= 8 ? 0 : 4;
   static constexpr int CXS = XS + CPAD;
   static constexpr int CYS = Q + CPAD;
+  // the column tile is staged by TMA when the shared memory allows it (Q <= 2048)
+  static constexpr bool TMA = LOGQ <= 11;
+  // float2 offset of the staged tile: after the exchange, twiddle and even-chain
+  // buffers, rounded up to 16 bytes
+  static constexpr int TBASE = (W * CXS + TWC + W * CYS + 1) / 2 * 2;
   // one-time spectrum build (16 elements per thread)
   static constexpr int T = Q / 16;
   static constexpr int HRPC = (256 / (2 * T)) > 1 ? (256 / (2 * T)) : 1;
@@ -258,37 +263,67 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS, RsCfg<LOGQ>::ROW_MIN
 // even chain FFT -> x S_even -> IFFT and odd chain (pre-twiddled) likewise,
 // combined in registers; only the ny rows that survive the crop are kept.
 // Lanes interleave the W columns so every warp access is 256 contiguous bytes.
+// A component's tile (ny x W, contiguous in the blocked layout) is staged into
+// shared memory by a TMA bulk copy; the next component's copy is issued once
+// the odd chain has read the current tile, so it overlaps that chain's work.
+__device__ unsigned int g_rs_timeouts;
+
 template <int LOGQ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const RsLaunch p) {
   using C = RsCfg<LOGQ>;
   constexpr int W = C::W, LPW = 32 / W;
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(16) float2 smem[];
   float2* xch = smem;                // W x CXS
   float2* stw = smem + W * C::CXS;   // TWC
   float2* yb = stw + C::TWC;         // W x CYS: even-chain result, held across the odd chain
+  float2* tb = smem + C::TBASE;      // ny x W: staged tile (TMA), 16-byte aligned
+  unsigned long long* mbar = (unsigned long long*)(tb + (C::TMA ? p.ny * W : 0));
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int w = lane % W;
   const int j = (tid >> 5) * LPW + lane / W;
   const int t = blockIdx.x;
   const int b = blockIdx.y;
+  const unsigned tile_bytes = (unsigned)(p.ny * W * sizeof(float2));
+  auto tile_of = [&](int c) {
+    return p.work + ((long long)b * p.cout + c) * p.ny * C::P + (long long)t * p.ny * W;
+  };
+  if (C::TMA && tid == 0) {
+    mbar_init(mbar, 1);
+    fence_mbar_init();
+  }
   fill_pass_twiddles<LOGQ, C::EC>(stw);
   __syncthreads();
+  if (C::TMA && tid == 0) bulk_g2s(tb, tile_of(0), tile_bytes, mbar);
   const float2* twP = tw_table(LOGQ + 1);
   const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * 2 * C::Q * W + w;
   float2* xb = xch + w * C::CXS;
   float2* y0 = yb + w * C::CYS;
+  unsigned phase = 0;
+  bool ok = true;
 
   for (int c = 0; c < p.cout; ++c) {
-    float2* tileA = p.work + ((long long)b * p.cout + c) * p.ny * C::P + (long long)t * p.ny * W + w;
+    float2* tileA = tile_of(c) + w;
+    const float2* src = C::TMA ? (const float2*)(tb + w) : (const float2*)tileA;
+    if (C::TMA) {
+      if (!mbar_wait_bounded(mbar, phase)) ok = false;
+      phase ^= 1u;
+    }
 #pragma unroll
     for (int par = 0; par < 2; ++par) {
       float2 v[C::EC];
 #pragma unroll
       for (int m = 0; m < C::EC; ++m) {
         const int n = j + m * C::TC;
-        const float2 a = n < p.ny ? tileA[(long long)n * W] : make_float2(0.f, 0.f);
+        const float2 a = n < p.ny ? src[(long long)n * W] : make_float2(0.f, 0.f);
         v[m] = par ? cmul(a, twP[n]) : a;
+      }
+      if (C::TMA && par == 1) {
+        __syncthreads();   // every thread has read the staged tile
+        if (tid == 0 && c + 1 < p.cout) {
+          fence_proxy_async();
+          bulk_g2s(tb, tile_of(c + 1), tile_bytes, mbar);
+        }
       }
       block_fft_s<LOGQ, C::EC, -1>(v, j, xb, stw);
       const float2* sp = spec + (long long)par * C::Q * W;
@@ -311,6 +346,10 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::CONV_THREADS) rs_cols_conv(const 
         }
       }
     }
+  }
+  if (!ok) {
+    atomicAdd(&g_rs_timeouts, 1u);
+    if (tid == 0) mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
   }
 }
 
@@ -431,7 +470,7 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     rs_rows_fwd<LOGQ><<<g_rows, C::ROW_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_rows_fwd");
   } else if (stage == 1) {
-    const size_t sm = (size_t)(C::W * C::CXS + C::TWC + C::W * C::CYS) * sizeof(float2);
+    const size_t sm = (size_t)(C::TBASE + (C::TMA ? p.ny * C::W + 1 : 0)) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
     rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::CONV_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
@@ -475,6 +514,21 @@ cudaError_t rs_upload_twiddles(const float2* host) {
 }  // namespace xl
 
 using namespace xl;
+
+extern "C" int xl_device_timeouts(unsigned int* count, int reset) {
+  if (!count) {
+    set_error("xl_device_timeouts: null output");
+    return XL_EINVAL;
+  }
+  cudaError_t e = cudaMemcpyFromSymbol(count, g_rs_timeouts, sizeof(unsigned int));
+  if (e != cudaSuccess) return cuda_fail(e, "xl_device_timeouts");
+  if (reset) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_rs_timeouts, &zero, sizeof(unsigned int));
+    if (e != cudaSuccess) return cuda_fail(e, "xl_device_timeouts reset");
+  }
+  return XL_OK;
+}
 
 extern "C" size_t xl_rs_spectrum_bytes(int ny, int nx) {
   if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE) return 0;

@@ -245,10 +245,35 @@ def op_lens(x, y, wavelength, radius, focal, vector):
     return JonesOp(_lib.OP_SEPMASK, ptrs=[c, r, tct, trt], sval=[1.0 if vector else 0.0])
 
 
+_highna_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def highna_coefficients(x, y, radius, f):
+    """The lens's 6 per-pixel coefficient planes, cached by geometry (computed by libxlgb)."""
+    key = (x.tobytes(), y.tobytes(), float(radius), float(f), torch.cuda.current_device())
+    with _LOCK:
+        t = _highna_cache.get(key)
+        if t is not None:
+            _highna_cache.move_to_end(key)
+            return t
+    t = torch.empty((6, len(y), len(x)), dtype=torch.float32, device=device())
+    _lib.check(lib().xl_highna_coefficients(stream_handle(), len(y), len(x), device_grid(x).data_ptr(),
+                                            device_grid(y).data_ptr(), float(radius), float(f), t.data_ptr()),
+               "xl_highna_coefficients")
+    torch.cuda.current_stream().synchronize()   # shared across streams once cached
+    with _LOCK:
+        _highna_cache[key] = t
+        while len(_highna_cache) > 8:
+            _highna_cache.popitem(last=False)
+    return t
+
+
 def op_high_na(x, y, radius, f):
     """optical_elements.py:515-594 as one per-pixel op (returns the op and sin(theta_max))."""
     s_max = radius / np.sqrt(radius ** 2 + f ** 2)
-    op = JonesOp(_lib.OP_HIGHNA, ptrs=[device_grid(x), device_grid(y)], dval=[radius, f, s_max])
+    coef = highna_coefficients(x, y, radius, f)
+    op = JonesOp(_lib.OP_HIGHNA, ptrs=[device_grid(x), device_grid(y), coef],
+                 dval=[radius, f, s_max, 1.0 / (radius * radius)])
     return op, s_max
 
 
