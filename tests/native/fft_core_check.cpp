@@ -29,6 +29,18 @@ static void emu_s(std::vector<Regs<E>>& V, float2* sm, const float2* stw) {
   }
 }
 
+// The pass sequence the zero-padded propagators run: pass tables, the first
+// pass pruned for a zero upper half of the input.
+template <int LOGN, int E, int DIR, int P>
+static void emu_x(std::vector<Regs<E>>& V, float2* sm, const float2* stw) {
+  using S = FftShape<LOGN, E>;
+  for (int j = 0; j < S::T; ++j) fft_pass_x<LOGN, E, P, DIR, P == 0, false>(V[j].v, j, sm, stw);
+  if constexpr (P < S::NPASS - 1) {
+    for (int j = 0; j < S::T; ++j) fft_gather<LOGN, E>(V[j].v, j, sm);
+    emu_x<LOGN, E, DIR, P + 1>(V, sm, stw);
+  }
+}
+
 static int g_use_stw = 0;
 
 static int g_e = 16;
@@ -47,7 +59,13 @@ static void run_e(const float* in, float* out) {
       int n = j + m * S::T;
       V[j].v[m] = make_float2(in[2 * n], in[2 * n + 1]);
     }
-  if (g_use_stw) {
+  if (g_use_stw == 2) {
+    if constexpr (E == 16) {
+      std::vector<float2> stw(FftTw<LOGN, E>::SIZE);
+      for (int i = 0; i < FftTw<LOGN, E>::SIZE; ++i) stw[i] = pass_twiddle_entry<LOGN, E>(i, tw.data());
+      emu_x<LOGN, E, DIR, 0>(V, sm.data(), stw.data());
+    }
+  } else if (g_use_stw) {
     std::vector<float2> stw(FftTw<LOGN, E>::SIZE);
     for (int i = 0; i < FftTw<LOGN, E>::SIZE; ++i) stw[i] = pass_twiddle_entry<LOGN, E>(i, tw.data());
     emu_s<LOGN, E, DIR, 0>(V, sm.data(), stw.data());
@@ -90,6 +108,18 @@ extern "C" void fft_core_set_e(int e) { g_e = e; }
 extern "C" int fft_core_check_stw(int logn, int dir, const float* in, float* out) {
   g_use_stw = 1;
   int rc = dir < 0 ? dispatch<-1>(logn, in, out) : dispatch<1>(logn, in, out);
+  g_use_stw = 0;
+  return rc;
+}
+
+// FFT of a line whose upper half is zero (in[N/2..N-1] are ignored), with the
+// first pass pruned; 16 elements per thread.
+extern "C" int fft_core_check_zu(int logn, int dir, const float* in, float* out) {
+  g_use_stw = 2;
+  const int saved = g_e;
+  g_e = 16;
+  int rc = (logn < 5) ? -1 : (dir < 0 ? dispatch<-1>(logn, in, out) : dispatch<1>(logn, in, out));
+  g_e = saved;
   g_use_stw = 0;
   return rc;
 }

@@ -17,6 +17,7 @@ def fftlib(tmp_path_factory):
     lib = ctypes.CDLL(str(out))
     lib.fft_core_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.fft_core_check_stw.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.fft_core_check_zu.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     return lib
 
 
@@ -32,6 +33,24 @@ def test_block_fft_matches_numpy(fftlib, logn, direction, tables, elems):
     fftlib.fft_core_set_e(elems)
     fn = fftlib.fft_core_check if tables == "global" else fftlib.fft_core_check_stw
     assert fn(logn, direction, x.ctypes.data, out.ctypes.data) == 0
+    ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
+    err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert err < 2e-7 * logn, err
+
+
+@pytest.mark.parametrize("logn", range(5, 14))
+@pytest.mark.parametrize("direction", [-1, 1])
+def test_zero_padded_fft_matches_numpy(fftlib, logn, direction):
+    """The pruned first pass of a line whose upper half is zero (the propagators'
+    zero padding): only the lower half is read, the result is the full FFT."""
+    n = 1 << logn
+    rng = np.random.default_rng(100 + logn)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    garbage = x.copy()
+    garbage[n // 2:] = 1e30   # never read
+    x[n // 2:] = 0
+    out = np.empty_like(x)
+    assert fftlib.fft_core_check_zu(logn, direction, garbage.ctypes.data, out.ctypes.data) == 0
     ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
     err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
     assert err < 2e-7 * logn, err

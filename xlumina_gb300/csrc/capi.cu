@@ -27,6 +27,21 @@ int cuda_fail(cudaError_t e, const char* where) {
 static std::mutex g_init_mu;
 static bool g_init_dev[256];
 
+struct DeviceTables {
+  TableUpload upload;
+  TimeoutCounter timeouts;
+};
+
+static std::vector<DeviceTables>& registry() {
+  static std::vector<DeviceTables> r;
+  return r;
+}
+
+bool register_device_tables(TableUpload upload, TimeoutCounter timeouts) {
+  registry().push_back({upload, timeouts});
+  return true;
+}
+
 // Twiddle tables for S = 1, 2, 4, ..., XL_MAX_FFT at offset S: e^{-2 pi i q / S},
 // computed in float64 and rounded once.
 static const std::vector<float2>& host_twiddles() {
@@ -53,9 +68,8 @@ int ensure_init() {
   std::lock_guard<std::mutex> lk(g_init_mu);
   if (g_init_dev[dev]) return XL_OK;
   const float2* h = host_twiddles().data();
-  if ((e = rs_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (rs)");
-  if ((e = czt_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (czt)");
-  if ((e = elem_upload_twiddles(h)) != cudaSuccess) return cuda_fail(e, "upload twiddles (elem)");
+  for (const DeviceTables& t : registry())
+    if ((e = t.upload(h)) != cudaSuccess) return cuda_fail(e, "upload device tables");
   g_init_dev[dev] = true;
   return XL_OK;
 }
@@ -67,3 +81,20 @@ extern "C" const char* xl_last_error(void) { return xl::g_err; }
 extern "C" int xl_version(void) { return 100; }
 
 extern "C" int xl_init(void) { return xl::ensure_init(); }
+
+extern "C" int xl_device_timeouts(unsigned int* count, int reset) {
+  if (!count) {
+    xl::set_error("xl_device_timeouts: null output");
+    return XL_EINVAL;
+  }
+  unsigned int total = 0;
+  for (const xl::DeviceTables& t : xl::registry()) {
+    if (!t.timeouts) continue;
+    unsigned int c = 0;
+    cudaError_t e = t.timeouts(&c, reset);
+    if (e != cudaSuccess) return xl::cuda_fail(e, "xl_device_timeouts");
+    total += c;
+  }
+  *count = total;
+  return XL_OK;
+}

@@ -111,37 +111,47 @@ __device__ __forceinline__ float op_param(const XlOp& op, int i, const PixelCtx&
   return op.sval[i];
 }
 
-// Apply one op to the pixel's (Ex, Ey, Ez) (scalar fields use e[0] only).
-__device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const PixelCtx& px) {
+// Per-pixel parameters read from the op's planes in global memory.
+struct GlobalParams {
+  __device__ __forceinline__ float operator()(const XlOp& op, int, int i, const PixelCtx& px) const {
+    return op_param(op, i, px);
+  }
+};
+
+// Apply op number k of a program to the pixel's (Ex, Ey, Ez) (scalar fields
+// use e[0] only); its real parameters come from the reader pr(op, k, i, px).
+template <class PR>
+__device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3], const PixelCtx& px,
+                                           const PR& pr) {
   switch (op.kind) {
     case XL_OP_PHASE: {  // scalar SLM: field * e^{i phi}
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
+      sincosf(pr(op, k, 0, px), &s, &c);
       e[0] = cmul(e[0], make_float2(c, s));
       break;
     }
     case XL_OP_SSLM: {  // diag(e^{i a}, e^{i p}); Ez unchanged
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
+      sincosf(pr(op, k, 0, px), &s, &c);
       e[0] = cmul(e[0], make_float2(c, s));
-      sincosf(op_param(op, 1, px), &s, &c);
+      sincosf(pr(op, k, 1, px), &s, &c);
       e[1] = cmul(e[1], make_float2(c, s));
       break;
     }
     case XL_OP_SSLM_AMP: {  // diag(A1 e^{i a}, A2 e^{i p}); Ez unchanged
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
-      e[0] = cscale(cmul(e[0], make_float2(c, s)), op_param(op, 2, px));
-      sincosf(op_param(op, 1, px), &s, &c);
-      e[1] = cscale(cmul(e[1], make_float2(c, s)), op_param(op, 3, px));
+      sincosf(pr(op, k, 0, px), &s, &c);
+      e[0] = cscale(cmul(e[0], make_float2(c, s)), pr(op, k, 2, px));
+      sincosf(pr(op, k, 1, px), &s, &c);
+      e[1] = cscale(cmul(e[1], make_float2(c, s)), pr(op, k, 3, px));
       break;
     }
     case XL_OP_LCD: {  // general retarder with delta = 0 (eta, theta); Ez unchanged
       float sh, ch, s2, c2;
       float st, ct;
-      if (op.pmask & 1) sincosf(0.5f * op_param(op, 0, px), &sh, &ch);
+      if (op.pmask & 1) sincosf(0.5f * pr(op, k, 0, px), &sh, &ch);
       else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
-      if (op.pmask & 2) sincosf(op_param(op, 1, px), &st, &ct);
+      if (op.pmask & 2) sincosf(pr(op, k, 1, px), &st, &ct);
       else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
       // a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2)
       c2 = ct * ct - st * st;
@@ -156,7 +166,7 @@ __device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const P
     }
     case XL_OP_LP: {  // linear polarizer at alpha; Ez set to zero
       float s, c;
-      if (op.pmask & 1) sincosf(op_param(op, 0, px), &s, &c);
+      if (op.pmask & 1) sincosf(pr(op, k, 0, px), &s, &c);
       else { c = op.sval[2]; s = op.sval[3]; }   // scalar alpha: cos, sin from the host
       const float2 x = e[0], y = e[1];
       e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
@@ -200,8 +210,17 @@ __device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const P
   }
 }
 
+template <class PR>
+__device__ __forceinline__ void apply_prog_r(const XlProg& prog, float2 (&e)[3], const PixelCtx& px, const PR& pr) {
+  for (int i = 0; i < prog.nops; ++i) apply_op_r(prog.ops[i], i, e, px, pr);
+}
+
+__device__ __forceinline__ void apply_op(const XlOp& op, float2 (&e)[3], const PixelCtx& px) {
+  apply_op_r(op, 0, e, px, GlobalParams{});
+}
+
 __device__ __forceinline__ void apply_prog(const XlProg& prog, float2 (&e)[3], const PixelCtx& px) {
-  for (int i = 0; i < prog.nops; ++i) apply_op(prog.ops[i], e, px);
+  apply_prog_r(prog, e, px, GlobalParams{});
 }
 
 // ---- backward of one op ----
@@ -355,12 +374,39 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* mbar, unsigned
   return ok != 0;
 }
 
-// Bounded wait for phase `phase` of the barrier.  Returns false if the
-// iteration limit ran out (the caller records the error and skips its work).
+// Arm the barrier for `bytes` of bulk copies (one arrival, by one thread).
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* mbar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// One bulk copy global -> shared completing on an armed barrier (16-byte
+// aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes,
+                                              unsigned long long* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for phase `phase` of the barrier: gives up after about a
+// second of wall time and returns false (the caller records the error and
+// carries on without the data; it never spins forever).
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* mbar, unsigned phase) {
-  for (int it = 0; it < (1 << 22); ++it)
+  if (mbar_try_wait(mbar, phase)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(mbar, phase)) return true;
-  return false;
+    if (global_ns() - t0 > 1000000000ull) return false;
+  }
 }
 
 }  // namespace xl

@@ -327,9 +327,11 @@ static int dispatch_cols(cudaStream_t st, const CztLaunch& p, int lq) {
   return XL_EUNSUPPORTED;
 }
 
-cudaError_t czt_upload_twiddles(const float2* host) {
+static cudaError_t czt_upload_twiddles(const float2* host) {
   return cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
 }
+
+static const bool czt_registered = register_device_tables(&czt_upload_twiddles, nullptr);
 
 }  // namespace xl
 

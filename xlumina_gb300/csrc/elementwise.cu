@@ -163,9 +163,11 @@ __global__ void highna_plane_kernel(int ny, int nx, XlOp op, float* out) {
   }
 }
 
-cudaError_t elem_upload_twiddles(const float2* host) {
+static cudaError_t elem_upload_twiddles(const float2* host) {
   return cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
 }
+
+static const bool elem_registered = register_device_tables(&elem_upload_twiddles, nullptr);
 
 }  // namespace xl
 

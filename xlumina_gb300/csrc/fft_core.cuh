@@ -108,12 +108,34 @@ template <int DIR> XL_HD void dft8(float2* a) {
   a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
 }
 
+template <int DIR> XL_HD void dft16_tail(float2* a);
+
 template <int DIR> XL_HD void dft16(float2* a) {
   // 4 x 4: inner DFT4 over stride-4 subsequences, twiddle w16^(n2 k1), outer DFT4.
   dft4<DIR>(a[0], a[4], a[8], a[12]);
   dft4<DIR>(a[1], a[5], a[9], a[13]);
   dft4<DIR>(a[2], a[6], a[10], a[14]);
   dft4<DIR>(a[3], a[7], a[11], a[15]);
+  dft16_tail<DIR>(a);
+}
+
+// 16-point DFT of a[0..7] when a[8..15] are zero (a zero-padded line): the
+// inner DFT4s see two nonzero inputs each.
+template <int DIR> XL_HD void dft16_half(float2* a) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    const float2 x0 = a[n2], x1 = a[n2 + 4];
+    const float2 ix1 = cmul_dir_i<DIR>(x1);
+    a[n2] = cadd(x0, x1);
+    a[n2 + 4] = cadd(x0, ix1);
+    a[n2 + 8] = csub(x0, x1);
+    a[n2 + 12] = csub(x0, ix1);
+  }
+  dft16_tail<DIR>(a);
+}
+
+// Second half of the 4 x 4 DFT16: twiddles w16^(n2 k1), outer DFT4s, transpose.
+template <int DIR> XL_HD void dft16_tail(float2* a) {
   // slot n2 + 4 k1 holds Y[n2][k1]
   a[5] = cmul_w16<DIR, 1>(a[5]);
   a[9] = cmul_w16<DIR, 2>(a[9]);
@@ -275,7 +297,97 @@ XL_HD void fft_pass_s(float2 (&v)[E], int j, float2* sm, const float2* stw) {
   }
 }
 
+// Twiddle read: the read-only data path for tables in global memory (GTW),
+// an ordinary load for tables in shared memory.
+template <bool GTW> XL_HD float2 tw_load(const float2* p) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (GTW) return __ldg(p);
+#endif
+  return *p;
+}
+
+// Stockham pass with twiddles from the pass tables (FftTw layout), either in
+// shared memory or in global memory (GTW).  ZU: this is pass 0 of a
+// zero-padded line whose upper half is zero, so v[E/2..E-1] are zero on entry
+// and are not read (E = 16, radix 16 only).
+template <int LOGN, int E, int P, int DIR, bool ZU, bool GTW>
+XL_HD void fft_pass_x(float2 (&v)[E], int j, float2* sm, const float2* stw, int toff = 0) {
+  using S = FftShape<LOGN, E>;
+  constexpr int R = S::template radix<P>();
+  constexpr int NS = S::template stride<P>();
+  constexpr bool LAST = (P == S::NPASS - 1);
+  constexpr int BPT = E / R;
+  constexpr int OFF = FftTw<LOGN, E>::template off<P>();
+  static_assert(!ZU || (P == 0 && R == 16 && E == 16), "input pruning is for a first radix-16 pass");
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = j + t * S::T;
+    const int k = b & (NS - 1);
+    float2 x[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) x[i] = (ZU && i >= R / 2) ? make_float2(0.f, 0.f) : v[t + i * BPT];
+    if constexpr (R == 16 && NS > 1) {
+      // twiddle the inputs of one inner DFT4 at a time (inputs n2 + 4 q), so
+      // only four twiddles are live at once
+#pragma unroll
+      for (int n2 = 0; n2 < 4; ++n2) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = n2 + 4 * q;
+          if (i == 0) continue;
+          const float2 w = tw_load<GTW>(stw + toff + OFF + (i - 1) * NS + k);
+          x[i] = DIR < 0 ? cmul(x[i], w) : cmulc(x[i], w);
+        }
+        dft4<DIR>(x[n2], x[n2 + 4], x[n2 + 8], x[n2 + 12]);
+      }
+      dft16_tail<DIR>(x);
+    } else {
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int i = 1; i < R; ++i) {
+          const float2 w = tw_load<GTW>(stw + toff + OFF + (i - 1) * NS + k);
+          x[i] = DIR < 0 ? cmul(x[i], w) : cmulc(x[i], w);
+        }
+      }
+      if constexpr (ZU) dft16_half<DIR>(x);
+      else dftR<R, DIR>(x);
+    }
+    if constexpr (LAST) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[t + i * BPT] = x[i];
+    } else {
+      const int base = (b / NS) * (NS * R) + k;
+#pragma unroll
+      for (int i = 0; i < R; ++i) sm[smpad(base + i * NS)] = x[i];
+    }
+  }
+}
+
 #if defined(__CUDACC__)
+// Whole FFT for a thread group, twiddles from pass tables (shared or global),
+// optional input pruning (ZU).  Every thread of the CTA must call it the same
+// number of times (it uses __syncthreads between passes).
+//
+// The twiddle offset is laundered through an empty asm statement at the start
+// of every transform: a kernel that runs several transforms in a row then
+// reloads the (identical) twiddles for each one instead of keeping them all
+// live in registers, which would cost about a hundred registers per thread.
+template <int LOGN, int E, int DIR, bool ZU, bool GTW, int P = 0>
+__device__ __forceinline__ void block_fft_x(float2 (&v)[E], int j, float2* sm, const float2* stw, int toff = -1) {
+  using S = FftShape<LOGN, E>;
+  if constexpr (P == 0) {
+    toff = 0;
+    asm volatile("" : "+r"(toff));
+  }
+  fft_pass_x<LOGN, E, P, DIR, ZU && P == 0, GTW>(v, j, sm, stw, toff);
+  if constexpr (P < S::NPASS - 1) {
+    __syncthreads();
+    fft_gather<LOGN, E>(v, j, sm);
+    __syncthreads();
+    block_fft_x<LOGN, E, DIR, false, GTW, P + 1>(v, j, sm, stw, toff);
+  }
+}
+
 // Whole FFT for a thread group.  Every thread of the CTA must call these the
 // same number of times (they use __syncthreads between passes).
 template <int LOGN, int E, int DIR, int P = 0>

@@ -32,9 +32,12 @@ inline cudaError_t allow_smem(K kernel, size_t bytes) {
     if (_e != cudaSuccess) return ::xl::cuda_fail(_e, where);   \
   } while (0)
 
-// Per-translation-unit twiddle upload hooks (each TU has its own table copy).
-cudaError_t rs_upload_twiddles(const float2* host);
-cudaError_t czt_upload_twiddles(const float2* host);
-cudaError_t elem_upload_twiddles(const float2* host);
+// Each translation unit with kernels holds its own copy of the device tables
+// (whole-program compilation, one device module per unit).  It registers,
+// from a static initialiser, the function that fills them from the host
+// twiddles and, optionally, a reader of its device timeout counter.
+using TableUpload = cudaError_t (*)(const float2* host_twiddles);
+using TimeoutCounter = cudaError_t (*)(unsigned int* count, int reset);
+bool register_device_tables(TableUpload upload, TimeoutCounter timeouts);
 
 }  // namespace xl

@@ -1,0 +1,674 @@
+// Rayleigh-Sommerfeld propagation (scalar RS and vectorial VRS) for sm_103a:
+// the kernels and their launch code, included by the rs_q*.cu translation units.
+//
+// The reference (wave_optics.py:281-289) zero-pads the N x N field to
+// (2N-1)^2, multiplies fft2(U) by fft2(H) and crops [N-1:, N-1:].  Here the
+// same linear convolution runs on a P x P grid, P = 2Q and Q the next power
+// of two >= N, which gives the identical result because the impulse response
+// is placed at wrapped offsets.  Three passes:
+//
+//   row pass (rs_rows_fwd): for each of the N input rows, the P-point
+//       spectrum of the zero-padded row (the first FFT pass is pruned: half
+//       its inputs are zero).  The Jones program and the VRS Ez derivation run
+//       here.  The kernel is persistent; each CTA stages its next rows (field
+//       planes and per-pixel parameter planes) into shared memory with TMA
+//       bulk copies while it transforms the current ones.
+//   column pass (rs_cols_conv): for each of the P spectrum columns, the
+//       P-point FFT along y (pruned input), the multiply by the transfer
+//       spectrum, the inverse FFT, and the N output rows that survive the crop
+//       (the last pass computes only those), written back in place.
+//   inverse row pass (rs_rows_inv): inverse P-point FFT of each row, crop to
+//       N columns, optional fused epilogue program, store.  The loads of the
+//       next row are in flight while the current one is transformed.
+//
+// Intermediate data per component: N rows x P complex64 in column tiles of W:
+// element (row r, column c) at ((c / W) * N + r) * W + c % W, so a column
+// tile is contiguous and a row is W-wide contiguous runs.  Transfer spectra
+// (P x P complex64, natural frequency order) are built once per
+// (z, wavelength, grid) by rs_hhat_rows / rs_hhat_cols in the same column-tile
+// layout with P rows: S[((kx / W) * P + ky) * W + kx % W].
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "rs_host.h"
+
+namespace xl {
+
+// Shapes of the RS kernels for Q = 2^LOGQ.  Every line transform is a
+// P-point FFT by T = P / 16 threads holding 16 elements each; thread j holds
+// elements j + m T, so the nonzero (and surviving) half of a line is m < 8.
+template <int LOGQ> struct RsCfg {
+  static constexpr int LOGP = LOGQ + 1;
+  static constexpr int Q = 1 << LOGQ;
+  static constexpr int P = 2 * Q;
+  static constexpr int E = 16;
+  static constexpr int H = E / 2;
+  static constexpr int T = P / E;
+  static constexpr int XS = P + P / 16;                       // exchange slots per line
+  static constexpr int G = (256 / T) > 1 ? (256 / T) : 1;     // lines per CTA in the row passes
+  static constexpr int ROW_THREADS = G * T;
+  // column-tile width; lanes of a warp interleave the W columns of a tile
+  static constexpr int W = LOGQ >= 12 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
+  // per-column padding of the column pass's exchange buffers: without it the
+  // W interleaved buffers would start on the same bank
+  static constexpr int CPAD = W >= 8 ? 0 : 4;
+  static constexpr int CXS = XS + CPAD;
+  static constexpr int COL_THREADS = W * T;
+  static constexpr int NTW = FftTw<LOGP, E>::SIZE;           // pass twiddle table entries
+  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024, "column CTA shape");
+};
+
+// Pass twiddle tables (FftTw layout, 16 elements per thread) for every
+// P = 2^5 .. 2^13, one after the other, filled at set-up from float64 values.
+__host__ __device__ constexpr int ptw_size(int logp) {
+  // sum over passes 1.. of (radix - 1) * stride, radix 16 then the remainder
+  int nfull = logp / 4, rem = logp % 4, npass = nfull + (rem ? 1 : 0), o = 0, ns = 1;
+  for (int q = 0; q < npass; ++q) {
+    const int r = q < nfull ? 16 : (1 << rem);
+    if (q >= 1) o += (r - 1) * ns;
+    ns *= r;
+  }
+  return o > 0 ? o : 1;
+}
+__host__ __device__ constexpr int ptw_off(int logp) {
+  int o = 0;
+  for (int l = 5; l < logp; ++l) o += ptw_size(l);
+  return o;
+}
+constexpr int PTW_TOTAL = ptw_off(14);
+
+// Each translation unit holds its own copy (filled by its registered upload).
+static __device__ float2 g_ptw[PTW_TOTAL];
+
+template <int LOGP> __device__ __forceinline__ const float2* pass_tw() {
+  static_assert(ptw_size(LOGP) == FftTw<LOGP, 16>::SIZE, "pass table size");
+  return g_ptw + ptw_off(LOGP);
+}
+
+// Address of (row r, column col) in a column-tiled plane with `rows` rows.
+template <int W>
+__device__ __forceinline__ long long tiled(int r, int col, int rows) {
+  return ((long long)(col / W) * rows + r) * W + (col % W);
+}
+
+// Element addresses of one row (columns j + m T) in a column-tiled plane.
+// The base pointer and stride pass through empty asm statements so that the
+// compiler recomputes them per row and component instead of keeping sixteen
+// 64-bit addresses live across the unrolled component loop.
+template <int LOGQ, class Tp>
+struct RowPtr {
+  Tp* q;
+  long long step;
+  __device__ __forceinline__ RowPtr(Tp* plane, int r, int j, int rows) {
+    using C = RsCfg<LOGQ>;
+    q = plane + tiled<C::W>(r, j, rows);
+    step = (long long)C::T * rows;
+    asm volatile("" : "+l"(q), "+l"(step));
+  }
+  __device__ __forceinline__ Tp& operator[](int m) const { return q[m * step]; }
+};
+
+// ---------------------------------------------------------------------------
+// Transfer spectrum, step 1: rows of the wrapped impulse response -> P-point
+// row spectra, row-major in natural order.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
+    rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double z,
+                 double inv_lambda, float k, float2* __restrict__ out) {
+  using C = RsCfg<LOGQ>;
+  extern __shared__ __align__(16) float2 smem[];
+  const int tid = threadIdx.x;
+  const int gi = tid / C::T, j = tid % C::T;
+  const int i = blockIdx.x * C::G + gi;   // row of the wrapped response (< P)
+  const bool vy = (i < ny) || (i > C::P - ny);
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int col = j + m * C::T;
+    const bool vx = (col < nx) || (col > C::P - nx);
+    v[m] = (vy && vx) ? rs_kernel_value(offx[col], offy[i], z, inv_lambda, k) : make_float2(0.f, 0.f);
+  }
+  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + gi * C::XS, pass_tw<C::LOGP>());
+  float2* dst = out + (long long)i * C::P;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) dst[j + m * C::T] = v[m];
+}
+
+// Transfer spectrum, step 2: P-point column transforms of the row spectra,
+// times `scale`, stored column-tiled: S[((kx / W) * P + ky) * W + kx % W].
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS)
+    rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
+  using C = RsCfg<LOGQ>;
+  constexpr int W = C::W, LPW = 32 / W;
+  extern __shared__ __align__(16) float2 smem[];
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
+  const int t = blockIdx.x;
+  float2 v[16];
+  const float2* src = in + t * W + w;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = src[(long long)(j + m * C::T) * C::P];
+  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + w * C::CXS, pass_tw<C::LOGP>());
+  float2* dst = out + (long long)t * C::P * W + w;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * W] = cscale(v[m], scale);
+}
+
+// ---------------------------------------------------------------------------
+// Rows of the forward row pass staged into shared memory by TMA bulk copies:
+// up to XL_RS_STREAMS planes (input components and per-pixel parameter
+// planes of the fused program), each copied G rows at a time.
+#define XL_RS_STREAMS 8
+struct RsStream {
+  const char* src;      // row 0 of batch entry 0
+  long long bstride;    // bytes between batch entries (0: shared by the batch)
+  int row_bytes;        // bytes of one row (the plane's row stride), a multiple of 16
+  int soff;             // byte offset of the stream's G rows in the stage
+};
+struct RsStage {
+  int n;                       // staged streams
+  int row_bytes;               // sum of the streams' row bytes
+  RsStream s[XL_RS_STREAMS];
+  int fld[3];                  // stage offset of input component c, -1: read from global memory
+  int prm[XL_MAX_OPS][4];      // stage offset of parameter plane i of op k, -1: global memory
+};
+
+// Per-pixel parameters of the fused program, from the stage when the plane is
+// staged, else from global memory.
+struct StagedParams {
+  const unsigned char* stage;
+  const RsStage* st;
+  int gi, nx, n;
+  __device__ __forceinline__ float operator()(const XlOp& op, int k, int i, const PixelCtx& px) const {
+    if (!(op.pmask & (1 << i))) return op.sval[i];
+    const int off = st->prm[k][i];
+    if (off >= 0) return ((const float*)(stage + off))[gi * nx + n];
+    return __ldg((const float*)op.ptr[i] + (long long)px.batch * op.pbstride + px.pix);
+  }
+};
+
+// Bounded waits that ran out, counted per translation unit (read by xl_device_timeouts).
+static __device__ unsigned int g_rs_timeouts;
+
+// Thread organisation of the row passes for NC transformed components: CG
+// component groups of G lines of T threads, where CG = NC (every component of
+// a row transformed at once) when the CTA can hold them, else 1 (the
+// components one after the other).
+template <int LOGQ, int NC> struct RowCfg {
+  using C = RsCfg<LOGQ>;
+  static constexpr int CG = (NC * C::G * C::T <= 1024) ? NC : 1;
+  static constexpr int LINES = CG * C::G;
+  static constexpr int THREADS = LINES * C::T;
+  static constexpr int MINB = (768 / THREADS) > 1 ? (768 / THREADS) : 1;   // resident CTAs per SM
+};
+
+// Forward row pass.  MODE 1: scalar RS (one component); 2: VRS (Ex, Ey in;
+// Ex, Ey, Ez out, Ez derived); 3: VRS adjoint (three gradients in and out).
+// Persistent: CTA c handles row groups c, c + grid, ...  Per row group the
+// prologue runs the fused program over every pixel and writes the components
+// to a shared buffer; the stage is then free, so the bulk copies of the next
+// row group start while the component groups transform this one.
+template <int LOGQ, int MODE>
+__global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowCfg<LOGQ, MODE == 1 ? 1 : 3>::MINB)
+    rs_rows_fwd(const __grid_constant__ RsLaunch p, const __grid_constant__ RsStage st) {
+  using C = RsCfg<LOGQ>;
+  constexpr int NC = MODE == 1 ? 1 : 3;
+  constexpr int CIN = MODE;
+  using F = RowCfg<LOGQ, NC>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = p.nx, ny = p.ny;
+  float2* xch = (float2*)smraw;                                      // LINES x XS
+  float2* post = xch + F::LINES * C::XS;                             // NC x G x nx
+  float* xf = (float*)(post + (size_t)NC * C::G * nx);               // nx (VRS: x as float32)
+  const size_t soff = ((size_t)(F::LINES * C::XS + NC * C::G * nx) * 8 + (MODE == 2 ? (size_t)nx * 4 : 0) + 15) /
+                      16 * 16;
+  unsigned char* stage = smraw + soff;
+  unsigned long long* mbar = (unsigned long long*)(stage + (size_t)C::G * st.row_bytes);
+  const int tid = threadIdx.x;
+  const int line = tid / C::T, j = tid % C::T;
+  const int cg = line / C::G, gi = line % C::G;
+  const int ngb = (ny + C::G - 1) / C::G;
+  const int total = p.B * ngb;
+  const bool staged = st.n > 0;
+
+  if (tid == 0 && staged) {
+    mbar_init(mbar, 1);
+    fence_mbar_init();
+  }
+  if constexpr (MODE == 2)
+    for (int i = tid; i < nx; i += blockDim.x) xf[i] = (float)p.x[i];
+  __syncthreads();
+
+  auto issue = [&](int grp) {
+    const int b = grp / ngb, r0 = (grp - b * ngb) * C::G;
+    const int rows = min(C::G, ny - r0);
+    mbar_arrive_expect_tx(mbar, (unsigned)(rows * st.row_bytes));
+    for (int s = 0; s < st.n; ++s) {
+      const RsStream& q = st.s[s];
+      bulk_copy_g2s(stage + q.soff, q.src + (long long)b * q.bstride + (long long)r0 * q.row_bytes,
+                    (unsigned)(rows * q.row_bytes), mbar);
+    }
+  };
+  if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
+
+  unsigned phase = 0;
+  bool ok = true;
+  for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
+    const int b = grp / ngb;
+    const int r0 = (grp - b * ngb) * C::G;
+    if (staged) {
+      if (!mbar_wait_bounded(mbar, phase)) ok = false;
+      phase ^= 1u;
+    }
+    // prologue over the row group's pixels
+    {
+      int last = -1;
+      float Y = 0.f, z2 = 0.f;
+      for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
+        const int g2 = idx / nx, n = idx - g2 * nx, r = r0 + g2;
+        if (r >= ny) break;
+        const long long pix = (long long)r * nx + n;
+        float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int c = 0; c < CIN; ++c) {
+          const int fo = st.fld[c];
+          e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+        }
+        if (p.pre.nops) {
+          PixelCtx px{r, n, pix, b};
+          apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
+        }
+        if constexpr (MODE == 2) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
+          if (g2 != last) {
+            last = g2;
+            Y = (float)p.y[r];
+            const float zb = (float)p.z[b];
+            z2 = Y * Y + zb * zb;
+          }
+          const float X = xf[n];
+          const float inv = rsqrtf(X * X + z2);
+          e[2] = cadd(cscale(e[0], X * inv), cscale(e[1], Y * inv));
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
+      }
+    }
+    __syncthreads();   // every thread has read the stage and written its pixels
+    if (tid == 0 && staged && grp + gridDim.x < total) {
+      fence_proxy_async();
+      issue(grp + gridDim.x);
+    }
+    const int r = r0 + gi;
+    const bool live = r < ny;
+    for (int c = cg; c < NC; c += F::CG) {
+      float2 v[16];
+      const float2* src = post + (c * C::G + gi) * nx;
+#pragma unroll
+      for (int m = 0; m < C::H; ++m) {
+        const int n = j + m * C::T;
+        v[m] = (live && n < nx) ? src[n] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+      block_fft_x<C::LOGP, 16, -1, true, true>(v, j, xch + line * C::XS, pass_tw<C::LOGP>());
+      if (live) {
+        float2* plane = p.work + ((long long)b * NC + c) * ny * C::P;
+        if constexpr (C::T % C::W == 0) {
+          const RowPtr<LOGQ, float2> o(plane, r, j, ny);
+#pragma unroll
+          for (int m = 0; m < 16; ++m) o[m] = v[m];
+        } else {
+#pragma unroll
+          for (int m = 0; m < 16; ++m) plane[tiled<C::W>(r, j + m * C::T, ny)] = v[m];
+        }
+      }
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicAdd(&g_rs_timeouts, 1u);
+      mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
+    }
+  }
+}
+
+// Column pass, in place on one tile of W spectrum columns: FFT along y of the
+// ny nonzero rows (pruned first pass), multiply by the transfer spectrum
+// (conjugate for the adjoint), inverse FFT, keep the ny surviving rows.
+// Lanes interleave the W columns so every warp access is one contiguous run.
+template <int LOGQ>
+__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const __grid_constant__ RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  constexpr int W = C::W, LPW = 32 / W;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* xch = smem;                 // W x CXS
+  float2* stw = smem + W * C::CXS;    // NTW
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
+  const int t = blockIdx.x, b = blockIdx.y;
+  const int ny = p.ny;
+  {
+    const float2* g = pass_tw<C::LOGP>();
+    for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
+  }
+  __syncthreads();
+  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * C::P * W + w;
+  float2* xb = xch + w * C::CXS;
+  for (int c = 0; c < p.cout; ++c) {
+    float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      v[m] = n < ny ? tile[(long long)n * W] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
+    if (p.adjoint) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(spec + (long long)(j + m * C::T) * W));
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(spec + (long long)(j + m * C::T) * W));
+    }
+    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      if (n < ny) tile[(long long)n * W] = v[m];
+    }
+  }
+}
+
+// Inverse row pass: inverse P-point FFT per row and component, crop to nx
+// columns (the last pass computes only the surviving half), optional fused
+// epilogue program (or, for the VRS adjoint, the fold of the Ez gradient into
+// Ex, Ey), store.  Persistent, with the component groups of RowCfg; each
+// thread's loads of its next row are in flight in registers while the
+// current one is transformed.  With an epilogue the transformed rows go to a
+// shared buffer first, since the program needs every component of a pixel.
+template <int LOGQ, int COUT, bool EPI>
+__global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT>::MINB) rs_rows_inv(const __grid_constant__ RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  using F = RowCfg<LOGQ, COUT>;
+  extern __shared__ __align__(16) float2 smem[];
+  const int tid = threadIdx.x;
+  const int line = tid / C::T, j = tid % C::T;
+  const int cg = line / C::G, gi = line % C::G;
+  const int nx = p.nx, ny = p.ny;
+  const int ngb = (ny + C::G - 1) / C::G;
+  const int total = p.B * ngb;
+  float2* xb = smem + line * C::XS;
+  float2* post = smem + F::LINES * C::XS;     // COUT x G x nx (epilogue only)
+
+  auto load = [&](int grp, int c, float2 (&dst)[16]) {
+    const int b = grp / ngb;
+    int r = (grp - b * ngb) * C::G + gi;
+    r = r < ny ? r : ny - 1;    // rows past the end load a valid row and discard it
+    const float2* plane = p.work + ((long long)b * COUT + c) * ny * C::P;
+    if constexpr (C::T % C::W == 0) {
+      const RowPtr<LOGQ, const float2> q(plane, r, j, ny);
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dst[m] = q[m];
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) dst[m] = plane[tiled<C::W>(r, j + m * C::T, ny)];
+    }
+  };
+
+  float2 nxt[16];
+  if (blockIdx.x < total) load(blockIdx.x, cg, nxt);
+  for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
+    const int b = grp / ngb;
+    const int r0 = (grp - b * ngb) * C::G;
+    const int r = r0 + gi;
+    const bool live = r < ny;
+    for (int c = cg; c < COUT; c += F::CG) {
+      float2 v[16];
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = nxt[m];
+      if (c + F::CG < COUT) load(grp, c + F::CG, nxt);
+      else if (grp + gridDim.x < total) load(grp + gridDim.x, cg, nxt);
+      block_fft_x<C::LOGP, 16, 1, false, true>(v, j, xb, pass_tw<C::LOGP>());
+      if constexpr (!EPI) {
+        if (live) {
+          float2* o = p.out[c] + (long long)b * p.obs + (long long)r * nx;
+#pragma unroll
+          for (int m = 0; m < C::H; ++m) {
+            const int n = j + m * C::T;
+            if (n < nx) o[n] = v[m];
+          }
+        }
+      } else {
+        float2* d = post + (c * C::G + gi) * nx;
+#pragma unroll
+        for (int m = 0; m < C::H; ++m) {
+          const int n = j + m * C::T;
+          if (n < nx) d[n] = v[m];
+        }
+      }
+    }
+    if constexpr (EPI) {
+      __syncthreads();
+      const bool fold = p.adjoint && COUT == 3;   // VRS adjoint: Ez gradient folded into Ex, Ey
+      int last = -1;
+      float Y = 0.f, z2 = 0.f;
+      for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
+        const int g2 = idx / nx, n = idx - g2 * nx, ro = r0 + g2;
+        if (ro >= ny) break;
+        const long long o = (long long)b * p.obs + (long long)ro * nx + n;
+        float2 e[3];
+        const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e[c] = c < COUT ? post[(c * C::G + g2) * nx + n] : zero;
+        if (fold) {  // adjoint of Ez = Ex X/r + Ey Y/r (vectorized_optics.py:258-261)
+          if (g2 != last) {
+            last = g2;
+            Y = (float)p.y[ro];
+            const float zb = (float)p.z[b];
+            z2 = Y * Y + zb * zb;
+          }
+          const float X = (float)p.x[n];
+          const float inv = rsqrtf(X * X + z2);
+          p.out[0][o] = cadd(e[0], cscale(e[2], X * inv));
+          p.out[1][o] = cadd(e[1], cscale(e[2], Y * inv));
+          continue;
+        }
+        PixelCtx px{ro, n, (long long)ro * nx + n, b};
+        apply_prog(p.post, e, px);
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) p.out[c][o] = e[c];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+// SM count of the current device (cached per device).
+static int device_sms() {
+  static int sms[256];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return 132;
+  if (!sms[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
+    sms[dev] = v;
+  }
+  return sms[dev];
+}
+
+// Grid of a persistent kernel: every resident CTA slot, at most `work` CTAs.
+template <typename K>
+static int persistent_grid(K kernel, int threads, size_t smem, int work) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const long long g = (long long)per_sm * device_sms();
+  return (int)(g < work ? g : work);
+}
+
+template <int LOGQ>
+int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy, double z,
+                double wavelength, double scale, float2* spec, float2* work) {
+  using C = RsCfg<LOGQ>;
+  const size_t sm1 = (size_t)C::G * C::XS * sizeof(float2);
+  cudaError_t e = allow_smem(rs_hhat_rows<LOGQ>, sm1);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
+  const float k = (float)(2.0 * M_PI / wavelength);
+  rs_hhat_rows<LOGQ><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength, k,
+                                                                  work);
+  XL_CHECK_LAUNCH("rs_hhat_rows");
+  const size_t sm2 = (size_t)C::W * C::CXS * sizeof(float2);
+  e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_cols smem");
+  rs_hhat_cols<LOGQ><<<C::P / C::W, C::COL_THREADS, sm2, st>>>(work, (float)scale, spec);
+  XL_CHECK_LAUNCH("rs_hhat_cols");
+  return XL_OK;
+}
+
+// Which planes the forward row pass stages by TMA: every input component and
+// every per-pixel parameter plane of the fused program whose rows are 16-byte
+// aligned, while the stage fits next to the exchange buffers.
+template <int LOGQ>
+static void plan_stage(const RsLaunch& p, size_t fixed_smem, RsStage& st) {
+  using C = RsCfg<LOGQ>;
+  const size_t cap = 226 * 1024;   // the CTA's shared memory, barrier included
+  st.n = 0;
+  st.row_bytes = 0;
+  for (int c = 0; c < 3; ++c) st.fld[c] = -1;
+  for (int k = 0; k < XL_MAX_OPS; ++k)
+    for (int i = 0; i < 4; ++i) st.prm[k][i] = -1;
+  int off = 0;
+  auto add = [&](const void* src, long long bstride_bytes, int row_bytes) -> int {
+    if (st.n >= XL_RS_STREAMS || !src) return -1;
+    if (((uintptr_t)src % 16) || (bstride_bytes % 16) || (row_bytes % 16)) return -1;
+    if (fixed_smem + (size_t)off + (size_t)C::G * row_bytes + 16 > cap) return -1;
+    RsStream& q = st.s[st.n++];
+    q.src = (const char*)src;
+    q.bstride = bstride_bytes;
+    q.row_bytes = row_bytes;
+    q.soff = off;
+    const int o = off;
+    off += C::G * row_bytes;
+    st.row_bytes += row_bytes;
+    return o;
+  };
+  for (int c = 0; c < p.cin && c < 3; ++c) st.fld[c] = add(p.in[c], p.ibs * 8, p.nx * 8);
+  for (int k = 0; k < p.pre.nops; ++k) {
+    const XlOp& op = p.pre.ops[k];
+    for (int i = 0; i < 4; ++i)
+      if (op.pmask & (1 << i)) st.prm[k][i] = add(op.ptr[i], op.pbstride * 4, p.nx * 4);
+  }
+}
+
+template <int LOGQ, int MODE>
+static int launch_rows_fwd(cudaStream_t s, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  constexpr int NC = MODE == 1 ? 1 : 3;
+  using F = RowCfg<LOGQ, NC>;
+  const size_t fixed = ((size_t)(F::LINES * C::XS + NC * C::G * p.nx) * 8 + (MODE == 2 ? (size_t)p.nx * 4 : 0) +
+                        15) / 16 * 16;
+  RsStage st;
+  plan_stage<LOGQ>(p, fixed, st);
+  const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;
+  if (sm > 227 * 1024) {
+    set_error("rs: row of %d columns too long for shared memory", p.nx);
+    return XL_EUNSUPPORTED;
+  }
+  cudaError_t e = allow_smem(rs_rows_fwd<LOGQ, MODE>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_rows_fwd smem");
+  const int total = p.B * ((p.ny + C::G - 1) / C::G);
+  const int grid = persistent_grid(rs_rows_fwd<LOGQ, MODE>, F::THREADS, sm, total);
+  rs_rows_fwd<LOGQ, MODE><<<grid, F::THREADS, sm, s>>>(p, st);
+  XL_CHECK_LAUNCH("rs_rows_fwd");
+  return XL_OK;
+}
+
+template <int LOGQ, int COUT, bool EPI>
+static int launch_rows_inv(cudaStream_t s, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  using F = RowCfg<LOGQ, COUT>;
+  const size_t sm = (size_t)(F::LINES * C::XS + (EPI ? COUT * C::G * p.nx : 0)) * sizeof(float2);
+  if (sm > 227 * 1024) {
+    set_error("rs: row of %d columns too long for shared memory", p.nx);
+    return XL_EUNSUPPORTED;
+  }
+  cudaError_t e = allow_smem(rs_rows_inv<LOGQ, COUT, EPI>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_rows_inv smem");
+  const int total = p.B * ((p.ny + C::G - 1) / C::G);
+  const int grid = persistent_grid(rs_rows_inv<LOGQ, COUT, EPI>, F::THREADS, sm, total);
+  rs_rows_inv<LOGQ, COUT, EPI><<<grid, F::THREADS, sm, s>>>(p);
+  XL_CHECK_LAUNCH("rs_rows_inv");
+  return XL_OK;
+}
+
+template <int LOGQ>
+static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
+  using C = RsCfg<LOGQ>;
+  cudaError_t e;
+  if (stage == 0) {
+    if (p.cout == 1) return launch_rows_fwd<LOGQ, 1>(st, p);
+    if (p.cin == 2) return launch_rows_fwd<LOGQ, 2>(st, p);
+    return launch_rows_fwd<LOGQ, 3>(st, p);
+  } else if (stage == 1) {
+    const size_t sm = (size_t)(C::W * C::CXS + C::NTW) * sizeof(float2);
+    if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
+    rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::COL_THREADS, sm, st>>>(p);
+    XL_CHECK_LAUNCH("rs_cols_conv");
+  } else {
+    const bool epi = p.post.nops > 0 || (p.adjoint && p.cout == 3);
+    if (p.cout == 1) return epi ? launch_rows_inv<LOGQ, 1, true>(st, p) : launch_rows_inv<LOGQ, 1, false>(st, p);
+    return epi ? launch_rows_inv<LOGQ, 3, true>(st, p) : launch_rows_inv<LOGQ, 3, false>(st, p);
+  }
+  return XL_OK;
+}
+
+template <int LOGQ>
+int rs_propagate(cudaStream_t st, const RsLaunch& p, int stage) {
+  if (stage >= 0) return launch_stage<LOGQ>(st, p, stage);
+  for (int s = 0; s < 3; ++s)
+    if (int rc = launch_stage<LOGQ>(st, p, s)) return rc;
+  return XL_OK;
+}
+
+template <int LOGP>
+static void fill_pass_tables(std::vector<float2>& out, const float2* host) {
+  const float2* twN = host + (1 << LOGP);
+  for (int i = 0; i < FftTw<LOGP, 16>::SIZE; ++i) out[ptw_off(LOGP) + i] = pass_twiddle_entry<LOGP, 16>(i, twN);
+  if constexpr (LOGP < 13) fill_pass_tables<LOGP + 1>(out, host);
+}
+
+// Device tables of this translation unit: the twiddle tables and the pass tables.
+static cudaError_t rs_tu_tables(const float2* host) {
+  cudaError_t e = cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
+  if (e != cudaSuccess) return e;
+  std::vector<float2> ptw(PTW_TOTAL, make_float2(1.f, 0.f));
+  fill_pass_tables<5>(ptw, host);
+  return cudaMemcpyToSymbol(g_ptw, ptw.data(), sizeof(g_ptw));
+}
+
+static cudaError_t rs_tu_timeouts(unsigned int* count, int reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(count, g_rs_timeouts, sizeof(unsigned int));
+  if (e != cudaSuccess || !reset) return e;
+  const unsigned int zero = 0;
+  return cudaMemcpyToSymbol(g_rs_timeouts, &zero, sizeof(unsigned int));
+}
+
+static const bool rs_tu_registered = register_device_tables(&rs_tu_tables, &rs_tu_timeouts);
+
+}  // namespace xl
+
+#define XL_RS_INSTANTIATE(L)                                                                        \
+  template int xl::rs_spectrum<L>(cudaStream_t, int, int, const double*, const double*, double, double, \
+                                  double, float2*, float2*);                                       \
+  template int xl::rs_propagate<L>(cudaStream_t, const RsLaunch&, int);
