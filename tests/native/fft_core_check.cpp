@@ -36,7 +36,7 @@ static void emu_x(std::vector<Regs<E>>& V, float2* sm, const float2* stw) {
   using S = FftShape<LOGN, E>;
   for (int j = 0; j < S::T; ++j) fft_pass_x<LOGN, E, P, DIR, P == 0, false>(V[j].v, j, sm, stw);
   if constexpr (P < S::NPASS - 1) {
-    for (int j = 0; j < S::T; ++j) fft_gather<LOGN, E>(V[j].v, j, sm);
+    for (int j = 0; j < S::T; ++j) fft_gather_x<LOGN, E>(V[j].v, j, sm);
     emu_x<LOGN, E, DIR, P + 1>(V, sm, stw);
   }
 }

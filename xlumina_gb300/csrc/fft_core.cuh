@@ -357,9 +357,31 @@ XL_HD void fft_pass_x(float2 (&v)[E], int j, float2* sm, const float2* stw, int 
       for (int i = 0; i < R; ++i) v[t + i * BPT] = x[i];
     } else {
       const int base = (b / NS) * (NS * R) + k;
+      if constexpr (NS % 16 == 0 || (NS == 1 && R == 16)) {
+        // padded slots at constant offsets from the first: base is a multiple
+        // of 16 (NS = 1) or the stride is (NS % 16 = 0)
+        constexpr int STEP = NS == 1 ? 1 : NS + NS / 16;
+        float2* d = sm + smpad(base);
 #pragma unroll
-      for (int i = 0; i < R; ++i) sm[smpad(base + i * NS)] = x[i];
+        for (int i = 0; i < R; ++i) d[i * STEP] = x[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; ++i) sm[smpad(base + i * NS)] = x[i];
+      }
     }
+  }
+}
+
+// fft_gather with the padded slots at constant offsets (T a multiple of 16).
+template <int LOGN, int E> XL_HD void fft_gather_x(float2 (&v)[E], int j, const float2* sm) {
+  using S = FftShape<LOGN, E>;
+  if constexpr (S::T % 16 == 0) {
+    const float2* s = sm + smpad(j);
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = s[m * (S::T + S::T / 16)];
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = sm[smpad(j + m * S::T)];
   }
 }
 
@@ -382,7 +404,7 @@ __device__ __forceinline__ void block_fft_x(float2 (&v)[E], int j, float2* sm, c
   fft_pass_x<LOGN, E, P, DIR, ZU && P == 0, GTW>(v, j, sm, stw, toff);
   if constexpr (P < S::NPASS - 1) {
     __syncthreads();
-    fft_gather<LOGN, E>(v, j, sm);
+    fft_gather_x<LOGN, E>(v, j, sm);
     __syncthreads();
     block_fft_x<LOGN, E, DIR, false, GTW, P + 1>(v, j, sm, stw, toff);
   }

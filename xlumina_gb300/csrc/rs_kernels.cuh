@@ -360,6 +360,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const _
   __syncthreads();
   const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * C::P * W + w;
   float2* xb = xch + w * C::CXS;
+#pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {
     float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
     float2 v[16];
@@ -371,12 +372,16 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const _
 #pragma unroll
     for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
     block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
+    // the spectrum loads stay here rather than ahead of the transform, where
+    // they would hold 32 registers through it
+    const float2* sp = spec;
+    asm volatile("" : "+l"(sp));
     if (p.adjoint) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(spec + (long long)(j + m * C::T) * W));
+      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * W));
     } else {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(spec + (long long)(j + m * C::T) * W));
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * W));
     }
     block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
 #pragma unroll
