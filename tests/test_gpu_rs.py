@@ -166,3 +166,61 @@ def test_bad_arguments_raise(xl):
         engine.rs_propagate([f], x[:32], y, 0.5, 1e3, vector=False)
     with pytest.raises(_lib.XlError):
         engine.build_rs_spectrum(x, y, 0.0, 0.5)
+
+
+def test_vrs_bench_workload_full_size(xl):
+    """The benchmark's workload at full size: 2048^2 VRS over a 4 mm window at
+    633 nm, radially polarised source (w = 1 mm) behind a per-pixel LCD and a
+    linear polarizer, z = 20 cm (the largest phase k r of the set)."""
+    wo, vo, oe = xl
+    n = 2048
+    x, y = ref.space(2000.0, n)
+    X, Y = np.meshgrid(x, y)
+    g = np.exp(-(X ** 2 + Y ** 2) / 1000.0 ** 2)
+    Ex, Ey = (X / 1000.0) * g, (Y / 1000.0) * g
+    rng = np.random.default_rng(1000)
+    eta = rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32)
+    theta = rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32)
+    alpha = float(rng.uniform(0, np.pi))
+    light = vo.VectorizedLight(x, y, 0.633)
+    light.Ex, light.Ey = Ex, Ey
+    out, _ = oe.linear_polarizer(oe.LCD(light, eta, theta), alpha).VRS_propagation(2e5)
+    ax, ay = ref.lcd(Ex, Ey, eta.astype(np.float64), theta.astype(np.float64))
+    ax, ay = ref.linear_polarizer(ax, ay, alpha * np.ones((n, n)))
+    exp = ref.vrs_propagate(ax, ay, x, y, 0.633, 2e5)
+    for o, e in zip((out.Ex, out.Ey, out.Ez), exp):
+        assert rel_l2(_np(o), e) < TOL
+
+
+def test_rs_longest_transform(xl):
+    """Q = 4096 (a 2100^2 field, 8192-point transforms), scalar RS."""
+    wo, vo, oe = xl
+    n = 2100
+    x, y = ref.space(1500.0, n)
+    rng = np.random.default_rng(21)
+    f = ref.gaussian_beam(x, y, 0.55, (400.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
+    light = wo.ScalarLight(x, y, 0.55)
+    light.field = f
+    out, _ = light.RS_propagation(3e4)
+    exp = ref.rs_propagate(f, x, y, 0.55, 3e4)
+    assert rel_l2(_np(out.field), exp) < TOL
+
+
+def test_mask_phases_of_any_size(xl):
+    """Mask phases are reduced to [-pi, pi] before the sine and cosine: the SLM
+    mask matches exp(i phase) of the float32 phase to 1e-6 + |phase| 1e-7
+    absolute, for phases up to +-1e4 rad."""
+    import torch
+
+    from xlumina_gb300 import engine
+    rng = np.random.default_rng(44)
+    ph = np.concatenate([rng.uniform(-np.pi, np.pi, 4096), rng.uniform(-50, 50, 4096),
+                         rng.uniform(-1e4, 1e4, 4096), np.array([0.0, np.pi, -np.pi, 2 * np.pi, 1e4])])
+    ph = ph.astype(np.float32)
+    m = ph.size
+    ones = torch.ones((1, m), dtype=torch.complex64, device="cuda")
+    out = engine.apply_ops([ones], [engine.op_phase(torch.as_tensor(ph[None], device="cuda"))], 1, m)[0]
+    got = _np(out)[0]
+    exp = np.exp(1j * ph.astype(np.float64))
+    err = np.abs(got - exp)
+    assert np.all(err <= 1e-6 + np.abs(ph) * 1e-7), float(np.max(err))

@@ -40,6 +40,12 @@ __device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, 
   return cmul(e, make_float2(a / rf, -a * k));
 }
 
+// sin and cos of a mask phase in radians (one place for every Jones op and
+// its backward).  The accurate sincosf: the high-NA focus sums millions of
+// pixels with heavy cancellation, and the hardware approximation's 4e-7
+// absolute error per pixel shows up there above the 1e-5 parity bar.
+__device__ __forceinline__ void phase_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+
 // ---- fused per-pixel Jones program ----
 
 struct PixelCtx;
@@ -126,32 +132,32 @@ __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3]
   switch (op.kind) {
     case XL_OP_PHASE: {  // scalar SLM: field * e^{i phi}
       float s, c;
-      sincosf(pr(op, k, 0, px), &s, &c);
+      phase_sincos(pr(op, k, 0, px), &s, &c);
       e[0] = cmul(e[0], make_float2(c, s));
       break;
     }
     case XL_OP_SSLM: {  // diag(e^{i a}, e^{i p}); Ez unchanged
       float s, c;
-      sincosf(pr(op, k, 0, px), &s, &c);
+      phase_sincos(pr(op, k, 0, px), &s, &c);
       e[0] = cmul(e[0], make_float2(c, s));
-      sincosf(pr(op, k, 1, px), &s, &c);
+      phase_sincos(pr(op, k, 1, px), &s, &c);
       e[1] = cmul(e[1], make_float2(c, s));
       break;
     }
     case XL_OP_SSLM_AMP: {  // diag(A1 e^{i a}, A2 e^{i p}); Ez unchanged
       float s, c;
-      sincosf(pr(op, k, 0, px), &s, &c);
+      phase_sincos(pr(op, k, 0, px), &s, &c);
       e[0] = cscale(cmul(e[0], make_float2(c, s)), pr(op, k, 2, px));
-      sincosf(pr(op, k, 1, px), &s, &c);
+      phase_sincos(pr(op, k, 1, px), &s, &c);
       e[1] = cscale(cmul(e[1], make_float2(c, s)), pr(op, k, 3, px));
       break;
     }
     case XL_OP_LCD: {  // general retarder with delta = 0 (eta, theta); Ez unchanged
       float sh, ch, s2, c2;
       float st, ct;
-      if (op.pmask & 1) sincosf(0.5f * pr(op, k, 0, px), &sh, &ch);
+      if (op.pmask & 1) phase_sincos(0.5f * pr(op, k, 0, px), &sh, &ch);
       else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
-      if (op.pmask & 2) sincosf(pr(op, k, 1, px), &st, &ct);
+      if (op.pmask & 2) phase_sincos(pr(op, k, 1, px), &st, &ct);
       else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
       // a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2)
       c2 = ct * ct - st * st;
@@ -166,7 +172,7 @@ __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3]
     }
     case XL_OP_LP: {  // linear polarizer at alpha; Ez set to zero
       float s, c;
-      if (op.pmask & 1) sincosf(pr(op, k, 0, px), &s, &c);
+      if (op.pmask & 1) phase_sincos(pr(op, k, 0, px), &s, &c);
       else { c = op.sval[2]; s = op.sval[3]; }   // scalar alpha: cos, sin from the host
       const float2 x = e[0], y = e[1];
       e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
@@ -235,7 +241,7 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
   switch (op.kind) {
     case XL_OP_PHASE: {
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
+      phase_sincos(op_param(op, 0, px), &s, &c);
       const float2 ph = make_float2(c, s);
       const float2 y = cmul(e[0], ph);
       pg[0] += re_gconj(g[0], make_float2(-y.y, y.x));   // dy/dphi = i y
@@ -246,9 +252,9 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
     case XL_OP_SSLM_AMP: {
       const bool amp = op.kind == XL_OP_SSLM_AMP;
       float s, c;
-      sincosf(op_param(op, 0, px), &s, &c);
+      phase_sincos(op_param(op, 0, px), &s, &c);
       const float2 p0 = make_float2(c, s);
-      sincosf(op_param(op, 1, px), &s, &c);
+      phase_sincos(op_param(op, 1, px), &s, &c);
       const float2 p1 = make_float2(c, s);
       const float a1 = amp ? op_param(op, 2, px) : 1.f, a2 = amp ? op_param(op, 3, px) : 1.f;
       const float2 u0 = cmul(e[0], p0), u1 = cmul(e[1], p1);   // before the amplitudes
@@ -264,9 +270,9 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
     }
     case XL_OP_LCD: {
       float sh, ch, st, ct;
-      if (op.pmask & 1) sincosf(0.5f * op_param(op, 0, px), &sh, &ch);
+      if (op.pmask & 1) phase_sincos(0.5f * op_param(op, 0, px), &sh, &ch);
       else { ch = op.dval[0]; sh = op.dval[1]; }
-      if (op.pmask & 2) sincosf(op_param(op, 1, px), &st, &ct);
+      if (op.pmask & 2) phase_sincos(op_param(op, 1, px), &st, &ct);
       else { ct = op.dval[2]; st = op.dval[3]; }
       const float c2 = ct * ct - st * st, s2 = 2.f * st * ct;
       const float2 a = make_float2(ch, -sh * c2), bb = make_float2(0.f, -sh * s2), d = make_float2(ch, sh * c2);
@@ -285,7 +291,7 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
     }
     case XL_OP_LP: {
       float s, c;
-      if (op.pmask & 1) sincosf(op_param(op, 0, px), &s, &c);
+      if (op.pmask & 1) phase_sincos(op_param(op, 0, px), &s, &c);
       else { c = op.sval[2]; s = op.sval[3]; }
       const float2 x = e[0], y = e[1];
       const float dcs = c * c - s * s, tcs = 2.f * c * s;

@@ -386,6 +386,19 @@ template <int LOGN, int E> XL_HD void fft_gather_x(float2 (&v)[E], int j, const 
 }
 
 #if defined(__CUDACC__)
+// Barrier between the passes of a transform: the whole CTA, or a named
+// barrier shared by the `count` threads (a multiple of 32) of one group, so
+// that groups of a CTA working on different lines do not wait for each other.
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupSync {
+  int id, count;   // barrier 1..15 (0 is __syncthreads)
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+};
+
 // Whole FFT for a thread group, twiddles from pass tables (shared or global),
 // optional input pruning (ZU).  Every thread of the CTA must call it the same
 // number of times (it uses __syncthreads between passes).
@@ -394,8 +407,9 @@ template <int LOGN, int E> XL_HD void fft_gather_x(float2 (&v)[E], int j, const 
 // of every transform: a kernel that runs several transforms in a row then
 // reloads the (identical) twiddles for each one instead of keeping them all
 // live in registers, which would cost about a hundred registers per thread.
-template <int LOGN, int E, int DIR, bool ZU, bool GTW, int P = 0>
-__device__ __forceinline__ void block_fft_x(float2 (&v)[E], int j, float2* sm, const float2* stw, int toff = -1) {
+template <int LOGN, int E, int DIR, bool ZU, bool GTW, class SYNC = CtaSync, int P = 0>
+__device__ __forceinline__ void block_fft_x(float2 (&v)[E], int j, float2* sm, const float2* stw,
+                                            const SYNC& sync = SYNC(), int toff = -1) {
   using S = FftShape<LOGN, E>;
   if constexpr (P == 0) {
     toff = 0;
@@ -403,10 +417,10 @@ __device__ __forceinline__ void block_fft_x(float2 (&v)[E], int j, float2* sm, c
   }
   fft_pass_x<LOGN, E, P, DIR, ZU && P == 0, GTW>(v, j, sm, stw, toff);
   if constexpr (P < S::NPASS - 1) {
-    __syncthreads();
+    sync();
     fft_gather_x<LOGN, E>(v, j, sm);
-    __syncthreads();
-    block_fft_x<LOGN, E, DIR, false, GTW, P + 1>(v, j, sm, stw, toff);
+    sync();
+    block_fft_x<LOGN, E, DIR, false, GTW, SYNC, P + 1>(v, j, sm, stw, sync, toff);
   }
 }
 

@@ -32,6 +32,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -52,15 +53,25 @@ template <int LOGQ> struct RsCfg {
   static constexpr int XS = P + P / 16;                       // exchange slots per line
   static constexpr int G = (256 / T) > 1 ? (256 / T) : 1;     // lines per CTA in the row passes
   static constexpr int ROW_THREADS = G * T;
-  // column-tile width; lanes of a warp interleave the W columns of a tile
+  // column-tile width of the intermediate and spectrum layouts
   static constexpr int W = LOGQ >= 12 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
-  // per-column padding of the column pass's exchange buffers: without it the
-  // W interleaved buffers would start on the same bank
-  static constexpr int CPAD = W >= 8 ? 0 : 4;
-  static constexpr int CXS = XS + CPAD;
+  // The column pass runs one CTA per tile of W columns, split into W / CW
+  // groups of CW columns (the lanes of a warp interleave a group's columns),
+  // each group on its own named barrier when there are several.  Measured at
+  // Q = 2048: two groups of two columns are slower than one group of four
+  // (a warp's loads then cover half sectors of the four-wide tiles).
+  static constexpr int CW = W;
+  static constexpr int NCG = W / CW;
+  // per-column padding of exchange buffers whose columns are interleaved in
+  // every warp: without it they would start on the same bank
+  static constexpr int CXS = XS + (CW >= 8 ? 0 : 16 / CW);      // column pass (CW columns)
+  static constexpr int WXS = XS + (W >= 8 ? 0 : 16 / W);        // spectrum build (W columns)
   static constexpr int COL_THREADS = W * T;
+  static constexpr int COL_MINB = (1024 / COL_THREADS) > 1 ? (1024 / COL_THREADS) : 1;
+  static constexpr int HCOL_THREADS = W * T;
   static constexpr int NTW = FftTw<LOGP, E>::SIZE;           // pass twiddle table entries
-  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024, "column CTA shape");
+  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024 && HCOL_THREADS <= 1024, "column CTA shape");
+  static_assert(W % CW == 0, "column-pass CTAs cover whole tiles");
 };
 
 // Pass twiddle tables (FftTw layout, 16 elements per thread) for every
@@ -142,7 +153,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
 // Transfer spectrum, step 2: P-point column transforms of the row spectra,
 // times `scale`, stored column-tiled: S[((kx / W) * P + ky) * W + kx % W].
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS)
+__global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS)
     rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
   constexpr int W = C::W, LPW = 32 / W;
@@ -154,7 +165,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS)
   const float2* src = in + t * W + w;
 #pragma unroll
   for (int m = 0; m < 16; ++m) v[m] = src[(long long)(j + m * C::T) * C::P];
-  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + w * C::CXS, pass_tw<C::LOGP>());
+  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + w * C::WXS, pass_tw<C::LOGP>());
   float2* dst = out + (long long)t * C::P * W + w;
 #pragma unroll
   for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * W] = cscale(v[m], scale);
@@ -271,7 +282,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
       int last = -1;
       float Y = 0.f, z2 = 0.f;
       for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
-        const int g2 = idx / nx, n = idx - g2 * nx, r = r0 + g2;
+        const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
         if (r >= ny) break;
         const long long pix = (long long)r * nx + n;
         float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
@@ -343,15 +354,24 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 // (conjugate for the adjoint), inverse FFT, keep the ny surviving rows.
 // Lanes interleave the W columns so every warp access is one contiguous run.
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const __grid_constant__ RsLaunch p) {
+__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
+    rs_cols_conv(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
-  constexpr int W = C::W, LPW = 32 / W;
+  constexpr int W = C::W, CW = C::CW, LPW = 32 / CW;
+  constexpr int GT = CW * C::T;        // threads per column group
   extern __shared__ __align__(16) float2 smem[];
-  float2* xch = smem;                 // W x CXS
-  float2* stw = smem + W * C::CXS;    // NTW
+  float2* xch = smem;                  // W x CXS
+  float2* stw = smem + W * C::CXS;     // NTW
   const int tid = threadIdx.x, lane = tid & 31;
-  const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
-  const int t = blockIdx.x, b = blockIdx.y;
+  const int grp = tid / GT;                                // column group
+  const int wc = lane % CW, j = ((tid % GT) >> 5) * LPW + lane / CW;
+  const int t = blockIdx.x;                                // column tile
+  const int w = grp * CW + wc;                             // column within the tile
+  const int b = blockIdx.y;
+  // one group: the whole CTA; several: a named barrier each
+  using Sync = std::conditional_t<C::NCG == 1, CtaSync, GroupSync>;
+  Sync gsync;
+  if constexpr (C::NCG > 1) gsync = GroupSync{1 + grp, GT};
   const int ny = p.ny;
   {
     const float2* g = pass_tw<C::LOGP>();
@@ -371,7 +391,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const _
     }
 #pragma unroll
     for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
-    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
+    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw, gsync);
     // the spectrum loads stay here rather than ahead of the transform, where
     // they would hold 32 registers through it
     const float2* sp = spec;
@@ -383,7 +403,7 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS) rs_cols_conv(const _
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * W));
     }
-    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
+    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw, gsync);
 #pragma unroll
     for (int m = 0; m < C::H; ++m) {
       const int n = j + m * C::T;
@@ -441,7 +461,11 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
       for (int m = 0; m < 16; ++m) v[m] = nxt[m];
       if (c + F::CG < COUT) load(grp, c + F::CG, nxt);
       else if (grp + gridDim.x < total) load(grp + gridDim.x, cg, nxt);
-      block_fft_x<C::LOGP, 16, 1, false, true>(v, j, xb, pass_tw<C::LOGP>());
+      if constexpr (!EPI && F::CG > 1)   // the component groups never meet: own barriers
+        block_fft_x<C::LOGP, 16, 1, false, true>(v, j, xb, pass_tw<C::LOGP>(),
+                                                 GroupSync{1 + cg, C::G * C::T});
+      else
+        block_fft_x<C::LOGP, 16, 1, false, true>(v, j, xb, pass_tw<C::LOGP>());
       if constexpr (!EPI) {
         if (live) {
           float2* o = p.out[c] + (long long)b * p.obs + (long long)r * nx;
@@ -466,7 +490,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
       int last = -1;
       float Y = 0.f, z2 = 0.f;
       for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
-        const int g2 = idx / nx, n = idx - g2 * nx, ro = r0 + g2;
+        const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, ro = r0 + g2;
         if (ro >= ny) break;
         const long long o = (long long)b * p.obs + (long long)ro * nx + n;
         float2 e[3];
@@ -533,10 +557,10 @@ int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const doubl
   rs_hhat_rows<LOGQ><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength, k,
                                                                   work);
   XL_CHECK_LAUNCH("rs_hhat_rows");
-  const size_t sm2 = (size_t)C::W * C::CXS * sizeof(float2);
+  const size_t sm2 = (size_t)C::W * C::WXS * sizeof(float2);
   e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
   if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_cols smem");
-  rs_hhat_cols<LOGQ><<<C::P / C::W, C::COL_THREADS, sm2, st>>>(work, (float)scale, spec);
+  rs_hhat_cols<LOGQ><<<C::P / C::W, C::HCOL_THREADS, sm2, st>>>(work, (float)scale, spec);
   XL_CHECK_LAUNCH("rs_hhat_cols");
   return XL_OK;
 }
