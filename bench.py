@@ -57,28 +57,39 @@ def make_inputs(batch, seed=1000):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling (every 100 ms) around the timed
+    region; summary() keeps the samples taken between mark_start() and
+    mark_end() (the nearest ones if the region is shorter than one interval)."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index=0):
         self.index = index
         self.proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
         except (OSError, ValueError):
             self.proc = None
         return self
 
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
     def __exit__(self, *exc):
         self.lines = []
         if self.proc is not None:
+            time.sleep(0.15)
             self.proc.terminate()
             try:
                 out, _ = self.proc.communicate(timeout=5)
@@ -87,25 +98,47 @@ class ClockSampler:
                 out, _ = self.proc.communicate()
             self.lines = [ln for ln in out.splitlines() if ln.strip()]
 
-    def summary(self):
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in getattr(self, "lines", []):
-            f = [v.strip() for v in ln.split(",")]
-            if len(f) < 9:
-                continue
+    @staticmethod
+    def _epoch(stamp):
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
             try:
-                sm.append(float(f[1]))
-                smax = float(f[2])
+                return datetime.datetime.strptime(stamp.strip(), fmt).timestamp()
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
+        return None
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        samples = []
+        for ln in getattr(self, "lines", []):
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                samples.append((self._epoch(f[0]), float(f[2]), float(f[3]), f[6:10]))
+            except ValueError:
+                continue
+        inside = [smp for smp in samples if smp[0] is not None and self.t0 is not None and
+                  self.t0 <= smp[0] <= self.t1]
+        if not inside and samples and self.t0 is not None:   # region shorter than the interval
+            mid = 0.5 * (self.t0 + self.t1)
+            inside = sorted((smp for smp in samples if smp[0] is not None), key=lambda smp: abs(smp[0] - mid))[:2]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        reasons = set()
+        for smp in inside:
+            for nm, v in zip(names, smp[3]):
                 if v.lower() == "active":
                     reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(smp[1] for smp in inside), "sm_max_mhz": inside[-1][2],
+                "reasons": sorted(reasons), "samples": len(inside)}
+
+
+# DRAM bytes (read + write) per 2048^2 VRS field of each pass, from the ncu
+# capture summarised in profiles/rs_kernels_vrs2048.md (batch 2, scaled per
+# field; every field is an independent slice of the launch).
+NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 275.96e6, "rs_cols_conv": 520.34e6, "rs_rows_inv": 283.98e6}
 
 
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
@@ -115,26 +148,33 @@ def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
     return ref.vrs_propagate(ax, ay, x, x, WAVELENGTH, z)
 
 
-def run_reference(args):
+def run_reference(args, budget_s=90.0):
+    """The reference algorithm on the host cores, one field per step.  A CPU
+    field takes over a second, so the timed steps are capped at about
+    `budget_s` of work (at least 3); the line reports how many were timed."""
     from oracle import xlumina_ref as ref
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     x, Ex, Ey, eta, theta, alpha, zs = make_inputs(1)
+    t_w = time.perf_counter()
     for _ in range(args.warmup):
         cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, zs[0])
+    per_field = (time.perf_counter() - t_w) / max(1, args.warmup)
+    steps = max(3, min(args.steps, int(budget_s / max(per_field, 1e-3))))
     t0 = time.perf_counter()
-    for i in range(args.steps):
+    for i in range(steps):
         cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, Z_SET[i % len(Z_SET)])
     dt = time.perf_counter() - t0
-    v = args.steps / dt
+    v = steps / dt
     cores = ref.WORKERS
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "fields/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "steps": steps, "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic", "config": {"workload": WORKLOAD, "batch": 1},
             "cpu_baseline": {"value": v, "unit": "fields/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} fields, one per step, scipy.fft with {cores} workers"},
+                             "sample": f"{steps} fields, one per step (capped at about {budget_s:.0f} s of work), "
+                                       f"scipy.fft with {cores} workers"},
             "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -189,6 +229,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
+        clk.mark_start()
         t_start.record(stream)
         for k in range(args.steps):
             ev[k][0].record(stream)
@@ -197,6 +238,7 @@ def run_gpu(args):
                 ev[k][s + 1].record(stream)
         t_end.record(stream)
         torch.cuda.synchronize()
+        clk.mark_end()
     total_ms = t_start.elapsed_time(t_end)
     stage_ms = [sum(ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps)) / args.steps
                 for s in range(3)]
@@ -283,7 +325,12 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (%.2f GB of fields and masks per step)" %
                          ((Ex_d.numel() + Ey_d.numel()) * 8 / 1e9 + (eta_d.numel() + theta_d.numel()) * 4 / 1e9)},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                     "frac": achieved / peak,
+                     "traffic": (NCU_TRAFFIC_PER_FIELD[names[dom]] * B
+                                 if NCU_TRAFFIC_PER_FIELD[names[dom]] is not None else None),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                       "profiles/rs_kernels_vrs2048.md, scaled to the launch's fields",
+                     "peak_source": peak_src,
                      "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
         "stages_ms": dict(zip(names, stage_ms)),
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
@@ -430,7 +477,7 @@ def run_serving(n_req=10000, seed=4000):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--impl", default="xlgb", choices=["xlgb", "reference"])
