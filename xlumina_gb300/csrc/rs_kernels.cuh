@@ -25,8 +25,8 @@
 // element (row r, column c) at ((c / W) * N + r) * W + c % W, so a column
 // tile is contiguous and a row is W-wide contiguous runs.  Transfer spectra
 // (P x P complex64, natural frequency order) are built once per
-// (z, wavelength, grid) by rs_hhat_rows / rs_hhat_cols in the same column-tile
-// layout with P rows: S[((kx / W) * P + ky) * W + kx % W].
+// (z, wavelength, grid) by rs_hhat_rows / rs_hhat_cols in column tiles of SW
+// with P rows: S[((kx / SW) * P + ky) * SW + kx % SW].
 #pragma once
 
 #include <math.h>
@@ -53,24 +53,23 @@ template <int LOGQ> struct RsCfg {
   static constexpr int XS = P + P / 16;                       // exchange slots per line
   static constexpr int G = (256 / T) > 1 ? (256 / T) : 1;     // lines per CTA in the row passes
   static constexpr int ROW_THREADS = G * T;
-  // column-tile width of the intermediate and spectrum layouts
-  static constexpr int W = LOGQ >= 12 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
-  // The column pass runs one CTA per tile of W columns, split into W / CW
-  // groups of CW columns (the lanes of a warp interleave a group's columns),
-  // each group on its own named barrier when there are several.  Measured at
-  // Q = 2048: two groups of two columns are slower than one group of four
-  // (a warp's loads then cover half sectors of the four-wide tiles).
-  static constexpr int CW = W;
-  static constexpr int NCG = W / CW;
-  // per-column padding of exchange buffers whose columns are interleaved in
-  // every warp: without it they would start on the same bank
-  static constexpr int CXS = XS + (CW >= 8 ? 0 : 16 / CW);      // column pass (CW columns)
-  static constexpr int WXS = XS + (W >= 8 ? 0 : 16 / W);        // spectrum build (W columns)
-  static constexpr int COL_THREADS = W * T;
+  // Column-tile width of the intermediate and spectrum layouts.  At Q = 2048
+  // the tiles are 8 columns wide, so a warp's row access is four 64-byte
+  // pieces; the column pass takes half a tile per CTA.
+  static constexpr int W = LOGQ >= 12 ? 2 : (LOGQ == 11 ? 8 : ((32 / T) > 4 ? (32 / T) : 4));
+  // Column-pass (and spectrum-build) CTAs take CW columns of a tile,
+  // interleaved in the lanes of every warp.
+  static constexpr int CW = LOGQ == 11 ? 4 : W;
+  // the transfer spectrum is tiled CW wide: exactly the columns of one
+  // column-pass CTA, so its reads are whole 32-byte pieces
+  static constexpr int SW = CW;
+  // per-column padding of the exchange buffers: without it the CW
+  // interleaved buffers would start on the same bank
+  static constexpr int CXS = XS + (CW >= 8 ? 0 : 16 / CW);
+  static constexpr int COL_THREADS = CW * T;
   static constexpr int COL_MINB = (1024 / COL_THREADS) > 1 ? (1024 / COL_THREADS) : 1;
-  static constexpr int HCOL_THREADS = W * T;
   static constexpr int NTW = FftTw<LOGP, E>::SIZE;           // pass twiddle table entries
-  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024 && HCOL_THREADS <= 1024, "column CTA shape");
+  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024, "column CTA shape");
   static_assert(W % CW == 0, "column-pass CTAs cover whole tiles");
 };
 
@@ -151,24 +150,26 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
 }
 
 // Transfer spectrum, step 2: P-point column transforms of the row spectra,
-// times `scale`, stored column-tiled: S[((kx / W) * P + ky) * W + kx % W].
+// times `scale`, stored column-tiled: S[((kx / SW) * P + ky) * SW + kx % SW].
 template <int LOGQ>
-__global__ void __launch_bounds__(RsCfg<LOGQ>::HCOL_THREADS)
+__global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS)
     rs_hhat_cols(const float2* __restrict__ in, float scale, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
-  constexpr int W = C::W, LPW = 32 / W;
+  constexpr int W = C::W, CW = C::CW, LPW = 32 / CW;
   extern __shared__ __align__(16) float2 smem[];
   const int tid = threadIdx.x, lane = tid & 31;
-  const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
-  const int t = blockIdx.x;
+  const int wc = lane % CW, j = (tid >> 5) * LPW + lane / CW;
+  const int t = blockIdx.x / (W / CW);                      // column tile
+  const int w = (blockIdx.x % (W / CW)) * CW + wc;          // column within the tile
   float2 v[16];
   const float2* src = in + t * W + w;
 #pragma unroll
   for (int m = 0; m < 16; ++m) v[m] = src[(long long)(j + m * C::T) * C::P];
-  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + w * C::WXS, pass_tw<C::LOGP>());
-  float2* dst = out + (long long)t * C::P * W + w;
+  block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + wc * C::CXS, pass_tw<C::LOGP>());
+  const int kx = t * W + w;
+  float2* dst = out + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
 #pragma unroll
-  for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * W] = cscale(v[m], scale);
+  for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * C::SW] = cscale(v[m], scale);
 }
 
 // ---------------------------------------------------------------------------
@@ -352,34 +353,31 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 // Column pass, in place on one tile of W spectrum columns: FFT along y of the
 // ny nonzero rows (pruned first pass), multiply by the transfer spectrum
 // (conjugate for the adjoint), inverse FFT, keep the ny surviving rows.
-// Lanes interleave the W columns so every warp access is one contiguous run.
+// A CTA takes CW columns of a tile; lanes interleave them, so every warp
+// access is one contiguous run of CW columns.
 template <int LOGQ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
     rs_cols_conv(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
   constexpr int W = C::W, CW = C::CW, LPW = 32 / CW;
-  constexpr int GT = CW * C::T;        // threads per column group
   extern __shared__ __align__(16) float2 smem[];
-  float2* xch = smem;                  // W x CXS
-  float2* stw = smem + W * C::CXS;     // NTW
+  float2* xch = smem;                  // CW x CXS
+  float2* stw = smem + CW * C::CXS;    // NTW
   const int tid = threadIdx.x, lane = tid & 31;
-  const int grp = tid / GT;                                // column group
-  const int wc = lane % CW, j = ((tid % GT) >> 5) * LPW + lane / CW;
-  const int t = blockIdx.x;                                // column tile
-  const int w = grp * CW + wc;                             // column within the tile
+  const int wc = lane % CW, j = (tid >> 5) * LPW + lane / CW;
+  const int t = blockIdx.x / (W / CW);                      // column tile
+  const int w = (blockIdx.x % (W / CW)) * CW + wc;          // column within the tile
   const int b = blockIdx.y;
-  // one group: the whole CTA; several: a named barrier each
-  using Sync = std::conditional_t<C::NCG == 1, CtaSync, GroupSync>;
-  Sync gsync;
-  if constexpr (C::NCG > 1) gsync = GroupSync{1 + grp, GT};
   const int ny = p.ny;
   {
     const float2* g = pass_tw<C::LOGP>();
     for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
   }
   __syncthreads();
-  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride + (long long)t * C::P * W + w;
-  float2* xb = xch + w * C::CXS;
+  const int kx = t * W + w;
+  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride +
+                       (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+  float2* xb = xch + wc * C::CXS;
 #pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {
     float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
@@ -391,19 +389,19 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
     }
 #pragma unroll
     for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
-    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw, gsync);
+    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
     // the spectrum loads stay here rather than ahead of the transform, where
     // they would hold 32 registers through it
     const float2* sp = spec;
     asm volatile("" : "+l"(sp));
     if (p.adjoint) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * W));
+      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
     } else {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * W));
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
     }
-    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw, gsync);
+    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
 #pragma unroll
     for (int m = 0; m < C::H; ++m) {
       const int n = j + m * C::T;
@@ -557,10 +555,10 @@ int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const doubl
   rs_hhat_rows<LOGQ><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength, k,
                                                                   work);
   XL_CHECK_LAUNCH("rs_hhat_rows");
-  const size_t sm2 = (size_t)C::W * C::WXS * sizeof(float2);
+  const size_t sm2 = (size_t)C::CW * C::CXS * sizeof(float2);
   e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
   if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_cols smem");
-  rs_hhat_cols<LOGQ><<<C::P / C::W, C::HCOL_THREADS, sm2, st>>>(work, (float)scale, spec);
+  rs_hhat_cols<LOGQ><<<C::P / C::CW, C::COL_THREADS, sm2, st>>>(work, (float)scale, spec);
   XL_CHECK_LAUNCH("rs_hhat_cols");
   return XL_OK;
 }
@@ -650,9 +648,9 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     if (p.cin == 2) return launch_rows_fwd<LOGQ, 2>(st, p);
     return launch_rows_fwd<LOGQ, 3>(st, p);
   } else if (stage == 1) {
-    const size_t sm = (size_t)(C::W * C::CXS + C::NTW) * sizeof(float2);
+    const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
-    rs_cols_conv<LOGQ><<<dim3(C::P / C::W, p.B), C::COL_THREADS, sm, st>>>(p);
+    rs_cols_conv<LOGQ><<<dim3(C::P / C::CW, p.B), C::COL_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
   } else {
     const bool epi = p.post.nops > 0 || (p.adjoint && p.cout == 3);
