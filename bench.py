@@ -279,14 +279,17 @@ def run_gpu(args):
     plain = nplain / (p0.elapsed_time(p1) / 1e3)
 
     # end to end through the public API: pinned host buffers in, propagated fields out.
-    # Steps alternate between two streams with their own pinned buffers, so the copies
-    # of one step overlap the kernels of the other.
+    # A step's inputs are the source (one Ex, Ey plane, shared by the batch: the
+    # workload is one source through B random LCD masks) and the B mask planes;
+    # its result is the B propagated fields (Ex, Ey, Ez).  Steps alternate
+    # between two streams with their own pinned buffers, so the copies of one
+    # step overlap the kernels of the other.
     streams = [torch.cuda.Stream(), torch.cuda.Stream()]
     hosts = []
     for _ in streams:
         hosts.append(dict(
-            Ex=torch.as_tensor(np.broadcast_to(Ex, (B, N, N)).astype(np.complex64)).pin_memory(),
-            Ey=torch.as_tensor(np.broadcast_to(Ey, (B, N, N)).astype(np.complex64)).pin_memory(),
+            Ex=torch.as_tensor(Ex.astype(np.complex64)[None]).pin_memory(),
+            Ey=torch.as_tensor(Ey.astype(np.complex64)[None]).pin_memory(),
             eta=torch.as_tensor(eta).pin_memory(), theta=torch.as_tensor(theta).pin_memory(),
             out=[torch.empty((B, N, N), dtype=torch.complex64).pin_memory() for _ in range(3)]))
     zarr = np.asarray(zs)
@@ -295,8 +298,8 @@ def run_gpu(args):
         h = hosts[i % 2]
         with torch.cuda.stream(streams[i % 2]):
             light = vo.VectorizedLight(x, x, WAVELENGTH)
-            light.Ex = h["Ex"].to(dev, non_blocking=True)
-            light.Ey = h["Ey"].to(dev, non_blocking=True)
+            light.Ex = h["Ex"].to(dev, non_blocking=True).expand(B, N, N)
+            light.Ey = h["Ey"].to(dev, non_blocking=True).expand(B, N, N)
             e_ = h["eta"].to(dev, non_blocking=True)
             t_ = h["theta"].to(dev, non_blocking=True)
             out, _ = oe.linear_polarizer(oe.LCD(light, e_, t_), alpha).VRS_propagation(zarr)

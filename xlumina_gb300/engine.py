@@ -41,13 +41,22 @@ def _ptr(t) -> int:
     return 0 if t is None else t.data_ptr()
 
 
+def _is_broadcast_batch(t: torch.Tensor) -> bool:
+    """One contiguous plane repeated along a leading batch dimension (stride 0)."""
+    return t.dim() == 3 and t.shape[0] > 1 and t.stride(0) == 0 and t[0].is_contiguous()
+
+
 def as_field(a, dev=None) -> torch.Tensor:
-    """complex64, contiguous, on the CUDA device."""
+    """complex64 on the CUDA device, contiguous; a batch that is one plane
+    broadcast along the batch (an ``expand``-ed view) stays a view, since
+    every launch takes it without copying (batch stride 0)."""
     dev = dev or device()
     if isinstance(a, torch.Tensor):
         t = a.to(device=dev)
         if t.dtype != torch.complex64:
             t = t.to(torch.complex64)
+        if _is_broadcast_batch(t):
+            return t
         return t.contiguous()
     return torch.as_tensor(np.asarray(a), device=dev).to(torch.complex64).contiguous()
 
@@ -64,7 +73,7 @@ def batch_planes(comps, ny, nx):
     if B > 1 and all(c.dim() == 3 and c.stride(0) == 0 and c.dtype == torch.complex64 and c.is_cuda and
                      c[0].is_contiguous() for c in comps):
         return [c[0] for c in comps], B, 0
-    return [as_field(c) for c in comps], B, ny * nx
+    return [as_field(c).contiguous() for c in comps], B, ny * nx
 
 
 def as_real_param(a, dev=None):
@@ -278,7 +287,7 @@ def op_high_na(x, y, radius, f):
 
 
 def op_cmul(mask: torch.Tensor):
-    return JonesOp(_lib.OP_CMUL, ptrs=[as_field(mask)])
+    return JonesOp(_lib.OP_CMUL, ptrs=[as_field(mask).contiguous()])
 
 
 def apply_ops(comps, ops, ny, nx):
