@@ -371,27 +371,57 @@ def _time_steps(fn, steps, warmup):
 
 def run_fwd_bwd(steps=10, warmup=3):
     """fwd+bwd optimisation steps through the hand-written adjoints: the batched
-    form (one step over the whole batch) and the plain form (one table per call)."""
+    form (one step over the whole batch, eager and replayed from a captured
+    CUDA graph) and the plain form (one table or field per call)."""
     import torch
 
-    from xlumina_gb300.tables import FourFTable, HighNATable
+    from xlumina_gb300.plans import CapturedStep
+    from xlumina_gb300.tables import FourFTable, HighNATable, VrsLcdTable
     out = {}
+
+    def captured_rate(make, nsteps):
+        t = make()
+        cs = CapturedStep(t)
+        dt = _time_steps(cs, nsteps, 2)
+        del cs, t
+        torch.cuda.empty_cache()
+        return 1.0 / dt
+
+    tv = VrsLcdTable()
+    dt = _time_steps(tv.step, steps, warmup)
+    single = lambda i=[0]: tv.step(slice(i[0] % tv.B, i[0] % tv.B + 1))  # noqa: E731
+    dt1 = _time_steps(single, tv.B, 2)
+    B = tv.B
+    del tv
+    torch.cuda.empty_cache()
+    cap = captured_rate(lambda: VrsLcdTable(capturable=True), steps)
+    out["vrs"] = {"workload": "VRS 2048^2, 8 fields, per-field LCD (eta, theta) + LP, z = 5 cm, "
+                              "intensity MSE vs per-field targets, AdamW",
+                  "steps_per_s": 1.0 / dt, "fields_per_s": B / dt, "captured_steps_per_s": cap,
+                  "captured_fields_per_s": B * cap, "plain_fields_per_s": 1.0 / dt1, "batch": B}
+
     t4 = FourFTable()
     dt = _time_steps(t4.step, steps, warmup)
     single = lambda i=[0]: t4.step(t4.inputs[i[0] % t4.B:i[0] % t4.B + 1], t4.target[i[0] % t4.B:i[0] % t4.B + 1])  # noqa: E731
     dt1 = _time_steps(single, t4.B, 2)
-    out["four_f"] = {"workload": "4f table 16 x 1024^2 (SLM1 -> RS 25 cm -> lens -> CZT 512^2 ROI -> SLM2 -> CZT), "
-                                 "532 nm, normalised intensity MSE, AdamW",
-                     "steps_per_s": 1.0 / dt, "tables_per_s": t4.B / dt, "plain_tables_per_s": 1.0 / dt1,
-                     "batch": t4.B}
+    B = t4.B
     del t4
     torch.cuda.empty_cache()
+    cap = captured_rate(lambda: FourFTable(capturable=True), steps)
+    out["four_f"] = {"workload": "4f table 16 x 1024^2 (SLM1 -> RS 25 cm -> lens -> CZT 512^2 ROI -> SLM2 -> CZT), "
+                                 "532 nm, normalised intensity MSE, AdamW",
+                     "steps_per_s": 1.0 / dt, "tables_per_s": B / dt, "captured_steps_per_s": cap,
+                     "captured_tables_per_s": B * cap, "plain_tables_per_s": 1.0 / dt1, "batch": B}
     th = HighNATable()
     dt = _time_steps(th.step, max(2, steps // 2), 2)
+    B = th.B
+    del th
+    torch.cuda.empty_cache()
+    cap = captured_rate(lambda: HighNATable(capturable=True), max(2, steps // 2))
     out["high_na"] = {"workload": "high-NA table 32 x 2048^2 -> 1024^2 focal ROI (2 um), 650 nm, NA 0.9, f 3 mm, "
                                   "LCD + sSLM, Ez spot loss, AdamW", "steps_per_s": 1.0 / dt,
-                      "tables_per_s": th.B / dt, "batch": th.B}
-    del th
+                      "tables_per_s": B / dt, "captured_steps_per_s": cap, "captured_tables_per_s": B * cap,
+                      "batch": B}
     torch.cuda.empty_cache()
     return out
 

@@ -113,7 +113,7 @@ typedef struct {
   const double* x;    /* device coordinates, nx (VRS Ez derivation) */
   const double* y;    /* device coordinates, ny */
   const double* z;    /* device, one distance per batch entry (VRS Ez derivation) */
-  const void* spectrum;        /* stacked transfer spectra */
+  const void* spectrum;        /* stacked transfer spectra (or NULL when `spectra` is set) */
   long long spectrum_stride;   /* complex64 elements between spectra */
   const int* spectrum_index;   /* device, spectrum used by each batch entry; NULL: entry 0 */
   void* work;                  /* >= xl_rs_work_bytes(batch, comps_out, ny, nx) */
@@ -124,6 +124,9 @@ typedef struct {
                                   gradient is folded back into Ex, Ey with the weights X/r, Y/r of
                                   the forward Ez derivation; outputs out[0], out[1].  pre/post must
                                   be empty. */
+  const void* const* spectra;  /* optional device array of `batch` spectrum pointers, one per batch
+                                  entry (entries of different distances need no stacked copy);
+                                  when set it replaces spectrum / spectrum_stride / spectrum_index */
 } XlRsArgs;
 
 size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx);

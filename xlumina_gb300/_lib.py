@@ -40,7 +40,7 @@ class XlRsArgs(ctypes.Structure):
                 ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
                 ("spectrum", ctypes.c_void_p), ("spectrum_stride", ctypes.c_longlong),
                 ("spectrum_index", ctypes.c_void_p), ("work", ctypes.c_void_p),
-                ("pre", XlProg), ("post", XlProg), ("adjoint", ctypes.c_int)]
+                ("pre", XlProg), ("post", XlProg), ("adjoint", ctypes.c_int), ("spectra", ctypes.c_void_p)]
 
 
 XL_CZT_SCALAR, XL_CZT_VECTOR, XL_CZT_PLAIN = 0, 1, 2

@@ -97,7 +97,7 @@ static int rs_run(void* stream, const XlRsArgs* a, int stage) {
     if (!a->in[c]) { set_error("xl_rs_propagate: null input plane %d", c); return XL_EINVAL; }
   for (int c = 0; c < nout; ++c)
     if (!a->out[c]) { set_error("xl_rs_propagate: null output plane %d", c); return XL_EINVAL; }
-  if (!a->spectrum || !a->work) {
+  if ((!a->spectrum && !a->spectra) || !a->work) {
     set_error("xl_rs_propagate: null spectrum or workspace");
     return XL_EINVAL;
   }
@@ -119,6 +119,7 @@ static int rs_run(void* stream, const XlRsArgs* a, int stage) {
   p.ibs = a->in_bstride; p.obs = a->out_bstride;
   p.x = a->x; p.y = a->y; p.z = a->z;
   p.spec = (const float2*)a->spectrum; p.sstride = a->spectrum_stride; p.sidx = a->spectrum_index;
+  p.specs = (const float2* const*)a->spectra;
   p.work = (float2*)a->work;
   p.pre = a->pre; p.post = a->post;
   p.adjoint = a->adjoint ? 1 : 0;

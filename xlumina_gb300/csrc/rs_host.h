@@ -20,6 +20,7 @@ struct RsLaunch {
   const float2* spec;
   long long sstride;
   const int* sidx;
+  const float2* const* specs;   // per batch entry (overrides spec / sstride / sidx when set)
   float2* work;
   XlProg pre, post;
   int adjoint;

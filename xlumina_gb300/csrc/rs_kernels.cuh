@@ -375,8 +375,8 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   }
   __syncthreads();
   const int kx = t * W + w;
-  const float2* spec = p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride +
-                       (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+  const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
+  const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
   float2* xb = xch + wc * C::CXS;
 #pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {

@@ -106,13 +106,74 @@ def device_grid(a: np.ndarray) -> torch.Tensor:
         t = _grid_cache.get(key)
         if t is not None:
             _grid_cache.move_to_end(key)
-            return t
+            return keep_for_capture(t)
     t = torch.as_tensor(a, dtype=torch.float64, device=device())
     with _LOCK:
         _grid_cache[key] = t
         while len(_grid_cache) > 64:
             _grid_cache.popitem(last=False)
+    return keep_for_capture(t)
+
+
+# Buffers handed out by the host caches while a CUDA graph is being captured
+# (see plans.py): the plan holds them for the graph's lifetime, since a cache
+# eviction must not free memory a replay will read.
+_capture_keep = threading.local()
+
+
+def keep_for_capture(t):
+    keep = getattr(_capture_keep, "items", None)
+    if keep is not None and t is not None:
+        keep.append(t)
     return t
+
+
+_array_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def device_array(a, dtype) -> torch.Tensor:
+    """A small constant array (distances, indices, pointers) on the device,
+    cached by value: repeated calls reuse it, and a call replayed from a
+    captured CUDA graph finds it already on the device."""
+    arr = np.ascontiguousarray(np.asarray(a))
+    key = (arr.tobytes(), arr.dtype.str, str(dtype), torch.cuda.current_device())
+    with _LOCK:
+        t = _array_cache.get(key)
+        if t is not None:
+            _array_cache.move_to_end(key)
+            return keep_for_capture(t)
+    t = torch.as_tensor(arr, device=device()).to(dtype)
+    with _LOCK:
+        _array_cache[key] = t
+        while len(_array_cache) > 256:
+            _array_cache.popitem(last=False)
+    return keep_for_capture(t)
+
+
+class _Built:
+    """A cached device buffer and the event recorded after the launch that
+    filled it.  A user on another stream waits for the event (only while it
+    is pending) and marks the buffer as used by its stream, so the caching
+    allocator cannot recycle it under that stream's pending work."""
+
+    __slots__ = ("t", "ev", "stream")
+
+    def __init__(self, t):
+        self.t = t
+        self.stream = torch.cuda.current_stream()
+        self.ev = torch.cuda.Event()
+        self.ev.record(self.stream)
+
+    def use(self) -> torch.Tensor:
+        if torch.cuda.is_current_stream_capturing():
+            # the plan's warm-up run built it; the plan keeps it alive
+            return keep_for_capture(self.t)
+        cur = torch.cuda.current_stream()
+        if cur != self.stream:
+            if not self.ev.query():
+                cur.wait_event(self.ev)
+            self.t.record_stream(cur)
+        return self.t
 
 
 # ------------------------------------------------------------- geometry --
@@ -246,11 +307,10 @@ def lens_factors(x, y, wavelength, radius, focal):
 
 def op_lens(x, y, wavelength, radius, focal, vector):
     colfac, rowfac, tc, tr = lens_factors(x, y, wavelength, radius, focal)
-    dev = device()
-    c = torch.as_tensor(colfac, device=dev).to(torch.complex64)
-    r = torch.as_tensor(rowfac, device=dev).to(torch.complex64)
-    tct = torch.as_tensor(tc, device=dev, dtype=torch.float64)
-    trt = torch.as_tensor(tr, device=dev, dtype=torch.float64)
+    c = device_array(colfac.astype(np.complex64), torch.complex64)
+    r = device_array(rowfac.astype(np.complex64), torch.complex64)
+    tct = device_array(np.asarray(tc, dtype=np.float64), torch.float64)
+    trt = device_array(np.asarray(tr, dtype=np.float64), torch.float64)
     return JonesOp(_lib.OP_SEPMASK, ptrs=[c, r, tct, trt], sval=[1.0 if vector else 0.0])
 
 
@@ -261,17 +321,18 @@ def highna_coefficients(x, y, radius, f):
     """The lens's 6 per-pixel coefficient planes, cached by geometry (computed by libxlgb)."""
     key = (x.tobytes(), y.tobytes(), float(radius), float(f), torch.cuda.current_device())
     with _LOCK:
-        t = _highna_cache.get(key)
-        if t is not None:
+        e = _highna_cache.get(key)
+        if e is not None:
             _highna_cache.move_to_end(key)
-            return t
+    if e is not None:
+        return e.use()
     t = torch.empty((6, len(y), len(x)), dtype=torch.float32, device=device())
     _lib.check(lib().xl_highna_coefficients(stream_handle(), len(y), len(x), device_grid(x).data_ptr(),
                                             device_grid(y).data_ptr(), float(radius), float(f), t.data_ptr()),
                "xl_highna_coefficients")
-    torch.cuda.current_stream().synchronize()   # shared across streams once cached
+    e = _Built(t)
     with _LOCK:
-        _highna_cache[key] = t
+        _highna_cache[key] = e
         while len(_highna_cache) > 8:
             _highna_cache.popitem(last=False)
     return t
@@ -364,19 +425,20 @@ class SpectrumCache:
     def get(self, x, y, z, wavelength):
         k = self.key(x, y, z, wavelength)
         with _LOCK:
-            s = self._d.get(k)
-            if s is not None:
+            e = self._d.get(k)
+            if e is not None:
                 self._d.move_to_end(k)
-                return s
+        if e is not None:
+            return e.use()
         s = build_rs_spectrum(x, y, z, wavelength)
         nb = s.numel() * 8
         with _LOCK:
-            self._d[k] = s
+            self._d[k] = _Built(s)
             self._bytes += nb
             self.builds += 1
             while self._bytes > self.max_bytes and len(self._d) > 1:
                 _, old = self._d.popitem(last=False)
-                self._bytes -= old.numel() * 8
+                self._bytes -= old.t.numel() * 8
         return s
 
     def clear(self):
@@ -394,8 +456,8 @@ def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
     lq = rs_logq(ny, nx)
     P = 2 << lq
     dev = device()
-    offx = torch.as_tensor(rs_wrapped_offsets(x, P), device=dev)
-    offy = torch.as_tensor(rs_wrapped_offsets(y, P), device=dev)
+    offx = device_array(rs_wrapped_offsets(x, P), torch.float64)
+    offy = device_array(rs_wrapped_offsets(y, P), torch.float64)
     spec = torch.empty(P * P, dtype=torch.complex64, device=dev)
     work = torch.empty(P * P, dtype=torch.complex64, device=dev)
     dx = x[1] - x[0]
@@ -404,8 +466,6 @@ def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
     _lib.check(L.xl_rs_transfer_spectrum(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(), float(z),
                                          float(wavelength), scale, spec.data_ptr(), work.data_ptr()),
                "xl_rs_transfer_spectrum")
-    # cached spectra are shared by every stream: finish the build before handing it out
-    torch.cuda.current_stream().synchronize()
     return spec
 
 
@@ -432,19 +492,19 @@ class RsCall:
         uniq = sorted(set(zs))
         specs = [SPECTRA.get(x, y, zz, wavelength) for zz in uniq]
         dev = comps[0].device
+        spec_ptrs = None
         if len(specs) == 1:
-            spec, sidx, sstride = specs[0], None, 0
-        else:
-            spec = torch.stack(specs)
-            sstride = specs[0].numel()
-            sidx = torch.as_tensor([uniq.index(v) for v in zs], dtype=torch.int32, device=dev)
+            spec = specs[0]
+        else:   # one spectrum pointer per batch entry, no stacked copy
+            spec = None
+            spec_ptrs = device_array([specs[uniq.index(v)].data_ptr() for v in zs], torch.int64)
         cout = 3 if vector else 1
         if work is None:
             work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
             nout = 2 if (adjoint and vector) else cout
             outs = [torch.empty(tuple(lead) + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(nout)]
-        zt = torch.as_tensor(zs, dtype=torch.float64, device=dev) if vector else None
+        zt = device_array(np.asarray(zs, dtype=np.float64), torch.float64) if vector else None
         a = _lib.XlRsArgs()
         a.batch = B
         a.comps_in = len(comps)
@@ -460,9 +520,10 @@ class RsCall:
             a.x = device_grid(x).data_ptr()
             a.y = device_grid(y).data_ptr()
             a.z = zt.data_ptr()
-        a.spectrum = spec.data_ptr()
-        a.spectrum_stride = sstride
-        a.spectrum_index = _ptr(sidx)
+        a.spectrum = _ptr(spec)
+        a.spectrum_stride = 0
+        a.spectrum_index = 0
+        a.spectra = _ptr(spec_ptrs)
         a.work = work.data_ptr()
         fill_prog(a.pre, pre, ny, nx)
         fill_prog(a.post, post, ny, nx)
@@ -470,7 +531,7 @@ class RsCall:
         self.args = a
         self.outs = outs
         self.batch, self.ny, self.nx, self.comps = B, ny, nx, cout
-        self._keep = (comps, spec, sidx, work, zt, list(pre or ()), list(post or ()))
+        self._keep = (comps, specs, spec_ptrs, work, zt, list(pre or ()), list(post or ()))
 
     def run(self):
         _lib.check(lib().xl_rs_propagate(stream_handle(), ctypes.byref(self.args)), "xl_rs_propagate")
@@ -574,6 +635,8 @@ def device_chirps(m, f1, f2, Dm, M, adjoint=False):
         v = _chirp_cache.get(key)
         if v is not None:
             _chirp_cache.move_to_end(key)
+            for t in v[1:]:
+                keep_for_capture(t)
             return v
     L, pre, g, post = bluestein_plan(m, f1, f2, Dm, M)
     if adjoint:

@@ -26,7 +26,7 @@ from .wave_optics import LightSource
 
 class FourFTable:
     def __init__(self, n=1024, roi_n=512, batch=16, wavelength=0.532, half_width=1500.0, f=2.5e5,
-                 roi_half_width=1000.0, waist=1200.0, seed=2000, device="cuda"):
+                 roi_half_width=1000.0, waist=1200.0, seed=2000, device="cuda", capturable=False):
         self.n, self.m, self.B, self.f = n, roi_n, batch, f
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
@@ -44,7 +44,8 @@ class FourFTable:
                                       device=device).requires_grad_(True)
         self.phase2 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32),
                                       device=device).requires_grad_(True)
-        self.opt = torch.optim.AdamW([self.phase1, self.phase2], lr=0.05)
+        # capturable: the step count lives on the device, so plans.CapturedStep can record a step
+        self.opt = torch.optim.AdamW([self.phase1, self.phase2], lr=0.05, capturable=capturable)
 
     def loss(self, inputs=None, target=None):
         inputs = self.inputs if inputs is None else inputs
@@ -78,7 +79,7 @@ def small_area_hybrid_batched(I):
 
 class HighNATable:
     def __init__(self, n=2048, roi_n=1024, batch=32, wavelength=0.650, half_width=2700.0, na=0.9,
-                 f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda"):
+                 f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda", capturable=False):
         self.n, self.m, self.B = n, roi_n, batch
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
@@ -94,7 +95,7 @@ class HighNATable:
                                      device=device).requires_grad_(True)
         self.phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
                                    device=device).requires_grad_(True)
-        self.opt = torch.optim.AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05)
+        self.opt = torch.optim.AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05, capturable=capturable)
 
     def loss(self):
         light = VectorizedLight(self.x, self.y, self.wavelength)
@@ -107,6 +108,53 @@ class HighNATable:
     def step(self):
         self.opt.zero_grad(set_to_none=True)
         L = self.loss()
+        L.backward()
+        self.opt.step()
+        return L
+
+
+class VrsLcdTable:
+    """2048^2 VRS optimisation: per-field LCD retarder maps (eta, theta) in
+    front of a linear polarizer shape a radially polarised source, which is
+    propagated by VRS to z; the loss is the intensity MSE (Ex, Ey and Ez
+    together) against per-field target intensities.  One step is a forward
+    through the fused kernels, the hand-written adjoints backward, and AdamW.
+    ``fields`` selects a subset of the batch (the plain form: one field per
+    call)."""
+
+    def __init__(self, n=2048, batch=8, wavelength=0.633, half_width=2000.0, waist=1000.0, z=5e4,
+                 seed=5000, device="cuda", capturable=False):
+        self.n, self.B, self.z, self.wavelength = n, batch, z, wavelength
+        self.x, self.y = toolbox.space(half_width, n)
+        X, Y = np.meshgrid(self.x, self.y)
+        g = np.exp(-(X ** 2 + Y ** 2) / waist ** 2)
+        self.Ex = torch.as_tensor(((X / waist) * g).astype(np.complex64), device=device)
+        self.Ey = torch.as_tensor(((Y / waist) * g).astype(np.complex64), device=device)
+        rng = np.random.default_rng(seed)
+        self.eta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
+                                   device=device).requires_grad_(True)
+        self.theta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
+                                     device=device).requires_grad_(True)
+        tgt = rng.uniform(0, 1, (batch, n, n)).astype(np.float32)
+        self.target = torch.as_tensor(tgt / tgt.sum(axis=(-2, -1), keepdims=True), device=device)
+        self.alpha = float(rng.uniform(0, np.pi))
+        self.opt = torch.optim.AdamW([self.eta, self.theta], lr=0.05, capturable=capturable)
+
+    def loss(self, fields=None):
+        sl = slice(None) if fields is None else fields
+        eta, theta, target = self.eta[sl], self.theta[sl], self.target[sl]
+        b = eta.shape[0]
+        light = VectorizedLight(self.x, self.y, self.wavelength)
+        light.Ex = self.Ex.expand(b, self.n, self.n)
+        light.Ey = self.Ey.expand(b, self.n, self.n)
+        out, _ = oe.linear_polarizer(oe.LCD(light, eta, theta), self.alpha).VRS_propagation(self.z)
+        I = torch.abs(out.Ex) ** 2 + torch.abs(out.Ey) ** 2 + torch.abs(out.Ez) ** 2
+        I = I / torch.sum(I, dim=(-2, -1), keepdim=True)
+        return torch.mean(torch.sum((I - target) ** 2, dim=(-2, -1)))
+
+    def step(self, fields=None):
+        self.opt.zero_grad(set_to_none=True)
+        L = self.loss(fields)
         L.backward()
         self.opt.step()
         return L
