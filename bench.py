@@ -348,6 +348,7 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         line["fwd_bwd"] = run_fwd_bwd()
     if not args.no_serving:
+        line["uneven_batch"] = run_uneven()
         line["serving"] = run_serving(args.serve_requests)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
@@ -426,6 +427,57 @@ def run_fwd_bwd(steps=10, warmup=3):
     return out
 
 
+def run_uneven(reps=20, seed=6000):
+    """Many setups of uneven size: 48 scalar RS at 256^2, 12 VRS at 512^2 and
+    4 scalar RS at 1024^2, each with its own SLM phase mask and distance.
+    Three forms: one public-API call per setup; one batched call per size
+    group (a distance per batch entry); and the grouped calls captured in one
+    CUDA graph, replayed with a single launch."""
+    import torch
+
+    from xlumina_gb300 import engine, toolbox
+    from xlumina_gb300.plans import CapturedPlan
+    rng = np.random.default_rng(seed)
+    groups = [("rs", 256, 48), ("vrs", 512, 12), ("rs", 1024, 4)]
+    data = []
+    for kind, n, cnt in groups:
+        x, y = toolbox.space(1000.0 * n / 1024, n)
+        comps = 1 if kind == "rs" else 2
+        f = torch.as_tensor((rng.standard_normal((comps, cnt, n, n)) + 1j * rng.standard_normal((comps, cnt, n, n)))
+                            .astype(np.complex64), device="cuda")
+        ph = torch.as_tensor(rng.uniform(-np.pi, np.pi, (cnt, n, n)).astype(np.float32), device="cuda")
+        zs = list(rng.choice([1e4, 2e4, 5e4, 1e5], cnt))
+        data.append((kind, n, cnt, x, y, f, ph, zs))
+    n_setups = sum(c for _, _, c in groups)
+
+    def one_by_one():
+        for kind, n, cnt, x, y, f, ph, zs in data:
+            for i in range(cnt):
+                engine.rs_propagate([f[c, i] for c in range(f.shape[0])], x, y, 0.6, zs[i], kind == "vrs",
+                                    pre=[engine.op_phase(ph[i])] if kind == "rs" else
+                                    [engine.op_sslm(ph[i], ph[i])])
+
+    def grouped():
+        outs = []
+        for kind, n, cnt, x, y, f, ph, zs in data:
+            outs += engine.rs_propagate([f[c] for c in range(f.shape[0])], x, y, 0.6, zs, kind == "vrs",
+                                        pre=[engine.op_phase(ph)] if kind == "rs" else [engine.op_sslm(ph, ph)])
+        return outs
+
+    res = {"workload": "uneven setups: 48 RS 256^2 + 12 VRS 512^2 + 4 RS 1024^2, per-setup SLM masks and distances",
+           "setups": n_setups}
+    dt = _time_steps(one_by_one, reps, 3)
+    res["one_call_per_setup_setups_per_s"] = n_setups / dt
+    dt = _time_steps(grouped, reps, 3)
+    res["grouped_setups_per_s"] = n_setups / dt
+    plan = CapturedPlan(grouped)
+    dt = _time_steps(plan.replay, reps, 3)
+    res["captured_graph_setups_per_s"] = n_setups / dt
+    del plan
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_serving(n_req=10000, seed=4000):
     """Poisson stream of mixed requests (sizes 256..2048 with weights .4/.3/.2/.1; RS, VRS, CZT
     or an SLM-phase gradient; z uniform in [1, 20] cm) through the continuous-batching server,
@@ -478,7 +530,15 @@ def run_serving(n_req=10000, seed=4000):
     rate = 0.8 * plain_rate * 1.5   # offered load: above the plain path's capacity, inside the batched one
     reqs = [make(i) for i in range(n_req)]
     gaps = rng.exponential(1.0 / rate, n_req)
-    srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2)
+    from xlumina_gb300.autotune import BatchTuner
+    srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2,
+                 tuner=BatchTuner(candidates=(1, 2, 4, 8, 16), repeats=2))
+    t_tune = time.perf_counter()
+    examples = {}
+    for r in reqs:
+        examples.setdefault((r.kind, len(r.x)), r)
+    packing = srv.tune(list(examples.values()))
+    t_tune = time.perf_counter() - t_tune
     futs = [None] * n_req
 
     def client():
@@ -503,6 +563,7 @@ def run_serving(n_req=10000, seed=4000):
                         "z U[1,20] cm, HBM budget 150 GB",
             "requests": n_req, "offered_req_per_s": rate, "served_req_per_s": n_req / wall,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_batch": st["mean_batch"],
+            "batch_packing": {f"{k[0]} {k[1]}^2": v for k, v in packing.items()}, "tuning_s": t_tune,
             "plain_req_per_s": plain_rate, "plain_p50_ms": float(np.percentile(np.asarray(lat) * 1e3, 50)),
             "plain_p99_ms": float(np.percentile(np.asarray(lat) * 1e3, 99))}
 

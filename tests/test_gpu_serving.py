@@ -70,3 +70,27 @@ def test_admission_budget_and_oversize_refusal():
         srv.submit(big).result(timeout=10)
     srv.close()
     assert srv.stats()["mean_batch"] <= 2.0 + 1e-9    # the budget admits at most two at a time
+
+
+def test_tuned_batch_packing(tmp_path):
+    import torch
+
+    from xlumina_gb300 import toolbox
+    from xlumina_gb300.autotune import BatchTuner
+    from xlumina_gb300.serving import Request, Server
+    n = 64
+    x, y = toolbox.space(100.0, n)
+    f = torch.randn((n, n), dtype=torch.complex64, device="cuda")
+    tuner = BatchTuner(path=str(tmp_path / "tune.json"), candidates=(1, 2, 4), repeats=1)
+    srv = Server(max_batch=4, tuner=tuner)
+    try:
+        packing = srv.tune([Request("rs", [f], x, y, 0.5, 1e3)])
+        b = packing[("rs", n, n)]
+        assert b in (1, 2, 4)
+        assert srv.batch_cap(Request("rs", [f], x, y, 0.5, 2e3)) == b
+        futs = [srv.submit(Request("rs", [f], x, y, 0.5, 1e3 * (i + 1))) for i in range(6)]
+        outs = [fu.result(timeout=120) for fu in futs]
+        assert all(o.shape == (n, n) for o in outs)
+    finally:
+        srv.close()
+    assert (tmp_path / "tune.json").exists()

@@ -1,0 +1,110 @@
+"""Batch packing chosen by measurement.
+
+For a class of requests (kind and grid side), the tuner times batched
+launches of 1, 2, 4, ... requests and keeps the smallest batch whose
+throughput (requests per second) is within ``tolerance`` of the best one:
+packing more requests into one launch past that point adds latency to the
+first of them and no throughput.  A small field leaves most SMs idle, so its
+class packs many requests per launch; a 2048^2 field fills the GPU alone.
+
+Choices are cached on disk as JSON, per GPU model and class, so the
+measurement runs once per machine type.  The cache file is
+``$XL_AUTOTUNE_CACHE`` if set, else ``~/.cache/xlumina_gb300/autotune.json``.
+"""
+from __future__ import annotations
+
+import json
+import os
+import statistics
+import threading
+import time
+
+DEFAULT_CANDIDATES = (1, 2, 4, 8, 16, 32)
+
+
+def default_cache_path() -> str:
+    p = os.environ.get("XL_AUTOTUNE_CACHE")
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "xlumina_gb300", "autotune.json")
+
+
+class BatchTuner:
+    """``best_batch(cls, measure)``: the batch size for request class ``cls``
+    (a tuple of str / int / float), measuring with ``measure(b)`` (seconds for
+    one launch of ``b`` requests, device work included) when the class is not
+    in the cache yet."""
+
+    def __init__(self, path: str | None = None, device_name: str | None = None, tolerance: float = 0.05,
+                 candidates=DEFAULT_CANDIDATES, repeats: int = 3):
+        self.path = path or default_cache_path()
+        self.device_name = device_name or self._device_name()
+        self.tolerance = float(tolerance)
+        self.candidates = tuple(sorted(set(int(c) for c in candidates)))
+        self.repeats = int(repeats)
+        self._lock = threading.Lock()
+        self._cache = self._load()
+
+    @staticmethod
+    def _device_name() -> str:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.get_device_name()
+        except Exception:   # no torch or no device: a host-only name
+            pass
+        return "cpu"
+
+    @staticmethod
+    def class_key(cls) -> str:
+        return "|".join(str(v) for v in cls)
+
+    def _load(self) -> dict:
+        try:
+            with open(self.path) as f:
+                data = json.load(f)
+            return data if isinstance(data, dict) else {}
+        except (OSError, ValueError):
+            return {}
+
+    def save(self) -> None:
+        d = os.path.dirname(self.path)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        tmp = f"{self.path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(self._cache, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+    def cached(self, cls):
+        return self._cache.get(self.device_name, {}).get(self.class_key(cls))
+
+    def choose(self, rates: dict) -> int:
+        """Smallest candidate within the tolerance of the best requests/s."""
+        best = max(rates.values())
+        for b in sorted(rates):
+            if rates[b] >= (1.0 - self.tolerance) * best:
+                return int(b)
+        return int(max(rates, key=rates.get))
+
+    def best_batch(self, cls, measure, max_batch: int | None = None) -> int:
+        with self._lock:
+            hit = self.cached(cls)
+        if hit is not None:
+            b = int(hit["batch"])
+            return min(b, max_batch) if max_batch else b
+        cands = [c for c in self.candidates if not max_batch or c <= max_batch] or [1]
+        rates = {}
+        for b in cands:
+            measure(b)                                     # warm-up (spectra, caches)
+            ts = [measure(b) for _ in range(self.repeats)]
+            rates[b] = b / max(statistics.median(ts), 1e-9)
+        b = self.choose(rates)
+        with self._lock:
+            self._cache.setdefault(self.device_name, {})[self.class_key(cls)] = {
+                "batch": b, "rates": {str(k): v for k, v in rates.items()}, "when": time.time()}
+            try:
+                self.save()
+            except OSError:
+                pass   # a read-only cache location still tunes, for this process
+        return b

@@ -93,10 +93,20 @@ def run_batch(reqs):
     raise ValueError(f"unknown request kind {r0.kind!r}")
 
 
+def request_class(r: Request):
+    """The batch-packing class of a request: its kind and grid."""
+    return (r.kind, len(r.y), len(r.x))
+
+
 class Server:
-    def __init__(self, hbm_budget_bytes=150e9, max_batch=16, streams=2, device=None):
+    """``tuner`` (an ``autotune.BatchTuner``): the batch size per request class
+    comes from it once the class is tuned (``tune``), else ``max_batch``."""
+
+    def __init__(self, hbm_budget_bytes=150e9, max_batch=16, streams=2, device=None, tuner=None):
         self.budget = float(hbm_budget_bytes)
         self.max_batch = int(max_batch)
+        self.tuner = tuner
+        self._caps = {}
         self.device = device or engine.device()
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(streams)]
         self._q = collections.deque()
@@ -109,6 +119,28 @@ class Server:
         self.completed = 0
         self._thread = threading.Thread(target=self._loop, daemon=True)
         self._thread.start()
+
+    def tune(self, examples) -> dict:
+        """Measure the batch packing of each example request's class (before
+        serving); returns {class: batch size}."""
+        if self.tuner is None:
+            return {}
+        out = {}
+        for r in examples:
+            cls = request_class(r)
+
+            def measure(b, r=r):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                run_batch([r] * b)
+                torch.cuda.synchronize()
+                return time.perf_counter() - t0
+
+            out[cls] = self._caps[cls] = self.tuner.best_batch(cls, measure, self.max_batch)
+        return out
+
+    def batch_cap(self, r: Request) -> int:
+        return self._caps.get(request_class(r), self.max_batch)
 
     # -- client side
     def submit(self, req: Request) -> Future:
@@ -166,11 +198,12 @@ class Server:
         """First queued request, plus every queued request compatible with it, inside the budget."""
         head = self._q[0]
         key = head.key()
+        cap = self.batch_cap(head)
         picked, rest = [], collections.deque()
         nb = 0.0
         while self._q:
             r = self._q.popleft()
-            if r.key() == key and len(picked) < self.max_batch and self._bytes + nb + r.nbytes() <= self.budget:
+            if r.key() == key and len(picked) < cap and self._bytes + nb + r.nbytes() <= self.budget:
                 picked.append(r)
                 nb += r.nbytes()
             else:
