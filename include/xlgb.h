@@ -234,6 +234,23 @@ int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const vo
                     long long in_bstride, const void* const* gout, long long gout_bstride,
                     void* const* gin, long long gin_bstride, const XlProg* prog, void* const* pgrad);
 
+/* ---- Losses ------------------------------------------------------------ */
+
+/* Intensity MSE, MSE_Intensity of loss_functions.py:137-149, per plane:
+ * out[p] = sum_i (|a_i|^2 - |b_i|^2)^2 / npix for planes p of npix complex64
+ * pixels (plane strides in elements; b_pstride 0 broadcasts one target).
+ * The sum runs in a fixed order (float64 partials in `work`, of
+ * xl_mse_intensity_work_bytes), so repeated calls give identical results. */
+size_t xl_mse_intensity_work_bytes(int planes, long long npix);
+int xl_mse_intensity(void* stream, int planes, long long npix, const void* a, long long a_pstride,
+                     const void* b, long long b_pstride, void* work, void* out);
+
+/* Its gradients for upstream gradients gloss[p] (torch's convention for
+ * complex tensors): ga = 4 gloss (|a|^2 - |b|^2) a / npix, gb = -4 gloss
+ * (|a|^2 - |b|^2) b / npix, written as contiguous planes (either may be NULL). */
+int xl_mse_intensity_grad(void* stream, int planes, long long npix, const void* a, long long a_pstride,
+                          const void* b, long long b_pstride, const void* gloss, void* ga, void* gb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,13 @@ SIGNATURES = {
                                        ctypes.POINTER(XlProg), ctypes.POINTER(ctypes.c_void_p)]),
     "xl_highna_coefficients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "xl_mse_intensity_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
+    "xl_mse_intensity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
+                                        ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "xl_mse_intensity_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
+                                             ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

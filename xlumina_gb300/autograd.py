@@ -100,7 +100,8 @@ class _Fused(torch.autograd.Function):
         if plan.ops:
             nb = len(gprog)
             b = list(base) + [None] * (nb - len(base))
-            gin, pgrads = engine.ops_backward(b[:nb], gprog, plan.ops, plan.ny, plan.nx)
+            gin, pgrads = engine.ops_backward(b[:nb], gprog, plan.ops, plan.ny, plan.nx,
+                                              want_input=any(t.requires_grad for t in base))
         else:
             gin, pgrads = gprog, {}
         gbase = []
@@ -131,9 +132,10 @@ class _Ops(torch.autograd.Function):
         base = ctx.saved_tensors
         ref = next((g for g in gouts if g is not None), None)
         gouts = [(g if g is not None else torch.zeros_like(ref)).to(torch.complex64).contiguous() for g in gouts]
-        gin, pgrads = engine.ops_backward(list(base), gouts, ctx.ops, ctx.ny, ctx.nx)
+        want = any(t.requires_grad for t in base)
+        gin, pgrads = engine.ops_backward(list(base), gouts, ctx.ops, ctx.ny, ctx.nx, want_input=want)
         trainable = _trainable(ctx.ops)
-        gbase = [gin[i] if base[i].requires_grad else None for i in range(len(base))]
+        gbase = [gin[i] if (base[i].requires_grad and gin[i] is not None) else None for i in range(len(base))]
         return (None, None, None, None, *gbase, *[pgrads.get((k, q)) for (k, q, _) in trainable])
 
 
@@ -142,3 +144,25 @@ def apply_ops(base, ops, ny, nx):
         params = [p for (_, _, p) in _trainable(ops)]
         return list(_Ops.apply(list(ops), ny, nx, len(base), *base, *params))
     return engine.apply_ops(base, ops, ny, nx)
+
+
+class _MseIntensity(torch.autograd.Function):
+    """Intensity MSE per plane with the hand-written gradient of libxlgb."""
+
+    @staticmethod
+    def forward(ctx, a, b):
+        ctx.save_for_backward(a, b)
+        return engine.mse_intensity(a, b)
+
+    @staticmethod
+    def backward(ctx, g):
+        a, b = ctx.saved_tensors
+        want_a, want_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        ga, gb = engine.mse_intensity_grad(a, b, g, want_a, want_b)
+        if gb is not None and tuple(b.shape) != tuple(gb.shape):   # a broadcast target
+            gb = gb.reshape((-1,) + tuple(b.shape[-2:])).sum(0).reshape(b.shape)
+        return ga, gb
+
+
+def mse_intensity(a, b):
+    return _MseIntensity.apply(a, b)

@@ -24,7 +24,7 @@ __global__ void apply_ops_kernel(const ElemLaunch p) {
     e[0] = p.in[0][off];
     if (p.C > 1) e[1] = p.in[1][off];
     if (p.C > 2) e[2] = p.in[2][off];
-    const int row = (int)(i / p.nx), col = (int)(i % p.nx);
+    const int row = (int)((unsigned)i / (unsigned)p.nx), col = (int)i - row * p.nx;
     PixelCtx px{row, col, i, b};
     apply_prog(p.prog, e, px);
     const long long o = (long long)b * p.obs + i;
@@ -46,25 +46,32 @@ struct OpsBwdLaunch {
   void* pgrad[XL_MAX_OPS * 4];
 };
 
-// One thread per pixel, looping over the batch so that gradients of
-// parameters shared by the batch are summed in a fixed order.  The op loops
-// are unrolled to XL_MAX_OPS so the per-op intermediates stay in registers;
-// the per-thread parameter-gradient accumulators live in shared memory,
-// [slot][thread] so that a warp's accesses fall in distinct banks.
+// One thread per pixel and batch entry, or (when a per-pixel parameter shared
+// by the whole batch needs its gradient) one thread per pixel looping over
+// the batch, so that the batch sum runs in a fixed order.  The op loops are
+// unrolled to KMAX so the per-op intermediates stay in registers.  Dynamic
+// shared memory holds, [slot][thread] so that a warp's accesses fall in
+// distinct banks: the scalar-parameter partial sums (when any scalar
+// gradient is asked for), then the shared-plane batch sums (when needed).
 template <int KMAX>
-__global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p) {
+__global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p, int scalar_acc, int plane_acc) {
   constexpr int NS = XL_MAX_OPS * 4;
   constexpr int NT = 128;
-  __shared__ float acc_s[NS * NT];    // scalar-parameter partial sums
-  __shared__ float acc_p[NS * NT];    // shared per-pixel parameters, summed over the batch
+  extern __shared__ float accm[];
+  float* acc_s = accm;                              // NS x NT, when scalar_acc
+  float* acc_p = accm + (scalar_acc ? NS * NT : 0); // NS x NT, when plane_acc
   const long long npix = (long long)p.ny * p.nx;
   const int K = p.prog.nops;
   const int tid = threadIdx.x;
-  for (int q = 0; q < NS; ++q) acc_s[q * NT + tid] = 0.f;
+  const int b_lo = gridDim.y > 1 ? blockIdx.y : 0;
+  const int b_hi = gridDim.y > 1 ? blockIdx.y + 1 : p.B;
+  if (scalar_acc)
+    for (int q = 0; q < NS; ++q) acc_s[q * NT + tid] = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
        i += (long long)gridDim.x * blockDim.x) {
-    const int row = (int)(i / p.nx), col = (int)(i % p.nx);
-    for (int q = 0; q < 4 * K; ++q) acc_p[q * NT + tid] = 0.f;
+    const int row = (int)((unsigned)i / (unsigned)p.nx), col = (int)i - row * p.nx;
+    if (plane_acc)
+      for (int q = 0; q < 4 * K; ++q) acc_p[q * NT + tid] = 0.f;
     // the high-NA lens depends on the pixel only: its coefficients are hoisted out of the batch loop
     float kc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int hk = -1;
@@ -77,7 +84,7 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p)
           hk = k;
         }
     }
-    for (int b = 0; b < p.B; ++b) {
+    for (int b = b_lo; b < b_hi; ++b) {
       PixelCtx px{row, col, i, b};
       float2 st[KMAX][3];
       float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
@@ -85,12 +92,15 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p)
       e[0] = p.in[0][off];
       if (p.C > 1 && p.in[1]) e[1] = p.in[1][off];
       if (p.C > 2 && p.in[2]) e[2] = p.in[2][off];
+      // forward recompute: the input of every op (the last op's output is not needed)
 #pragma unroll
       for (int k = 0; k < KMAX; ++k) {
         if (k < K) {
           st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
-          if (k == hk) apply_highna(kc, e);
-          else apply_op(p.prog.ops[k], e, px);
+          if (k + 1 < K) {
+            if (k == hk) apply_highna(kc, e);
+            else apply_op(p.prog.ops[k], e, px);
+          }
         }
       }
       float2 g[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
@@ -124,13 +134,15 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p)
       if (p.C > 1 && p.gin[1]) p.gin[1][gi] = g[1];
       if (p.C > 2 && p.gin[2]) p.gin[2][gi] = g[2];
     }
-    for (int k = 0; k < K; ++k)
-      for (int q = 0; q < 4; ++q) {
-        const XlOp& op = p.prog.ops[k];
-        if (p.pgrad[k * 4 + q] && (op.pmask & (1 << q)) && !op.pbstride)
-          ((float*)p.pgrad[k * 4 + q])[i] = acc_p[(k * 4 + q) * NT + tid];
-      }
+    if (plane_acc)
+      for (int k = 0; k < K; ++k)
+        for (int q = 0; q < 4; ++q) {
+          const XlOp& op = p.prog.ops[k];
+          if (p.pgrad[k * 4 + q] && (op.pmask & (1 << q)) && !op.pbstride)
+            ((float*)p.pgrad[k * 4 + q])[i] = acc_p[(k * 4 + q) * NT + tid];
+        }
   }
+  if (!scalar_acc) return;
   // scalar parameters: block reduction, one float64 atomic per block and slot
   __shared__ float red[8];
   const int lane = tid & 31, warp = tid >> 5;
@@ -155,12 +167,81 @@ __global__ void highna_plane_kernel(int ny, int nx, XlOp op, float* out) {
   const long long npix = (long long)ny * nx;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
        i += (long long)gridDim.x * blockDim.x) {
-    PixelCtx px{(int)(i / nx), (int)(i % nx), i, 0};
+    const int row = (int)((unsigned)i / (unsigned)nx);
+    PixelCtx px{row, (int)i - row * nx, i, 0};
     float kc[6];
     highna_coeffs(op, px, kc);
 #pragma unroll
     for (int q = 0; q < 6; ++q) out[q * npix + i] = kc[q];
   }
+}
+
+// ---- intensity MSE (loss_functions.py:137-149) ----
+// loss[p] = sum_i (|a_i|^2 - |b_i|^2)^2 / npix for plane p; the sum runs in two
+// fixed-order stages (per-block float partials in float64, then per plane),
+// so the result does not depend on scheduling.
+constexpr int MSE_THREADS = 256;
+
+__global__ void __launch_bounds__(MSE_THREADS) mse_int_partial(const float2* __restrict__ a, long long aps,
+                                                               const float2* __restrict__ b, long long bps,
+                                                               long long npix, double* __restrict__ partial) {
+  const int plane = blockIdx.y;
+  a += (long long)plane * aps;
+  b += (long long)plane * bps;
+  float acc = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 u = a[i], v = b[i];
+    const float d = (u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y);
+    acc = fmaf(d, d, acc);
+  }
+  __shared__ float red[MSE_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < MSE_THREADS / 32; ++w) t += red[w];
+    partial[(long long)plane * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// One warp per plane: lane l sums partials l, l + 32, ... in order, then a
+// fixed shuffle tree (the same order on every call).
+__global__ void mse_int_finish(const double* __restrict__ partial, int nblk, int planes, double inv_n,
+                               float* __restrict__ out) {
+  const int plane = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (plane >= planes) return;
+  double t = 0.0;
+  for (int k = lane; k < nblk; k += 32) t += partial[(long long)plane * nblk + k];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[plane] = (float)(t * inv_n);
+}
+
+// Gradients of loss[p] with upstream gradient g[p] (torch's convention for
+// complex tensors, 2 dL/d conj): ga = 4 g (|a|^2 - |b|^2) a / npix and
+// gb = -4 g (|a|^2 - |b|^2) b / npix (either may be NULL).
+__global__ void mse_int_grad(const float2* __restrict__ a, long long aps, const float2* __restrict__ b,
+                             long long bps, long long npix, const float* __restrict__ g, float four_inv_n,
+                             float2* __restrict__ ga, float2* __restrict__ gb) {
+  const int plane = blockIdx.y;
+  a += (long long)plane * aps;
+  b += (long long)plane * bps;
+  const float s = g[plane] * four_inv_n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 u = a[i], v = b[i];
+    const float d = s * ((u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y));
+    if (ga) ga[(long long)plane * npix + i] = make_float2(d * u.x, d * u.y);
+    if (gb) gb[(long long)plane * npix + i] = make_float2(-d * v.x, -d * v.y);
+  }
+}
+
+static int mse_blocks(long long npix) {
+  long long nb = (npix + MSE_THREADS * 8 - 1) / (MSE_THREADS * 8);
+  if (nb > 152 * 4) nb = 152 * 4;
+  return nb < 1 ? 1 : (int)nb;
 }
 
 static cudaError_t elem_upload_twiddles(const float2* host) {
@@ -199,11 +280,32 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
   }
   p.prog = *prog;
   for (int q = 0; q < XL_MAX_OPS * 4; ++q) p.pgrad[q] = pgrad ? pgrad[q] : nullptr;
+  // which gradients need accumulation: scalar parameters (summed over all
+  // pixels) and per-pixel parameters shared by the batch (summed over it)
+  int scalar_acc = 0, plane_acc = 0;
+  for (int k = 0; k < prog->nops; ++k)
+    for (int q = 0; q < 4; ++q) {
+      if (!p.pgrad[k * 4 + q]) continue;
+      const XlOp& op = prog->ops[k];
+      if (!(op.pmask & (1 << q))) scalar_acc = 1;
+      else if (!op.pbstride) plane_acc = 1;
+    }
   const long long npix = (long long)ny * nx;
+  if (npix > 0x7fffffffLL) {
+    set_error("xl_ops_backward: plane too large");
+    return XL_EINVAL;
+  }
   int blocks = (int)((npix + 127) / 128);
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  if (prog->nops <= 4) ops_backward_kernel<4><<<blocks, 128, 0, (cudaStream_t)stream>>>(p);
-  else ops_backward_kernel<XL_MAX_OPS><<<blocks, 128, 0, (cudaStream_t)stream>>>(p);
+  // without batch sums, one thread per pixel and batch entry (grid.y = batch)
+  const int gy = (plane_acc || batch > 65535) ? 1 : batch;
+  const int cap = gy > 1 ? (152 * 16 + gy - 1) / gy : 152 * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  const size_t sm = (size_t)(scalar_acc + plane_acc) * XL_MAX_OPS * 4 * 128 * sizeof(float);
+  if (prog->nops <= 4)
+    ops_backward_kernel<4><<<dim3(blocks, gy), 128, sm, (cudaStream_t)stream>>>(p, scalar_acc, plane_acc);
+  else
+    ops_backward_kernel<XL_MAX_OPS><<<dim3(blocks, gy), 128, sm, (cudaStream_t)stream>>>(p, scalar_acc, plane_acc);
   XL_CHECK_LAUNCH("ops_backward_kernel");
   return XL_OK;
 }
@@ -257,5 +359,42 @@ extern "C" int xl_apply_ops(void* stream, int batch, int comps, int ny, int nx, 
   if (blocks > 152 * 8) blocks = 152 * 8;
   apply_ops_kernel<<<dim3(blocks, batch), 256, 0, (cudaStream_t)stream>>>(p);
   XL_CHECK_LAUNCH("apply_ops_kernel");
+  return XL_OK;
+}
+
+extern "C" size_t xl_mse_intensity_work_bytes(int planes, long long npix) {
+  if (planes < 1 || npix < 1) return 0;
+  return (size_t)planes * mse_blocks(npix) * sizeof(double);
+}
+
+extern "C" int xl_mse_intensity(void* stream, int planes, long long npix, const void* a, long long a_pstride,
+                                const void* b, long long b_pstride, void* work, void* out) {
+  if (planes < 1 || planes > 65535 || npix < 1 || !a || !b || !work || !out) {
+    set_error("xl_mse_intensity: bad arguments");
+    return XL_EINVAL;
+  }
+  const int nb = mse_blocks(npix);
+  cudaStream_t st = (cudaStream_t)stream;
+  mse_int_partial<<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
+                                                            b_pstride, npix, (double*)work);
+  XL_CHECK_LAUNCH("mse_int_partial");
+  mse_int_finish<<<(planes + 3) / 4, 128, 0, st>>>((const double*)work, nb, planes, 1.0 / (double)npix,
+                                                    (float*)out);
+  XL_CHECK_LAUNCH("mse_int_finish");
+  return XL_OK;
+}
+
+extern "C" int xl_mse_intensity_grad(void* stream, int planes, long long npix, const void* a, long long a_pstride,
+                                     const void* b, long long b_pstride, const void* gloss, void* ga, void* gb) {
+  if (planes < 1 || planes > 65535 || npix < 1 || !a || !b || !gloss || (!ga && !gb)) {
+    set_error("xl_mse_intensity_grad: bad arguments");
+    return XL_EINVAL;
+  }
+  long long nblk = (npix + 255) / 256;
+  if (nblk > 152 * 8) nblk = 152 * 8;
+  mse_int_grad<<<dim3((unsigned)nblk, planes), 256, 0, (cudaStream_t)stream>>>(
+      (const float2*)a, a_pstride, (const float2*)b, b_pstride, npix, (const float*)gloss,
+      (float)(4.0 / (double)npix), (float2*)ga, (float2*)gb);
+  XL_CHECK_LAUNCH("mse_int_grad");
   return XL_OK;
 }

@@ -721,3 +721,57 @@ class CztCall:
 def czt_propagate(comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None):
     """Scalar CZT, VCZT or the high-NA focus; returns 1 or 3 output tensors."""
     return CztCall(comps, x, y, wavelength, z, xout, yout, mode, pre, lens).run()
+
+
+# ------------------------------------------------------------------ losses --
+
+def _planes(t: torch.Tensor):
+    """(contiguous view, number of planes, plane stride) of a (..., ny, nx) complex64 tensor;
+    a single plane repeated by an expand-ed view keeps plane stride 0."""
+    ny, nx = t.shape[-2:]
+    if t.dim() == 3 and t.shape[0] > 1 and t.stride(0) == 0 and t[0].is_contiguous():
+        return t[0], t.shape[0], 0
+    t = t.contiguous()
+    n = t.numel() // (ny * nx)
+    return t, n, ny * nx
+
+
+def mse_intensity(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """sum((|a|^2 - |b|^2)^2) / npix over the last two dims (libxlgb, fixed-order sums)."""
+    a = as_field(a)
+    b = as_field(b)
+    ny, nx = a.shape[-2:]
+    if b.shape[-2:] != (ny, nx):
+        raise ValueError(f"input {tuple(a.shape)} and target {tuple(b.shape)} planes differ")
+    av, na, aps = _planes(a)
+    if b.shape[:-2] == a.shape[:-2]:
+        bv, nb, bps = _planes(b)
+    elif b.dim() == 2 or b.numel() == ny * nx:
+        bv, nb, bps = b.reshape(ny, nx).contiguous(), 1, 0
+    else:
+        raise ValueError(f"target of shape {tuple(b.shape)} does not broadcast over input {tuple(a.shape)}")
+    npix = ny * nx
+    L = lib()
+    work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(na, npix) // 8), dtype=torch.float64, device=a.device)
+    out = torch.empty(na, dtype=torch.float32, device=a.device)
+    _lib.check(L.xl_mse_intensity(stream_handle(), na, npix, av.data_ptr(), aps, bv.data_ptr(), bps,
+                                  work.data_ptr(), out.data_ptr()), "xl_mse_intensity")
+    return out.reshape(a.shape[:-2])
+
+
+def mse_intensity_grad(a, b, g, want_a=True, want_b=False):
+    """Gradients of ``mse_intensity`` for the upstream gradient ``g`` (shape a.shape[:-2])."""
+    a = as_field(a)
+    b = as_field(b)
+    ny, nx = a.shape[-2:]
+    av, na, aps = _planes(a)
+    if b.shape[:-2] == a.shape[:-2]:
+        bv, nb, bps = _planes(b)
+    else:
+        bv, bps = b.reshape(ny, nx).contiguous(), 0
+    g = g.to(device=a.device, dtype=torch.float32).reshape(-1).contiguous()
+    ga = torch.empty(a.shape, dtype=torch.complex64, device=a.device) if want_a else None
+    gb = torch.empty(a.shape, dtype=torch.complex64, device=a.device) if want_b else None
+    _lib.check(lib().xl_mse_intensity_grad(stream_handle(), na, ny * nx, av.data_ptr(), aps, bv.data_ptr(), bps,
+                                           g.data_ptr(), _ptr(ga), _ptr(gb)), "xl_mse_intensity_grad")
+    return ga, gb

@@ -18,6 +18,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from . import loss_functions as lf
 from . import optical_elements as oe
 from . import toolbox
 from .vectorized_optics import VectorizedLight
@@ -116,11 +117,12 @@ class HighNATable:
 class VrsLcdTable:
     """2048^2 VRS optimisation: per-field LCD retarder maps (eta, theta) in
     front of a linear polarizer shape a radially polarised source, which is
-    propagated by VRS to z; the loss is the intensity MSE (Ex, Ey and Ez
-    together) against per-field target intensities.  One step is a forward
-    through the fused kernels, the hand-written adjoints backward, and AdamW.
-    ``fields`` selects a subset of the batch (the plain form: one field per
-    call)."""
+    propagated by VRS to z; the loss is the reference's vectorial intensity
+    MSE (vMSE_Intensity, loss_functions.py:93-107: Ex, Ey and Ez each against
+    a target field), averaged.  One step is a forward through the fused
+    kernels, the hand-written adjoints backward (the fused loss gradient
+    first), and AdamW.  ``fields`` selects a subset of the batch (the plain
+    form: one field per call)."""
 
     def __init__(self, n=2048, batch=8, wavelength=0.633, half_width=2000.0, waist=1000.0, z=5e4,
                  seed=5000, device="cuda", capturable=False):
@@ -135,22 +137,23 @@ class VrsLcdTable:
                                    device=device).requires_grad_(True)
         self.theta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
                                      device=device).requires_grad_(True)
-        tgt = rng.uniform(0, 1, (batch, n, n)).astype(np.float32)
-        self.target = torch.as_tensor(tgt / tgt.sum(axis=(-2, -1), keepdims=True), device=device)
+        g = torch.Generator(device=device).manual_seed(seed)
+        self.target = [0.01 * torch.randn((batch, n, n), dtype=torch.complex64, device=device, generator=g)
+                       for _ in range(3)]
         self.alpha = float(rng.uniform(0, np.pi))
         self.opt = torch.optim.AdamW([self.eta, self.theta], lr=0.05, capturable=capturable)
 
     def loss(self, fields=None):
         sl = slice(None) if fields is None else fields
-        eta, theta, target = self.eta[sl], self.theta[sl], self.target[sl]
+        eta, theta = self.eta[sl], self.theta[sl]
         b = eta.shape[0]
         light = VectorizedLight(self.x, self.y, self.wavelength)
         light.Ex = self.Ex.expand(b, self.n, self.n)
         light.Ey = self.Ey.expand(b, self.n, self.n)
         out, _ = oe.linear_polarizer(oe.LCD(light, eta, theta), self.alpha).VRS_propagation(self.z)
-        I = torch.abs(out.Ex) ** 2 + torch.abs(out.Ey) ** 2 + torch.abs(out.Ez) ** 2
-        I = I / torch.sum(I, dim=(-2, -1), keepdim=True)
-        return torch.mean(torch.sum((I - target) ** 2, dim=(-2, -1)))
+        target = VectorizedLight(self.x, self.y, self.wavelength)
+        target.Ex, target.Ey, target.Ez = (t[sl] for t in self.target)
+        return torch.mean(lf.vMSE_Intensity(out, target))
 
     def step(self, fields=None):
         self.opt.zero_grad(set_to_none=True)
