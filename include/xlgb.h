@@ -181,8 +181,8 @@ typedef struct {
   double z, wavelength;
   double cte_re, cte_im; /* constant output factor */
   /* complex64 chirp data per axis (wave_optics.py:385-460, float64 on the host):
-   * pre[n] = A^-n h[m-1+n] (m values); g = fft(1/h[:m+M], L) in parity-split
-   * order (even entries, then odd); post[l] = h[m-1+l] e^{-i 2 pi l_f (1/2 - m/2)/Dm} / L */
+   * pre[n] = A^-n h[m-1+n] (m values); g = fft(1/h[:m+M], L) in natural
+   * order; post[l] = h[m-1+l] e^{-i 2 pi l_f (1/2 - m/2)/Dm} / L */
   const void* pre_x;
   const void* g_x;
   const void* post_x;

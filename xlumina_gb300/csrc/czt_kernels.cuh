@@ -1,0 +1,315 @@
+// Chirp-z (Bluestein) propagation for sm_103a: scalar CZT, vectorial VCZT and
+// the high-NA objective-lens focus, forward and adjoint; the kernels and their
+// launch code, included by the czt_l*.cu translation units.
+//
+// The reference (wave_optics.py:333-460) runs Bluestein's algorithm along y
+// and then along x, each as: multiply the input line by a pre-chirp,
+// zero-pad to L = next_pow2(m+M-1), FFT, multiply by the spectrum of the
+// inverse chirp, inverse FFT, keep entries [m, m+M) and multiply by a
+// post-chirp.  The 2-D transform is separable, so here the x transform runs
+// first over rows (czt_rows) and the y transform second over column tiles
+// (czt_cols).  A line is one L-point FFT pair by L/16 threads holding 16
+// elements each; when the input window lies in the first half of the line
+// (the forward transform: positions 0 .. m-1 <= L/2) the first pass is
+// pruned.
+//
+// czt_rows is persistent: each CTA stages its next rows (field planes and
+// per-pixel parameter planes) into shared memory with TMA bulk copies; the
+// prologue applies the Jones program (masks, high-NA lens), the VCZT
+// Ez = (Ex X/r + Ey Y/r) z/r and the input-plane transfer function F, and
+// writes the components to a shared buffer; then one thread group per
+// component transforms them.  czt_cols applies the output-plane transfer
+// function F0, the constant factor (z dx dy lambda, or -i sin^2(theta_max) /
+// (f lambda)) and, for the VCZT adjoint, the fold of the Ez gradient into
+// Ex, Ey.  The intermediate (after the x transform) is stored in column tiles
+// of 2^lw: element (row r, column l) at ((l >> lw) ny + r) 2^lw + (l mod 2^lw),
+// planes of ny x mxp (mx rounded up to the tile width).
+#pragma once
+
+#include <math.h>
+
+#include "czt_host.h"
+#include "line_fft.cuh"
+
+namespace xl {
+
+template <int LOGL> struct CztCfg {
+  static constexpr int L = 1 << LOGL;
+  static constexpr int E = 16;
+  static constexpr int H = E / 2;
+  static constexpr int T = L / E;                              // threads per line
+  static constexpr int XS = L + L / 16;                        // exchange slots per line
+  static constexpr int G = (256 / T) > 1 ? (256 / T) : 1;      // rows per group in the x transform
+  // y transform: W columns per CTA (one tile), interleaved in the lanes of every warp
+  static constexpr int W = LOGL >= 13 ? 2 : ((32 / T) > 4 ? (32 / T) : 4);
+  static constexpr int CXS = XS + (W >= 8 ? 0 : 16 / W);
+  static constexpr int COL_THREADS = W * T;
+  static constexpr int COL_MINB = (1024 / COL_THREADS) > 1 ? (1024 / COL_THREADS) : 1;
+  static constexpr int NTW = FftTw<LOGL, E>::SIZE;
+  static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024, "column CTA shape");
+};
+
+// x transform organisation for NC line components: CG component groups of G
+// rows of T threads; CG = NC (every component of a row at once) when the CTA
+// can hold them, else 1.
+template <int LOGL, int NC> struct CztRowCfg {
+  using C = CztCfg<LOGL>;
+  static constexpr int CG = (NC * C::G * C::T <= 1024) ? NC : 1;
+  static constexpr int ITER = (NC + CG - 1) / CG;              // transforms per group and row
+  static constexpr int LINES = CG * C::G;
+  static constexpr int THREADS = LINES * C::T;
+  static constexpr int MINB = (768 / THREADS) > 1 ? (768 / THREADS) : 1;
+};
+
+__device__ __forceinline__ long long tiled_rt(int r, int col, int rows, int lw) {
+  return ((((long long)(col >> lw)) * rows + r) << lw) + (col & ((1 << lw) - 1));
+}
+
+// x transform.  NC: components per row (1, or 3 for VCZT and the high-NA
+// focus; a plain transform of 2 components runs as 3 with the third idle).
+// ZU: the input window lies in the first half of the line.
+template <int LOGL, int NC, bool ZU>
+__global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, NC>::MINB)
+    czt_rows(const __grid_constant__ CztLaunch p, const __grid_constant__ RowStage st) {
+  using C = CztCfg<LOGL>;
+  using F = CztRowCfg<LOGL, NC>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = p.nx, ny = p.ny;
+  float2* xch = (float2*)smraw;                                    // LINES x XS
+  float2* post = xch + F::LINES * C::XS;                           // NC x G x nx
+  const size_t soff = ((size_t)(F::LINES * C::XS + NC * C::G * nx) * 8 + 15) / 16 * 16;
+  unsigned char* stage = smraw + soff;
+  unsigned long long* mbar = (unsigned long long*)(stage + (size_t)C::G * st.row_bytes);
+  const int tid = threadIdx.x;
+  const int line = tid / C::T, j = tid % C::T;
+  const int cg = line / C::G, gi = line % C::G;
+  const int ngb = (ny + C::G - 1) / C::G;
+  const int total = p.B * ngb;
+  const bool staged = st.n > 0;
+  const bool fwd_phase = p.mode != XL_CZT_PLAIN;
+  const bool vczt = p.mode == XL_CZT_VECTOR && !p.adjoint;
+  const float zf = (float)p.z;
+
+  if (tid == 0 && staged) {
+    mbar_init(mbar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0 && staged && blockIdx.x < total) {
+    const int b = blockIdx.x / ngb, r0 = (blockIdx.x - b * ngb) * C::G;
+    stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
+  }
+
+  unsigned phase = 0;
+  bool ok = true;
+  for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
+    const int b = grp / ngb;
+    const int r0 = (grp - b * ngb) * C::G;
+    if (staged) {
+      if (!mbar_wait_bounded(mbar, phase)) ok = false;
+      phase ^= 1u;
+    }
+    // prologue over the row group's pixels
+    for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
+      const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
+      if (r >= ny) break;
+      const long long pix = (long long)r * nx + n;
+      float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (c < p.cin) {
+          const int fo = st.fld[c];
+          e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+        }
+      }
+      if (p.pre.nops) {
+        PixelCtx px{r, n, pix, b};
+        apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
+      }
+      if (fwd_phase) {
+        if (vczt) {  // vectorized_optics.py:340-344
+          const float X = (float)p.x[n], Y = (float)p.y[r];
+          const float rr = sqrtf(X * X + Y * Y + zf * zf);
+          e[2] = cscale(cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr)), zf / rr);
+        }
+        // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
+        float2 Fv = rs_kernel_value(p.x[n], p.y[r], p.z, p.inv_lambda, p.k);
+        if (p.adjoint) Fv = cconj(Fv);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e[c] = cmul(e[c], Fv);
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
+    }
+    __syncthreads();   // every thread has read the stage and written its pixels
+    if (tid == 0 && staged && grp + gridDim.x < total) {
+      fence_proxy_async();
+      const int g = grp + gridDim.x, bn = g / ngb, rn = (g - bn * ngb) * C::G;
+      stage_rows(st, stage, mbar, bn, rn, min(C::G, ny - rn));
+    }
+    const int r = r0 + gi;
+    const bool live = r < ny;
+#pragma unroll 1
+    for (int it = 0; it < F::ITER; ++it) {
+      const int c = cg + it * F::CG;
+      const bool act = live && c < p.cout;
+      float2 v[16];
+      const float2* src = post + (c < NC ? c * C::G + gi : 0) * nx;
+      constexpr int MN = ZU ? C::H : 16;
+#pragma unroll
+      for (int m = 0; m < MN; ++m) {
+        const int i = j + m * C::T - p.ioff_x;
+        v[m] = (act && i >= 0 && i < nx) ? cmul(src[i], __ldg(p.pre_x + i)) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+      block_fft_x<LOGL, 16, -1, ZU, true>(v, j, xch + line * C::XS, pass_tw<LOGL>());
+      {
+        const float2* g = p.g_x;
+        asm volatile("" : "+l"(g));
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
+      }
+      block_fft_x<LOGL, 16, 1, false, true>(v, j, xch + line * C::XS, pass_tw<LOGL>());
+      if (act) {
+        float2* plane = p.work + ((long long)b * p.cout + c) * ny * p.mxp;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          const int o = j + m * C::T - p.ooff_x;
+          if (o >= 0 && o < p.mx) plane[tiled_rt(r, o, ny, p.lw)] = cmul(v[m], __ldg(p.post_x + o));
+        }
+      }
+    }
+  }
+  if (!ok && tid == 0) {
+    atomicAdd(&g_line_timeouts, 1u);
+    mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
+  }
+}
+
+// y transform over tiles of W columns, with the epilogue.  Lanes interleave
+// the W columns of a tile, so every warp load of the intermediate is one
+// contiguous run.
+template <int LOGL, bool ZU>
+__global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_MINB)
+    czt_cols(const __grid_constant__ CztLaunch p) {
+  using C = CztCfg<LOGL>;
+  constexpr int W = C::W, LPW = 32 / W;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* xch = smem;                  // W x CXS
+  float2* stw = smem + W * C::CXS;     // NTW
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
+  const int t = blockIdx.x, b = blockIdx.y;
+  const int col = t * W + w;
+  const bool live = col < p.mx;
+  const int ny = p.ny;
+  {
+    const float2* g = pass_tw<LOGL>();
+    for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
+  }
+  __syncthreads();
+  float2* xb = xch + w * C::CXS;
+  const bool fold = p.adjoint && p.mode == XL_CZT_VECTOR;
+  const float zf = (float)p.z;
+#pragma unroll 1
+  for (int c = 0; c < p.cout; ++c) {
+    const float2* tileT = p.work + ((long long)b * p.cout + c) * ny * p.mxp + (long long)t * ny * W + w;
+    float2 v[16];
+    constexpr int MN = ZU ? C::H : 16;
+#pragma unroll
+    for (int m = 0; m < MN; ++m) {
+      const int n = j + m * C::T - p.ioff_y;
+      v[m] = (live && n >= 0 && n < ny) ? cmul(tileT[(long long)n * W], __ldg(p.pre_y + n)) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+    block_fft_x<LOGL, 16, -1, ZU, false>(v, j, xb, stw);
+    {
+      const float2* g = p.g_y;
+      asm volatile("" : "+l"(g));
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
+    }
+    block_fft_x<LOGL, 16, 1, false, false>(v, j, xb, stw);
+    if (!live) continue;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int o = j + m * C::T - p.ooff_y;
+      if (o < 0 || o >= p.my) continue;
+      float2 val = cmul(v[m], __ldg(p.post_y + o));
+      if (p.mode != XL_CZT_PLAIN) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
+        const float2 Fv = rs_kernel_value(p.xo[col], p.yo[o], p.z, p.inv_lambda, p.k);
+        val = p.adjoint ? cmulc(val, Fv) : cmul(val, Fv);
+      }
+      val = cmul(val, p.cte);
+      const long long pix = (long long)b * p.obs + (long long)o * p.mx + col;
+      if (fold && c == 2) {  // adjoint of Ez = (Ex X/r + Ey Y/r) z/r, vectorized_optics.py:341-344
+        const float X = (float)p.xo[col], Y = (float)p.yo[o];
+        const float r2 = X * X + Y * Y + zf * zf;
+        p.out[0][pix] = cadd(p.out[0][pix], cscale(val, X * zf / r2));
+        p.out[1][pix] = cadd(p.out[1][pix], cscale(val, Y * zf / r2));
+      } else {
+        p.out[c][pix] = val;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch code.
+
+template <int LOGL, int NC, bool ZU>
+static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
+  using C = CztCfg<LOGL>;
+  using F = CztRowCfg<LOGL, NC>;
+  const size_t fixed = ((size_t)(F::LINES * C::XS + NC * C::G * p.nx) * 8 + 15) / 16 * 16;
+  RowStage st;
+  plan_row_stage(p.cin, p.in, p.ibs, p.nx, p.pre, C::G, fixed, st);
+  const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;
+  if (sm > 227 * 1024) {
+    set_error("czt: input row of %d columns too long for shared memory", p.nx);
+    return XL_EUNSUPPORTED;
+  }
+  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "czt_rows smem");
+  const int total = p.B * ((p.ny + C::G - 1) / C::G);
+  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU>, F::THREADS, sm, total);
+  czt_rows<LOGL, NC, ZU><<<grid, F::THREADS, sm, s>>>(p, st);
+  XL_CHECK_LAUNCH("czt_rows");
+  return XL_OK;
+}
+
+template <int LOGL>
+int czt_rows_launch(cudaStream_t s, const CztLaunch& p) {
+  const bool zu = p.ioff_x >= 0 && p.ioff_x + p.nx <= (1 << LOGL) / 2;
+  if (p.cout == 1) return zu ? launch_czt_rows<LOGL, 1, true>(s, p) : launch_czt_rows<LOGL, 1, false>(s, p);
+  return zu ? launch_czt_rows<LOGL, 3, true>(s, p) : launch_czt_rows<LOGL, 3, false>(s, p);
+}
+
+template <int LOGL, bool ZU>
+static int launch_czt_cols(cudaStream_t s, const CztLaunch& p) {
+  using C = CztCfg<LOGL>;
+  const size_t sm = (size_t)(C::W * C::CXS + C::NTW) * sizeof(float2);
+  cudaError_t e = allow_smem(czt_cols<LOGL, ZU>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "czt_cols smem");
+  czt_cols<LOGL, ZU><<<dim3((p.mx + C::W - 1) / C::W, p.B), C::COL_THREADS, sm, s>>>(p);
+  XL_CHECK_LAUNCH("czt_cols");
+  return XL_OK;
+}
+
+template <int LOGL>
+int czt_cols_launch(cudaStream_t s, const CztLaunch& p) {
+  if ((1 << p.lw) != CztCfg<LOGL>::W) {
+    set_error("czt: intermediate tile width does not match the y transform");
+    return XL_EINVAL;
+  }
+  const bool zu = p.ioff_y >= 0 && p.ioff_y + p.ny <= (1 << LOGL) / 2;
+  return zu ? launch_czt_cols<LOGL, true>(s, p) : launch_czt_cols<LOGL, false>(s, p);
+}
+
+}  // namespace xl
+
+#define XL_CZT_INSTANTIATE(L)                                                 \
+  template int xl::czt_rows_launch<L>(cudaStream_t, const xl::CztLaunch&);    \
+  template int xl::czt_cols_launch<L>(cudaStream_t, const xl::CztLaunch&);

@@ -35,7 +35,7 @@
 #include <type_traits>
 #include <vector>
 
-#include "common.cuh"
+#include "line_fft.cuh"
 #include "rs_host.h"
 
 namespace xl {
@@ -72,39 +72,6 @@ template <int LOGQ> struct RsCfg {
   static_assert(COL_THREADS >= 32 && COL_THREADS <= 1024, "column CTA shape");
   static_assert(W % CW == 0, "column-pass CTAs cover whole tiles");
 };
-
-// Pass twiddle tables (FftTw layout, 16 elements per thread) for every
-// P = 2^5 .. 2^13, one after the other, filled at set-up from float64 values.
-__host__ __device__ constexpr int ptw_size(int logp) {
-  // sum over passes 1.. of (radix - 1) * stride, radix 16 then the remainder
-  int nfull = logp / 4, rem = logp % 4, npass = nfull + (rem ? 1 : 0), o = 0, ns = 1;
-  for (int q = 0; q < npass; ++q) {
-    const int r = q < nfull ? 16 : (1 << rem);
-    if (q >= 1) o += (r - 1) * ns;
-    ns *= r;
-  }
-  return o > 0 ? o : 1;
-}
-__host__ __device__ constexpr int ptw_off(int logp) {
-  int o = 0;
-  for (int l = 5; l < logp; ++l) o += ptw_size(l);
-  return o;
-}
-constexpr int PTW_TOTAL = ptw_off(14);
-
-// Each translation unit holds its own copy (filled by its registered upload).
-static __device__ float2 g_ptw[PTW_TOTAL];
-
-template <int LOGP> __device__ __forceinline__ const float2* pass_tw() {
-  static_assert(ptw_size(LOGP) == FftTw<LOGP, 16>::SIZE, "pass table size");
-  return g_ptw + ptw_off(LOGP);
-}
-
-// Address of (row r, column col) in a column-tiled plane with `rows` rows.
-template <int W>
-__device__ __forceinline__ long long tiled(int r, int col, int rows) {
-  return ((long long)(col / W) * rows + r) * W + (col % W);
-}
 
 // Element addresses of one row (columns j + m T) in a column-tiled plane.
 // The base pointer and stride pass through empty asm statements so that the
@@ -172,42 +139,6 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS)
   for (int m = 0; m < 16; ++m) dst[(long long)(j + m * C::T) * C::SW] = cscale(v[m], scale);
 }
 
-// ---------------------------------------------------------------------------
-// Rows of the forward row pass staged into shared memory by TMA bulk copies:
-// up to XL_RS_STREAMS planes (input components and per-pixel parameter
-// planes of the fused program), each copied G rows at a time.
-#define XL_RS_STREAMS 8
-struct RsStream {
-  const char* src;      // row 0 of batch entry 0
-  long long bstride;    // bytes between batch entries (0: shared by the batch)
-  int row_bytes;        // bytes of one row (the plane's row stride), a multiple of 16
-  int soff;             // byte offset of the stream's G rows in the stage
-};
-struct RsStage {
-  int n;                       // staged streams
-  int row_bytes;               // sum of the streams' row bytes
-  RsStream s[XL_RS_STREAMS];
-  int fld[3];                  // stage offset of input component c, -1: read from global memory
-  int prm[XL_MAX_OPS][4];      // stage offset of parameter plane i of op k, -1: global memory
-};
-
-// Per-pixel parameters of the fused program, from the stage when the plane is
-// staged, else from global memory.
-struct StagedParams {
-  const unsigned char* stage;
-  const RsStage* st;
-  int gi, nx, n;
-  __device__ __forceinline__ float operator()(const XlOp& op, int k, int i, const PixelCtx& px) const {
-    if (!(op.pmask & (1 << i))) return op.sval[i];
-    const int off = st->prm[k][i];
-    if (off >= 0) return ((const float*)(stage + off))[gi * nx + n];
-    return __ldg((const float*)op.ptr[i] + (long long)px.batch * op.pbstride + px.pix);
-  }
-};
-
-// Bounded waits that ran out, counted per translation unit (read by xl_device_timeouts).
-static __device__ unsigned int g_rs_timeouts;
-
 // Thread organisation of the row passes for NC transformed components: CG
 // component groups of G lines of T threads, where CG = NC (every component of
 // a row transformed at once) when the CTA can hold them, else 1 (the
@@ -228,7 +159,7 @@ template <int LOGQ, int NC> struct RowCfg {
 // row group start while the component groups transform this one.
 template <int LOGQ, int MODE>
 __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowCfg<LOGQ, MODE == 1 ? 1 : 3>::MINB)
-    rs_rows_fwd(const __grid_constant__ RsLaunch p, const __grid_constant__ RsStage st) {
+    rs_rows_fwd(const __grid_constant__ RsLaunch p, const __grid_constant__ RowStage st) {
   using C = RsCfg<LOGQ>;
   constexpr int NC = MODE == 1 ? 1 : 3;
   constexpr int CIN = MODE;
@@ -259,13 +190,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 
   auto issue = [&](int grp) {
     const int b = grp / ngb, r0 = (grp - b * ngb) * C::G;
-    const int rows = min(C::G, ny - r0);
-    mbar_arrive_expect_tx(mbar, (unsigned)(rows * st.row_bytes));
-    for (int s = 0; s < st.n; ++s) {
-      const RsStream& q = st.s[s];
-      bulk_copy_g2s(stage + q.soff, q.src + (long long)b * q.bstride + (long long)r0 * q.row_bytes,
-                    (unsigned)(rows * q.row_bytes), mbar);
-    }
+    stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
   };
   if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
 
@@ -344,7 +269,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   }
   if (!ok) {
     if (tid == 0) {
-      atomicAdd(&g_rs_timeouts, 1u);
+      atomicAdd(&g_line_timeouts, 1u);
       mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
     }
   }
@@ -520,30 +445,6 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
 // ---------------------------------------------------------------------------
 // Host side.
 
-// SM count of the current device (cached per device).
-static int device_sms() {
-  static int sms[256];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return 132;
-  if (!sms[dev]) {
-    int v = 0;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
-    sms[dev] = v;
-  }
-  return sms[dev];
-}
-
-// Grid of a persistent kernel: every resident CTA slot, at most `work` CTAs.
-template <typename K>
-static int persistent_grid(K kernel, int threads, size_t smem, int work) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
-  const long long g = (long long)per_sm * device_sms();
-  return (int)(g < work ? g : work);
-}
-
 template <int LOGQ>
 int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy, double z,
                 double wavelength, double scale, float2* spec, float2* work) {
@@ -563,41 +464,6 @@ int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const doubl
   return XL_OK;
 }
 
-// Which planes the forward row pass stages by TMA: every input component and
-// every per-pixel parameter plane of the fused program whose rows are 16-byte
-// aligned, while the stage fits next to the exchange buffers.
-template <int LOGQ>
-static void plan_stage(const RsLaunch& p, size_t fixed_smem, RsStage& st) {
-  using C = RsCfg<LOGQ>;
-  const size_t cap = 226 * 1024;   // the CTA's shared memory, barrier included
-  st.n = 0;
-  st.row_bytes = 0;
-  for (int c = 0; c < 3; ++c) st.fld[c] = -1;
-  for (int k = 0; k < XL_MAX_OPS; ++k)
-    for (int i = 0; i < 4; ++i) st.prm[k][i] = -1;
-  int off = 0;
-  auto add = [&](const void* src, long long bstride_bytes, int row_bytes) -> int {
-    if (st.n >= XL_RS_STREAMS || !src) return -1;
-    if (((uintptr_t)src % 16) || (bstride_bytes % 16) || (row_bytes % 16)) return -1;
-    if (fixed_smem + (size_t)off + (size_t)C::G * row_bytes + 16 > cap) return -1;
-    RsStream& q = st.s[st.n++];
-    q.src = (const char*)src;
-    q.bstride = bstride_bytes;
-    q.row_bytes = row_bytes;
-    q.soff = off;
-    const int o = off;
-    off += C::G * row_bytes;
-    st.row_bytes += row_bytes;
-    return o;
-  };
-  for (int c = 0; c < p.cin && c < 3; ++c) st.fld[c] = add(p.in[c], p.ibs * 8, p.nx * 8);
-  for (int k = 0; k < p.pre.nops; ++k) {
-    const XlOp& op = p.pre.ops[k];
-    for (int i = 0; i < 4; ++i)
-      if (op.pmask & (1 << i)) st.prm[k][i] = add(op.ptr[i], op.pbstride * 4, p.nx * 4);
-  }
-}
-
 template <int LOGQ, int MODE>
 static int launch_rows_fwd(cudaStream_t s, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
@@ -605,8 +471,8 @@ static int launch_rows_fwd(cudaStream_t s, const RsLaunch& p) {
   using F = RowCfg<LOGQ, NC>;
   const size_t fixed = ((size_t)(F::LINES * C::XS + NC * C::G * p.nx) * 8 + (MODE == 2 ? (size_t)p.nx * 4 : 0) +
                         15) / 16 * 16;
-  RsStage st;
-  plan_stage<LOGQ>(p, fixed, st);
+  RowStage st;
+  plan_row_stage(p.cin, p.in, p.ibs, p.nx, p.pre, C::G, fixed, st);
   const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;
   if (sm > 227 * 1024) {
     set_error("rs: row of %d columns too long for shared memory", p.nx);
@@ -667,31 +533,6 @@ int rs_propagate(cudaStream_t st, const RsLaunch& p, int stage) {
     if (int rc = launch_stage<LOGQ>(st, p, s)) return rc;
   return XL_OK;
 }
-
-template <int LOGP>
-static void fill_pass_tables(std::vector<float2>& out, const float2* host) {
-  const float2* twN = host + (1 << LOGP);
-  for (int i = 0; i < FftTw<LOGP, 16>::SIZE; ++i) out[ptw_off(LOGP) + i] = pass_twiddle_entry<LOGP, 16>(i, twN);
-  if constexpr (LOGP < 13) fill_pass_tables<LOGP + 1>(out, host);
-}
-
-// Device tables of this translation unit: the twiddle tables and the pass tables.
-static cudaError_t rs_tu_tables(const float2* host) {
-  cudaError_t e = cudaMemcpyToSymbol(g_tw, host, sizeof(g_tw));
-  if (e != cudaSuccess) return e;
-  std::vector<float2> ptw(PTW_TOTAL, make_float2(1.f, 0.f));
-  fill_pass_tables<5>(ptw, host);
-  return cudaMemcpyToSymbol(g_ptw, ptw.data(), sizeof(g_ptw));
-}
-
-static cudaError_t rs_tu_timeouts(unsigned int* count, int reset) {
-  cudaError_t e = cudaMemcpyFromSymbol(count, g_rs_timeouts, sizeof(unsigned int));
-  if (e != cudaSuccess || !reset) return e;
-  const unsigned int zero = 0;
-  return cudaMemcpyToSymbol(g_rs_timeouts, &zero, sizeof(unsigned int));
-}
-
-static const bool rs_tu_registered = register_device_tables(&rs_tu_tables, &rs_tu_timeouts);
 
 }  // namespace xl
 

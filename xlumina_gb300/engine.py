@@ -599,8 +599,8 @@ def czt_grid(z, wavelength, xin, yin, xout, yout):
 def bluestein_plan(m, f1, f2, Dm, M):
     """Chirp data of wave_optics.py:385-460 for an m-point input and M outputs, float64.
 
-    Returns (L, pre, g_split, post): L the transform length; pre[n] = A^-n
-    h[m-1+n]; g = fft(1/h[:m+M], L) reordered even entries then odd entries;
+    Returns (L, pre, g, post): L the transform length; pre[n] = A^-n
+    h[m-1+n]; g = fft(1/h[:m+M], L) in natural order;
     post[l] = h[m-1+l] exp(-i 2 pi l_f (1/2 - m/2) / Dm) / L, where
     h[q] = W^((q-m+1)^2/2) with the complex power's principal branch.
     """
@@ -622,7 +622,7 @@ def bluestein_plan(m, f1, f2, Dm, M):
     pre = A ** (-np.arange(m)) * h[m - 1:2 * m - 1]
     lf = np.linspace(0, M - 1, M) / M * (D2 - D1) + D1
     post = h[m - 1:mp] * np.exp(-1j * 2 * np.pi * lf * (-m / 2 + 0.5) / Dm) / Lk
-    return Lk, pre, np.concatenate([g[0::2], g[1::2]]), post
+    return Lk, pre, g, post
 
 
 _chirp_cache: "collections.OrderedDict" = collections.OrderedDict()
