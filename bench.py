@@ -346,6 +346,8 @@ def run_gpu(args):
     if not args.no_fwd_bwd:
         del call, Ex_d, Ey_d, eta_d, theta_d, hosts
         torch.cuda.empty_cache()
+        line["czt_high_na"] = run_czt()
+        torch.cuda.empty_cache()
         line["fwd_bwd"] = run_fwd_bwd()
     if not args.no_serving:
         line["uneven_batch"] = run_uneven()
@@ -353,6 +355,56 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
     print(json.dumps(line))
+
+
+def run_czt(batch=8, steps=20, warmup=3):
+    """The high-NA objective-lens focus (VCZT_objective_lens, optical_elements.py:600-638):
+    2048^2 (Ex, Ey) behind a per-pixel LCD and sSLM -> lens -> 1024^2 focal ROI
+    (Ex, Ey, Ez), forward, `batch` fields per launch; per-kernel times from
+    CUDA events on the launching stream."""
+    import torch
+
+    from xlumina_gb300 import engine, toolbox
+    n, m = 2048, 1024
+    x, y = toolbox.space(2700.0, n)
+    xo, yo = toolbox.space(1.0, m)
+    f, r = 3000.0, 2700.0
+    rng = np.random.default_rng(7000)
+    X, Y = np.meshgrid(x, y)
+    src = np.exp(-(X ** 2 + Y ** 2) / 1500.0 ** 2).astype(np.complex64)
+    ex = torch.as_tensor(src, device="cuda").expand(batch, n, n)
+    ey = torch.zeros((n, n), dtype=torch.complex64, device="cuda").expand(batch, n, n)
+    eta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32), device="cuda")
+    theta = torch.as_tensor(rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32), device="cuda")
+    alpha = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32), device="cuda")
+    phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32), device="cuda")
+    lens_op, s_max = engine.op_high_na(x, y, r, f)
+    pre = [engine.op_lcd(eta, theta), engine.op_sslm(alpha, phi), lens_op]
+    call = engine.CztCall([ex, ey], x, y, 0.650, 0.0, xo, yo, "high_na", pre=pre, lens=(r, f, s_max))
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        call.stage(0)
+        call.stage(1)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * steps)]
+    for k in range(steps):
+        ev[3 * k].record(stream)
+        call.stage(0)
+        ev[3 * k + 1].record(stream)
+        call.stage(1)
+        ev[3 * k + 2].record(stream)
+    torch.cuda.synchronize()
+    rows = sum(ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(steps)) / steps
+    cols = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(steps)) / steps
+    # algorithmic bytes per field: rows read Ex, Ey 16 n^2 (shared by the batch), the sSLM
+    # planes 8 n^2 (per field), LCD planes 8 n^2 and lens coefficients 24 n^2 (shared), and
+    # write 3 n m complex64; columns read 3 n m and write 3 m^2
+    rows_b = 8 * n * n + 3 * n * m * 8 + (16 + 8 + 24) * n * n / batch
+    cols_b = 3 * n * m * 8 + 3 * m * m * 8
+    return {"workload": "high-NA focus 2048^2 -> 1024^2 ROI (2 um), LCD + sSLM + lens fused, Ez derived, forward",
+            "batch": batch, "fields_per_s": batch / ((rows + cols) / 1e3),
+            "czt_rows_ms": rows, "czt_cols_ms": cols,
+            "czt_rows_gbs": batch * rows_b / (rows / 1e3) / 1e9, "czt_cols_gbs": batch * cols_b / (cols / 1e3) / 1e9}
 
 
 def _time_steps(fn, steps, warmup):
@@ -580,7 +632,12 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--only", choices=["czt"], default=None,
+                    help="run one section alone (for profiling): czt = the high-NA focus")
     args = ap.parse_args()
+    if args.only == "czt":
+        print(json.dumps({"czt_high_na": run_czt(batch=args.batch, steps=args.steps, warmup=args.warmup)}))
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
       block_fft_x<LOGL, 16, -1, ZU, true>(v, j, xch + line * C::XS, pass_tw<LOGL>());
       {
         const float2* g = p.g_x;
-        asm volatile("" : "+l"(g));
+        asm volatile("" : "+l"(g) : : "memory");
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
       }
