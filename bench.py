@@ -138,7 +138,7 @@ class ClockSampler:
 # DRAM bytes (read + write) per 2048^2 VRS field of each pass, from the ncu
 # capture summarised in profiles/rs_kernels_vrs2048.md (batch 2, scaled per
 # field; every field is an independent slice of the launch).
-NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 275.96e6, "rs_cols_conv": 520.34e6, "rs_rows_inv": 283.98e6}
+NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 275.75e6, "rs_cols_conv": 521.35e6, "rs_rows_inv": 283.74e6}
 
 
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
