@@ -85,6 +85,13 @@ int xl_init(void);
 
 /* ---- Rayleigh-Sommerfeld (RS / VRS) ----------------------------------- */
 
+/* The spectrum of dH/dz, the z-derivative of the same impulse response
+ * (same arguments and layout as xl_rs_transfer_spectrum).  Propagating with
+ * it gives d(output)/dz, the gradient with respect to a distance that jax.grad
+ * takes through RS_propagation_jit (z is traced there, wave_optics.py:281-297). */
+int xl_rs_transfer_spectrum_dz(void* stream, int ny, int nx, const double* offx, const double* offy,
+                               double z, double wavelength, double scale, void* spectrum, void* work);
+
 /* Bytes of one transfer spectrum for an ny x nx field: (2Q)^2 complex64,
  * Q = next power of two >= max(ny, nx). */
 size_t xl_rs_spectrum_bytes(int ny, int nx);
@@ -122,8 +129,9 @@ typedef struct {
   int adjoint;                 /* 1: adjoint propagation (conjugate spectrum).  Scalar: 1 -> 1.
                                   VRS: comps_in = comps_out = 3 gradients (Ex, Ey, Ez) in; the Ez
                                   gradient is folded back into Ex, Ey with the weights X/r, Y/r of
-                                  the forward Ez derivation; outputs out[0], out[1].  pre/post must
-                                  be empty. */
+                                  the forward Ez derivation; outputs out[0], out[1], and out[2]
+                                  (optional) the propagated Ez gradient before the fold.  pre/post
+                                  must be empty. */
   const void* const* spectra;  /* optional device array of `batch` spectrum pointers, one per batch
                                   entry (entries of different distances need no stacked copy);
                                   when set it replaces spectrum / spectrum_stride / spectrum_index */
@@ -233,6 +241,21 @@ int xl_highna_coefficients(void* stream, int ny, int nx, const double* x, const 
 int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const void* const* in,
                     long long in_bstride, const void* const* gout, long long gout_bstride,
                     void* const* gin, long long gin_bstride, const XlProg* prog, void* const* pgrad);
+
+/* ---- Reductions for gradients -------------------------------------------- */
+
+/* out[p] = sum_i Re(conj(a_i) b_i) over planes p of npix complex64 pixels, in
+ * a fixed order (work: xl_mse_intensity_work_bytes(planes, npix)). */
+int xl_re_inner(void* stream, int planes, long long npix, const void* a, long long a_pstride, const void* b,
+                long long b_pstride, void* work, void* out);
+
+/* The distance gradient through the VRS Ez derivation (vectorized_optics.py:258-261):
+ * out[b] = sum_i Re(conj(gez_i) dEz_i/dz), dEz/dz = -(Ex X + Ey Y) z / r^3, for
+ * the Jones-program output (ex, ey) and the propagated Ez gradient gez of each
+ * batch entry; x, y, z (one per entry) are device float64.  work as above. */
+int xl_vrs_dz_ez(void* stream, int batch, int ny, int nx, const void* ex, const void* ey, long long e_bstride,
+                 const void* gez, long long g_bstride, const double* x, const double* y, const double* z,
+                 void* work, void* out);
 
 /* ---- Losses ------------------------------------------------------------ */
 

@@ -71,6 +71,16 @@ SIGNATURES = {
     "xl_rs_transfer_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_rs_transfer_spectrum_dz": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_re_inner": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
+                                   ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                   ctypes.c_void_p]),
+    "xl_vrs_dz_ez": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]),
     "xl_rs_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_rs_propagate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
     "xl_rs_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs), ctypes.c_int]),

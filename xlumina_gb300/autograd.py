@@ -11,8 +11,15 @@ fused forward kernels (Jones program + propagator), and whose backward runs:
 
 This replaces ``jax.grad`` through RS_propagation_jit / CZT_jit and the masks
 (e.g. experiments/four_f_optimizer.py:43, experiments/hybrid_optimizer.py:60).
-Gradients follow torch's convention for complex tensors.  Distances z,
-wavelengths and lens geometry are not differentiable here.
+Gradients follow torch's convention for complex tensors.
+
+An RS / VRS distance given as a tensor that requires grad is differentiable
+too (jax traces z through RS_propagation_jit, wave_optics.py:281-297):
+dL/dz = sum Re(conj(g) dout/dz), with dout/dz one more propagation of the
+Jones program's output through the spectrum of dH/dz, plus, for VRS, the
+term of the input-plane Ez's own z-dependence (vectorized_optics.py:258-261)
+reduced against the adjoint's unfolded Ez gradient.  Wavelengths, chirp-z
+distances and lens geometry are not differentiable here.
 """
 from __future__ import annotations
 
@@ -31,10 +38,12 @@ def _trainable(ops):
     return out
 
 
-def needs_grad(base, ops) -> bool:
+def needs_grad(base, ops, z=None) -> bool:
     if not torch.is_grad_enabled():
         return False
     if any(isinstance(b, torch.Tensor) and b.requires_grad for b in base):
+        return True
+    if isinstance(z, torch.Tensor) and z.requires_grad:
         return True
     return bool(_trainable(ops))
 
@@ -43,7 +52,8 @@ class RsPlan:
     """RS (one component) or VRS ((Ex, Ey) -> (Ex, Ey, Ez)) with a fused Jones prologue."""
 
     def __init__(self, x, y, wavelength, z, vector, ops):
-        self.x, self.y, self.wavelength, self.z, self.vector = x, y, wavelength, z, vector
+        self.z, self.z_tensor = engine.z_values(z)
+        self.x, self.y, self.wavelength, self.vector = x, y, wavelength, vector
         self.ops = list(ops or ())
         self.ny, self.nx = len(y), len(x)
 
@@ -51,9 +61,28 @@ class RsPlan:
         return engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector,
                              pre=self.ops).run()
 
-    def adjoint(self, grads):
+    def adjoint(self, grads, want_ez=False):
         return engine.RsCall(list(grads), self.x, self.y, self.wavelength, self.z, self.vector,
-                             adjoint=True).run()
+                             adjoint=True, want_ez=want_ez).run()
+
+    def z_grad(self, base, gouts, gez):
+        """dL/dz for output gradients ``gouts``; ``gez``: the adjoint's unfolded
+        Ez gradient (VRS).  Shaped like the distance tensor (summed over the
+        batch for one distance)."""
+        douts = engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector, pre=self.ops,
+                              dz=True).run()
+        acc = engine.re_inner(gouts[0], douts[0])
+        for g, d in zip(gouts[1:], douts[1:]):
+            acc = acc + engine.re_inner(g, d)
+        if self.vector:
+            e = engine.apply_ops(list(base), self.ops, self.ny, self.nx) if self.ops else list(base)
+            acc = acc + engine.vrs_dz_ez(e[0], e[1], gez, self.x, self.y, self.z).reshape(acc.shape)
+        zt = self.z_tensor
+        if zt.numel() == 1:
+            return acc.sum().reshape(zt.shape).to(device=zt.device, dtype=zt.dtype)
+        if acc.numel() != zt.numel():
+            raise ValueError(f"{zt.numel()} distances for a batch of {acc.numel()} fields")
+        return acc.reshape(zt.shape).to(device=zt.device, dtype=zt.dtype)
 
 
 class CztPlan:
@@ -78,6 +107,11 @@ class CztPlan:
                               self.mode, lens=self.lens, adjoint=True).run()
 
 
+def _z_tensor(plan):
+    zt = getattr(plan, "z_tensor", None)
+    return zt if (zt is not None and zt.requires_grad) else None
+
+
 class _Fused(torch.autograd.Function):
     @staticmethod
     def forward(ctx, plan, n_base, n_out, *tensors):
@@ -95,7 +129,13 @@ class _Fused(torch.autograd.Function):
         ref = next((g for g in gouts if g is not None), None)
         gouts = [g if g is not None else torch.zeros_like(ref) for g in gouts]
         gouts = [g.to(torch.complex64).contiguous() for g in gouts]
-        gprog = plan.adjoint(gouts)           # gradient of the Jones program's output
+        want_z = _z_tensor(plan) is not None and ctx.needs_input_grad[-1]
+        gez = None
+        if want_z and plan.vector:
+            gprog = plan.adjoint(gouts, want_ez=True)
+            gprog, gez = gprog[:2], gprog[2]
+        else:
+            gprog = plan.adjoint(gouts)           # gradient of the Jones program's output
         trainable = _trainable(plan.ops)
         if plan.ops:
             nb = len(gprog)
@@ -108,13 +148,18 @@ class _Fused(torch.autograd.Function):
         for i, t in enumerate(base):
             gbase.append(gin[i] if (t.requires_grad and i < len(gin)) else None)
         gparams = [pgrads.get((k, q)) for (k, q, _) in trainable]
-        return (None, None, None, *gbase, *gparams)
+        if _z_tensor(plan) is None:
+            return (None, None, None, *gbase, *gparams)
+        gz = plan.z_grad(base, gouts, gez) if want_z else None
+        return (None, None, None, *gbase, *gparams, gz)
 
 
 def fused_propagate(plan, base, n_out):
     """Run ``plan`` through autograd; ``base`` are the input planes."""
     params = [p for (_, _, p) in _trainable(plan.ops)]
-    return list(_Fused.apply(plan, len(base), n_out, *base, *params))
+    zt = _z_tensor(plan)
+    extra = [zt] if zt is not None else []
+    return list(_Fused.apply(plan, len(base), n_out, *base, *params, *extra))
 
 
 class _Ops(torch.autograd.Function):

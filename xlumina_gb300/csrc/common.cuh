@@ -46,6 +46,27 @@ __device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, 
 // absolute error per pixel shows up there above the 1e-5 parity bar.
 __device__ __forceinline__ void phase_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
 
+// Derivative of the impulse response with respect to z, dH/dz, from
+// H = e^{i s k r} a(r, z), a = z (1/r - i k) / (2 pi r^2), s = sign(z), dr/dz = z/r:
+// dH/dz = e^{i s k r} (i s k (z/r) a + da/dz),
+// da/dz = ((1/r^3 - i k / r^2) + z^2 (-3/r^5 + 2 i k / r^4)) / (2 pi).
+__device__ __forceinline__ float2 rs_kernel_dz_value(double X, double Y, double z, double inv_lambda,
+                                                     float k) {
+  const double r = sqrt(X * X + Y * Y + z * z);
+  const double t = r * inv_lambda;
+  const float2 e = cis_turns(z > 0 ? t : -t);
+  const float rf = (float)r, zf = (float)z, s = z > 0 ? 1.f : -1.f;
+  const float ir = 1.f / rf, ir2 = ir * ir, ir3 = ir2 * ir;
+  const float inv2pi = 0.15915494309189533577f;
+  const float2 a = make_float2(zf * ir3 * inv2pi, -zf * k * ir2 * inv2pi);
+  const float z2 = zf * zf;
+  const float2 da = make_float2((ir3 - 3.f * z2 * ir3 * ir2) * inv2pi, (-k * ir2 + 2.f * k * z2 * ir2 * ir2) * inv2pi);
+  // i s k (z / r) a
+  const float w = s * k * zf * ir;
+  const float2 ia = make_float2(-w * a.y, w * a.x);
+  return cmul(e, cadd(ia, da));
+}
+
 // ---- fused per-pixel Jones program ----
 
 struct PixelCtx;

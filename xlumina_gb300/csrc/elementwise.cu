@@ -182,9 +182,12 @@ __global__ void highna_plane_kernel(int ny, int nx, XlOp op, float* out) {
 // so the result does not depend on scheduling.
 constexpr int MSE_THREADS = 256;
 
-__global__ void __launch_bounds__(MSE_THREADS) mse_int_partial(const float2* __restrict__ a, long long aps,
-                                                               const float2* __restrict__ b, long long bps,
-                                                               long long npix, double* __restrict__ partial) {
+// Per-plane reductions of a pixel function f(a_i, b_i): KIND 0 the intensity
+// MSE term (|a|^2 - |b|^2)^2, KIND 1 the real inner product Re(conj(a) b).
+template <int KIND>
+__global__ void __launch_bounds__(MSE_THREADS) plane_sum_partial(const float2* __restrict__ a, long long aps,
+                                                                 const float2* __restrict__ b, long long bps,
+                                                                 long long npix, double* __restrict__ partial) {
   const int plane = blockIdx.y;
   a += (long long)plane * aps;
   b += (long long)plane * bps;
@@ -192,8 +195,12 @@ __global__ void __launch_bounds__(MSE_THREADS) mse_int_partial(const float2* __r
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
        i += (long long)gridDim.x * blockDim.x) {
     const float2 u = a[i], v = b[i];
-    const float d = (u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y);
-    acc = fmaf(d, d, acc);
+    if (KIND == 0) {
+      const float d = (u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y);
+      acc = fmaf(d, d, acc);
+    } else {
+      acc = fmaf(u.x, v.x, fmaf(u.y, v.y, acc));
+    }
   }
   __shared__ float red[MSE_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -235,6 +242,44 @@ __global__ void mse_int_grad(const float2* __restrict__ a, long long aps, const 
     const float d = s * ((u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y));
     if (ga) ga[(long long)plane * npix + i] = make_float2(d * u.x, d * u.y);
     if (gb) gb[(long long)plane * npix + i] = make_float2(-d * v.x, -d * v.y);
+  }
+}
+
+// The z-derivative of the VRS Ez derivation, reduced against the Ez gradient:
+// per batch entry b, sum_i Re(conj(g_i) dEz_i/dz) with
+// dEz/dz = -(Ex X + Ey Y) z / r^3, r^2 = X^2 + Y^2 + z^2 (vectorized_optics.py:258-261).
+__global__ void __launch_bounds__(MSE_THREADS) vrs_dz_ez_partial(const float2* __restrict__ ex,
+                                                                 const float2* __restrict__ ey, long long ebs,
+                                                                 const float2* __restrict__ g, long long gbs,
+                                                                 int ny, int nx, const double* __restrict__ x,
+                                                                 const double* __restrict__ y,
+                                                                 const double* __restrict__ z,
+                                                                 double* __restrict__ partial) {
+  const int b = blockIdx.y;
+  const long long npix = (long long)ny * nx;
+  ex += (long long)b * ebs;
+  ey += (long long)b * ebs;
+  g += (long long)b * gbs;
+  const float zf = (float)z[b];
+  float acc = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int row = (int)((unsigned)i / (unsigned)nx), col = (int)i - row * nx;
+    const float X = (float)x[col], Y = (float)y[row];
+    const float ir = rsqrtf(X * X + Y * Y + zf * zf);
+    const float w = -zf * ir * ir * ir;
+    const float2 u = ex[i], v = ey[i], gg = g[i];
+    const float2 d = make_float2(w * (u.x * X + v.x * Y), w * (u.y * X + v.y * Y));
+    acc = fmaf(gg.x, d.x, fmaf(gg.y, d.y, acc));
+  }
+  __shared__ float red[MSE_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w2 = 0; w2 < MSE_THREADS / 32; ++w2) t += red[w2];
+    partial[(long long)b * gridDim.x + blockIdx.x] = t;
   }
 }
 
@@ -375,9 +420,9 @@ extern "C" int xl_mse_intensity(void* stream, int planes, long long npix, const 
   }
   const int nb = mse_blocks(npix);
   cudaStream_t st = (cudaStream_t)stream;
-  mse_int_partial<<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
-                                                            b_pstride, npix, (double*)work);
-  XL_CHECK_LAUNCH("mse_int_partial");
+  plane_sum_partial<0><<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
+                                                                  b_pstride, npix, (double*)work);
+  XL_CHECK_LAUNCH("plane_sum_partial");
   mse_int_finish<<<(planes + 3) / 4, 128, 0, st>>>((const double*)work, nb, planes, 1.0 / (double)npix,
                                                     (float*)out);
   XL_CHECK_LAUNCH("mse_int_finish");
@@ -396,5 +441,41 @@ extern "C" int xl_mse_intensity_grad(void* stream, int planes, long long npix, c
       (const float2*)a, a_pstride, (const float2*)b, b_pstride, npix, (const float*)gloss,
       (float)(4.0 / (double)npix), (float2*)ga, (float2*)gb);
   XL_CHECK_LAUNCH("mse_int_grad");
+  return XL_OK;
+}
+
+extern "C" int xl_re_inner(void* stream, int planes, long long npix, const void* a, long long a_pstride,
+                           const void* b, long long b_pstride, void* work, void* out) {
+  if (planes < 1 || planes > 65535 || npix < 1 || !a || !b || !work || !out) {
+    set_error("xl_re_inner: bad arguments");
+    return XL_EINVAL;
+  }
+  const int nb = mse_blocks(npix);
+  cudaStream_t st = (cudaStream_t)stream;
+  plane_sum_partial<1><<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
+                                                                  b_pstride, npix, (double*)work);
+  XL_CHECK_LAUNCH("plane_sum_partial");
+  mse_int_finish<<<(planes + 3) / 4, 128, 0, st>>>((const double*)work, nb, planes, 1.0, (float*)out);
+  XL_CHECK_LAUNCH("mse_int_finish");
+  return XL_OK;
+}
+
+extern "C" int xl_vrs_dz_ez(void* stream, int batch, int ny, int nx, const void* ex, const void* ey,
+                            long long e_bstride, const void* gez, long long g_bstride, const double* x,
+                            const double* y, const double* z, void* work, void* out) {
+  if (batch < 1 || batch > 65535 || ny < 1 || nx < 1 || (long long)ny * nx > 0x7fffffffLL || !ex || !ey || !gez ||
+      !x || !y || !z || !work || !out) {
+    set_error("xl_vrs_dz_ez: bad arguments");
+    return XL_EINVAL;
+  }
+  const long long npix = (long long)ny * nx;
+  const int nb = mse_blocks(npix);
+  cudaStream_t st = (cudaStream_t)stream;
+  vrs_dz_ez_partial<<<dim3(nb, batch), MSE_THREADS, 0, st>>>((const float2*)ex, (const float2*)ey, e_bstride,
+                                                             (const float2*)gez, g_bstride, ny, nx, x, y, z,
+                                                             (double*)work);
+  XL_CHECK_LAUNCH("vrs_dz_ez_partial");
+  mse_int_finish<<<(batch + 3) / 4, 128, 0, st>>>((const double*)work, nb, batch, 1.0, (float*)out);
+  XL_CHECK_LAUNCH("mse_int_finish");
   return XL_OK;
 }

@@ -44,31 +44,44 @@ extern "C" size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx) {
   return (size_t)batch * comps * ny * P * sizeof(float2);
 }
 
-extern "C" int xl_rs_transfer_spectrum(void* stream, int ny, int nx, const double* offx,
-                                       const double* offy, double z, double wavelength,
-                                       double scale, void* spectrum, void* work) {
+static int transfer_spectrum(const char* what, void* stream, int ny, int nx, const double* offx,
+                             const double* offy, double z, double wavelength, double scale, void* spectrum,
+                             void* work, int dz) {
   if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE) {
-    set_error("xl_rs_transfer_spectrum: field side out of range (2..%d): %d x %d", XL_MAX_SIDE, ny, nx);
+    set_error("%s: field side out of range (2..%d): %d x %d", what, XL_MAX_SIDE, ny, nx);
     return XL_EINVAL;
   }
   if (!offx || !offy || !spectrum || !work) {
-    set_error("xl_rs_transfer_spectrum: null pointer argument");
+    set_error("%s: null pointer argument", what);
     return XL_EINVAL;
   }
   if (!(z != 0.0) || !(wavelength > 0.0)) {
-    set_error("xl_rs_transfer_spectrum: need z != 0 and wavelength > 0 (got z=%g, wavelength=%g)", z,
-              wavelength);
+    set_error("%s: need z != 0 and wavelength > 0 (got z=%g, wavelength=%g)", what, z, wavelength);
     return XL_EINVAL;
   }
   if (int rc = ensure_init()) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int lq = rs_logq(ny, nx);
 #define CALL(L) rs_spectrum<L>(st, ny, nx, offx, offy, z, wavelength, scale, (float2*)spectrum, \
-                                   (float2*)work)
+                               (float2*)work, dz)
   XL_RS_DISPATCH(lq, CALL)
 #undef CALL
-  set_error("xl_rs_transfer_spectrum: unsupported size");
+  set_error("%s: unsupported size", what);
   return XL_EUNSUPPORTED;
+}
+
+extern "C" int xl_rs_transfer_spectrum(void* stream, int ny, int nx, const double* offx,
+                                       const double* offy, double z, double wavelength,
+                                       double scale, void* spectrum, void* work) {
+  return transfer_spectrum("xl_rs_transfer_spectrum", stream, ny, nx, offx, offy, z, wavelength, scale,
+                           spectrum, work, 0);
+}
+
+extern "C" int xl_rs_transfer_spectrum_dz(void* stream, int ny, int nx, const double* offx,
+                                          const double* offy, double z, double wavelength,
+                                          double scale, void* spectrum, void* work) {
+  return transfer_spectrum("xl_rs_transfer_spectrum_dz", stream, ny, nx, offx, offy, z, wavelength, scale,
+                           spectrum, work, 1);
 }
 
 static int rs_run(void* stream, const XlRsArgs* a, int stage) {

@@ -93,7 +93,8 @@ struct RowPtr {
 // ---------------------------------------------------------------------------
 // Transfer spectrum, step 1: rows of the wrapped impulse response -> P-point
 // row spectra, row-major in natural order.
-template <int LOGQ>
+// DZ: the rows of dH/dz instead (the spectrum of the z-derivative).
+template <int LOGQ, bool DZ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
     rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double z,
                  double inv_lambda, float k, float2* __restrict__ out) {
@@ -108,7 +109,9 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
   for (int m = 0; m < 16; ++m) {
     const int col = j + m * C::T;
     const bool vx = (col < nx) || (col > C::P - nx);
-    v[m] = (vy && vx) ? rs_kernel_value(offx[col], offy[i], z, inv_lambda, k) : make_float2(0.f, 0.f);
+    v[m] = (vy && vx) ? (DZ ? rs_kernel_dz_value(offx[col], offy[i], z, inv_lambda, k)
+                            : rs_kernel_value(offx[col], offy[i], z, inv_lambda, k))
+                      : make_float2(0.f, 0.f);
   }
   block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + gi * C::XS, pass_tw<C::LOGP>());
   float2* dst = out + (long long)i * C::P;
@@ -431,6 +434,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
           const float inv = rsqrtf(X * X + z2);
           p.out[0][o] = cadd(e[0], cscale(e[2], X * inv));
           p.out[1][o] = cadd(e[1], cscale(e[2], Y * inv));
+          if (p.out[2]) p.out[2][o] = e[2];   // the unfolded Ez gradient, when asked for
           continue;
         }
         PixelCtx px{ro, n, (long long)ro * nx + n, b};
@@ -447,14 +451,20 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
 
 template <int LOGQ>
 int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy, double z,
-                double wavelength, double scale, float2* spec, float2* work) {
+                double wavelength, double scale, float2* spec, float2* work, int dz) {
   using C = RsCfg<LOGQ>;
   const size_t sm1 = (size_t)C::G * C::XS * sizeof(float2);
-  cudaError_t e = allow_smem(rs_hhat_rows<LOGQ>, sm1);
-  if (e != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
   const float k = (float)(2.0 * M_PI / wavelength);
-  rs_hhat_rows<LOGQ><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength, k,
-                                                                  work);
+  cudaError_t e;
+  if (dz) {
+    if ((e = allow_smem(rs_hhat_rows<LOGQ, true>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
+    rs_hhat_rows<LOGQ, true><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength,
+                                                                          k, work);
+  } else {
+    if ((e = allow_smem(rs_hhat_rows<LOGQ, false>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
+    rs_hhat_rows<LOGQ, false><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength,
+                                                                           k, work);
+  }
   XL_CHECK_LAUNCH("rs_hhat_rows");
   const size_t sm2 = (size_t)C::CW * C::CXS * sizeof(float2);
   e = allow_smem(rs_hhat_cols<LOGQ>, sm2);
@@ -538,5 +548,5 @@ int rs_propagate(cudaStream_t st, const RsLaunch& p, int stage) {
 
 #define XL_RS_INSTANTIATE(L)                                                                        \
   template int xl::rs_spectrum<L>(cudaStream_t, int, int, const double*, const double*, double, double, \
-                                  double, float2*, float2*);                                       \
+                                  double, float2*, float2*, int);                                  \
   template int xl::rs_propagate<L>(cudaStream_t, const RsLaunch&, int);

@@ -419,18 +419,19 @@ class SpectrumCache:
         self.builds = 0
 
     @staticmethod
-    def key(x, y, z, wavelength):
-        return (x.tobytes(), y.tobytes(), float(z), float(wavelength), torch.cuda.current_device())
+    def key(x, y, z, wavelength, dz=False):
+        return (x.tobytes(), y.tobytes(), float(z), float(wavelength), bool(dz), torch.cuda.current_device())
 
-    def get(self, x, y, z, wavelength):
-        k = self.key(x, y, z, wavelength)
+    def get(self, x, y, z, wavelength, dz=False):
+        """The transfer spectrum, or with ``dz`` the spectrum of its z-derivative."""
+        k = self.key(x, y, z, wavelength, dz)
         with _LOCK:
             e = self._d.get(k)
             if e is not None:
                 self._d.move_to_end(k)
         if e is not None:
             return e.use()
-        s = build_rs_spectrum(x, y, z, wavelength)
+        s = build_rs_spectrum(x, y, z, wavelength, dz)
         nb = s.numel() * 8
         with _LOCK:
             self._d[k] = _Built(s)
@@ -450,7 +451,7 @@ class SpectrumCache:
 SPECTRA = SpectrumCache()
 
 
-def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
+def build_rs_spectrum(x, y, z, wavelength, dz=False) -> torch.Tensor:
     L = lib()
     ny, nx = len(y), len(x)
     lq = rs_logq(ny, nx)
@@ -463,9 +464,9 @@ def build_rs_spectrum(x, y, z, wavelength) -> torch.Tensor:
     dx = x[1] - x[0]
     dy = y[1] - y[0]
     scale = dx * dy / float(P * P)
-    _lib.check(L.xl_rs_transfer_spectrum(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(), float(z),
-                                         float(wavelength), scale, spec.data_ptr(), work.data_ptr()),
-               "xl_rs_transfer_spectrum")
+    fn = L.xl_rs_transfer_spectrum_dz if dz else L.xl_rs_transfer_spectrum
+    _lib.check(fn(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(), float(z), float(wavelength), scale,
+                  spec.data_ptr(), work.data_ptr()), "xl_rs_transfer_spectrum")
     return spec
 
 
@@ -477,7 +478,10 @@ class RsCall:
     distinct value, from the cache)."""
 
     def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None,
-                 adjoint=False):
+                 adjoint=False, dz=False, want_ez=False):
+        """``dz``: propagate with the spectrum of dH/dz (the output's z-derivative);
+        ``want_ez``: a VRS adjoint also returns the propagated Ez gradient before
+        it is folded into Ex, Ey (third output)."""
         L = lib()
         x = as_grid(x)
         y = as_grid(y)
@@ -490,7 +494,7 @@ class RsCall:
         comps, B, ibs = batch_planes(comps, ny, nx)
         zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
         uniq = sorted(set(zs))
-        specs = [SPECTRA.get(x, y, zz, wavelength) for zz in uniq]
+        specs = [SPECTRA.get(x, y, zz, wavelength, dz) for zz in uniq]
         dev = comps[0].device
         spec_ptrs = None
         if len(specs) == 1:
@@ -502,7 +506,7 @@ class RsCall:
         if work is None:
             work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
-            nout = 2 if (adjoint and vector) else cout
+            nout = (3 if want_ez else 2) if (adjoint and vector) else cout
             outs = [torch.empty(tuple(lead) + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(nout)]
         zt = device_array(np.asarray(zs, dtype=np.float64), torch.float64) if vector else None
         a = _lib.XlRsArgs()
@@ -775,3 +779,50 @@ def mse_intensity_grad(a, b, g, want_a=True, want_b=False):
     _lib.check(lib().xl_mse_intensity_grad(stream_handle(), na, ny * nx, av.data_ptr(), aps, bv.data_ptr(), bps,
                                            g.data_ptr(), _ptr(ga), _ptr(gb)), "xl_mse_intensity_grad")
     return ga, gb
+
+
+def z_values(z):
+    """(distances as python floats, a tensor that needs their gradient or None).
+    A distance given as a tensor that requires grad is read back to the host
+    (its transfer spectrum is built from the value) and kept for autograd."""
+    if isinstance(z, torch.Tensor):
+        vals = z.detach().to("cpu", torch.float64).numpy()
+        zt = z if z.requires_grad else None
+        return (float(vals) if vals.ndim == 0 else [float(v) for v in vals.ravel()]), zt
+    return z, None
+
+
+def re_inner(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """sum over the last two dims of Re(conj(a) b), one value per plane (fixed-order sums)."""
+    a = as_field(a)
+    b = as_field(b)
+    ny, nx = a.shape[-2:]
+    av, na, aps = _planes(a)
+    bv, nb, bps = _planes(b)
+    if nb != na:
+        raise ValueError("re_inner: plane counts differ")
+    L = lib()
+    work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(na, ny * nx) // 8), dtype=torch.float64,
+                       device=a.device)
+    out = torch.empty(na, dtype=torch.float32, device=a.device)
+    _lib.check(L.xl_re_inner(stream_handle(), na, ny * nx, av.data_ptr(), aps, bv.data_ptr(), bps, work.data_ptr(),
+                             out.data_ptr()), "xl_re_inner")
+    return out.reshape(a.shape[:-2])
+
+
+def vrs_dz_ez(ex, ey, gez, x, y, zs) -> torch.Tensor:
+    """Per batch entry: sum Re(conj(gez) dEz/dz) for the VRS Ez derivation (libxlgb)."""
+    ex, ey, gez = as_field(ex), as_field(ey), as_field(gez)
+    ny, nx = gez.shape[-2:]
+    B = gez.numel() // (ny * nx)
+    (exv, eyv), _, ebs = batch_planes([ex, ey], ny, nx)
+    gv = gez.contiguous()
+    x, y = as_grid(x), as_grid(y)
+    zt = device_array(np.broadcast_to(np.asarray(zs, dtype=np.float64), (B,)).copy(), torch.float64)
+    L = lib()
+    work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(B, ny * nx) // 8), dtype=torch.float64, device=gv.device)
+    out = torch.empty(B, dtype=torch.float32, device=gv.device)
+    _lib.check(L.xl_vrs_dz_ez(stream_handle(), B, ny, nx, exv.data_ptr(), eyv.data_ptr(), ebs, gv.data_ptr(),
+                              ny * nx, device_grid(x).data_ptr(), device_grid(y).data_ptr(), zt.data_ptr(),
+                              work.data_ptr(), out.data_ptr()), "xl_vrs_dz_ez")
+    return out

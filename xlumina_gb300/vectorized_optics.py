@@ -79,13 +79,14 @@ class VectorizedLight(_Grid):
     def VRS_propagation(self, z):
         """vectorized_optics.py:244-284: Ez derived from Ex, Ey; returns (light, quality_factor)."""
         tic = time.perf_counter()
-        qf = engine.quality_factor(self.x, self.y, self.wavelength, z)
+        zv, _ = engine.z_values(z)
+        qf = engine.quality_factor(self.x, self.y, self.wavelength, np.asarray(zv))
         E = self._base(2)
-        if autograd.needs_grad(E, self._ops):
+        if autograd.needs_grad(E, self._ops, z):
             plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, True, self._ops)
             Ex, Ey, Ez = autograd.fused_propagate(plan, E, 3)
         else:
-            Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, z, vector=True, pre=self._ops)
+            Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, zv, vector=True, pre=self._ops)
         _report("VRS", tic)
         return VectorizedLight._wrap(self.x, self.y, self.wavelength, [Ex, Ey, Ez]), qf
 

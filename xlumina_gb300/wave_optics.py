@@ -135,13 +135,14 @@ class ScalarLight(_Grid):
     def RS_propagation(self, z):
         """wave_optics.py:173-196: returns (ScalarLight, quality_factor)."""
         tic = time.perf_counter()
-        qf = engine.quality_factor(self.x, self.y, self.wavelength, z)
+        zv, _ = engine.z_values(z)
+        qf = engine.quality_factor(self.x, self.y, self.wavelength, np.asarray(zv))
         base = [self._base()]
-        if autograd.needs_grad(base, self._ops):
+        if autograd.needs_grad(base, self._ops, z):
             plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, False, self._ops)
             out = autograd.fused_propagate(plan, base, 1)[0]
         else:
-            out = engine.rs_propagate(base, self.x, self.y, self.wavelength, z, vector=False, pre=self._ops)[0]
+            out = engine.rs_propagate(base, self.x, self.y, self.wavelength, zv, vector=False, pre=self._ops)[0]
         _report("RS", tic)
         return ScalarLight._wrap(self.x, self.y, self.wavelength, out), qf
 
