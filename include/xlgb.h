@@ -242,6 +242,39 @@ int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const vo
                     long long in_bstride, const void* const* gout, long long gout_bstride,
                     void* const* gin, long long gin_bstride, const XlProg* prog, void* const* pgrad);
 
+/* ---- Beam splitters ----------------------------------------------------- */
+
+/* Two-port mixing of (Ex, Ey) planes by a complex 2x2 matrix M (row-major):
+ * c = M00 a + M01 b, d = M10 a + M11 b.  This is BS_symmetric
+ * (optical_elements.py:334-391: M = [[R, iT], [iT, R]] with the 1% loss of
+ * :380-383), BS_symmetric_SI (:393-460: one input port, b absent) and the
+ * lossless BS (:462-512: M = [[sqrt T, sqrt R e^{i phase}], [-sqrt R
+ * e^{-i phase}, sqrt T]]).  The outputs' Ez is zero (not written). */
+typedef struct {
+  int batch, ny, nx;
+  const void* in[2][2];       /* [port a, b][Ex, Ey] complex64 planes; port b may be NULL (zero) */
+  long long in_bstride[2];    /* elements between batch entries, per port (0: one plane for the batch) */
+  void* out[2][2];            /* [port c, d][Ex, Ey]; NULL planes are not written */
+  long long out_bstride;
+  const void* m;              /* device complex64 M, 4 entries per batch entry */
+  long long m_bstride;        /* 0 (one M for the batch) or 4 */
+} XlBsArgs;
+
+int xl_beam_splitter(void* stream, const XlBsArgs* args);
+
+/* Bytes of workspace xl_beam_splitter_backward needs to return s. */
+size_t xl_beam_splitter_work_bytes(int batch, int ny, int nx);
+
+/* Backward of xl_beam_splitter (args as in the forward; args->out unused).
+ * gout[4] = gradients of (c.Ex, c.Ey, d.Ex, d.Ey) (torch convention; NULL is
+ * zero); gin[4] receives the gradients of (a.Ex, a.Ey, b.Ex, b.Ey) = M^H gout
+ * (NULL skips); s (complex64, 4 per batch entry, may be NULL) receives
+ * S_ij = sum conj(gout_i) in_j over pixels and both components, whose
+ * conjugate is the gradient of M_ij (fixed-order sums). */
+int xl_beam_splitter_backward(void* stream, const XlBsArgs* args, const void* const* gout,
+                              long long gout_bstride, void* const* gin, long long gin_bstride, void* s,
+                              void* work);
+
 /* ---- Reductions for gradients -------------------------------------------- */
 
 /* out[p] = sum_i Re(conj(a_i) b_i) over planes p of npix complex64 pixels, in

@@ -139,6 +139,31 @@ def lens(field, x, y, wavelength, radius, focal):
     return field * torch.as_tensor(ref.lens_mask(x, y, wavelength, radius, focal))
 
 
+def bs_symmetric(aEx, aEy, bEx, bEy, theta):
+    """optical_elements.py:334-391."""
+    theta = _t(theta).to(torch.float64)
+    T, R = torch.abs(torch.cos(theta)), torch.abs(torch.sin(theta))
+    noise = T * 0.01
+    T, R = T - noise, R - noise
+    return R * aEx + 1j * T * bEx, R * aEy + 1j * T * bEy, 1j * T * aEx + R * bEx, 1j * T * aEy + R * bEy
+
+
+def bs_symmetric_si(aEx, aEy, theta, port=0):
+    """optical_elements.py:393-460."""
+    theta = _t(theta).to(torch.float64)
+    T, R = torch.abs(torch.cos(theta)), torch.abs(torch.sin(theta))
+    noise = T * 0.01
+    T, R = T - noise, R - noise
+    if port == 0:
+        return R * aEx, R * aEy, 1j * T * aEx, 1j * T * aEy
+    return 1j * T * aEx, 1j * T * aEy, R * aEx, R * aEy
+
+
+def fluorescence(i_ex, i_dep, beta=1):
+    """optical_elements.py:941-954."""
+    return i_ex * (1 - beta * (1 - torch.exp(-(i_dep / (i_ex + 1e-8)))))
+
+
 def mse_intensity(a, b):
     """loss_functions.py:137-149."""
     return torch.sum((torch.abs(a) ** 2 - torch.abs(b) ** 2) ** 2) / (a.shape[0] * a.shape[1])

@@ -355,6 +355,43 @@ def plane_wave(x, y, wavelength, A=1.0, theta=0.0, phi=0.0, z0=0.0):
                                 + z0 * np.cos(theta)))
 
 
+# ------------------------------------------------------- beam splitters --
+
+def bs_loss_rt(theta):
+    """optical_elements.py:376-383 -- R = |sin|, T = |cos|, both less 1% of |cos|."""
+    T = np.abs(np.cos(theta))
+    R = np.abs(np.sin(theta))
+    noise = T * 0.01
+    return R - noise, T - noise
+
+
+def bs_symmetric(aEx, aEy, bEx, bEy, theta):
+    """optical_elements.py:334-391 -- returns (cEx, cEy, dEx, dEy); Ez of c, d is zero."""
+    R, T = bs_loss_rt(theta)
+    return R * aEx + 1j * T * bEx, R * aEy + 1j * T * bEy, 1j * T * aEx + R * bEx, 1j * T * aEy + R * bEy
+
+
+def bs_symmetric_si(aEx, aEy, theta, port=0):
+    """optical_elements.py:393-460 -- single input; port 0: c = R a, d = iT a; port 1 swaps."""
+    R, T = bs_loss_rt(theta)
+    if port == 0:
+        return R * aEx, R * aEy, 1j * T * aEx, 1j * T * aEy
+    return 1j * T * aEx, 1j * T * aEy, R * aEx, R * aEy
+
+
+def bs_lossless(a1Ex, a1Ey, a2Ex, a2Ey, R, T, phase):
+    """optical_elements.py:462-512 -- returns (b1Ex, b1Ey, b2Ex, b2Ey)."""
+    sT, sR = np.sqrt(T), np.sqrt(R)
+    e, ec = np.exp(1j * phase), np.exp(-1j * phase)
+    return (sT * a1Ex + sR * e * a2Ex, sT * a1Ey + sR * e * a2Ey,
+            -sR * ec * a1Ex + sT * a2Ex, -sR * ec * a1Ey + sT * a2Ey)
+
+
+def fluorescence(i_ex, i_dep, beta=1):
+    """optical_elements.py:941-954 -- i_ex (1 - beta (1 - exp(-i_dep / (i_ex + 1e-8))))."""
+    return i_ex * (1 - beta * (1 - np.exp(-(i_dep / (i_ex + 1e-8)))))
+
+
 # -------------------------------------------------------------- losses --
 
 def mse_intensity(a, b):

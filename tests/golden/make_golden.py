@@ -199,6 +199,32 @@ def main(ref_root):
               phase2=p2, after_rs=l2.field, after_lens=l3.field, after_czt1=l4.field, out=l6.field,
               intensity=I, target=target)
 
+        # 12. beam splitters (lossy symmetric, single input on both ports,
+        # lossless) and the fluorescence model.
+        x, y = tb.space(120.0, 40)
+        wl = 0.65
+        la = VectorizedLight(x, y, wl)
+        lb = VectorizedLight(x, y, wl)
+        la.Ex = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        la.Ey = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        lb.Ex = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        lb.Ey = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        th = 0.7
+        c, d = oe.BS_symmetric(la, lb, th)
+        c0, d0 = oe.BS_symmetric_SI(la, th, port=0)
+        c1, d1 = oe.BS_symmetric_SI(la, -2.2, port=1)
+        b1, b2 = oe.BS(la, lb, 0.3, 0.7, 1.1)
+        i_ex = np.abs(rng.standard_normal((3, 40, 40))) ** 2
+        i_dep = np.abs(rng.standard_normal((3, 40, 40))) ** 2
+        fl = oe.fluorescence(i_ex[0], i_dep[0], beta=0.8)
+        vfl = oe.vectorized_fluorophores(i_ex, i_dep)
+        _save("beam_splitters", x=x, y=y, wavelength=wl, aEx=la.Ex, aEy=la.Ey, bEx=lb.Ex, bEy=lb.Ey, theta=th,
+              cEx=c.Ex, cEy=c.Ey, cEz=c.Ez, dEx=d.Ex, dEy=d.Ey, dEz=d.Ez,
+              si0_cEx=c0.Ex, si0_cEy=c0.Ey, si0_dEx=d0.Ex, si0_dEy=d0.Ey, theta_si1=-2.2,
+              si1_cEx=c1.Ex, si1_cEy=c1.Ey, si1_dEx=d1.Ex, si1_dEy=d1.Ey,
+              R=0.3, T=0.7, phase=1.1, b1Ex=b1.Ex, b1Ey=b1.Ey, b2Ex=b2.Ex, b2Ey=b2.Ey,
+              i_ex=i_ex, i_dep=i_dep, beta=0.8, fluorescence=fl, vfluorophores=vfl)
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

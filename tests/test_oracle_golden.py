@@ -183,3 +183,22 @@ def test_torch_restatement_gradients_match_finite_differences():
                 t[i, j] += h
             fd = (lp - lm) / (2 * h)
             assert abs(fd - gt[i, j].item()) <= 1e-6 * max(1.0, abs(fd)) + 1e-9 * abs(L.item())
+
+
+def test_beam_splitters_and_fluorescence():
+    g = golden("beam_splitters")
+    a, b = (g["aEx"], g["aEy"]), (g["bEx"], g["bEy"])
+    out = ref.bs_symmetric(*a, *b, float(g["theta"]))
+    for got, key in zip(out, ("cEx", "cEy", "dEx", "dEy")):
+        assert rel_l2(got, g[key]) < 1e-14
+    assert not np.any(g["cEz"]) and not np.any(g["dEz"])
+    for port, th in ((0, float(g["theta"])), (1, float(g["theta_si1"]))):
+        out = ref.bs_symmetric_si(*a, th, port)
+        for got, key in zip(out, ("cEx", "cEy", "dEx", "dEy")):
+            assert rel_l2(got, g[f"si{port}_{key}"]) < 1e-14
+    out = ref.bs_lossless(*a, *b, float(g["R"]), float(g["T"]), float(g["phase"]))
+    for got, key in zip(out, ("b1Ex", "b1Ey", "b2Ex", "b2Ey")):
+        assert rel_l2(got, g[key]) < 1e-14
+    fl = ref.fluorescence(g["i_ex"][0], g["i_dep"][0], float(g["beta"]))
+    assert rel_l2(fl, g["fluorescence"]) < 1e-14
+    assert rel_l2(ref.fluorescence(g["i_ex"], g["i_dep"]), g["vfluorophores"]) < 1e-14

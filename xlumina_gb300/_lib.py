@@ -60,6 +60,13 @@ class XlCztArgs(ctypes.Structure):
                 ("work", ctypes.c_void_p), ("pre", XlProg), ("adjoint", ctypes.c_int)]
 
 
+class XlBsArgs(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("ny", ctypes.c_int), ("nx", ctypes.c_int),
+                ("inp", (ctypes.c_void_p * 2) * 2), ("in_bstride", ctypes.c_longlong * 2),
+                ("out", (ctypes.c_void_p * 2) * 2), ("out_bstride", ctypes.c_longlong),
+                ("m", ctypes.c_void_p), ("m_bstride", ctypes.c_longlong)]
+
+
 # name -> (restype, argtypes); every symbol include/xlgb.h declares.
 SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
@@ -102,6 +109,12 @@ SIGNATURES = {
     "xl_mse_intensity_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
                                              ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_beam_splitter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlBsArgs)]),
+    "xl_beam_splitter_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "xl_beam_splitter_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlBsArgs),
+                                                 ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                                 ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
+                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

@@ -211,3 +211,50 @@ class _MseIntensity(torch.autograd.Function):
 
 def mse_intensity(a, b):
     return _MseIntensity.apply(a, b)
+
+
+def _sum_to(g, shape):
+    """Sum a per-batch gradient down to a broadcast input's shape."""
+    if g is None or tuple(g.shape) == tuple(shape):
+        return g
+    return g.reshape((-1,) + tuple(g.shape[-2:])).sum(0).reshape(shape)
+
+
+class _BeamSplitter(torch.autograd.Function):
+    """Two-port mixing c, d = M [a; b] with the hand-written backward of libxlgb."""
+
+    @staticmethod
+    def forward(ctx, m, a_ex, a_ey, b_ex, b_ey):
+        b = None if b_ex is None else [b_ex, b_ey]
+        ctx.has_b = b is not None
+        ctx.save_for_backward(m, a_ex, a_ey, b_ex, b_ey)
+        return tuple(engine.beam_splitter([a_ex, a_ey], b, m))
+
+    @staticmethod
+    def backward(ctx, *gouts):
+        m, a_ex, a_ey, b_ex, b_ey = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        want_m, want_a = need[0], need[1] or need[2]
+        want_b = ctx.has_b and (need[3] or need[4])
+        b = [b_ex, b_ey] if ctx.has_b else None
+        ga, gb, s = engine.beam_splitter_backward([a_ex, a_ey], b, m, list(gouts), want_a, want_b, want_m)
+        gm = None
+        if want_m:
+            gm = torch.conj(s)
+            gm = gm.sum(0) if m.dim() == 2 else gm
+            gm = gm.to(m.dtype)
+        out = [gm, None, None, None, None]
+        if ga is not None:
+            out[1], out[2] = _sum_to(ga[0], a_ex.shape), _sum_to(ga[1], a_ey.shape)
+        if gb is not None:
+            out[3], out[4] = _sum_to(gb[0], b_ex.shape), _sum_to(gb[1], b_ey.shape)
+        return tuple(out)
+
+
+def beam_splitter(a, b, m):
+    """[c.Ex, c.Ey, d.Ex, d.Ey] = M [a; b]; differentiable in a, b and M."""
+    tensors = [m] + list(a) + (list(b) if b is not None else [])
+    if torch.is_grad_enabled() and any(isinstance(t, torch.Tensor) and t.requires_grad for t in tensors):
+        bx, by = (b[0], b[1]) if b is not None else (None, None)
+        return list(_BeamSplitter.apply(m, a[0], a[1], bx, by))
+    return engine.beam_splitter(a, b, m)

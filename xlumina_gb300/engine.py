@@ -826,3 +826,91 @@ def vrs_dz_ez(ex, ey, gez, x, y, zs) -> torch.Tensor:
                               ny * nx, device_grid(x).data_ptr(), device_grid(y).data_ptr(), zt.data_ptr(),
                               work.data_ptr(), out.data_ptr()), "xl_vrs_dz_ez")
     return out
+
+
+# ---------------------------------------------------------- beam splitters --
+
+def _bs_port(comps, B, ny, nx):
+    """(Ex, Ey) planes of one port for a launch of batch B: (planes, batch stride)."""
+    if comps is None:
+        return [None, None], 0
+    comps = [as_field(c) for c in comps]
+    lead = comps[0].shape[:-2]
+    nb = int(np.prod(lead)) if len(lead) else 1
+    if nb == 1:
+        return [c.reshape(ny, nx).contiguous() for c in comps], 0
+    if nb != B:
+        raise ValueError(f"beam splitter ports hold {nb} and {B} fields")
+    planes, _, bs = batch_planes(comps, ny, nx)
+    return planes, bs
+
+
+def _bs_batch(a, b, m):
+    leads = [c.shape[:-2] for c in list(a) + list(b or [])]
+    sizes = [int(np.prod(s)) if len(s) else 1 for s in leads]
+    if m.dim() == 3:
+        sizes.append(m.shape[0])
+    B = max(sizes)
+    lead = next((s for s, n in zip(leads, sizes) if n == B), (B,))
+    return B, tuple(lead) if B > 1 else ()
+
+
+def _bs_args(a, b, m, ny, nx):
+    B, lead = _bs_batch(a, b, m)
+    pa, sa = _bs_port(a, B, ny, nx)
+    pb, sb = _bs_port(b, B, ny, nx)
+    if m.dim() == 3 and m.shape[0] != B:
+        raise ValueError(f"{m.shape[0]} splitter matrices for a batch of {B}")
+    m = m.to(torch.complex64).contiguous()
+    args = _lib.XlBsArgs()
+    args.batch, args.ny, args.nx = B, ny, nx
+    for j, port in enumerate((pa, pb)):
+        for c in range(2):
+            args.inp[j][c] = _ptr(port[c])
+    args.in_bstride[0], args.in_bstride[1] = sa, sb
+    args.m = m.data_ptr()
+    args.m_bstride = 4 if m.dim() == 3 else 0
+    return args, B, lead, (pa, pb, m)
+
+
+def beam_splitter(a, b, m):
+    """[c.Ex, c.Ey, d.Ex, d.Ey] = M [a; b] on the (Ex, Ey) planes (libxlgb).
+    ``a``, ``b``: [Ex, Ey] tensors of shape (ny, nx) or (B, ny, nx) (``b`` may be
+    None); ``m``: complex device tensor (2, 2) or (B, 2, 2)."""
+    ny, nx = a[0].shape[-2:]
+    args, B, lead, keep = _bs_args(a, b, m, ny, nx)
+    dev = keep[0][0].device
+    outs = [torch.empty(lead + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(4)]
+    for i in range(2):
+        for c in range(2):
+            args.out[i][c] = outs[2 * i + c].data_ptr()
+    args.out_bstride = ny * nx
+    _lib.check(lib().xl_beam_splitter(stream_handle(), ctypes.byref(args)), "xl_beam_splitter")
+    return outs
+
+
+def beam_splitter_backward(a, b, m, gouts, want_a=True, want_b=True, want_m=True):
+    """Gradients of ``beam_splitter``: (ga [Ex, Ey] or None, gb or None,
+    S (B, 2, 2) complex64 or None) with S_ij = sum conj(g_i) in_j, per batch entry."""
+    ny, nx = a[0].shape[-2:]
+    args, B, lead, keep = _bs_args(a, b, m, ny, nx)
+    dev = keep[0][0].device
+    gs = [None if g is None else as_field(g).reshape((B, ny, nx) if B > 1 else (ny, nx)).contiguous()
+          for g in gouts]
+    gin = [None] * 4
+    if want_a:
+        gin[0:2] = [torch.empty(lead + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(2)]
+    if want_b and b is not None:
+        gin[2:4] = [torch.empty(lead + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(2)]
+    s = work = None
+    if want_m:
+        s = torch.empty((B, 2, 2), dtype=torch.complex64, device=dev)
+        work = torch.empty(max(1, lib().xl_beam_splitter_work_bytes(B, ny, nx) // 8), dtype=torch.float64,
+                           device=dev)
+    gp = (ctypes.c_void_p * 4)(*[_ptr(g) for g in gs])
+    ip = (ctypes.c_void_p * 4)(*[_ptr(g) for g in gin])
+    _lib.check(lib().xl_beam_splitter_backward(stream_handle(), ctypes.byref(args), gp, ny * nx, ip, ny * nx,
+                                               _ptr(s), _ptr(work)), "xl_beam_splitter_backward")
+    ga = gin[0:2] if want_a else None
+    gb = gin[2:4] if (want_b and b is not None) else None
+    return ga, gb, s

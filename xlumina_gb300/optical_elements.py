@@ -104,19 +104,96 @@ def linear_polarizer(input_field, alpha):
     return input_field._with_op(engine.op_lp(alpha))
 
 
-def BS_symmetric(a, b, theta):
-    """optical_elements.py:334-391: lossy symmetric beam splitter (1% loss of T), on the device."""
-    T = abs(np.cos(theta))
-    R = abs(np.sin(theta))
+def _is_t(v):
+    return isinstance(v, torch.Tensor)
+
+
+def _bs_loss_rt(theta):
+    """(R, T) of the lossy symmetric splitter: |sin|, |cos| less 1% of |cos|
+    (optical_elements.py:376-383)."""
+    if _is_t(theta):
+        th = theta.to(device=engine.device(), dtype=torch.float64)
+        T, R = torch.abs(torch.cos(th)), torch.abs(torch.sin(th))
+    else:
+        th = np.asarray(theta, dtype=np.float64)
+        T, R = np.abs(np.cos(th)), np.abs(np.sin(th))
     noise = T * 0.01
-    T, R = T - noise, R - noise
-    c = VectorizedLight(a.x, a.y, a.wavelength)
-    d = VectorizedLight(a.x, a.y, a.wavelength)
-    c.Ex = R * a.Ex + 1j * T * b.Ex
-    c.Ey = R * a.Ey + 1j * T * b.Ey
-    d.Ex = 1j * T * a.Ex + R * b.Ex
-    d.Ey = 1j * T * a.Ey + R * b.Ey
+    return R - noise, T - noise
+
+
+def _bs_matrix(entries, like):
+    """Complex 2x2 splitter matrix (row-major entries), on the device: a
+    differentiable torch tensor when any entry is one, else a cached copy."""
+    if any(_is_t(e) for e in entries):
+        dev = engine.device()
+        shape = torch.broadcast_shapes(*[e.shape for e in entries if _is_t(e)])
+        ents = [e.to(device=dev, dtype=torch.complex128) if _is_t(e) else
+                torch.full(shape, complex(e), dtype=torch.complex128, device=dev) for e in entries]
+        m = torch.stack([e.expand(shape) for e in ents], -1).reshape(tuple(shape) + (2, 2))
+        return m.to(torch.complex64)
+    m = np.stack([np.broadcast_to(np.asarray(e, dtype=np.complex128), np.shape(like)) for e in entries], -1)
+    return engine.device_array(m.reshape(np.shape(like) + (2, 2)), torch.complex64)
+
+
+def _i_times(v):
+    return torch.complex(torch.zeros_like(v), v) if _is_t(v) else 1j * v
+
+
+def _bs_apply(a, b, m):
+    """Mix the (Ex, Ey) of lights a, b (b may be None); outputs (c, d) with Ez zero."""
+    pa = [a.Ex, a.Ey]
+    pb = [b.Ex, b.Ey] if b is not None else None
+    cx, cy, dx, dy = autograd.beam_splitter(pa, pb, m)
+    c = VectorizedLight._wrap(a.x, a.y, a.wavelength, [cx, cy, None])
+    d = VectorizedLight._wrap(a.x, a.y, a.wavelength, [dx, dy, None])
     return c, d
+
+
+def BS_symmetric(a, b, theta):
+    """optical_elements.py:334-391: lossy symmetric beam splitter, c = R a + iT b,
+    d = iT a + R b (R = |sin theta|, T = |cos theta|, both less 1% of T), as one
+    fused kernel; differentiable in the fields and in a tensor theta."""
+    R, T = _bs_loss_rt(theta)
+    iT = _i_times(T)
+    return _bs_apply(a, b, _bs_matrix([R, iT, iT, R], theta))
+
+
+def bs_port0(a_Ex, a_Ey, c_Ex, c_Ey, d_Ex, d_Ey, T, R):
+    """optical_elements.py:393-400: single input at port 0."""
+    return R * a_Ex, R * a_Ey, 1j * T * a_Ex, 1j * T * a_Ey
+
+
+def bs_port1(a_Ex, a_Ey, c_Ex, c_Ey, d_Ex, d_Ey, T, R):
+    """optical_elements.py:402-409: single input at port 1."""
+    return 1j * T * a_Ex, 1j * T * a_Ey, R * a_Ex, R * a_Ey
+
+
+def BS_symmetric_SI(a, theta, port=0):
+    """optical_elements.py:411-460: single-input lossy splitter; port 0 gives
+    c = R a, d = iT a, port 1 gives c = iT a, d = R a."""
+    R, T = _bs_loss_rt(theta)
+    iT = _i_times(T)
+    zero = 0.0
+    if int(port) == 0:
+        m = _bs_matrix([R, zero, iT, zero], theta)
+    else:
+        m = _bs_matrix([iT, zero, R, zero], theta)
+    return _bs_apply(a, None, m)
+
+
+def BS(a1, a2, R, T, phase):
+    """optical_elements.py:462-512: lossless splitter, b1 = sqrt(T) a1 + sqrt(R)
+    e^{i phase} a2, b2 = -sqrt(R) e^{-i phase} a1 + sqrt(T) a2."""
+    if any(_is_t(v) for v in (R, T, phase)):
+        dev = engine.device()
+        R, T, phase = (v.to(device=dev, dtype=torch.float64) if _is_t(v) else
+                       torch.tensor(float(v), dtype=torch.float64, device=dev) for v in (R, T, phase))
+        sT, sR = torch.sqrt(T).to(torch.complex128), torch.sqrt(R)
+        m = _bs_matrix([sT, torch.polar(sR, phase), -torch.polar(sR, -phase), sT], None)
+    else:
+        sT, sR = np.sqrt(T), np.sqrt(R)
+        m = _bs_matrix([sT, sR * np.exp(1j * phase), -sR * np.exp(-1j * phase), sT], np.asarray(0.0))
+    return _bs_apply(a1, a2, m)
 
 
 def high_NA_objective_lens(input_field, radius, f):
@@ -199,3 +276,17 @@ def building_block(input_light, alpha, phi, z, eta, theta):
     l_mod = sSLM(input_light, alpha, phi)
     l_prop, _ = l_mod.VRS_propagation(z)
     return LCD(l_prop, eta, theta)
+
+
+def fluorescence(i_ex, i_dep, beta=1):
+    """optical_elements.py:941-954: STED effective intensity
+    i_ex (1 - beta (1 - exp(-i_dep / (i_ex + 1e-8)))), elementwise on the device."""
+    i_ex = engine.as_real_param(i_ex) if not _is_t(i_ex) else i_ex
+    i_dep = engine.as_real_param(i_dep) if not _is_t(i_dep) else i_dep
+    return i_ex * (1 - beta * (1 - torch.exp(-(i_dep / (i_ex + 1e-8)))))
+
+
+def vectorized_fluorophores(i_ex, i_dep):
+    """optical_elements.py:956-962: fluorescence over a stack of detectors
+    (the vmap over the leading axis is the elementwise expression itself)."""
+    return fluorescence(i_ex, i_dep)
