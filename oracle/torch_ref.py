@@ -21,12 +21,23 @@ def _t(a):
     return a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a))
 
 
+def rs_transfer(z, Xe, Ye, k):
+    """wave_optics.py:291-297 with a distance that may be a tensor (differentiable in z)."""
+    if not isinstance(z, torch.Tensor):
+        return torch.as_tensor(ref.rs_transfer(z, Xe, Ye, k))
+    z = z.to(torch.float64).reshape(())
+    r = torch.sqrt(torch.as_tensor(Xe) ** 2 + torch.as_tensor(Ye) ** 2 + z ** 2)
+    amp = z / (2.0 * np.pi * r ** 2) * (1.0 / r - 1j * k)
+    sgn = 1.0 if float(z.detach()) > 0 else -1.0
+    return torch.exp(sgn * 1j * k * r) * amp
+
+
 def rs_propagate(field, x, y, wavelength, z):
     """wave_optics.py:281-289."""
     ny, nx = len(y), len(x)
     k = 2 * np.pi / wavelength
     Xe, Ye = np.meshgrid(ref.rs_offset_axis(x), ref.rs_offset_axis(y))
-    H = torch.as_tensor(ref.rs_transfer(z, Xe, Ye, k))
+    H = rs_transfer(z, Xe, Ye, k)
     U = torch.zeros((2 * ny - 1, 2 * nx - 1), dtype=C128)
     U = U.index_put((torch.arange(ny)[:, None], torch.arange(nx)[None, :]), _t(field).to(C128))
     out = torch.fft.ifft2(torch.fft.fft2(U) * torch.fft.fft2(H)) * (x[1] - x[0]) * (y[1] - y[0])
@@ -35,9 +46,10 @@ def rs_propagate(field, x, y, wavelength, z):
 
 def vrs_propagate(Ex, Ey, x, y, wavelength, z):
     """vectorized_optics.py:244-284."""
-    X, Y = np.meshgrid(x, y)
-    r = np.sqrt(X ** 2 + Y ** 2 + z ** 2)
-    Ez = Ex * torch.as_tensor(X / r) + Ey * torch.as_tensor(Y / r)
+    X, Y = (torch.as_tensor(a) for a in np.meshgrid(x, y))
+    zz = z.to(torch.float64).reshape(()) if isinstance(z, torch.Tensor) else z
+    r = torch.sqrt(X ** 2 + Y ** 2 + zz ** 2)
+    Ez = Ex * (X / r) + Ey * (Y / r)
     return tuple(rs_propagate(c, x, y, wavelength, z) for c in (Ex, Ey, Ez))
 
 
@@ -174,3 +186,68 @@ def small_area_hybrid(I):
     In = I / (torch.sum(I) + 1e-08)
     mask = (In > 0.7 * torch.max(In)).to(In.dtype)
     return torch.sum(mask) / (torch.sum(mask * In) + 1e-08)
+
+
+def building_block(Ex, Ey, x, y, wavelength, alpha, phi, z, eta, theta):
+    """optical_elements.py:919-939: sSLM -> VRS(z) -> LCD (Ez of the output is the VRS's)."""
+    ax, ay = sslm(Ex, Ey, alpha, phi)
+    px, py, pz = vrs_propagate(ax, ay, x, y, wavelength, z)
+    lx, ly = lcd(px, py, eta, theta)
+    return lx, ly, pz
+
+
+def hybrid_setup_sharp_focus(src, x, y, wavelength, parameters, r, f, xout, yout, distance_offset=8.9):
+    """optical_elements.py:1503-1649 restated step by step (every source is
+    ``src`` = (Ex, Ey)); returns the six detectors' |Ez|^2 stacked."""
+    cm = 1e4
+
+    def ang(p):
+        return _t(p).to(torch.float64) * 2 * np.pi - np.pi
+
+    def dist(p):
+        return (torch.abs(_t(p).to(torch.float64)) * 100 + distance_offset) * cm
+
+    P = parameters
+    ph = [(ang(P[6 * b]), ang(P[6 * b + 1])) for b in range(3)]
+    eta = [ang(P[6 * b + 2]) for b in range(3)]
+    th = [ang(P[6 * b + 3]) for b in range(3)]
+    z = [(dist(P[6 * b + 4]), dist(P[6 * b + 5])) for b in range(3)]
+    bs = [ang(P[18 + k]) for k in range(9)]
+    z4, z5 = dist(P[27]), dist(P[28])
+
+    def V(E, zz):
+        return vrs_propagate(E[0], E[1], x, y, wavelength, zz)
+
+    def BB(E, b, z1, z2):
+        lx, ly, _ = building_block(E[0], E[1], x, y, wavelength, ph[b][0], ph[b][1], z1, eta[b], th[b])
+        return V((lx, ly), z2)
+
+    def BS(a, b, t):
+        cx, cy, dx, dy = bs_symmetric(a[0], a[1], b[0], b[1], t)
+        return (cx, cy), (dx, dy)
+
+    def det(E):
+        return vczt_objective_lens(E[0], E[1], x, y, wavelength, r, f, xout, yout)
+
+    c1, d1 = BS(src, src, bs[0])
+    b2 = BB(c1, 0, z[0][0], z[0][1])
+    c2, d2 = BS(src, b2, bs[1])
+    b3 = V(c2, z[1][0] + z[1][1])
+    c3, d3 = BS(src, b3, bs[2])
+    det1 = det(V(c3, z[2][0] + z[2][1]))
+    a5, a6 = V(d2, z4), V(d3, z4)
+    c4, d4 = BS(d1, src, bs[3])
+    b5 = V(c4, z[0][0] + z[0][1])
+    c5, d5 = BS(a5, b5, bs[4])
+    b6 = BB(c5, 1, z[1][0], z[1][1])
+    c6, d6 = BS(a6, b6, bs[5])
+    det2 = det(V(c6, z[2][0] + z[2][1]))
+    a8, a9 = V(d5, z5), V(d6, z5)
+    c7, d7 = BS(d4, src, bs[6])
+    b8 = V(c7, z[0][0] + z[0][1])
+    c8, d8 = BS(a8, b8, bs[7])
+    b9 = V(c8, z[1][0] + z[1][1])
+    c9, d9 = BS(a9, b9, bs[8])
+    det3 = det(BB(c9, 2, z[2][0], z[2][1]))
+    dets = [det1, det2, det3, det(d7), det(d8), det(d9)]
+    return torch.stack([torch.abs(d[2]) ** 2 for d in dets])

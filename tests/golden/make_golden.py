@@ -225,6 +225,48 @@ def main(ref_root):
               R=0.3, T=0.7, phase=1.1, b1Ex=b1.Ex, b1Ey=b1.Ey, b2Ex=b2.Ex, b2Ey=b2.Ey,
               i_ex=i_ex, i_dep=i_dep, beta=0.8, fluorescence=fl, vfluorophores=vfl)
 
+        # 13. the prebuilt hybrid tables on a small grid (32 x 32, 16 x 16 focus).
+        n = 32
+        x, y = tb.space(2500.0, n)
+        xo, yo = tb.space(10.0, 16)
+        r_lens, f_lens = 1800.0, 2000.0
+        red = PolarizedLightSource(x, y, 0.65)
+        red.gaussian_beam(w0=(1200.0, 1200.0), jones_vector=(1, 1))
+        green = PolarizedLightSource(x, y, 0.532)
+        green.gaussian_beam(w0=(1200.0, 1200.0), jones_vector=(1, -1))
+
+        def scal(k):
+            return rng.uniform(0, 1, (k, 1))
+
+        p_sharp = [rng.uniform(0, 1, (n, n)) if (k % 6) in (0, 1) and k < 18 else scal(1)[0] for k in range(29)]
+        i_sharp, _ = oe.hybrid_setup_sharp_focus(red, red, red, red, red, red, p_sharp, [r_lens, f_lens, xo, yo])
+        i_sted = oe.hybrid_setup_fluorophores(red, green, red, green, red, green, p_sharp, [r_lens, f_lens, xo, yo],
+                                              distance_offset=10)
+        pms = [rng.uniform(-np.pi, np.pi, (n, n)) for _ in range(6)]
+        p_fixed = [scal(1)[0] for _ in range(25)]
+        fixed = [r_lens, f_lens, xo, yo] + pms
+        i_fixed, _ = oe.hybrid_setup_fixed_slms(red, red, red, red, red, red, p_fixed, fixed)
+        i_fixed_sted = oe.hybrid_setup_fixed_slms_fluorophores(red, green, red, green, red, green, p_fixed, fixed)
+        p_robust = [rng.uniform(0, 1, (n, n)) if (k % 8) in (0, 1, 2, 3) and k < 24 else scal(1)[0]
+                    for k in range(35)]
+        nz = [rng.normal(0, 50.0, 1) for _ in range(8)]
+        ns = [rng.normal(0, 0.1, (n, n)) for _ in range(6)]
+        nw = [rng.normal(0, 0.05, 1) for _ in range(6)]
+        na = [rng.normal(0, 0.02, (n, n)) for _ in range(6)]
+        i_robust = oe.robust_discovery(red, red, red, red, red, red, p_robust, [r_lens, f_lens, xo, yo], nz, ns, nw, na)
+        p_six = [scal(1)[0] for _ in range(52)]
+        six_fixed = [r_lens, f_lens, xo, yo] + pms[:4]
+        i_six = oe.six_times_six_ansatz(*([red] * 12), p_six, six_fixed, distance_offset=9.5)
+        _save("hybrid_tables", x=x, y=y, xout=xo, yout=yo, r=r_lens, f=f_lens, red_Ex=red.Ex, red_Ey=red.Ey,
+              green_Ex=green.Ex, green_Ey=green.Ey,
+              **{f"p_sharp_{k}": v for k, v in enumerate(p_sharp)}, i_sharp=i_sharp, i_sted=i_sted,
+              **{f"pm_{k}": v for k, v in enumerate(pms)}, **{f"p_fixed_{k}": v for k, v in enumerate(p_fixed)},
+              i_fixed=i_fixed, i_fixed_sted=i_fixed_sted,
+              **{f"p_robust_{k}": v for k, v in enumerate(p_robust)},
+              **{f"noise_d_{k}": v for k, v in enumerate(nz)}, **{f"noise_s_{k}": v for k, v in enumerate(ns)},
+              **{f"noise_w_{k}": v for k, v in enumerate(nw)}, **{f"noise_a_{k}": v for k, v in enumerate(na)},
+              i_robust=i_robust, **{f"p_six_{k}": v for k, v in enumerate(p_six)}, i_six=i_six)
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

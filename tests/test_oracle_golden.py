@@ -202,3 +202,17 @@ def test_beam_splitters_and_fluorescence():
     fl = ref.fluorescence(g["i_ex"][0], g["i_dep"][0], float(g["beta"]))
     assert rel_l2(fl, g["fluorescence"]) < 1e-14
     assert rel_l2(ref.fluorescence(g["i_ex"], g["i_dep"]), g["vfluorophores"]) < 1e-14
+
+
+def test_torch_restatement_of_the_sharp_focus_table():
+    """The step-by-step complex128 restatement of hybrid_setup_sharp_focus (the
+    table's gradient oracle) against the reference's own output."""
+    import torch
+
+    from oracle import torch_ref as tr
+    g = golden("hybrid_tables")
+    src = (torch.as_tensor(g["red_Ex"]), torch.as_tensor(g["red_Ey"]))
+    params = [g[f"p_sharp_{k}"] for k in range(29)]
+    I = tr.hybrid_setup_sharp_focus(src, g["x"], g["y"], 0.65, params, float(g["r"]), float(g["f"]), g["xout"],
+                                    g["yout"])
+    assert rel_l2(I.numpy(), g["i_sharp"]) < 1e-9   # 16 chained propagations of rounding

@@ -241,7 +241,8 @@ class _BeamSplitter(torch.autograd.Function):
         gm = None
         if want_m:
             gm = torch.conj(s)
-            gm = gm.sum(0) if m.dim() == 2 else gm
+            if gm.shape != m.shape:       # one matrix for the batch
+                gm = gm.sum(0).reshape(m.shape)
             gm = gm.to(m.dtype)
         out = [gm, None, None, None, None]
         if ga is not None:

@@ -216,7 +216,7 @@ def quality_factor(x, y, wavelength, z):
 class JonesOp:
     """One per-pixel operation of a fused program (see XL_OP_* in xlgb.h)."""
 
-    __slots__ = ("kind", "params", "ptrs", "sval", "dval", "keep")
+    __slots__ = ("kind", "params", "ptrs", "sval", "dval", "keep", "planes")
 
     def __init__(self, kind, params=(), ptrs=(), sval=(), dval=(), keep=()):
         self.kind = kind
@@ -225,15 +225,27 @@ class JonesOp:
         self.sval = list(sval)
         self.dval = list(dval)
         self.keep = list(keep)
+        self.planes = {}             # slot -> plane a one-element tensor parameter was expanded to
+
+    @staticmethod
+    def is_scalar_tensor(p) -> bool:
+        """A one-element tensor parameter (a trainable global setting): it is
+        expanded to a plane for the launch and its gradient is the plane's sum."""
+        return isinstance(p, torch.Tensor) and p.dim() < 2 and p.numel() == 1
 
     def fill(self, op: _lib.XlOp, ny: int, nx: int) -> None:
         op.kind = self.kind
         pmask = 0
         pbstride = 0
         for i, p in enumerate(self.params):
-            if isinstance(p, torch.Tensor) and p.dim() < 2:
-                raise ValueError("a mask parameter must be a scalar or an (ny, nx) plane; a 0-d tensor "
-                                 "that requires grad must be expanded to the plane by the caller")
+            if self.is_scalar_tensor(p):
+                plane = self.planes.get(i)
+                if plane is None or plane.shape != (ny, nx):
+                    plane = p.detach().to(torch.float32).reshape(1, 1).expand(ny, nx).contiguous()
+                    self.planes[i] = plane
+                p = keep_for_capture(plane)
+            elif isinstance(p, torch.Tensor) and p.dim() < 2:
+                raise ValueError("a mask parameter must be a scalar, a one-element tensor or an (ny, nx) plane")
             if isinstance(p, torch.Tensor):
                 if p.shape[-2:] != (ny, nx):
                     raise ValueError(f"mask parameter has shape {tuple(p.shape)}, field is {(ny, nx)}")
@@ -384,12 +396,17 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
            for i in range(C)]
     pgrad = (ctypes.c_void_p * (_lib.XL_MAX_OPS * 4))()
     grads = {}
+    scalars = []
     for k, o in enumerate(ops):
         for q, p in enumerate(o.params):
             if isinstance(p, torch.Tensor):
                 if not p.requires_grad:
                     continue
-                t = torch.empty(p.shape, dtype=torch.float32, device=dev)
+                if JonesOp.is_scalar_tensor(p):
+                    t = torch.empty((ny, nx), dtype=torch.float32, device=dev)
+                    scalars.append((k, q, p.shape))
+                else:
+                    t = torch.empty(p.shape, dtype=torch.float32, device=dev)
             else:
                 continue
             grads[(k, q)] = t
@@ -401,6 +418,8 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
     gi = (ctypes.c_void_p * 3)(*[(g.data_ptr() if g is not None else 0) for g in gin] + [0] * (3 - C))
     _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ibs, go, ny * nx, gi, ny * nx,
                                  ctypes.byref(prog), pgrad), "xl_ops_backward")
+    for k, q, shape in scalars:
+        grads[(k, q)] = grads[(k, q)].sum().reshape(shape)
     return gin, grads
 
 
@@ -859,6 +878,8 @@ def _bs_args(a, b, m, ny, nx):
     B, lead = _bs_batch(a, b, m)
     pa, sa = _bs_port(a, B, ny, nx)
     pb, sb = _bs_port(b, B, ny, nx)
+    if m.dim() == 3 and m.shape[0] == 1:
+        m = m[0]
     if m.dim() == 3 and m.shape[0] != B:
         raise ValueError(f"{m.shape[0]} splitter matrices for a batch of {B}")
     m = m.to(torch.complex64).contiguous()

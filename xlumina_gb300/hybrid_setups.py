@@ -1,0 +1,309 @@
+"""The prebuilt large-scale optical tables of optical_elements.py:964-2120.
+
+Each reference table is a grid of lossy beam splitters (``BS_symmetric``)
+whose outputs travel right (port c) and down (port d) to the next splitters,
+with free-space propagation or a building block on each edge, and
+objective-lens detectors at the grid's edges.  Here every table is written as
+data -- its sources, splitter angles, edges and detectors -- and one grid
+executor runs it:
+
+* splitter (i, j) takes ``a`` from above (a top source in row 0, else the d
+  port of splitter (i-1, j) through the vertical edge) and ``b`` from the
+  left (a left source in column 0, else the c port of (i, j-1) through the
+  horizontal edge); with one input absent it is ``BS_symmetric_SI`` on the
+  matching port (port 0 for ``a``, port 1 for ``b``);
+* an edge is ``None`` (the light passes unchanged), a VRS over a distance, or
+  a building block (sSLM [with amplitude] -> VRS -> LCD) followed by a VRS;
+* a detector is ``VCZT_objective_lens`` of a splitter port, optionally after a
+  VRS.
+
+Distances, angles and mask settings follow the reference's parametrisation
+(``(|p| * 100 + offset) cm`` and ``p * 2 pi - pi``) and may be tensors that
+require grad: the gradients of splitter angles, distances, LCD settings and
+phase masks all run through the hand-written adjoints.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import cm
+
+# ------------------------------------------------------------ parameters --
+
+
+def _abs(p):
+    return torch.abs(p) if isinstance(p, torch.Tensor) else np.abs(p)
+
+
+def _angle(p):
+    """optical_elements.py:1041-1056 etc.: a raw parameter in (0, 1) to (-pi, pi)."""
+    return p * 2 * np.pi - np.pi
+
+
+def _dist(p, offset):
+    """optical_elements.py:1039-1040 etc.: (|p| * 100 + offset) cm, in float64
+    (a float32 distance of 10 cm is off by ~0.01 um, a tenth of a radian of
+    phase at visible wavelengths)."""
+    if isinstance(p, torch.Tensor):
+        p = p.to(torch.float64)
+    return (_abs(p) * 100 + offset) * cm
+
+
+# ----------------------------------------------------------------- edges --
+
+def vrs(z):
+    """Edge: free-space VRS over ``z``."""
+    return ("vrs", z)
+
+
+def block(alpha, phi, z1, eta, theta, z2):
+    """Edge: building_block (sSLM -> VRS(z1) -> LCD) then VRS(z2), optical_elements.py:919-939."""
+    return ("bb", alpha, phi, z1, eta, theta, z2)
+
+
+def block_amp(alpha, phi, a1, a2, z1, eta, theta, z2):
+    """Edge: bb_amplitude_and_phase_mod then VRS(z2), optical_elements.py:894-917."""
+    return ("bba", alpha, phi, a1, a2, z1, eta, theta, z2)
+
+
+def _run_edge(edge, light):
+    from . import optical_elements as oe
+    if edge is None:
+        return light
+    kind = edge[0]
+    if kind == "vrs":
+        return light.VRS_propagation(edge[1])[0]
+    if kind == "bb":
+        _, alpha, phi, z1, eta, theta, z2 = edge
+        return oe.building_block(light, alpha, phi, z1, eta, theta).VRS_propagation(z2)[0]
+    if kind == "bba":
+        _, alpha, phi, a1, a2, z1, eta, theta, z2 = edge
+        return oe.bb_amplitude_and_phase_mod(light, alpha, phi, a1, a2, z1, eta, theta).VRS_propagation(z2)[0]
+    raise ValueError(f"unknown edge {kind!r}")
+
+
+# -------------------------------------------------------------- executor --
+
+def _splitter(a, b, theta):
+    from . import optical_elements as oe
+    if a is not None and b is not None:
+        return oe.BS_symmetric(a, b, theta)
+    if a is not None:
+        return oe.BS_symmetric_SI(a, theta, port=0)
+    if b is not None:
+        return oe.BS_symmetric_SI(b, theta, port=1)
+    raise ValueError("a splitter of the table has no input")
+
+
+def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, yout):
+    """Run a splitter grid.
+
+    top[j] / left[i]: source lights entering splitters (0, j) from above and
+    (i, 0) from the left (None: no source); thetas[i][j]: splitter angles;
+    horizontal[i][j]: the edge from (i, j)'s c port to (i, j+1);
+    vertical[i][j]: the edge from (i, j)'s d port to (i+1, j); detectors: list
+    of (i, j, port 'c' or 'd', edge).  Returns the detectors' lights."""
+    from . import optical_elements as oe
+    rows, cols = len(thetas), len(thetas[0])
+    ports = {}
+    for i in range(rows):
+        for j in range(cols):
+            a = top[j] if i == 0 else _run_edge(vertical[i - 1][j], ports[(i - 1, j)][1])
+            b = left[i] if j == 0 else _run_edge(horizontal[i][j - 1], ports[(i, j - 1)][0])
+            ports[(i, j)] = _splitter(a, b, thetas[i][j])
+    out = []
+    for i, j, port, edge in detectors:
+        light = ports[(i, j)][0 if port == "c" else 1]
+        out.append(oe.VCZT_objective_lens(_run_edge(edge, light), r, f, xout, yout))
+    return out
+
+
+def _ez_intensities(dets):
+    return torch.stack([torch.abs(d.Ez) ** 2 for d in dets])
+
+
+def _fluorescence_from(dets_ex, dets_dep):
+    """optical_elements.py:1324-1345: normalised |Ex|^2 + |Ey|^2 of the
+    excitation and depletion detectors, then the fluorescence model."""
+    from . import optical_elements as oe
+
+    def norm(d):
+        i = torch.abs(d.Ex) ** 2 + torch.abs(d.Ey) ** 2
+        return i / torch.sum(i)
+    iex = torch.stack([norm(d) for d in dets_ex])
+    idep = torch.stack([norm(d) for d in dets_dep])
+    return oe.vectorized_fluorophores(iex, idep)
+
+
+def _grid_3x3(thetas9):
+    return [thetas9[0:3], thetas9[3:6], thetas9[6:9]]
+
+
+_DETECTORS_3X3 = [(0, 2, "c"), (1, 2, "c"), (2, 2, "c"), (2, 0, "d"), (2, 1, "d"), (2, 2, "d")]
+
+
+def _detectors(outs):
+    return [(i, j, port, e) for (i, j, port), e in zip(_DETECTORS_3X3, list(outs) + [None] * 3)]
+
+
+# ---------------------------------------------------------------- tables --
+
+def _sharp_focus_edges(ph, eta, theta, z, z4, z5, block_edge):
+    """The edges shared by robust_discovery, hybrid_setup_sharp_focus and
+    hybrid_setup_fluorophores (optical_elements.py:1063-1094, 1595-1626,
+    1742-1823): building blocks on (0,0)->(0,1), (1,1)->(1,2) and before
+    detector 3; VRS(z4) / VRS(z5) down the middle and right columns."""
+    (z11, z12), (z21, z22), (z31, z32) = z
+    horizontal = [[block_edge(0, z11, z12), vrs(z21 + z22)],
+                  [vrs(z11 + z12), block_edge(1, z21, z22)],
+                  [vrs(z11 + z12), vrs(z21 + z22)]]
+    vertical = [[None, vrs(z4), vrs(z4)],
+                [None, vrs(z5), vrs(z5)]]
+    outs = [vrs(z31 + z32), vrs(z31 + z32), block_edge(2, z31, z32)]
+    return horizontal, vertical, outs
+
+
+def _fixed_slms_edges(ph, eta, theta, z):
+    """The edges of hybrid_setup_fixed_slms and its fluorophore variant
+    (optical_elements.py:1449-1478, 1219-1307): fixed phase masks on
+    (0,0)->(0,1), (1,1)->(1,2), (0,2)->(1,2) and (1,0)->(2,0)."""
+    (z11, z12), (z21, z22), (z31, z32), (z41, z42) = z
+    horizontal = [[block(ph[0][0], ph[0][1], z11, eta[0], theta[0], z12), vrs(z21 + z22)],
+                  [vrs(z11 + z12), block(ph[1][0], ph[1][1], z21, eta[1], theta[1], z22)],
+                  [vrs(z11 + z12), vrs(z21 + z22)]]
+    vertical = [[None, vrs(z31 + z32), block(ph[2][0], ph[2][1], z31, eta[2], theta[2], z32)],
+                [block(ph[3][0], ph[3][1], z41, eta[3], theta[3], z42), vrs(z41 + z42), vrs(z41 + z42)]]
+    return horizontal, vertical, [None, None, None]
+
+
+def _unpack_blocks(parameters, offset, n_blocks=3):
+    """[phase_1, phase_2, eta, theta, z_1, z_2] per block (optical_elements.py:1553-1576)."""
+    ph, eta, theta, z = [], [], [], []
+    for b in range(n_blocks):
+        p = parameters[6 * b:6 * b + 6]
+        ph.append((_angle(p[0]), _angle(p[1])))
+        eta.append(_angle(p[2]))
+        theta.append(_angle(p[3]))
+        z.append((_dist(p[4], offset), _dist(p[5], offset)))
+    return ph, eta, theta, z
+
+
+def robust_discovery(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, noise_distances, noise_slms,
+                     noise_wps, noise_amps, distance_offset=15):
+    """optical_elements.py:964-1117: the 3x3 table with amplitude-and-phase
+    building blocks and noise on every setting; returns the detectors' |Ez|^2."""
+    r, f, xout, yout = fixed_params[0:4]
+    ph, amp, eta, theta, z = [], [], [], [], []
+    for b in range(3):
+        p = parameters[8 * b:8 * b + 8]
+        ph.append((_angle(p[0]) + noise_slms[2 * b], _angle(p[1]) + noise_slms[2 * b + 1]))
+        amp.append((p[2] + noise_amps[2 * b], p[3] + noise_amps[2 * b + 1]))
+        eta.append(_angle(p[4]) + noise_wps[2 * b])
+        theta.append(_angle(p[5]) + noise_wps[2 * b + 1])
+        z.append((_dist(p[6], distance_offset) + noise_distances[2 * b],
+                  _dist(p[7], distance_offset) + noise_distances[2 * b + 1]))
+    thetas = [_angle(parameters[24 + k]) for k in range(9)]
+    z4 = _dist(parameters[33], distance_offset) + noise_distances[6]
+    z5 = _dist(parameters[34], distance_offset) + noise_distances[7]
+
+    def blk(b, z1, z2):
+        return block_amp(ph[b][0], ph[b][1], amp[b][0], amp[b][1], z1, eta[b], theta[b], z2)
+    horizontal, vertical, outs = _sharp_focus_edges(ph, eta, theta, z, z4, z5, blk)
+    dets = run_grid([ls1, ls2, ls3], [ls4, ls5, ls6], _grid_3x3(thetas), horizontal, vertical,
+                    _detectors(outs), r, f, xout, yout)
+    return _ez_intensities(dets)
+
+
+def hybrid_setup_sharp_focus(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9):
+    """optical_elements.py:1503-1649: returns (stacked |Ez|^2 of the six
+    detectors, the detectors' lights)."""
+    r, f, xout, yout = fixed_params[0:4]
+    ph, eta, theta, z = _unpack_blocks(parameters, distance_offset)
+    thetas = [_angle(parameters[18 + k]) for k in range(9)]
+    z4, z5 = _dist(parameters[27], distance_offset), _dist(parameters[28], distance_offset)
+
+    def blk(b, z1, z2):
+        return block(ph[b][0], ph[b][1], z1, eta[b], theta[b], z2)
+    horizontal, vertical, outs = _sharp_focus_edges(ph, eta, theta, z, z4, z5, blk)
+    dets = run_grid([ls1, ls2, ls3], [ls4, ls5, ls6], _grid_3x3(thetas), horizontal, vertical,
+                    _detectors(outs), r, f, xout, yout)
+    return _ez_intensities(dets), dets
+
+
+def hybrid_setup_fluorophores(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9):
+    """optical_elements.py:1651-1853: the sharp-focus table run twice, the
+    depletion beam (ls1, ls3, ls5) and the excitation beam (ls2, ls4, ls6)
+    entering different ports; returns the fluorescence of the six detectors."""
+    r, f, xout, yout = fixed_params[0:4]
+    ph, eta, theta, z = _unpack_blocks(parameters, distance_offset)
+    thetas = _grid_3x3([_angle(parameters[18 + k]) for k in range(9)])
+    z4, z5 = _dist(parameters[27], distance_offset), _dist(parameters[28], distance_offset)
+
+    def blk(b, z1, z2):
+        return block(ph[b][0], ph[b][1], z1, eta[b], theta[b], z2)
+    horizontal, vertical, outs = _sharp_focus_edges(ph, eta, theta, z, z4, z5, blk)
+    dets_r = run_grid([ls1, None, ls3], [None, ls5, None], thetas, horizontal, vertical, _detectors(outs),
+                      r, f, xout, yout)
+    dets_g = run_grid([None, ls2, None], [ls4, None, ls6], thetas, horizontal, vertical, _detectors(outs),
+                      r, f, xout, yout)
+    return _fluorescence_from(dets_g, dets_r)
+
+
+def _fixed_slms_params(parameters, fixed_params, offset):
+    ph = [(fixed_params[4], fixed_params[5]), (fixed_params[6], fixed_params[6]),
+          (fixed_params[7], fixed_params[7]), (fixed_params[8], fixed_params[9])]
+    z = [(_dist(parameters[2 * b], offset), _dist(parameters[2 * b + 1], offset)) for b in range(4)]
+    thetas = _grid_3x3([_angle(parameters[8 + k]) for k in range(9)])
+    eta = [_angle(parameters[17 + 2 * b]) for b in range(4)]
+    theta = [_angle(parameters[18 + 2 * b]) for b in range(4)]
+    return ph, z, thetas, eta, theta
+
+
+def hybrid_setup_fixed_slms(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9):
+    """optical_elements.py:1347-1501: fixed phase masks (fixed_params[4:10]) at
+    four places of the 3x3 table; returns (stacked |Ez|^2, detectors)."""
+    r, f, xout, yout = fixed_params[0:4]
+    ph, z, thetas, eta, theta = _fixed_slms_params(parameters, fixed_params, distance_offset)
+    horizontal, vertical, outs = _fixed_slms_edges(ph, eta, theta, z)
+    dets = run_grid([ls1, ls2, ls3], [ls4, ls5, ls6], thetas, horizontal, vertical, _detectors(outs),
+                    r, f, xout, yout)
+    return _ez_intensities(dets), dets
+
+
+def hybrid_setup_fixed_slms_fluorophores(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params,
+                                         distance_offset=8.9):
+    """optical_elements.py:1119-1345: the fixed-mask table for the depletion
+    (ls1, ls3, ls5) and excitation (ls2, ls4, ls6) beams; returns the
+    fluorescence of the six detectors."""
+    r, f, xout, yout = fixed_params[0:4]
+    ph, z, thetas, eta, theta = _fixed_slms_params(parameters, fixed_params, distance_offset)
+    horizontal, vertical, outs = _fixed_slms_edges(ph, eta, theta, z)
+    dets_r = run_grid([ls1, None, ls3], [None, ls5, None], thetas, horizontal, vertical, _detectors(outs),
+                      r, f, xout, yout)
+    dets_g = run_grid([None, ls2, None], [ls4, None, ls6], thetas, horizontal, vertical, _detectors(outs),
+                      r, f, xout, yout)
+    return _fluorescence_from(dets_g, dets_r)
+
+
+def six_times_six_ansatz(ls1, ls2, ls3, ls4, ls5, ls6, ls7, ls8, ls9, ls10, ls11, ls12, parameters, fixed_params,
+                         distance_offset=7.6):
+    """optical_elements.py:1855-2120: a 6x6 splitter grid with two fixed-mask
+    building blocks; returns the |Ez|^2 of its twelve detectors (the right
+    column's c ports, the bottom row's c ports of columns 0-4 -- which also
+    travel on to the right, as in the reference -- and the last d port)."""
+    r, f, xout, yout = fixed_params[0:4]
+    (p11, p12, p21, p22) = fixed_params[4:8]
+    z = [_dist(parameters[k], distance_offset) for k in range(12)]
+    bs = [_angle(parameters[12 + k]) for k in range(36)]
+    eta1, theta1, eta2, theta2 = (_angle(parameters[48 + k]) for k in range(4))
+    thetas = [bs[6 * i:6 * i + 6] for i in range(6)]
+    row = [vrs(z[0]), vrs(z[1] + z[2]), vrs(z[3]), vrs(z[4] + z[5]), vrs(z[6])]
+    horizontal = [list(row) for _ in range(6)]
+    horizontal[1][1] = block(p11, p12, z[1], eta1, theta1, z[2])
+    horizontal[3][3] = block(p21, p22, z[4], eta2, theta2, z[5])
+    vertical = [[vrs(z[7 + i])] * 6 for i in range(5)]
+    detectors = [(i, 5, "c", None) for i in range(6)] + [(5, j, "c", None) for j in range(5)] + [(5, 5, "d", None)]
+    dets = run_grid([ls1, ls2, ls3, ls4, ls5, ls6], [ls7, ls8, ls9, ls10, ls11, ls12], thetas, horizontal,
+                    vertical, detectors, r, f, xout, yout)
+    return _ez_intensities(dets)

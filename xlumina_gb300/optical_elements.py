@@ -290,3 +290,10 @@ def vectorized_fluorophores(i_ex, i_dep):
     """optical_elements.py:956-962: fluorescence over a stack of detectors
     (the vmap over the leading axis is the elementwise expression itself)."""
     return fluorescence(i_ex, i_dep)
+
+
+# The prebuilt large-scale tables (optical_elements.py:964-2120) live in
+# hybrid_setups.py; exported here under the reference's names.
+from .hybrid_setups import (hybrid_setup_fixed_slms, hybrid_setup_fixed_slms_fluorophores,  # noqa: E402,F401
+                            hybrid_setup_fluorophores, hybrid_setup_sharp_focus, robust_discovery,
+                            six_times_six_ansatz)
