@@ -349,6 +349,8 @@ def run_gpu(args):
         line["czt_high_na"] = run_czt()
         torch.cuda.empty_cache()
         line["fwd_bwd"] = run_fwd_bwd()
+        torch.cuda.empty_cache()
+        line["hybrid_sharp_focus"] = run_hybrid()
     if not args.no_serving:
         line["uneven_batch"] = run_uneven()
         line["serving"] = run_serving(args.serve_requests)
@@ -477,6 +479,29 @@ def run_fwd_bwd(steps=10, warmup=3):
                       "batch": B}
     torch.cuda.empty_cache()
     return out
+
+
+def run_hybrid(steps=5, warmup=2):
+    """The hybrid sharp-focus discovery step (9 splitters, 16 VRS and 6
+    objective-lens focuses at 1024^2, every distance, angle, LCD setting and
+    phase mask trainable): fwd + bwd + AdamW per step."""
+    import torch
+
+    from xlumina_gb300.plans import CapturedStep
+    from xlumina_gb300.tables import SharpFocusTable
+    t = SharpFocusTable()
+    dt = _time_steps(t.step, steps, warmup)
+    del t
+    torch.cuda.empty_cache()
+    t = SharpFocusTable(capturable=True)
+    cs = CapturedStep(t)
+    dtc = _time_steps(cs, steps, 2)
+    del cs, t
+    torch.cuda.empty_cache()
+    return {"workload": "hybrid_setup_sharp_focus 1024^2 (2.5 mm, 635 nm) -> 6 x VCZT objective lens 400^2 "
+                        "(10 um, NA 0.9), softmin(vectorized_loss_hybrid), AdamW over 29 parameters",
+            "steps_per_s": 1.0 / dt, "ms_per_step": dt * 1e3, "captured_steps_per_s": 1.0 / dtc,
+            "captured_ms_per_step": dtc * 1e3}
 
 
 def run_uneven(reps=20, seed=6000):
@@ -632,11 +657,15 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--only", choices=["czt"], default=None,
-                    help="run one section alone (for profiling): czt = the high-NA focus")
+    ap.add_argument("--only", choices=["czt", "hybrid"], default=None,
+                    help="run one section alone (for profiling): czt = the high-NA focus, "
+                         "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
     if args.only == "czt":
         print(json.dumps({"czt_high_na": run_czt(batch=args.batch, steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only == "hybrid":
+        print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -92,6 +92,17 @@ int xl_init(void);
 int xl_rs_transfer_spectrum_dz(void* stream, int ny, int nx, const double* offx, const double* offy,
                                double z, double wavelength, double scale, void* spectrum, void* work);
 
+/* Transfer spectra (dz = 0) or their z-derivatives (dz = 1) for `count`
+ * distances held in device memory (z[0 .. count-1], float64), written
+ * spectrum_stride complex64 elements apart: what xl_rs_transfer_spectrum /
+ * xl_rs_transfer_spectrum_dz give per distance, without reading the distances
+ * back to the host, so that a distance being optimised stays on the device
+ * and the call can be captured in a CUDA graph.  A distance of 0 gives NaN at
+ * the zero offset, as the reference's formula (wave_optics.py:291-297). */
+int xl_rs_transfer_spectra_device_z(void* stream, int ny, int nx, const double* offx, const double* offy,
+                                    const double* z, int count, double wavelength, double scale, int dz,
+                                    void* spectra, long long spectrum_stride, void* work);
+
 /* Bytes of one transfer spectrum for an ny x nx field: (2Q)^2 complex64,
  * Q = next power of two >= max(ny, nx). */
 size_t xl_rs_spectrum_bytes(int ny, int nx);

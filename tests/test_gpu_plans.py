@@ -77,7 +77,7 @@ def test_captured_table_step_matches_eager_steps():
     for _ in range(3):     # the capture's warm-up steps
         eager.step()
     for _ in range(4):
-        le = float(eager.step())
+        le = float(eager.step().detach())
         lc = float(step())
         assert abs(le - lc) <= 1e-5 * abs(le) + 1e-12, (le, lc)
     assert torch.allclose(eager.phase1, capt.phase1, rtol=1e-5, atol=1e-6)
@@ -96,9 +96,32 @@ def test_vrs_lcd_table_captured_matches_eager():
         eager.step()
     l0 = None
     for _ in range(4):
-        le = float(eager.step())
+        le = float(eager.step().detach())
         lc = float(step())
         l0 = le if l0 is None else l0
         assert abs(le - lc) <= 1e-5 * abs(le) + 1e-12, (le, lc)
     assert le < l0
     assert torch.allclose(eager.eta, capt.eta, rtol=1e-5, atol=1e-6)
+
+
+def test_captured_hybrid_table_step_matches_eager():
+    """The sharp-focus discovery step (trainable distances, splitter angles,
+    LCD settings and masks) records into one CUDA graph: distances stay on the
+    device, so nothing in the step reads back to the host."""
+    import torch
+
+    from xlumina_gb300.plans import CapturedStep
+    from xlumina_gb300.tables import SharpFocusTable
+    kw = dict(n=128, roi_n=48, seed=7)
+    eager = SharpFocusTable(**kw, capturable=True)
+    cap = SharpFocusTable(**kw, capturable=True)
+    for a, b in zip(eager.params, cap.params):
+        b.data.copy_(a.data)
+    cs = CapturedStep(cap, warmup=3)
+    for _ in range(3):          # the warm-up steps the plan took
+        eager.step()
+    le = [float(eager.step().detach()) for _ in range(3)]
+    lc = [float(cs().detach()) for _ in range(3)]
+    assert all(abs(a - b) <= 1e-4 * abs(a) for a, b in zip(le, lc)), (le, lc)
+    for a, b in zip(eager.params, cap.params):
+        assert torch.allclose(a, b, rtol=1e-4, atol=1e-5)

@@ -81,6 +81,11 @@ SIGNATURES = {
     "xl_rs_transfer_spectrum_dz": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
                                                   ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_rs_transfer_spectra_device_z": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                       ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                                       ctypes.c_void_p]),
     "xl_re_inner": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
                                    ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
                                    ctypes.c_void_p]),

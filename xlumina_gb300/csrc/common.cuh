@@ -18,24 +18,70 @@ static __device__ float2 g_tw[2 * XL_MAX_FFT];
 
 __device__ __forceinline__ const float2* tw_table(int logn) { return g_tw + (1 << logn); }
 
-// e^{i 2 pi t}: the argument in turns is reduced in float64, then the
-// reduced fraction goes to sincospif (argument in [-1, 1]).
-__device__ __forceinline__ float2 cis_turns(double t) {
-  const double f = t - rint(t);
+// ---- float-float arithmetic: a value hi + lo held in two floats, ~48
+// significant bits (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2).  The RS phase
+// k r needs more than float precision (k r ~ 1e6 rad at 10 cm), and GB300's
+// FP64 rate is a small fraction of its FP32 rate.  The _rn intrinsics are
+// never contracted into FMAs, which would break the error terms.
+struct ffloat {
+  float hi, lo;
+};
+__device__ __forceinline__ ffloat ff_split(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ ffloat ff_fast_two_sum(float a, float b) {   // needs |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ffloat ff_add(ffloat x, ffloat y) {
+  const float s = __fadd_rn(x.hi, y.hi);
+  const float bb = __fsub_rn(s, x.hi);
+  const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+  return ff_fast_two_sum(s, __fadd_rn(e, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ ffloat ff_mul(ffloat x, ffloat y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  const float e = fmaf(x.hi, y.hi, -p);
+  return ff_fast_two_sum(p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e)));
+}
+// One Newton step from the float square root: r + (x - r^2) / (2 r), the
+// residual taken exactly by an FMA.
+__device__ __forceinline__ ffloat ff_sqrt(ffloat x) {
+  const float r = sqrtf(x.hi);
+  const float d = __fadd_rn(fmaf(-r, r, x.hi), x.lo);
+  return ff_fast_two_sum(r, __fdiv_rn(d, __fmul_rn(2.f, r)));
+}
+
+// r = sqrt(X^2 + Y^2 + z^2) in float-float and the fraction of r / lambda
+// (in turns, in [-0.5, 0.5]) that sets the phase.
+__device__ __forceinline__ void rs_distance(double X, double Y, double z, double inv_lambda, float* rf,
+                                            float* frac) {
+  const ffloat x = ff_split(X), y = ff_split(Y), zz = ff_split(z);
+  const ffloat s = ff_add(ff_add(ff_mul(zz, zz), ff_mul(y, y)), ff_mul(x, x));
+  const ffloat r = ff_sqrt(s);
+  const ffloat t = ff_mul(r, ff_split(inv_lambda));
+  float f = __fadd_rn(__fsub_rn(t.hi, rintf(t.hi)), t.lo);
+  f = __fsub_rn(f, rintf(f));
+  *rf = r.hi;
+  *frac = f;
+}
+
+// e^{i 2 pi f} for a fraction of a turn |f| <= 1/2.
+__device__ __forceinline__ float2 cis_frac(float f) {
   float s, c;
-  sincospif(2.0f * (float)f, &s, &c);
+  sincospif(2.0f * f, &s, &c);
   return make_float2(c, s);
 }
 
 // Rayleigh-Sommerfeld impulse response at offset (X, Y), distance z:
 // exp(+-i k r) * z / (2 pi r^2) * (1/r - i k), r = sqrt(X^2 + Y^2 + z^2);
-// the exponent's sign follows the sign of z.  r and k r are float64.
+// the exponent's sign follows the sign of z.  r and k r are float-float.
 __device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, double inv_lambda,
                                                   float k) {
-  const double r = sqrt(X * X + Y * Y + z * z);
-  const double t = r * inv_lambda;
-  const float2 e = cis_turns(z > 0 ? t : -t);
-  const float rf = (float)r;
+  float rf, f;
+  rs_distance(X, Y, z, inv_lambda, &rf, &f);
+  const float2 e = cis_frac(z > 0 ? f : -f);
   const float a = (float)z / (6.283185307179586f * rf * rf);
   return cmul(e, make_float2(a / rf, -a * k));
 }
@@ -52,10 +98,10 @@ __device__ __forceinline__ void phase_sincos(float x, float* s, float* c) { sinc
 // da/dz = ((1/r^3 - i k / r^2) + z^2 (-3/r^5 + 2 i k / r^4)) / (2 pi).
 __device__ __forceinline__ float2 rs_kernel_dz_value(double X, double Y, double z, double inv_lambda,
                                                      float k) {
-  const double r = sqrt(X * X + Y * Y + z * z);
-  const double t = r * inv_lambda;
-  const float2 e = cis_turns(z > 0 ? t : -t);
-  const float rf = (float)r, zf = (float)z, s = z > 0 ? 1.f : -1.f;
+  float rf, f;
+  rs_distance(X, Y, z, inv_lambda, &rf, &f);
+  const float2 e = cis_frac(z > 0 ? f : -f);
+  const float zf = (float)z, s = z > 0 ? 1.f : -1.f;
   const float ir = 1.f / rf, ir2 = ir * ir, ir3 = ir2 * ir;
   const float inv2pi = 0.15915494309189533577f;
   const float2 a = make_float2(zf * ir3 * inv2pi, -zf * k * ir2 * inv2pi);

@@ -45,8 +45,8 @@ extern "C" size_t xl_rs_work_bytes(int batch, int comps, int ny, int nx) {
 }
 
 static int transfer_spectrum(const char* what, void* stream, int ny, int nx, const double* offx,
-                             const double* offy, double z, double wavelength, double scale, void* spectrum,
-                             void* work, int dz) {
+                             const double* offy, double z, const double* zp, int count, long long sstride,
+                             double wavelength, double scale, void* spectrum, void* work, int dz) {
   if (ny < 2 || nx < 2 || ny > XL_MAX_SIDE || nx > XL_MAX_SIDE) {
     set_error("%s: field side out of range (2..%d): %d x %d", what, XL_MAX_SIDE, ny, nx);
     return XL_EINVAL;
@@ -55,33 +55,57 @@ static int transfer_spectrum(const char* what, void* stream, int ny, int nx, con
     set_error("%s: null pointer argument", what);
     return XL_EINVAL;
   }
-  if (!(z != 0.0) || !(wavelength > 0.0)) {
+  if ((!zp && !(z != 0.0)) || !(wavelength > 0.0)) {
     set_error("%s: need z != 0 and wavelength > 0 (got z=%g, wavelength=%g)", what, z, wavelength);
+    return XL_EINVAL;
+  }
+  if (count < 1 || (count > 1 && sstride < (long long)(xl_rs_spectrum_bytes(ny, nx) / sizeof(float2)))) {
+    set_error("%s: bad spectrum count %d or stride %lld", what, count, sstride);
     return XL_EINVAL;
   }
   if (int rc = ensure_init()) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int lq = rs_logq(ny, nx);
-#define CALL(L) rs_spectrum<L>(st, ny, nx, offx, offy, z, wavelength, scale, (float2*)spectrum, \
-                               (float2*)work, dz)
-  XL_RS_DISPATCH(lq, CALL)
+  for (int e = 0; e < count; ++e) {
+    float2* spec = (float2*)spectrum + (long long)e * sstride;
+    const double* zpe = zp ? zp + e : nullptr;
+    int rc = XL_EUNSUPPORTED;
+#define CALL(L) rc = rs_spectrum<L>(st, ny, nx, offx, offy, z, zpe, wavelength, scale, spec, (float2*)work, dz); break
+    switch (lq) {
+      case 4: CALL(4); case 5: CALL(5); case 6: CALL(6); case 7: CALL(7); case 8: CALL(8);
+      case 9: CALL(9); case 10: CALL(10); case 11: CALL(11); case 12: CALL(12);
+      default: set_error("%s: unsupported size", what);
+    }
 #undef CALL
-  set_error("%s: unsupported size", what);
-  return XL_EUNSUPPORTED;
+    if (rc) return rc;
+  }
+  return XL_OK;
 }
 
 extern "C" int xl_rs_transfer_spectrum(void* stream, int ny, int nx, const double* offx,
                                        const double* offy, double z, double wavelength,
                                        double scale, void* spectrum, void* work) {
-  return transfer_spectrum("xl_rs_transfer_spectrum", stream, ny, nx, offx, offy, z, wavelength, scale,
-                           spectrum, work, 0);
+  return transfer_spectrum("xl_rs_transfer_spectrum", stream, ny, nx, offx, offy, z, nullptr, 1, 0, wavelength,
+                           scale, spectrum, work, 0);
 }
 
 extern "C" int xl_rs_transfer_spectrum_dz(void* stream, int ny, int nx, const double* offx,
                                           const double* offy, double z, double wavelength,
                                           double scale, void* spectrum, void* work) {
-  return transfer_spectrum("xl_rs_transfer_spectrum_dz", stream, ny, nx, offx, offy, z, wavelength, scale,
-                           spectrum, work, 1);
+  return transfer_spectrum("xl_rs_transfer_spectrum_dz", stream, ny, nx, offx, offy, z, nullptr, 1, 0,
+                           wavelength, scale, spectrum, work, 1);
+}
+
+extern "C" int xl_rs_transfer_spectra_device_z(void* stream, int ny, int nx, const double* offx,
+                                               const double* offy, const double* z, int count, double wavelength,
+                                               double scale, int dz, void* spectra, long long spectrum_stride,
+                                               void* work) {
+  if (!z) {
+    set_error("xl_rs_transfer_spectra_device_z: null distance array");
+    return XL_EINVAL;
+  }
+  return transfer_spectrum("xl_rs_transfer_spectra_device_z", stream, ny, nx, offx, offy, 0.0, z, count,
+                           spectrum_stride, wavelength, scale, spectra, work, dz ? 1 : 0);
 }
 
 static int rs_run(void* stream, const XlRsArgs* a, int stage) {

@@ -37,7 +37,7 @@ inline int rs_logq(int ny, int nx) {
 // instantiated for LOGQ = 4..12 in the kernel translation units).
 template <int LOGQ>
 int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy, double z,
-                double wavelength, double scale, float2* spec, float2* work, int dz);
+                const double* zp, double wavelength, double scale, float2* spec, float2* work, int dz);
 template <int LOGQ>
 int rs_propagate(cudaStream_t st, const RsLaunch& p, int stage);
 

@@ -96,9 +96,10 @@ struct RowPtr {
 // DZ: the rows of dH/dz instead (the spectrum of the z-derivative).
 template <int LOGQ, bool DZ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
-    rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double z,
-                 double inv_lambda, float k, float2* __restrict__ out) {
+    rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double zh,
+                 const double* __restrict__ zp, double inv_lambda, float k, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
+  const double z = zp ? __ldg(zp) : zh;   // a distance in device memory, or the host's value
   extern __shared__ __align__(16) float2 smem[];
   const int tid = threadIdx.x;
   const int gi = tid / C::T, j = tid % C::T;
@@ -451,19 +452,19 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
 
 template <int LOGQ>
 int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const double* offy, double z,
-                double wavelength, double scale, float2* spec, float2* work, int dz) {
+                const double* zp, double wavelength, double scale, float2* spec, float2* work, int dz) {
   using C = RsCfg<LOGQ>;
   const size_t sm1 = (size_t)C::G * C::XS * sizeof(float2);
   const float k = (float)(2.0 * M_PI / wavelength);
   cudaError_t e;
   if (dz) {
     if ((e = allow_smem(rs_hhat_rows<LOGQ, true>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
-    rs_hhat_rows<LOGQ, true><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength,
-                                                                          k, work);
+    rs_hhat_rows<LOGQ, true><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, zp,
+                                                                          1.0 / wavelength, k, work);
   } else {
     if ((e = allow_smem(rs_hhat_rows<LOGQ, false>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
-    rs_hhat_rows<LOGQ, false><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, 1.0 / wavelength,
-                                                                           k, work);
+    rs_hhat_rows<LOGQ, false><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, zp,
+                                                                           1.0 / wavelength, k, work);
   }
   XL_CHECK_LAUNCH("rs_hhat_rows");
   const size_t sm2 = (size_t)C::CW * C::CXS * sizeof(float2);
@@ -547,6 +548,6 @@ int rs_propagate(cudaStream_t st, const RsLaunch& p, int stage) {
 }  // namespace xl
 
 #define XL_RS_INSTANTIATE(L)                                                                        \
-  template int xl::rs_spectrum<L>(cudaStream_t, int, int, const double*, const double*, double, double, \
-                                  double, float2*, float2*, int);                                  \
+  template int xl::rs_spectrum<L>(cudaStream_t, int, int, const double*, const double*, double,      \
+                                  const double*, double, double, float2*, float2*, int);           \
   template int xl::rs_propagate<L>(cudaStream_t, const RsLaunch&, int);

@@ -202,11 +202,17 @@ def rs_wrapped_offsets(x: np.ndarray, P: int) -> np.ndarray:
 
 
 def quality_factor(x, y, wavelength, z):
-    """wave_optics.py:187-191 / vectorized_optics.py:264-270."""
+    """wave_optics.py:187-191 / vectorized_optics.py:264-270 (a tensor distance
+    gives a device tensor, computed without a host read)."""
     dx = x[1] - x[0]
     dy = y[1] - y[0]
     dr_real = np.sqrt(dx ** 2 + dy ** 2)
     rmax = np.sqrt((x ** 2).max() + (y ** 2).max())
+    if isinstance(z, torch.Tensor):
+        z = z.detach().to(torch.float64)
+        return (torch.sqrt(wavelength ** 2 + rmax ** 2 + 2 * wavelength * torch.sqrt(rmax ** 2 + z ** 2)) -
+                rmax) / dr_real
+    z = np.asarray(z, dtype=np.float64)
     dr_ideal = np.sqrt(wavelength ** 2 + rmax ** 2 + 2 * wavelength * np.sqrt(rmax ** 2 + z ** 2)) - rmax
     return dr_ideal / dr_real
 
@@ -489,6 +495,35 @@ def build_rs_spectrum(x, y, z, wavelength, dz=False) -> torch.Tensor:
     return spec
 
 
+def device_z(z, B) -> torch.Tensor:
+    """A distance tensor as a contiguous float64 device array of 1 or B values
+    (never read back to the host)."""
+    zd = z.detach().to(device=device(), dtype=torch.float64).reshape(-1).contiguous()
+    if zd.numel() not in (1, B):
+        raise ValueError(f"{zd.numel()} distances for a batch of {B} fields")
+    return zd
+
+
+def build_rs_spectra_device(x, y, zd: torch.Tensor, wavelength, dz=False) -> torch.Tensor:
+    """Transfer spectra (or dH/dz spectra) for the distances of a device array,
+    one per entry, stacked: shape (len(zd), P*P).  No host synchronisation."""
+    L = lib()
+    ny, nx = len(y), len(x)
+    P = 2 << rs_logq(ny, nx)
+    dev = zd.device
+    offx = device_array(rs_wrapped_offsets(x, P), torch.float64)
+    offy = device_array(rs_wrapped_offsets(y, P), torch.float64)
+    n = zd.numel()
+    spec = torch.empty((n, P * P), dtype=torch.complex64, device=dev)
+    work = torch.empty(P * P, dtype=torch.complex64, device=dev)
+    scale = (x[1] - x[0]) * (y[1] - y[0]) / float(P * P)
+    _lib.check(L.xl_rs_transfer_spectra_device_z(stream_handle(), ny, nx, offx.data_ptr(), offy.data_ptr(),
+                                                 zd.data_ptr(), n, float(wavelength), scale, 1 if dz else 0,
+                                                 spec.data_ptr(), P * P, work.data_ptr()),
+               "xl_rs_transfer_spectra_device_z")
+    return spec
+
+
 class RsCall:
     """One prepared RS / VRS launch: arguments, outputs and the buffers they point at.
 
@@ -511,23 +546,33 @@ class RsCall:
             raise ValueError("RS takes one field, VRS takes (Ex, Ey) (adjoint: three gradients)")
         lead = comps[0].shape[:-2]
         comps, B, ibs = batch_planes(comps, ny, nx)
-        zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
-        uniq = sorted(set(zs))
-        specs = [SPECTRA.get(x, y, zz, wavelength, dz) for zz in uniq]
         dev = comps[0].device
-        spec_ptrs = None
-        if len(specs) == 1:
-            spec = specs[0]
-        else:   # one spectrum pointer per batch entry, no stacked copy
-            spec = None
-            spec_ptrs = device_array([specs[uniq.index(v)].data_ptr() for v in zs], torch.int64)
+        spec_ptrs = spec_index = None
+        if isinstance(z, torch.Tensor):
+            # distances on the device (e.g. being optimised): spectra built
+            # from them in this call, stacked one per distance
+            zd = device_z(z, B)
+            spec = build_rs_spectra_device(x, y, zd, wavelength, dz)
+            specs = [spec]
+            if zd.numel() > 1:
+                spec_index = device_array(np.arange(B, dtype=np.int32), torch.int32)
+            zt = (zd if zd.numel() == B else zd.expand(B).contiguous()) if vector else None
+        else:
+            zs = [float(v) for v in np.broadcast_to(np.asarray(z, dtype=np.float64), (B,))]
+            uniq = sorted(set(zs))
+            specs = [SPECTRA.get(x, y, zz, wavelength, dz) for zz in uniq]
+            if len(specs) == 1:
+                spec = specs[0]
+            else:   # one spectrum pointer per batch entry, no stacked copy
+                spec = None
+                spec_ptrs = device_array([specs[uniq.index(v)].data_ptr() for v in zs], torch.int64)
+            zt = device_array(np.asarray(zs, dtype=np.float64), torch.float64) if vector else None
         cout = 3 if vector else 1
         if work is None:
             work = torch.empty(L.xl_rs_work_bytes(B, cout, ny, nx) // 8, dtype=torch.complex64, device=dev)
         if outs is None:
             nout = (3 if want_ez else 2) if (adjoint and vector) else cout
             outs = [torch.empty(tuple(lead) + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(nout)]
-        zt = device_array(np.asarray(zs, dtype=np.float64), torch.float64) if vector else None
         a = _lib.XlRsArgs()
         a.batch = B
         a.comps_in = len(comps)
@@ -544,8 +589,8 @@ class RsCall:
             a.y = device_grid(y).data_ptr()
             a.z = zt.data_ptr()
         a.spectrum = _ptr(spec)
-        a.spectrum_stride = 0
-        a.spectrum_index = 0
+        a.spectrum_stride = spec.shape[-1] if spec_index is not None else 0
+        a.spectrum_index = _ptr(spec_index)
         a.spectra = _ptr(spec_ptrs)
         a.work = work.data_ptr()
         fill_prog(a.pre, pre, ny, nx)
@@ -554,7 +599,7 @@ class RsCall:
         self.args = a
         self.outs = outs
         self.batch, self.ny, self.nx, self.comps = B, ny, nx, cout
-        self._keep = (comps, specs, spec_ptrs, work, zt, list(pre or ()), list(post or ()))
+        self._keep = (comps, specs, spec_ptrs, spec_index, work, zt, list(pre or ()), list(post or ()))
 
     def run(self):
         _lib.check(lib().xl_rs_propagate(stream_handle(), ctypes.byref(self.args)), "xl_rs_propagate")
@@ -801,13 +846,11 @@ def mse_intensity_grad(a, b, g, want_a=True, want_b=False):
 
 
 def z_values(z):
-    """(distances as python floats, a tensor that needs their gradient or None).
-    A distance given as a tensor that requires grad is read back to the host
-    (its transfer spectrum is built from the value) and kept for autograd."""
+    """(the distance as the propagators take it, the tensor that needs its
+    gradient or None).  A tensor distance stays on the device: its transfer
+    spectra are built there from its values, with no host read."""
     if isinstance(z, torch.Tensor):
-        vals = z.detach().to("cpu", torch.float64).numpy()
-        zt = z if z.requires_grad else None
-        return (float(vals) if vals.ndim == 0 else [float(v) for v in vals.ravel()]), zt
+        return z.detach(), (z if z.requires_grad else None)
     return z, None
 
 
@@ -837,7 +880,11 @@ def vrs_dz_ez(ex, ey, gez, x, y, zs) -> torch.Tensor:
     (exv, eyv), _, ebs = batch_planes([ex, ey], ny, nx)
     gv = gez.contiguous()
     x, y = as_grid(x), as_grid(y)
-    zt = device_array(np.broadcast_to(np.asarray(zs, dtype=np.float64), (B,)).copy(), torch.float64)
+    if isinstance(zs, torch.Tensor):
+        zd = device_z(zs, B)
+        zt = zd if zd.numel() == B else zd.expand(B).contiguous()
+    else:
+        zt = device_array(np.broadcast_to(np.asarray(zs, dtype=np.float64), (B,)).copy(), torch.float64)
     L = lib()
     work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(B, ny * nx) // 8), dtype=torch.float64, device=gv.device)
     out = torch.empty(B, dtype=torch.float32, device=gv.device)

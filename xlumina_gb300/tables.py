@@ -161,3 +161,46 @@ class VrsLcdTable:
         L.backward()
         self.opt.step()
         return L
+
+
+class SharpFocusTable:
+    """The hybrid sharp-focus discovery step of
+    experiments/hybrid_sharp_optical_table.py and hybrid_optimizer.py:
+    hybrid_setup_sharp_focus on a 1024^2 grid (2.5 mm, 635 nm, every source
+    the same polarised Gaussian), six objective-lens detectors onto 400^2
+    (10 um, NA 0.9), loss softmin(vectorized_loss_hybrid(|Ez|^2)), AdamW over
+    all 29 parameters (six phase masks, three LCDs, nine splitter angles,
+    eight distances)."""
+
+    def __init__(self, n=1024, roi_n=400, wavelength=0.635, half_width=2500.0, waist=1200.0, seed=2100,
+                 device="cuda", capturable=False):
+        from .vectorized_optics import PolarizedLightSource
+        self.x, self.y = toolbox.space(half_width, n)
+        self.xo, self.yo = toolbox.space(10.0, roi_n)
+        r_lens = 3.6e3 / 2
+        self.fixed = [r_lens, r_lens / 0.9, self.xo, self.yo]
+        self.src = PolarizedLightSource(self.x, self.y, wavelength)
+        self.src.gaussian_beam(w0=(waist, waist), jones_vector=(1, 1))
+        rng = np.random.default_rng(seed)
+        self.params = []
+        for k in range(29):
+            # phase masks in float32 (the kernels' precision); the settings in
+            # float64, as distances need it
+            plane = k < 18 and k % 6 in (0, 1)
+            self.params.append(torch.as_tensor(rng.uniform(0, 1, (n, n) if plane else (1,)),
+                                               dtype=torch.float32 if plane else torch.float64,
+                                               device=device).requires_grad_(True))
+        # capturable: the step count lives on the device, so plans.CapturedStep can record a step
+        self.opt = torch.optim.AdamW(self.params, lr=0.05, weight_decay=1e-4, capturable=capturable)
+
+    def loss(self):
+        s = self.src
+        I, _ = oe.hybrid_setup_sharp_focus(s, s, s, s, s, s, self.params, self.fixed)
+        return toolbox.softmin(lf.vectorized_loss_hybrid(I))
+
+    def step(self):
+        self.opt.zero_grad(set_to_none=True)
+        L = self.loss()
+        L.backward()
+        self.opt.step()
+        return L

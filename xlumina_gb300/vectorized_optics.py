@@ -80,7 +80,7 @@ class VectorizedLight(_Grid):
         """vectorized_optics.py:244-284: Ez derived from Ex, Ey; returns (light, quality_factor)."""
         tic = time.perf_counter()
         zv, _ = engine.z_values(z)
-        qf = engine.quality_factor(self.x, self.y, self.wavelength, np.asarray(zv))
+        qf = engine.quality_factor(self.x, self.y, self.wavelength, zv)
         E = self._base(2)
         if autograd.needs_grad(E, self._ops, z):
             plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, True, self._ops)

@@ -136,7 +136,7 @@ class ScalarLight(_Grid):
         """wave_optics.py:173-196: returns (ScalarLight, quality_factor)."""
         tic = time.perf_counter()
         zv, _ = engine.z_values(z)
-        qf = engine.quality_factor(self.x, self.y, self.wavelength, np.asarray(zv))
+        qf = engine.quality_factor(self.x, self.y, self.wavelength, zv)
         base = [self._base()]
         if autograd.needs_grad(base, self._ops, z):
             plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, False, self._ops)
