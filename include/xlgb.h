@@ -301,6 +301,17 @@ int xl_vrs_dz_ez(void* stream, int batch, int ny, int nx, const void* ex, const 
                  const void* gez, long long g_bstride, const double* x, const double* y, const double* z,
                  void* work, void* out);
 
+/* The distance gradient of one RS / VRS call per batch entry, in one pass:
+ * out[b] = sum_c sum_i Re(conj(g_c) d_c) + [VRS] sum_i Re(conj(gez_i) dEz_i/dz)
+ * for the output gradients g (comps planes), the propagation d of the same
+ * input through the dH/dz spectrum (xl_rs_transfer_spectrum_dz), and for VRS
+ * (ex non-NULL) the Jones-program output (ex, ey), the adjoint's unfolded Ez
+ * gradient gez and the grid / distances as in xl_vrs_dz_ez.  g, d and gez
+ * share bstride; work: xl_mse_intensity_work_bytes(batch, ny * nx). */
+int xl_rs_z_gradient(void* stream, int batch, int ny, int nx, int comps, const void* const* g, const void* const* d,
+                     long long bstride, const void* ex, const void* ey, long long e_bstride, const void* gez,
+                     const double* x, const double* y, const double* z, void* work, void* out);
+
 /* ---- Losses ------------------------------------------------------------ */
 
 /* Intensity MSE, MSE_Intensity of loss_functions.py:137-149, per plane:

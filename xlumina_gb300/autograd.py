@@ -71,12 +71,11 @@ class RsPlan:
         batch for one distance)."""
         douts = engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector, pre=self.ops,
                               dz=True).run()
-        acc = engine.re_inner(gouts[0], douts[0])
-        for g, d in zip(gouts[1:], douts[1:]):
-            acc = acc + engine.re_inner(g, d)
         if self.vector:
             e = engine.apply_ops(list(base), self.ops, self.ny, self.nx) if self.ops else list(base)
-            acc = acc + engine.vrs_dz_ez(e[0], e[1], gez, self.x, self.y, self.z).reshape(acc.shape)
+            acc = engine.rs_z_gradient(gouts, douts, self.x, self.y, self.z, e[0], e[1], gez)
+        else:
+            acc = engine.rs_z_gradient(gouts, douts, self.x, self.y, self.z)
         zt = self.z_tensor
         if zt.numel() == 1:
             return acc.sum().reshape(zt.shape).to(device=zt.device, dtype=zt.dtype)

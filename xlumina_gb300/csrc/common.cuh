@@ -53,37 +53,73 @@ __device__ __forceinline__ ffloat ff_sqrt(ffloat x) {
   return ff_fast_two_sum(r, __fdiv_rn(d, __fmul_rn(2.f, r)));
 }
 
-// r = sqrt(X^2 + Y^2 + z^2) in float-float and the fraction of r / lambda
-// (in turns, in [-0.5, 0.5]) that sets the phase.
-__device__ __forceinline__ void rs_distance(double X, double Y, double z, double inv_lambda, float* rf,
-                                            float* frac) {
-  const ffloat x = ff_split(X), y = ff_split(Y), zz = ff_split(z);
-  const ffloat s = ff_add(ff_add(ff_mul(zz, zz), ff_mul(y, y)), ff_mul(x, x));
+// Per-launch constants of the RS impulse response, split into float-float
+// once per thread: z^2, 1/lambda, and float copies for the amplitude.
+struct RsGeom {
+  ffloat z2, invl;
+  float zf, k, sgn;   // z, 2 pi / lambda, sign of z (the exponent's sign)
+};
+__device__ __forceinline__ RsGeom rs_geom(double z, double inv_lambda, float k) {
+  RsGeom g;
+  const ffloat zz = ff_split(z);
+  g.z2 = ff_mul(zz, zz);
+  g.invl = ff_split(inv_lambda);
+  g.zf = (float)z;
+  g.k = k;
+  g.sgn = z > 0 ? 1.f : -1.f;
+  return g;
+}
+
+// s = X^2 + Y^2 + z^2 in float-float for an offset split into float-float
+// parts (z^2 + Y^2 first: it is the larger term).
+__device__ __forceinline__ ffloat rs_s(const RsGeom& g, ffloat x, ffloat y) {
+  return ff_add(ff_add(g.z2, ff_mul(y, y)), ff_mul(x, x));
+}
+
+// e^{+-i 2 pi r / lambda} for r = sqrt(s) (sign of z), and r as a float.
+__device__ __forceinline__ float2 rs_phase(const RsGeom& g, ffloat s, float* rf) {
   const ffloat r = ff_sqrt(s);
-  const ffloat t = ff_mul(r, ff_split(inv_lambda));
+  const ffloat t = ff_mul(r, g.invl);
   float f = __fadd_rn(__fsub_rn(t.hi, rintf(t.hi)), t.lo);
   f = __fsub_rn(f, rintf(f));
   *rf = r.hi;
-  *frac = f;
+  float sn, cs;
+  sincospif(2.0f * g.sgn * f, &sn, &cs);
+  return make_float2(cs, sn);
 }
 
-// e^{i 2 pi f} for a fraction of a turn |f| <= 1/2.
-__device__ __forceinline__ float2 cis_frac(float f) {
-  float s, c;
-  sincospif(2.0f * f, &s, &c);
-  return make_float2(c, s);
+// Rayleigh-Sommerfeld impulse response at s = X^2 + Y^2 + z^2:
+// exp(+-i k r) * z / (2 pi r^2) * (1/r - i k), r = sqrt(s); the exponent's
+// sign follows the sign of z.  r and k r are float-float.
+__device__ __forceinline__ float2 rs_value_s(const RsGeom& g, ffloat s) {
+  float rf;
+  const float2 e = rs_phase(g, s, &rf);
+  const float a = g.zf / (6.283185307179586f * rf * rf);
+  return cmul(e, make_float2(a / rf, -a * g.k));
 }
 
-// Rayleigh-Sommerfeld impulse response at offset (X, Y), distance z:
-// exp(+-i k r) * z / (2 pi r^2) * (1/r - i k), r = sqrt(X^2 + Y^2 + z^2);
-// the exponent's sign follows the sign of z.  r and k r are float-float.
-__device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, double inv_lambda,
-                                                  float k) {
-  float rf, f;
-  rs_distance(X, Y, z, inv_lambda, &rf, &f);
-  const float2 e = cis_frac(z > 0 ? f : -f);
-  const float a = (float)z / (6.283185307179586f * rf * rf);
-  return cmul(e, make_float2(a / rf, -a * k));
+// Its derivative with respect to z, from H = e^{i s k r} a(r, z),
+// a = z (1/r - i k) / (2 pi r^2), s = sign(z), dr/dz = z/r:
+// dH/dz = e^{i s k r} (i s k (z/r) a + da/dz),
+// da/dz = ((1/r^3 - i k / r^2) + z^2 (-3/r^5 + 2 i k / r^4)) / (2 pi).
+__device__ __forceinline__ float2 rs_dz_value_s(const RsGeom& g, ffloat s) {
+  float rf;
+  const float2 e = rs_phase(g, s, &rf);
+  const float zf = g.zf, k = g.k;
+  const float ir = 1.f / rf, ir2 = ir * ir, ir3 = ir2 * ir;
+  const float inv2pi = 0.15915494309189533577f;
+  const float2 a = make_float2(zf * ir3 * inv2pi, -zf * k * ir2 * inv2pi);
+  const float z2 = zf * zf;
+  const float2 da = make_float2((ir3 - 3.f * z2 * ir3 * ir2) * inv2pi, (-k * ir2 + 2.f * k * z2 * ir2 * ir2) * inv2pi);
+  const float w = g.sgn * k * zf * ir;   // i s k (z / r) a
+  const float2 ia = make_float2(-w * a.y, w * a.x);
+  return cmul(e, cadd(ia, da));
+}
+
+// The same at an offset (X, Y) given in float64.
+__device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, double inv_lambda, float k) {
+  const RsGeom g = rs_geom(z, inv_lambda, k);
+  return rs_value_s(g, rs_s(g, ff_split(X), ff_split(Y)));
 }
 
 // sin and cos of a mask phase in radians (one place for every Jones op and
@@ -91,27 +127,6 @@ __device__ __forceinline__ float2 rs_kernel_value(double X, double Y, double z, 
 // pixels with heavy cancellation, and the hardware approximation's 4e-7
 // absolute error per pixel shows up there above the 1e-5 parity bar.
 __device__ __forceinline__ void phase_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
-
-// Derivative of the impulse response with respect to z, dH/dz, from
-// H = e^{i s k r} a(r, z), a = z (1/r - i k) / (2 pi r^2), s = sign(z), dr/dz = z/r:
-// dH/dz = e^{i s k r} (i s k (z/r) a + da/dz),
-// da/dz = ((1/r^3 - i k / r^2) + z^2 (-3/r^5 + 2 i k / r^4)) / (2 pi).
-__device__ __forceinline__ float2 rs_kernel_dz_value(double X, double Y, double z, double inv_lambda,
-                                                     float k) {
-  float rf, f;
-  rs_distance(X, Y, z, inv_lambda, &rf, &f);
-  const float2 e = cis_frac(z > 0 ? f : -f);
-  const float zf = (float)z, s = z > 0 ? 1.f : -1.f;
-  const float ir = 1.f / rf, ir2 = ir * ir, ir3 = ir2 * ir;
-  const float inv2pi = 0.15915494309189533577f;
-  const float2 a = make_float2(zf * ir3 * inv2pi, -zf * k * ir2 * inv2pi);
-  const float z2 = zf * zf;
-  const float2 da = make_float2((ir3 - 3.f * z2 * ir3 * ir2) * inv2pi, (-k * ir2 + 2.f * k * z2 * ir2 * ir2) * inv2pi);
-  // i s k (z / r) a
-  const float w = s * k * zf * ir;
-  const float2 ia = make_float2(-w * a.y, w * a.x);
-  return cmul(e, cadd(ia, da));
-}
 
 // ---- fused per-pixel Jones program ----
 

@@ -283,6 +283,57 @@ __global__ void __launch_bounds__(MSE_THREADS) vrs_dz_ez_partial(const float2* _
   }
 }
 
+// The whole distance gradient of one RS / VRS call per batch entry b:
+// sum_c sum_i Re(conj(g_c) d_c) over the propagated components (d: the
+// propagation through the dH/dz spectrum) plus, for VRS, sum_i Re(conj(gez)
+// dEz/dz) of the input-plane Ez derivation -- one pass instead of a reduction
+// per component.
+struct ZGradArgs {
+  const float2* g[3];
+  const float2* d[3];
+  long long bs;          // batch stride of g and d (elements)
+  int ncomp;
+  const float2* ex;      // VRS: the Jones program's output (NULL: scalar RS)
+  const float2* ey;
+  long long ebs;
+  const float2* gez;     // VRS: the propagated Ez gradient before its fold
+  const double* x;
+  const double* y;
+  const double* z;       // one per batch entry
+  int ny, nx;
+};
+
+__global__ void __launch_bounds__(MSE_THREADS) rs_zgrad_partial(ZGradArgs p, double* __restrict__ partial) {
+  const int b = blockIdx.y;
+  const long long npix = (long long)p.ny * p.nx;
+  const long long o = (long long)b * p.bs;
+  float acc = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    for (int c = 0; c < p.ncomp; ++c) {
+      const float2 u = p.g[c][o + i], v = p.d[c][o + i];
+      acc = fmaf(u.x, v.x, fmaf(u.y, v.y, acc));
+    }
+    if (p.ex) {
+      const int row = (int)((unsigned)i / (unsigned)p.nx), col = (int)i - row * p.nx;
+      const float X = (float)p.x[col], Y = (float)p.y[row], zf = (float)p.z[b];
+      const float ir = rsqrtf(X * X + Y * Y + zf * zf);
+      const float w = -zf * ir * ir * ir;
+      const float2 u = p.ex[(long long)b * p.ebs + i], v = p.ey[(long long)b * p.ebs + i], gg = p.gez[o + i];
+      acc = fmaf(gg.x, w * (u.x * X + v.x * Y), fmaf(gg.y, w * (u.y * X + v.y * Y), acc));
+    }
+  }
+  __shared__ float red[MSE_THREADS / 32];
+  for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < MSE_THREADS / 32; ++w) t += red[w];
+    partial[(long long)b * gridDim.x + blockIdx.x] = t;
+  }
+}
+
 static int mse_blocks(long long npix) {
   long long nb = (npix + MSE_THREADS * 8 - 1) / (MSE_THREADS * 8);
   if (nb > 152 * 4) nb = 152 * 4;
@@ -475,6 +526,44 @@ extern "C" int xl_vrs_dz_ez(void* stream, int batch, int ny, int nx, const void*
                                                              (const float2*)gez, g_bstride, ny, nx, x, y, z,
                                                              (double*)work);
   XL_CHECK_LAUNCH("vrs_dz_ez_partial");
+  mse_int_finish<<<(batch + 3) / 4, 128, 0, st>>>((const double*)work, nb, batch, 1.0, (float*)out);
+  XL_CHECK_LAUNCH("mse_int_finish");
+  return XL_OK;
+}
+
+extern "C" int xl_rs_z_gradient(void* stream, int batch, int ny, int nx, int comps, const void* const* g,
+                                const void* const* d, long long bstride, const void* ex, const void* ey,
+                                long long e_bstride, const void* gez, const double* x, const double* y,
+                                const double* z, void* work, void* out) {
+  if (batch < 1 || batch > 65535 || ny < 1 || nx < 1 || (long long)ny * nx > 0x7fffffffLL || comps < 1 ||
+      comps > 3 || !g || !d || !work || !out || (ex && (!ey || !gez || !x || !y || !z))) {
+    set_error("xl_rs_z_gradient: bad arguments");
+    return XL_EINVAL;
+  }
+  ZGradArgs p;
+  for (int c = 0; c < 3; ++c) {
+    p.g[c] = c < comps ? (const float2*)g[c] : nullptr;
+    p.d[c] = c < comps ? (const float2*)d[c] : nullptr;
+    if (c < comps && (!p.g[c] || !p.d[c])) {
+      set_error("xl_rs_z_gradient: null plane %d", c);
+      return XL_EINVAL;
+    }
+  }
+  p.bs = bstride;
+  p.ncomp = comps;
+  p.ex = (const float2*)ex;
+  p.ey = (const float2*)ey;
+  p.ebs = e_bstride;
+  p.gez = (const float2*)gez;
+  p.x = x;
+  p.y = y;
+  p.z = z;
+  p.ny = ny;
+  p.nx = nx;
+  const int nb = mse_blocks((long long)ny * nx);
+  cudaStream_t st = (cudaStream_t)stream;
+  rs_zgrad_partial<<<dim3(nb, batch), MSE_THREADS, 0, st>>>(p, (double*)work);
+  XL_CHECK_LAUNCH("rs_zgrad_partial");
   mse_int_finish<<<(batch + 3) / 4, 128, 0, st>>>((const double*)work, nb, batch, 1.0, (float*)out);
   XL_CHECK_LAUNCH("mse_int_finish");
   return XL_OK;

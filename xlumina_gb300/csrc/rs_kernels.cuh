@@ -91,28 +91,47 @@ struct RowPtr {
 };
 
 // ---------------------------------------------------------------------------
+// Transfer spectrum, step 0: the wrapped offsets split into float-float
+// (hi, lo) pairs, offx into off[0 .. P), offy into off[P .. 2P).  `off` is the
+// spectrum buffer, which step 2 overwrites afterwards.
+static __global__ void rs_split_offsets(const double* __restrict__ offx, const double* __restrict__ offy, int P,
+                                 float2* __restrict__ off) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * P) return;
+  const ffloat v = ff_split(i < P ? offx[i] : offy[i - P]);
+  off[i] = make_float2(v.hi, v.lo);
+}
+
 // Transfer spectrum, step 1: rows of the wrapped impulse response -> P-point
 // row spectra, row-major in natural order.
 // DZ: the rows of dH/dz instead (the spectrum of the z-derivative).
 template <int LOGQ, bool DZ>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::ROW_THREADS)
-    rs_hhat_rows(int ny, int nx, const double* __restrict__ offx, const double* __restrict__ offy, double zh,
-                 const double* __restrict__ zp, double inv_lambda, float k, float2* __restrict__ out) {
+    rs_hhat_rows(int ny, int nx, const float2* __restrict__ off, double zh, const double* __restrict__ zp,
+                 double inv_lambda, float k, float2* __restrict__ out) {
   using C = RsCfg<LOGQ>;
-  const double z = zp ? __ldg(zp) : zh;   // a distance in device memory, or the host's value
+  // a distance in device memory, or the host's value
+  const RsGeom g = rs_geom(zp ? __ldg(zp) : zh, inv_lambda, k);
   extern __shared__ __align__(16) float2 smem[];
   const int tid = threadIdx.x;
   const int gi = tid / C::T, j = tid % C::T;
   const int i = blockIdx.x * C::G + gi;   // row of the wrapped response (< P)
   const bool vy = (i < ny) || (i > C::P - ny);
+  const float2 oy = off[C::P + i];
+  const ffloat y = {oy.x, oy.y};
+  const ffloat zy = ff_add(g.z2, ff_mul(y, y));
   float2 v[16];
 #pragma unroll
   for (int m = 0; m < 16; ++m) {
     const int col = j + m * C::T;
     const bool vx = (col < nx) || (col > C::P - nx);
-    v[m] = (vy && vx) ? (DZ ? rs_kernel_dz_value(offx[col], offy[i], z, inv_lambda, k)
-                            : rs_kernel_value(offx[col], offy[i], z, inv_lambda, k))
-                      : make_float2(0.f, 0.f);
+    v[m] = make_float2(0.f, 0.f);
+    if (vy && vx) {
+      const float2 ox = off[col];
+      const ffloat x = {ox.x, ox.y};
+      const ffloat sq = ff_add(zy, ff_mul(x, x));
+      v[m] = DZ ? rs_dz_value_s(g, sq) : rs_value_s(g, sq);
+    }
   }
   block_fft_x<C::LOGP, 16, -1, false, true>(v, j, smem + gi * C::XS, pass_tw<C::LOGP>());
   float2* dst = out + (long long)i * C::P;
@@ -457,14 +476,16 @@ int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const doubl
   const size_t sm1 = (size_t)C::G * C::XS * sizeof(float2);
   const float k = (float)(2.0 * M_PI / wavelength);
   cudaError_t e;
+  rs_split_offsets<<<(2 * C::P + 255) / 256, 256, 0, st>>>(offx, offy, C::P, spec);
+  XL_CHECK_LAUNCH("rs_split_offsets");
   if (dz) {
     if ((e = allow_smem(rs_hhat_rows<LOGQ, true>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
-    rs_hhat_rows<LOGQ, true><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, zp,
-                                                                          1.0 / wavelength, k, work);
+    rs_hhat_rows<LOGQ, true><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, spec, z, zp, 1.0 / wavelength,
+                                                                          k, work);
   } else {
     if ((e = allow_smem(rs_hhat_rows<LOGQ, false>, sm1)) != cudaSuccess) return cuda_fail(e, "rs_hhat_rows smem");
-    rs_hhat_rows<LOGQ, false><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, offx, offy, z, zp,
-                                                                           1.0 / wavelength, k, work);
+    rs_hhat_rows<LOGQ, false><<<C::P / C::G, C::ROW_THREADS, sm1, st>>>(ny, nx, spec, z, zp, 1.0 / wavelength,
+                                                                           k, work);
   }
   XL_CHECK_LAUNCH("rs_hhat_rows");
   const size_t sm2 = (size_t)C::CW * C::CXS * sizeof(float2);

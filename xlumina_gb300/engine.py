@@ -894,6 +894,42 @@ def vrs_dz_ez(ex, ey, gez, x, y, zs) -> torch.Tensor:
     return out
 
 
+def rs_z_gradient(gouts, douts, x, y, z, ex=None, ey=None, gez=None) -> torch.Tensor:
+    """dL/dz of one RS / VRS call per batch entry (libxlgb, one pass): the
+    output gradients ``gouts`` against the dH/dz propagation ``douts``, plus
+    for VRS the Ez term of the Jones-program output (ex, ey) against the
+    adjoint's unfolded Ez gradient ``gez``."""
+    ny, nx = gouts[0].shape[-2:]
+    B = gouts[0].numel() // (ny * nx)
+    gs = [as_field(g).contiguous() for g in gouts]
+    ds = [as_field(d).contiguous() for d in douts]
+    dev = gs[0].device
+    L = lib()
+    work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(B, ny * nx) // 8), dtype=torch.float64, device=dev)
+    out = torch.empty(B, dtype=torch.float32, device=dev)
+    keep = []
+    exp = eyp = gp = xp = yp = zp = 0
+    ebs = 0
+    if ex is not None:
+        (exv, eyv), _, ebs = batch_planes([ex, ey], ny, nx)
+        gv = as_field(gez).contiguous()
+        x, y = as_grid(x), as_grid(y)
+        if isinstance(z, torch.Tensor):
+            zd = device_z(z, B)
+            zt = zd if zd.numel() == B else zd.expand(B).contiguous()
+        else:
+            zt = device_array(np.broadcast_to(np.asarray(z, dtype=np.float64), (B,)).copy(), torch.float64)
+        keep = [exv, eyv, gv, zt]
+        exp, eyp, gp = exv.data_ptr(), eyv.data_ptr(), gv.data_ptr()
+        xp, yp, zp = device_grid(x).data_ptr(), device_grid(y).data_ptr(), zt.data_ptr()
+    gpp = (ctypes.c_void_p * 3)(*[t.data_ptr() for t in gs] + [0] * (3 - len(gs)))
+    dpp = (ctypes.c_void_p * 3)(*[t.data_ptr() for t in ds] + [0] * (3 - len(ds)))
+    _lib.check(L.xl_rs_z_gradient(stream_handle(), B, ny, nx, len(gs), gpp, dpp, ny * nx, exp, eyp, ebs, gp, xp, yp,
+                                  zp, work.data_ptr(), out.data_ptr()), "xl_rs_z_gradient")
+    del keep
+    return out.reshape(gouts[0].shape[:-2])
+
+
 # ---------------------------------------------------------- beam splitters --
 
 def _bs_port(comps, B, ny, nx):
