@@ -20,6 +20,7 @@
 #define XLGB_H_
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -311,6 +312,36 @@ int xl_vrs_dz_ez(void* stream, int batch, int ny, int nx, const void* ex, const 
 int xl_rs_z_gradient(void* stream, int batch, int ny, int nx, int comps, const void* const* g, const void* const* d,
                      long long bstride, const void* ex, const void* ey, long long e_bstride, const void* gez,
                      const double* x, const double* y, const double* z, void* work, void* out);
+
+/* ---- Table noise --------------------------------------------------------- */
+
+/* The noise of shake_setup (optical_elements.py:2127-2217) for many optical
+ * tables in one launch, from a counter-based generator (Philox4x32-10) keyed
+ * per table: distance misalignment uniform in [min_d, max_d); phase and
+ * amplitude noise planes +-uniform(min_phase, max_phase) that share their
+ * magnitudes (as the reference's draws do) and differ in their signs, a
+ * negative sign being 255 when `discretize` (the reference's uint8 cast);
+ * waveplate noise +-uniform(min_phase, max_phase). */
+#define XL_NOISE_MAX_TABLES 256
+typedef struct {
+  int tables;                   /* optical tables, one key each (<= XL_NOISE_MAX_TABLES) */
+  int resolution;               /* side of the noise planes */
+  int planes;                   /* planes per table (2 x the number of sSLMs) */
+  int n_distances, n_wps;       /* distances and waveplate angles per table */
+  double min_d, max_d;          /* misalignment range (um) */
+  double min_phase, max_phase;  /* phase / amplitude noise range */
+  int discretize;
+  double* distances;            /* device, tables x n_distances */
+  float* slms;                  /* device, tables x planes x resolution^2 (NULL: not drawn) */
+  float* amps;                  /* device, same shape (NULL: not drawn) */
+  double* wps;                  /* device, tables x n_wps */
+} XlNoiseArgs;
+
+/* keys: host array of 2 words per table. */
+int xl_table_noise(void* stream, const XlNoiseArgs* args, const uint32_t* keys);
+
+/* The generator on the host: out = Philox4x32-10(counter[4], key[2]). */
+int xl_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out);
 
 /* ---- Losses ------------------------------------------------------------ */
 

@@ -404,3 +404,53 @@ def small_area_hybrid(I):
     In = I / (np.sum(I) + 1e-08)
     mask = np.where(In > 0.7 * np.max(In), 1, 0)
     return np.sum(mask) / (np.sum(mask * In) + 1e-08)
+
+
+# ---------------------------------------------------------------- noise --
+# The table noise is drawn with Philox4x32-10 (Salmon et al., SC 2011), not
+# with jax's streams; this restatement pins the device generator bit for bit.
+
+def philox4x32_10(counter, key):
+    """Philox4x32 with 10 rounds on python ints: 4-word counter, 2-word key."""
+    c = [int(v) & 0xFFFFFFFF for v in counter]
+    k0, k1 = int(key[0]) & 0xFFFFFFFF, int(key[1]) & 0xFFFFFFFF
+    for r in range(10):
+        p0 = 0xD2511F53 * c[0]
+        p1 = 0xCD9E8D57 * c[2]
+        c = [((p1 >> 32) ^ c[1] ^ k0) & 0xFFFFFFFF, p1 & 0xFFFFFFFF,
+             ((p0 >> 32) ^ c[3] ^ k1) & 0xFFFFFFFF, p0 & 0xFFFFFFFF]
+        if r < 9:
+            k0 = (k0 + 0x9E3779B9) & 0xFFFFFFFF
+            k1 = (k1 + 0xBB67AE85) & 0xFFFFFFFF
+    return c
+
+
+def table_noise_element(key, plane_index, min_phase, max_phase, discretize=False):
+    """(slm, amp) noise value of flat plane element ``plane_index`` of a table
+    keyed ``key``: one magnitude (stream 2), two signs (streams 3 and 4)."""
+    e = int(plane_index)
+    cm = philox4x32_10((e & 0xFFFFFFFF, e >> 32, 2, 0), key)
+    cs = philox4x32_10((e & 0xFFFFFFFF, e >> 32, 3, 0), key)
+    ca = philox4x32_10((e & 0xFFFFFFFF, e >> 32, 4, 0), key)
+    lo = np.float32(min_phase)
+    span = np.float32(float(max_phase) - float(min_phase))
+    u = np.float32((cm[0] >> 8) * (1.0 / 16777216.0))
+    mag = np.float32(lo + np.float32(span * u))        # float32 product, then float32 sum
+    neg = np.float32(255.0 if discretize else -1.0)
+    return (np.float32((1.0 if cs[0] & 1 else neg) * mag), np.float32((1.0 if ca[0] & 1 else neg) * mag))
+
+
+def table_noise_scalars(key, n_distances, n_wps, min_d, max_d, min_phase, max_phase):
+    """(distances, waveplate noise) of a table keyed ``key`` (streams 1, 5, 6)."""
+    def u53(a, b):
+        return ((a >> 5) * 67108864.0 + (b >> 6)) * (1.0 / 9007199254740992.0)
+    d = []
+    for i in range(n_distances):
+        c = philox4x32_10((i, 0, 1, 0), key)
+        d.append(min_d + (max_d - min_d) * u53(c[0], c[1]))
+    w = []
+    for i in range(n_wps):
+        cs = philox4x32_10((i, 0, 5, 0), key)
+        cm = philox4x32_10((i, 0, 6, 0), key)
+        w.append((1.0 if cs[0] & 1 else -1.0) * (min_phase + (max_phase - min_phase) * u53(cm[0], cm[1])))
+    return np.array(d), np.array(w)

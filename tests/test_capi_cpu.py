@@ -122,3 +122,32 @@ def test_czt_argument_errors(lib):
     a.log2_lx, a.log2_ly = 6, 7   # 64 < 64 + 32
     assert lib.xl_czt(None, ctypes.byref(a)) == _lib.XL_EINVAL
     assert b"Bluestein" in lib.xl_last_error()
+
+
+def test_philox_known_answers():
+    """The table-noise generator against the Random123 known-answer vectors of
+    Philox4x32-10, through the library (host code) and the oracle."""
+    import ctypes
+
+    from oracle import xlumina_ref as ref
+    from xlumina_gb300 import _lib
+    L = _lib.load()
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+           ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+           ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+            (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1))]
+    for ctr, key, want in kat:
+        out = (ctypes.c_uint32 * 4)()
+        assert L.xl_philox4x32_10((ctypes.c_uint32 * 4)(*ctr), (ctypes.c_uint32 * 2)(*key), out) == 0
+        assert tuple(out) == want
+        assert tuple(ref.philox4x32_10(ctr, key)) == want
+
+
+def test_noise_keys():
+    from xlumina_gb300 import noise
+    k = noise.PRNGKey(42)
+    assert k.tolist() == [0, 42]
+    a, b = noise.split(k, 2), noise.split(k, 2)
+    assert (a == b).all() and not (a[0] == a[1]).all()
+    chain = noise.keychain_optical_tables(7, 3)
+    assert chain.shape == (3, 2) and chain[:, 1].tolist() == [7, 8, 9]

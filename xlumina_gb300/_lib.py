@@ -67,6 +67,17 @@ class XlBsArgs(ctypes.Structure):
                 ("m", ctypes.c_void_p), ("m_bstride", ctypes.c_longlong)]
 
 
+XL_NOISE_MAX_TABLES = 256
+
+
+class XlNoiseArgs(ctypes.Structure):
+    _fields_ = [("tables", ctypes.c_int), ("resolution", ctypes.c_int), ("planes", ctypes.c_int),
+                ("n_distances", ctypes.c_int), ("n_wps", ctypes.c_int), ("min_d", ctypes.c_double),
+                ("max_d", ctypes.c_double), ("min_phase", ctypes.c_double), ("max_phase", ctypes.c_double),
+                ("discretize", ctypes.c_int), ("distances", ctypes.c_void_p), ("slms", ctypes.c_void_p),
+                ("amps", ctypes.c_void_p), ("wps", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); every symbol include/xlgb.h declares.
 SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
@@ -125,6 +136,9 @@ SIGNATURES = {
                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                                  ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_table_noise": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlNoiseArgs), ctypes.POINTER(ctypes.c_uint32)]),
+    "xl_philox4x32_10": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                        ctypes.POINTER(ctypes.c_uint32)]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

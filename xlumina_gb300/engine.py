@@ -235,9 +235,15 @@ class JonesOp:
 
     @staticmethod
     def is_scalar_tensor(p) -> bool:
-        """A one-element tensor parameter (a trainable global setting): it is
-        expanded to a plane for the launch and its gradient is the plane's sum."""
-        return isinstance(p, torch.Tensor) and p.dim() < 2 and p.numel() == 1
+        """A tensor parameter of one value, or of one value per batch entry (a
+        trainable global setting, e.g. an LCD's retardance, or one per noisy
+        table): it is expanded to planes for the launch and its gradient is
+        the planes' sums."""
+        return isinstance(p, torch.Tensor) and p.dim() < 2
+
+    @staticmethod
+    def plane_shape(p, ny, nx):
+        return (ny, nx) if p.numel() == 1 else (p.numel(), ny, nx)
 
     def fill(self, op: _lib.XlOp, ny: int, nx: int) -> None:
         op.kind = self.kind
@@ -245,13 +251,13 @@ class JonesOp:
         pbstride = 0
         for i, p in enumerate(self.params):
             if self.is_scalar_tensor(p):
+                shape = self.plane_shape(p, ny, nx)
                 plane = self.planes.get(i)
-                if plane is None or plane.shape != (ny, nx):
-                    plane = p.detach().to(torch.float32).reshape(1, 1).expand(ny, nx).contiguous()
+                if plane is None or tuple(plane.shape) != shape:
+                    plane = p.detach().to(torch.float32).reshape((-1, 1, 1)[-len(shape):]).expand(shape)
+                    plane = plane.contiguous()
                     self.planes[i] = plane
                 p = keep_for_capture(plane)
-            elif isinstance(p, torch.Tensor) and p.dim() < 2:
-                raise ValueError("a mask parameter must be a scalar, a one-element tensor or an (ny, nx) plane")
             if isinstance(p, torch.Tensor):
                 if p.shape[-2:] != (ny, nx):
                     raise ValueError(f"mask parameter has shape {tuple(p.shape)}, field is {(ny, nx)}")
@@ -409,7 +415,7 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
                 if not p.requires_grad:
                     continue
                 if JonesOp.is_scalar_tensor(p):
-                    t = torch.empty((ny, nx), dtype=torch.float32, device=dev)
+                    t = torch.empty(JonesOp.plane_shape(p, ny, nx), dtype=torch.float32, device=dev)
                     scalars.append((k, q, p.shape))
                 else:
                     t = torch.empty(p.shape, dtype=torch.float32, device=dev)
@@ -425,7 +431,7 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
     _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ibs, go, ny * nx, gi, ny * nx,
                                  ctypes.byref(prog), pgrad), "xl_ops_backward")
     for k, q, shape in scalars:
-        grads[(k, q)] = grads[(k, q)].sum().reshape(shape)
+        grads[(k, q)] = grads[(k, q)].sum(dim=(-2, -1)).reshape(shape)
     return gin, grads
 
 

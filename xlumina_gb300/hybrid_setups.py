@@ -215,6 +215,33 @@ def robust_discovery(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, noi
     return _ez_intensities(dets)
 
 
+def _table_batch(light, T):
+    """A source light as a batch of T tables (stride-0 views, no copies)."""
+    from .vectorized_optics import VectorizedLight
+    ex, ey = light.Ex, light.Ey
+    ny, nx = ex.shape[-2:]
+    return VectorizedLight._wrap(light.x, light.y, light.wavelength,
+                                 [ex.expand(T, ny, nx), ey.expand(T, ny, nx), None])
+
+
+def batch_robust_discovery(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, noise_distances, noise_slms,
+                           noise_wps, noise_amps, distance_offset=15):
+    """robust_discovery over many noisy copies of one table
+    (examples/noisy_optimization.ipynb, a vmap there): the noise arrays carry a
+    leading table axis -- distances (T, 8), slms and amps (T, 6, R, R), wps
+    (T, 6) -- and every table runs in the same launches, as one batch of T
+    fields with per-table distances, masks and waveplate settings.  Returns
+    the detected |Ez|^2 as (T, 6, M, M)."""
+    T = noise_slms.shape[0]
+    nd = noise_distances.reshape(T, -1)
+    nw = noise_wps.reshape(T, -1)
+    srcs = [_table_batch(ls, T) for ls in (ls1, ls2, ls3, ls4, ls5, ls6)]
+    I = robust_discovery(*srcs, parameters, fixed_params, [nd[:, k] for k in range(nd.shape[1])],
+                         [noise_slms[:, k] for k in range(noise_slms.shape[1])], [nw[:, k] for k in range(nw.shape[1])],
+                         [noise_amps[:, k] for k in range(noise_amps.shape[1])], distance_offset)
+    return I.transpose(0, 1)
+
+
 def hybrid_setup_sharp_focus(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9):
     """optical_elements.py:1503-1649: returns (stacked |Ez|^2 of the six
     detectors, the detectors' lights)."""

@@ -294,6 +294,8 @@ def vectorized_fluorophores(i_ex, i_dep):
 
 # The prebuilt large-scale tables (optical_elements.py:964-2120) live in
 # hybrid_setups.py; exported here under the reference's names.
-from .hybrid_setups import (hybrid_setup_fixed_slms, hybrid_setup_fixed_slms_fluorophores,  # noqa: E402,F401
-                            hybrid_setup_fluorophores, hybrid_setup_sharp_focus, robust_discovery,
-                            six_times_six_ansatz)
+from .hybrid_setups import (batch_robust_discovery, hybrid_setup_fixed_slms,  # noqa: E402,F401
+                            hybrid_setup_fixed_slms_fluorophores, hybrid_setup_fluorophores,
+                            hybrid_setup_sharp_focus, robust_discovery, six_times_six_ansatz)
+# Table noise (optical_elements.py:2127-2301; shake_setup_jit reads noise.NS).
+from .noise import batch_shake_setup, keychain_optical_tables, shake_setup, shake_setup_jit  # noqa: E402,F401
