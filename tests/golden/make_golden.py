@@ -267,6 +267,29 @@ def main(ref_root):
               **{f"noise_w_{k}": v for k, v in enumerate(nw)}, **{f"noise_a_{k}": v for k, v in enumerate(na)},
               i_robust=i_robust, **{f"p_six_{k}": v for k, v in enumerate(p_six)}, i_six=i_six)
 
+        # 14. cylindrical and axicon lenses, and the geometric masks.
+        x, y = tb.space(400.0, 40)
+        X, Y = np.meshgrid(x, y)
+        sl = LightSource(x, y, 0.6)
+        sl.gaussian_beam(w0=(150.0, 150.0), E0=1)
+        vl = VectorizedLight(x, y, 0.6)
+        vl.Ex = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        vl.Ey = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        vl.Ez = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+        cyl_s, cyl_mask = oe.cylindrical_lens(sl, 5000.0, 1.5, angle=0.4)
+        cyl_v, _ = oe.cylindrical_lens(vl, 5000.0, 1.5, angle=0.4)
+        ax_s, ax_mask = oe.axicon_lens(sl, 0.02, 1.45)
+        ax_v, _ = oe.axicon_lens(vl, 0.02, 1.45)
+        tri = oe.triangular_mask(X, Y, (10.0, 60.0), 20.0, 1.2, 150.0)
+        rect = oe.rectangular_mask(X, Y, (15.0, -10.0), 180.0, 90.0, 30.0)
+        ann = oe.annular_aperture(100.0, 300.0, X, Y)
+        fg_a = oe.forked_grating(X, Y, (5.0, 5.0), 10.0, 60.0, 2, kind='Amplitude')
+        fg_p = oe.forked_grating(X, Y, (5.0, 5.0), 10.0, 60.0, 2, kind='Phase')
+        _save("lenses_masks", x=x, y=y, source=sl.field, vEx=vl.Ex, vEy=vl.Ey, vEz=vl.Ez,
+              cyl_scalar=cyl_s.field, cyl_mask=cyl_mask, cyl_Ex=cyl_v.Ex, cyl_Ey=cyl_v.Ey, cyl_Ez=cyl_v.Ez,
+              ax_scalar=ax_s.field, ax_mask=ax_mask, ax_Ex=ax_v.Ex, ax_Ey=ax_v.Ey, ax_Ez=ax_v.Ez,
+              triangle=tri, rectangle=rect, annulus=ann, forked_amplitude=fg_a, forked_phase=fg_p)
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

@@ -262,6 +262,78 @@ def lens(input_field, radius, focal):
     return out, mask
 
 
+def _apply_phase_mask(input_field, mask):
+    """Multiply a light by a complex mask as a pending op; a vector light's Ez
+    becomes zero (the reference builds a new light from Ex, Ey only)."""
+    op = engine.op_cmul(mask)
+    if input_field.info in _SCALAR:
+        return input_field._with_op(op)
+    if input_field.info in _VECTOR:
+        E = input_field._E
+        return VectorizedLight._wrap(input_field.x, input_field.y, input_field.wavelength, [E[0], E[1], None],
+                                     input_field._ops + [op])
+    raise ValueError("Invalid input. Please use ScalarLight or VectorizedLight object.")
+
+
+def cylindrical_lens(input_field, focal_length, refractive_index=1.5, angle=0):
+    """optical_elements.py:705-744: plano-convex cylindrical lens (phase along
+    the rotated x axis); returns (light, lens mask)."""
+    X, Y = input_field.X, input_field.Y
+    c, s = np.cos(angle), np.sin(angle)
+    Xrot = X * c + Y * s
+    R = focal_length * (refractive_index - 1)
+    thickness = R - torch.sqrt(R ** 2 - Xrot ** 2)
+    phase = input_field.k * (refractive_index - 1) * (Xrot ** 2 / (2 * focal_length) + thickness)
+    mask = torch.polar(torch.ones_like(phase), -phase).to(torch.complex64)
+    return _apply_phase_mask(input_field, mask), mask
+
+
+def axicon_lens(input_field, alpha, n=1.5):
+    """optical_elements.py:746-779: axicon phase k r (n-1) sin(alpha) tan(alpha);
+    returns (light, axicon mask)."""
+    r = torch.sqrt(input_field.X ** 2 + input_field.Y ** 2)
+    phase = input_field.k * r * (n - 1) * np.sin(alpha) * np.tan(alpha)
+    mask = torch.polar(torch.ones_like(phase), -phase).to(torch.complex64)
+    return _apply_phase_mask(input_field, mask), mask
+
+
+def triangular_mask(X, Y, r, angle, m, height):
+    """optical_elements.py:797-817 (angle in degrees)."""
+    x0, y0 = r
+    Xrot, Yrot = rotate_mask(X, Y, angle * (np.pi / 180), r)
+    Yl = -m * torch.abs(Xrot - x0) + y0
+    return torch.where((Yrot < Yl) & (Yrot > y0 - height), 1, 0)
+
+
+def rectangular_mask(X, Y, center, width, height, angle):
+    """optical_elements.py:819-836 (angle in degrees)."""
+    Xrot, Yrot = rotate_mask(X, Y, angle * (np.pi / 180), center)
+    return torch.where((Xrot < width / 2) & (Xrot > -width / 2) & (Yrot < height / 2) & (Yrot > -height / 2), 1, 0)
+
+
+def annular_aperture(di, do, X, Y):
+    """optical_elements.py:838-854: ring between diameters di and do."""
+    di, do = di / 2, do / 2
+    r2 = X ** 2 + Y ** 2
+    stop = torch.where(r2 / di ** 2 < 1, 0, 1)
+    ring = torch.where(r2 / do ** 2 < 1, 1, 0)
+    return stop * ring
+
+
+def forked_grating(X, Y, center, angle, period, l, kind=''):
+    """optical_elements.py:856-889: 'Amplitude' gives the binary mask, 'Phase'
+    exp(i pi mask); any other kind returns None, as the reference."""
+    Xrot, Yrot = rotate_mask(X, Y, angle * (np.pi / 180), center)
+    theta = torch.atan2(Xrot, Yrot)
+    g = torch.angle(torch.exp(1j * torch.cos(l * theta - 2 * np.pi / period * Xrot)))
+    amp = torch.where(g < 0, 0, 1)
+    if kind == 'Amplitude':
+        return amp
+    if kind == 'Phase':
+        return torch.exp(1j * np.pi * amp.to(torch.float64))
+    return None
+
+
 # --------------------------------------------------------- prebuilt blocks --
 
 def bb_amplitude_and_phase_mod(input_light, alpha, phi, amp1, amp2, z, eta, theta):

@@ -58,3 +58,7 @@ def rotate_mask(X, Y, angle, origin=None):
     Yrot = -(X - x0) * lib.sin(torch.as_tensor(angle) if lib is torch else angle) + \
         (Y - y0) * lib.cos(torch.as_tensor(angle) if lib is torch else angle)
     return Xrot, Yrot
+
+
+# toolbox.py:698-739: the 4f training-data loader (device batches, prefetched).
+from .datasets import MultiHDF5DataLoader  # noqa: E402,F401
