@@ -58,12 +58,13 @@ class RsPlan:
         self.ny, self.nx = len(y), len(x)
 
     def forward(self, base):
-        return engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector,
-                             pre=self.ops).run()
+        call = engine.RsCall(list(base), self.x, self.y, self.wavelength, self.z, self.vector, pre=self.ops)
+        self._spectra = call.device_spectra   # a device distance's spectra, reused by the adjoint
+        return call.run()
 
     def adjoint(self, grads, want_ez=False):
         return engine.RsCall(list(grads), self.x, self.y, self.wavelength, self.z, self.vector,
-                             adjoint=True, want_ez=want_ez).run()
+                             adjoint=True, want_ez=want_ez, spectra=getattr(self, "_spectra", None)).run()
 
     def z_grad(self, base, gouts, gez):
         """dL/dz for output gradients ``gouts``; ``gez``: the adjoint's unfolded

@@ -538,10 +538,12 @@ class RsCall:
     distinct value, from the cache)."""
 
     def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None,
-                 adjoint=False, dz=False, want_ez=False):
+                 adjoint=False, dz=False, want_ez=False, spectra=None):
         """``dz``: propagate with the spectrum of dH/dz (the output's z-derivative);
         ``want_ez``: a VRS adjoint also returns the propagated Ez gradient before
-        it is folded into Ex, Ey (third output)."""
+        it is folded into Ex, Ey (third output); ``spectra``: for a device
+        distance, the stacked spectra an earlier call built for the same
+        distances (``self.device_spectra``), reused instead of rebuilt."""
         L = lib()
         x = as_grid(x)
         y = as_grid(y)
@@ -558,7 +560,7 @@ class RsCall:
             # distances on the device (e.g. being optimised): spectra built
             # from them in this call, stacked one per distance
             zd = device_z(z, B)
-            spec = build_rs_spectra_device(x, y, zd, wavelength, dz)
+            spec = spectra if spectra is not None else build_rs_spectra_device(x, y, zd, wavelength, dz)
             specs = [spec]
             if zd.numel() > 1:
                 spec_index = device_array(np.arange(B, dtype=np.int32), torch.int32)
@@ -604,6 +606,7 @@ class RsCall:
         a.adjoint = 1 if adjoint else 0
         self.args = a
         self.outs = outs
+        self.device_spectra = spec if isinstance(z, torch.Tensor) else None
         self.batch, self.ny, self.nx, self.comps = B, ny, nx, cout
         self._keep = (comps, specs, spec_ptrs, spec_index, work, zt, list(pre or ()), list(post or ()))
 
