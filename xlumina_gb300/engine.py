@@ -27,10 +27,22 @@ def lib():
     return _lib.load()
 
 
+_cuda_checked = False
+_devices: dict = {}
+
+
 def device() -> torch.device:
-    if not torch.cuda.is_available():
-        raise RuntimeError("xlumina_gb300 needs a CUDA device (sm_103a); there is no CPU path")
-    return torch.device("cuda", torch.cuda.current_device())
+    """The current CUDA device (checked once; no CPU path)."""
+    global _cuda_checked
+    if not _cuda_checked:
+        if not torch.cuda.is_available():
+            raise RuntimeError("xlumina_gb300 needs a CUDA device (sm_103a); there is no CPU path")
+        _cuda_checked = True
+    i = torch.cuda.current_device()
+    d = _devices.get(i)
+    if d is None:
+        d = _devices[i] = torch.device("cuda", i)
+    return d
 
 
 def stream_handle() -> int:
@@ -50,6 +62,8 @@ def as_field(a, dev=None) -> torch.Tensor:
     """complex64 on the CUDA device, contiguous; a batch that is one plane
     broadcast along the batch (an ``expand``-ed view) stays a view, since
     every launch takes it without copying (batch stride 0)."""
+    if isinstance(a, torch.Tensor) and a.is_cuda and a.dtype == torch.complex64 and dev is None:
+        return a if (a.is_contiguous() or _is_broadcast_batch(a)) else a.contiguous()
     dev = dev or device()
     if isinstance(a, torch.Tensor):
         t = a.to(device=dev)
@@ -510,6 +524,22 @@ def device_z(z, B) -> torch.Tensor:
     return zd
 
 
+_offsets_cache: dict = {}
+
+
+def device_offsets(a: np.ndarray, P: int) -> torch.Tensor:
+    """The wrapped impulse-response offsets of a grid axis on the device (cached)."""
+    key = (a.tobytes(), P, torch.cuda.current_device())
+    t = _offsets_cache.get(key)
+    if t is None:
+        t = device_array(rs_wrapped_offsets(a, P), torch.float64)
+        with _LOCK:
+            if len(_offsets_cache) > 64:
+                _offsets_cache.clear()
+            _offsets_cache[key] = t
+    return keep_for_capture(t)
+
+
 def build_rs_spectra_device(x, y, zd: torch.Tensor, wavelength, dz=False) -> torch.Tensor:
     """Transfer spectra (or dH/dz spectra) for the distances of a device array,
     one per entry, stacked: shape (len(zd), P*P).  No host synchronisation."""
@@ -517,8 +547,8 @@ def build_rs_spectra_device(x, y, zd: torch.Tensor, wavelength, dz=False) -> tor
     ny, nx = len(y), len(x)
     P = 2 << rs_logq(ny, nx)
     dev = zd.device
-    offx = device_array(rs_wrapped_offsets(x, P), torch.float64)
-    offy = device_array(rs_wrapped_offsets(y, P), torch.float64)
+    offx = device_offsets(x, P)
+    offy = device_offsets(y, P)
     n = zd.numel()
     spec = torch.empty((n, P * P), dtype=torch.complex64, device=dev)
     work = torch.empty(P * P, dtype=torch.complex64, device=dev)

@@ -96,6 +96,75 @@ def _splitter(a, b, theta):
     raise ValueError("a splitter of the table has no input")
 
 
+def _stack_lights(lights):
+    """One light holding the (Ex, Ey) of lights on the same grid with no
+    pending program, stacked along a new leading axis (flattened with the
+    lights' own batch axes)."""
+    from .vectorized_optics import VectorizedLight
+    l0 = lights[0]
+    ex = torch.stack([l.Ex for l in lights])
+    ey = torch.stack([l.Ey for l in lights])
+    ny, nx = ex.shape[-2:]
+    return VectorizedLight._wrap(l0.x, l0.y, l0.wavelength, [ex.reshape(-1, ny, nx), ey.reshape(-1, ny, nx), None])
+
+
+def _split_light(light, n, lead):
+    """Undo _stack_lights: n lights of batch shape ``lead``."""
+    from .vectorized_optics import VectorizedLight
+    comps = [c.reshape((n,) + tuple(lead) + tuple(c.shape[-2:])) for c in (light.Ex, light.Ey, light.Ez)]
+    return [VectorizedLight._wrap(light.x, light.y, light.wavelength, [c[k] for c in comps]) for k in range(n)]
+
+
+def _z_per_field(z, lead):
+    """A distance as a device float64 tensor with one value per field of a light of batch shape ``lead``."""
+    from . import engine
+    t = z if isinstance(z, torch.Tensor) else torch.full((), float(z), dtype=torch.float64, device=engine.device())
+    t = t.to(dtype=torch.float64).reshape(-1) if t.numel() > 1 else t.to(dtype=torch.float64).reshape(())
+    return t.expand(lead) if len(lead) else t.reshape(())
+
+
+def _batchable(edge, light):
+    return edge is not None and edge[0] == "vrs" and not light._ops
+
+
+def _run_edges(jobs):
+    """Run the edges leaving one wavefront of splitters.  Free-space edges of
+    lights with no pending program and the same grid and wavelength run as
+    one batched VRS with a distance per field; the others one by one."""
+    out = [None] * len(jobs)
+    groups = {}
+    for k, (edge, light) in enumerate(jobs):
+        if _batchable(edge, light):
+            key = (light.x.tobytes(), light.y.tobytes(), float(light.wavelength), tuple(light.Ex.shape))
+            groups.setdefault(key, []).append(k)
+        else:
+            out[k] = _run_edge(edge, light)
+    for ks in groups.values():
+        if len(ks) == 1:
+            out[ks[0]] = _run_edge(*jobs[ks[0]])
+            continue
+        lights = [jobs[k][1] for k in ks]
+        lead = tuple(lights[0].Ex.shape[:-2])
+        z = torch.stack([_z_per_field(jobs[k][0][1], lead) for k in ks]).reshape(-1)
+        res, _ = _stack_lights(lights).VRS_propagation(z)
+        for k, l in zip(ks, _split_light(res, len(ks), lead)):
+            out[k] = l
+    return out
+
+
+def _detect(lights, r, f, xout, yout):
+    """VCZT_objective_lens of every detector's light, as one batched focus
+    where the lights allow it."""
+    from . import optical_elements as oe
+    l0 = lights[0]
+    same = all(not l._ops and l.Ex.shape == l0.Ex.shape and l.wavelength == l0.wavelength and
+               np.array_equal(l.x, l0.x) and np.array_equal(l.y, l0.y) for l in lights)
+    if len(lights) < 2 or not same:
+        return [oe.VCZT_objective_lens(l, r, f, xout, yout) for l in lights]
+    det = oe.VCZT_objective_lens(_stack_lights(lights), r, f, xout, yout)
+    return _split_light(det, len(lights), tuple(l0.Ex.shape[:-2]))
+
+
 def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, yout):
     """Run a splitter grid.
 
@@ -103,20 +172,38 @@ def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, you
     (i, 0) from the left (None: no source); thetas[i][j]: splitter angles;
     horizontal[i][j]: the edge from (i, j)'s c port to (i, j+1);
     vertical[i][j]: the edge from (i, j)'s d port to (i+1, j); detectors: list
-    of (i, j, port 'c' or 'd', edge).  Returns the detectors' lights."""
-    from . import optical_elements as oe
+    of (i, j, port 'c' or 'd', edge).  Returns the detectors' lights.
+
+    The grid runs by wavefronts (the splitters with i + j = k depend only on
+    wavefront k - 1): the free-space edges leaving a wavefront run as one
+    batched VRS, and the detectors as one batched focus."""
     rows, cols = len(thetas), len(thetas[0])
-    ports = {}
-    for i in range(rows):
-        for j in range(cols):
-            a = top[j] if i == 0 else _run_edge(vertical[i - 1][j], ports[(i - 1, j)][1])
-            b = left[i] if j == 0 else _run_edge(horizontal[i][j - 1], ports[(i, j - 1)][0])
-            ports[(i, j)] = _splitter(a, b, thetas[i][j])
-    out = []
-    for i, j, port, edge in detectors:
-        light = ports[(i, j)][0 if port == "c" else 1]
-        out.append(oe.VCZT_objective_lens(_run_edge(edge, light), r, f, xout, yout))
-    return out
+    a_in = {(0, j): top[j] for j in range(cols)}
+    b_in = {(i, 0): left[i] for i in range(rows)}
+    det_in = [None] * len(detectors)
+    for k in range(rows + cols - 1):
+        cells = [(i, k - i) for i in range(rows) if 0 <= k - i < cols]
+        jobs, targets = [], []
+        for i, j in cells:
+            c, d = _splitter(a_in.get((i, j)), b_in.get((i, j)), thetas[i][j])
+            if j + 1 < cols:
+                jobs.append((horizontal[i][j], c))
+                targets.append(("b", (i, j + 1)))
+            if i + 1 < rows:
+                jobs.append((vertical[i][j], d))
+                targets.append(("a", (i + 1, j)))
+            for q, (di, dj, port, edge) in enumerate(detectors):
+                if (di, dj) == (i, j):
+                    jobs.append((edge, c if port == "c" else d))
+                    targets.append(("det", q))
+        for (kind, key), light in zip(targets, _run_edges(jobs)):
+            if kind == "a":
+                a_in[key] = light
+            elif kind == "b":
+                b_in[key] = light
+            else:
+                det_in[key] = light
+    return _detect(det_in, r, f, xout, yout)
 
 
 def _ez_intensities(dets):
