@@ -290,6 +290,37 @@ def main(ref_root):
               ax_scalar=ax_s.field, ax_mask=ax_mask, ax_Ex=ax_v.Ex, ax_Ey=ax_v.Ey, ax_Ez=ax_v.Ez,
               triangle=tri, rectangle=rect, annulus=ann, forked_amplitude=fg_a, forked_phase=fg_p)
 
+        # 15. the array-level entry points: RS / VRS jit, the transfer function,
+        # CZT jit, the plain Bluestein pair, Bluestein_method and the lens helper.
+        from xlumina import vectorized_optics as vo
+        from xlumina import wave_optics as wo
+        x, y = tb.space(140.0, 36)
+        wl = 0.6
+        kk = 2 * np.pi / wl
+        f_in = rng.standard_normal((36, 36)) + 1j * rng.standard_normal((36, 36))
+        E3 = rng.standard_normal((3, 36, 36)) + 1j * rng.standard_normal((3, 36, 36))
+        nx_, ny_, dx_, dy_, Xe, Ye = wo.build_grid(x, y)
+        rs_jit = wo.RS_propagation_jit(f_in, 2100.0, nx_, ny_, dx_, dy_, Xe, Ye, kk)
+        vrs_jit = vo.VRS_propagation_jit(E3, 2100.0, nx_, ny_, dx_, dy_, Xe, Ye, kk)
+        H = wo.transfer_function_RS(2100.0, Xe, Ye, kk)
+        xo = np.linspace(-30.0, 30.0, 24)
+        yo = np.linspace(-20.0, 20.0, 20)
+        cnx, cny, cdx, cdy, Xo, Yo, Dm, fy1, fy2, fx1, fx2 = wo.build_CZT_grid(2500.0, wl, x, y, xo, yo)
+        Xg, Yg = np.meshgrid(x, y)
+        czt_jit = wo.CZT_jit(f_in, 2500.0, wl, kk, cnx, cny, cdx, cdy, Xo, Yo, Xg, Yg, Dm, fy1, fy2, fx1, fx2)
+        g = (Dm, fy1, fy2, fx1, fx2)
+        hg = oe.build_high_NA_VCZT_grid(2000.0, 1800.0, wl, x, xo, yo)
+        plain = wo.CZT_for_high_NA_jit(f_in, *hg)
+        blu = wo.Bluestein_method(f_in, -12.0, 15.0, 60.0, 20)
+        th = rng.uniform(0, 0.8, (36, 36))
+        phv = rng.uniform(-np.pi, np.pi, (36, 36))
+        Gv = rng.uniform(0, 1, (36, 36))
+        lens_h = oe._high_NA_objective_lens_(np.moveaxis(E3, 0, -1), th, phv, Gv)
+        _save("array_api", x=x, y=y, wavelength=wl, field=f_in, E3=E3, rs_jit=rs_jit, vrs_jit=vrs_jit, H=H,
+              xout=xo, yout=yo, czt_grid=np.array(g, dtype=np.float64), czt_jit=czt_jit,
+              hna_grid=np.array(hg, dtype=np.float64), plain=plain, bluestein=blu, theta=th, phi=phv, G=Gv,
+              lens_helper=lens_h)
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

@@ -825,6 +825,41 @@ class CztCall:
         _lib.check(lib().xl_czt_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_czt_stage")
 
 
+def czt_plain(comps, mx, my, Dm, fy1, fy2, fx1, fx2, cte=1.0):
+    """The two Bluestein transforms alone (CZT_for_high_NA_jit,
+    wave_optics.py:359-371): each (ny, nx) plane onto my x mx outputs over the
+    frequency ranges given; ``comps`` are 1 to 3 components, each of shape
+    (ny, nx) or (B, ny, nx).  Returns the output planes."""
+    L = lib()
+    ny, nx = comps[0].shape[-2:]
+    lead = comps[0].shape[:-2]
+    planes, B, ibs = batch_planes(comps, ny, nx)
+    dev = planes[0].device
+    Lx, prex, gx, postx = device_chirps(nx, float(fx1), float(fx2), float(Dm), int(mx))
+    Ly, prey, gy, posty = device_chirps(ny, float(fy1), float(fy2), float(Dm), int(my))
+    C = len(planes)
+    work = torch.empty(L.xl_czt_work_bytes(B, C, ny, mx) // 8, dtype=torch.complex64, device=dev)
+    outs = [torch.empty(tuple(lead) + (my, mx), dtype=torch.complex64, device=dev) for _ in range(C)]
+    a = _lib.XlCztArgs()
+    a.batch, a.comps_in, a.comps_out, a.mode = B, C, C, _lib.XL_CZT_PLAIN
+    a.ny, a.nx, a.my, a.mx = ny, nx, int(my), int(mx)
+    a.log2_lx, a.log2_ly = int(Lx).bit_length() - 1, int(Ly).bit_length() - 1
+    for i, c in enumerate(planes):
+        a.inp[i] = c.data_ptr()
+    for i, o in enumerate(outs):
+        a.out[i] = o.data_ptr()
+    a.in_bstride, a.out_bstride = ibs, int(my) * int(mx)
+    a.cte_re, a.cte_im = complex(cte).real, complex(cte).imag
+    a.pre_x, a.g_x, a.post_x = prex.data_ptr(), gx.data_ptr(), postx.data_ptr()
+    a.pre_y, a.g_y, a.post_y = prey.data_ptr(), gy.data_ptr(), posty.data_ptr()
+    a.work = work.data_ptr()
+    fill_prog(a.pre, [], ny, nx)
+    keep = (planes, work, prex, gx, postx, prey, gy, posty)
+    _lib.check(L.xl_czt(stream_handle(), ctypes.byref(a)), "xl_czt")
+    del keep
+    return outs
+
+
 def czt_propagate(comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None):
     """Scalar CZT, VCZT or the high-NA focus; returns 1 or 3 output tensors."""
     return CztCall(comps, x, y, wavelength, z, xout, yout, mode, pre, lens).run()

@@ -371,3 +371,7 @@ from .hybrid_setups import (batch_robust_discovery, hybrid_setup_fixed_slms,  # 
                             hybrid_setup_sharp_focus, robust_discovery, six_times_six_ansatz)
 # Table noise (optical_elements.py:2127-2301; shake_setup_jit reads noise.NS).
 from .noise import batch_shake_setup, keychain_optical_tables, shake_setup, shake_setup_jit  # noqa: E402,F401
+
+
+# The array-level entry points the reference's classes call inside.
+from .functional import _high_NA_objective_lens_  # noqa: E402,F401

@@ -141,3 +141,7 @@ class PolarizedLightSource(VectorizedLight):
         pw = engine.plane_wave_field(self.x, self.y, self.wavelength, 1.0, theta, phi, z0)
         self._ops = []
         self._E = [pw * complex(jv[0]), pw * complex(jv[1]), self._zeros()]
+
+
+# The array-level entry points the reference's classes call inside.
+from .functional import VRS_propagation_jit, VCZT_jit, vectorized_CZT_for_high_NA  # noqa: E402,F401

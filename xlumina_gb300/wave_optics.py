@@ -210,3 +210,7 @@ def build_CZT_grid(z, wavelength, xin, yin, xout, yout):
                         engine.as_grid(yout))
     Xout, Yout = np.meshgrid(xout, yout)
     return g["nx"], g["ny"], g["dx"], g["dy"], Xout, Yout, g["Dm"], g["fy1"], g["fy2"], g["fx1"], g["fx2"]
+
+
+# The array-level entry points the reference's classes call inside.
+from .functional import transfer_function_RS, RS_propagation_jit, CZT_jit, CZT_for_high_NA_jit, compute_fft, Bluestein_method  # noqa: E402,F401
