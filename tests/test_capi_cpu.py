@@ -50,6 +50,7 @@ def test_size_helpers(lib):
     assert lib.xl_rs_spectrum_bytes(2048, 2048) == 4096 * 4096 * 8
     assert lib.xl_rs_spectrum_bytes(1000, 1000) == 2048 * 2048 * 8
     assert lib.xl_rs_work_bytes(8, 3, 2048, 2048) == 8 * 3 * 2048 * 4096 * 8
+    assert lib.xl_rs_spectrum_bytes(10, 10) == 64 * 64 * 8     # the smallest transform, P = 64
     assert lib.xl_rs_spectrum_bytes(1, 10) == 0
     assert lib.xl_rs_spectrum_bytes(8192, 8192) == 0
 

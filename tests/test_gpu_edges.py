@@ -1,0 +1,63 @@
+"""Edge cases of the propagators against the FP64 oracle: the smallest
+grids, odd and non-square grids (the oracle restates the (2ny-1) x (2nx-1)
+pad for any shape; the reference's own build_grid assumes nx == ny),
+negative distances for VRS, and one batch mixing distances of both signs.
+Bar: rel-L2 1e-5 (complex64)."""
+import numpy as np
+import pytest
+
+from oracle import xlumina_ref as ref
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _rnd(rng, *s):
+    return rng.standard_normal(s) + 1j * rng.standard_normal(s)
+
+
+@pytest.mark.parametrize("ny,nx", [(2, 2), (3, 3), (5, 7), (17, 16), (33, 64), (100, 37)])
+def test_rs_small_odd_and_non_square(ny, nx):
+    from xlumina_gb300 import engine
+    rng = np.random.default_rng(ny * 100 + nx)
+    x = np.linspace(-40.0, 40.0, nx)
+    y = np.linspace(-30.0, 30.0, ny) if ny > 1 else np.array([0.0])
+    f = _rnd(rng, ny, nx)
+    out = engine.rs_propagate([engine.as_field(f)], x, y, 0.6, 900.0, vector=False)[0].cpu().numpy()
+    assert rel_l2(out, ref.rs_propagate(f, x, y, 0.6, 900.0)) < TOL
+
+
+def test_vrs_negative_distance_and_mixed_batch():
+    import torch
+
+    from xlumina_gb300 import engine
+    rng = np.random.default_rng(77)
+    n = 96
+    x, y = ref.space(240.0, n)
+    Ex, Ey = _rnd(rng, 3, n, n), _rnd(rng, 3, n, n)
+    zs = [-2200.0, 1500.0, -900.0]
+    outs = engine.rs_propagate([torch.as_tensor(Ex.astype(np.complex64), device="cuda"),
+                                torch.as_tensor(Ey.astype(np.complex64), device="cuda")], x, y, 0.55, zs, vector=True)
+    for b, z in enumerate(zs):
+        exp = ref.vrs_propagate(Ex[b], Ey[b], x, y, 0.55, z)
+        for o, e in zip(outs, exp):
+            assert rel_l2(o[b].cpu().numpy(), e) < TOL
+    # the same batch with the distances on the device (spectra built there)
+    zt = torch.tensor(zs, dtype=torch.float64, device="cuda")
+    outs_d = engine.rs_propagate([torch.as_tensor(Ex.astype(np.complex64), device="cuda"),
+                                  torch.as_tensor(Ey.astype(np.complex64), device="cuda")], x, y, 0.55, zt, vector=True)
+    for o, od in zip(outs, outs_d):
+        assert torch.equal(o, od)
+
+
+def test_czt_non_square_roi_and_negative_distance():
+    from xlumina_gb300 import engine
+    rng = np.random.default_rng(78)
+    x, y = ref.space(300.0, 80)
+    f = _rnd(rng, 80, 80)
+    xo = np.linspace(-50.0, 40.0, 33)
+    yo = np.linspace(-20.0, 60.0, 18)
+    for z in (3000.0, -3000.0):
+        out = engine.czt_propagate([engine.as_field(f)], x, y, 0.6, z, xo, yo, "scalar")[0].cpu().numpy()
+        assert rel_l2(out, ref.czt(f, x, y, 0.6, z, xo, yo)) < TOL

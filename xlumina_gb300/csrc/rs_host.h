@@ -27,10 +27,12 @@ struct RsLaunch {
 };
 
 // Q = 2^logq is the half transform length: the smallest power of two >= the field side.
+// Q = 2^logq >= the field side, at least 32: the transfer-spectrum row pass
+// takes G = 256 / T rows per CTA, which for Q = 16 (P = 32) exceeds P.
 inline int rs_logq(int ny, int nx) {
   const int n = ny > nx ? ny : nx;
   const int l = ilog2_ceil(n);
-  return l < 4 ? 4 : l;
+  return l < 5 ? 5 : l;
 }
 
 // Transfer spectrum and propagation passes for Q = 2^LOGQ (explicitly

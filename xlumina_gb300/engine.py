@@ -193,9 +193,10 @@ class _Built:
 # ------------------------------------------------------------- geometry --
 
 def rs_logq(ny: int, nx: int) -> int:
-    """Q = 2^logq is the half transform length: the smallest power of two >= the field side."""
+    """Q = 2^logq is the half transform length: the smallest power of two >= the
+    field side, at least 32 (the kernels' smallest CTA shapes need P >= 64)."""
     n = max(ny, nx)
-    return max(4, int(math.ceil(math.log2(n))))
+    return max(5, int(math.ceil(math.log2(n))))
 
 
 def rs_offset_axis(x: np.ndarray) -> np.ndarray:
