@@ -61,3 +61,15 @@ def test_czt_non_square_roi_and_negative_distance():
     for z in (3000.0, -3000.0):
         out = engine.czt_propagate([engine.as_field(f)], x, y, 0.6, z, xo, yo, "scalar")[0].cpu().numpy()
         assert rel_l2(out, ref.czt(f, x, y, 0.6, z, xo, yo)) < TOL
+
+
+@pytest.mark.parametrize("n,mx,my", [(5, 3, 5), (9, 6, 2), (31, 7, 11)])
+def test_czt_small_grids(n, mx, my):
+    from xlumina_gb300 import engine
+    rng = np.random.default_rng(n * 7 + mx)
+    x = np.linspace(-20.0, 20.0, n)
+    f = _rnd(rng, n, n)
+    xo = np.linspace(-5.0, 6.0, mx)
+    yo = np.linspace(-4.0, 3.0, my)
+    out = engine.czt_propagate([engine.as_field(f)], x, x, 0.5, 800.0, xo, yo, "scalar")[0].cpu().numpy()
+    assert rel_l2(out, ref.czt(f, x, x, 0.5, 800.0, xo, yo)) < TOL
