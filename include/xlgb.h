@@ -262,14 +262,25 @@ int xl_ops_backward(void* stream, int batch, int comps, int ny, int nx, const vo
  * :380-383), BS_symmetric_SI (:393-460: one input port, b absent) and the
  * lossless BS (:462-512: M = [[sqrt T, sqrt R e^{i phase}], [-sqrt R
  * e^{-i phase}, sqrt T]]).  The outputs' Ez is zero (not written). */
+enum {
+  XL_BS_MATRIX = 0,        /* M given in `m` */
+  XL_BS_SYMMETRIC = 1,     /* BS_symmetric: M = [[R, iT], [iT, R]] from the angle `theta` */
+  XL_BS_SINGLE_PORT0 = 2,  /* BS_symmetric_SI, port 0: c = R a, d = iT a */
+  XL_BS_SINGLE_PORT1 = 3   /* BS_symmetric_SI, port 1: c = iT a, d = R a */
+};
+
 typedef struct {
   int batch, ny, nx;
   const void* in[2][2];       /* [port a, b][Ex, Ey] complex64 planes; port b may be NULL (zero) */
   long long in_bstride[2];    /* elements between batch entries, per port (0: one plane for the batch) */
   void* out[2][2];            /* [port c, d][Ex, Ey]; NULL planes are not written */
   long long out_bstride;
-  const void* m;              /* device complex64 M, 4 entries per batch entry */
+  const void* m;              /* XL_BS_MATRIX: device complex64 M, 4 entries per batch entry */
   long long m_bstride;        /* 0 (one M for the batch) or 4 */
+  const double* theta;        /* the other kinds: device splitter angle(s), R = |sin| - 0.01 |cos|,
+                                 T = 0.99 |cos| (optical_elements.py:376-383) */
+  long long theta_bstride;    /* 0 (one angle for the batch) or 1 */
+  int kind;                   /* XL_BS_* */
 } XlBsArgs;
 
 int xl_beam_splitter(void* stream, const XlBsArgs* args);
@@ -282,10 +293,12 @@ size_t xl_beam_splitter_work_bytes(int batch, int ny, int nx);
  * zero); gin[4] receives the gradients of (a.Ex, a.Ey, b.Ex, b.Ey) = M^H gout
  * (NULL skips); s (complex64, 4 per batch entry, may be NULL) receives
  * S_ij = sum conj(gout_i) in_j over pixels and both components, whose
- * conjugate is the gradient of M_ij (fixed-order sums). */
+ * conjugate is the gradient of M_ij (fixed-order sums); for the angle kinds,
+ * dtheta (device float64 per batch entry, may be NULL; needs s) receives
+ * dL/dtheta = sum_ij Re(dM_ij/dtheta S_ij). */
 int xl_beam_splitter_backward(void* stream, const XlBsArgs* args, const void* const* gout,
                               long long gout_bstride, void* const* gin, long long gin_bstride, void* s,
-                              void* work);
+                              void* work, void* dtheta);
 
 /* ---- Reductions for gradients -------------------------------------------- */
 

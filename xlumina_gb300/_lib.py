@@ -64,7 +64,11 @@ class XlBsArgs(ctypes.Structure):
     _fields_ = [("batch", ctypes.c_int), ("ny", ctypes.c_int), ("nx", ctypes.c_int),
                 ("inp", (ctypes.c_void_p * 2) * 2), ("in_bstride", ctypes.c_longlong * 2),
                 ("out", (ctypes.c_void_p * 2) * 2), ("out_bstride", ctypes.c_longlong),
-                ("m", ctypes.c_void_p), ("m_bstride", ctypes.c_longlong)]
+                ("m", ctypes.c_void_p), ("m_bstride", ctypes.c_longlong), ("theta", ctypes.c_void_p),
+                ("theta_bstride", ctypes.c_longlong), ("kind", ctypes.c_int)]
+
+
+XL_BS_MATRIX, XL_BS_SYMMETRIC, XL_BS_SINGLE_PORT0, XL_BS_SINGLE_PORT1 = 0, 1, 2, 3
 
 
 XL_NOISE_MAX_TABLES = 256
@@ -135,7 +139,7 @@ SIGNATURES = {
     "xl_beam_splitter_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlBsArgs),
                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
-                                                 ctypes.c_void_p, ctypes.c_void_p]),
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "xl_table_noise": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlNoiseArgs), ctypes.POINTER(ctypes.c_uint32)]),
     "xl_philox4x32_10": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                         ctypes.POINTER(ctypes.c_uint32)]),

@@ -221,41 +221,45 @@ def _sum_to(g, shape):
 
 
 class _BeamSplitter(torch.autograd.Function):
-    """Two-port mixing c, d = M [a; b] with the hand-written backward of libxlgb."""
+    """Two-port mixing c, d = M [a; b] with the hand-written backward of
+    libxlgb; ``m`` is the matrix (kind 0) or the splitting angle (the lossy
+    kinds, M built inside the kernels)."""
 
     @staticmethod
-    def forward(ctx, m, a_ex, a_ey, b_ex, b_ey):
+    def forward(ctx, kind, m, a_ex, a_ey, b_ex, b_ey):
         b = None if b_ex is None else [b_ex, b_ey]
         ctx.has_b = b is not None
+        ctx.kind = kind
         ctx.save_for_backward(m, a_ex, a_ey, b_ex, b_ey)
-        return tuple(engine.beam_splitter([a_ex, a_ey], b, m))
+        return tuple(engine.beam_splitter([a_ex, a_ey], b, m, kind))
 
     @staticmethod
     def backward(ctx, *gouts):
         m, a_ex, a_ey, b_ex, b_ey = ctx.saved_tensors
         need = ctx.needs_input_grad
-        want_m, want_a = need[0], need[1] or need[2]
-        want_b = ctx.has_b and (need[3] or need[4])
+        want_m, want_a = need[1], need[2] or need[3]
+        want_b = ctx.has_b and (need[4] or need[5])
         b = [b_ex, b_ey] if ctx.has_b else None
-        ga, gb, s = engine.beam_splitter_backward([a_ex, a_ey], b, m, list(gouts), want_a, want_b, want_m)
+        ga, gb, s = engine.beam_splitter_backward([a_ex, a_ey], b, m, list(gouts), want_a, want_b, want_m,
+                                                  ctx.kind)
         gm = None
         if want_m:
-            gm = torch.conj(s)
-            if gm.shape != m.shape:       # one matrix for the batch
-                gm = gm.sum(0).reshape(m.shape)
-            gm = gm.to(m.dtype)
-        out = [gm, None, None, None, None]
+            gm = torch.conj(s) if ctx.kind == 0 else s
+            if gm.numel() != m.numel():     # one matrix / angle for the batch
+                gm = gm.sum(0)
+            gm = gm.reshape(m.shape).to(device=m.device, dtype=m.dtype)
+        out = [None, gm, None, None, None, None]
         if ga is not None:
-            out[1], out[2] = _sum_to(ga[0], a_ex.shape), _sum_to(ga[1], a_ey.shape)
+            out[2], out[3] = _sum_to(ga[0], a_ex.shape), _sum_to(ga[1], a_ey.shape)
         if gb is not None:
-            out[3], out[4] = _sum_to(gb[0], b_ex.shape), _sum_to(gb[1], b_ey.shape)
+            out[4], out[5] = _sum_to(gb[0], b_ex.shape), _sum_to(gb[1], b_ey.shape)
         return tuple(out)
 
 
-def beam_splitter(a, b, m):
-    """[c.Ex, c.Ey, d.Ex, d.Ey] = M [a; b]; differentiable in a, b and M."""
+def beam_splitter(a, b, m, kind=0):
+    """[c.Ex, c.Ey, d.Ex, d.Ey] = M [a; b]; differentiable in a, b and M (or the angle)."""
     tensors = [m] + list(a) + (list(b) if b is not None else [])
     if torch.is_grad_enabled() and any(isinstance(t, torch.Tensor) and t.requires_grad for t in tensors):
         bx, by = (b[0], b[1]) if b is not None else (None, None)
-        return list(_BeamSplitter.apply(m, a[0], a[1], bx, by))
-    return engine.beam_splitter(a, b, m)
+        return list(_BeamSplitter.apply(kind, m, a[0], a[1], bx, by))
+    return engine.beam_splitter(a, b, m, kind)

@@ -4,8 +4,10 @@
 // lossless BS (:462-512) are all one complex 2x2 matrix M applied to the
 // (Ex, Ey) planes of the input ports a, b:
 //   c = M00 a + M01 b,   d = M10 a + M11 b     (Ez of c, d is zero).
-// M is read from device memory (per batch entry, or one for the batch), so a
-// differentiable splitting angle never has to be read back to the host.
+// M is read from device memory (per batch entry, or one for the batch), or,
+// for the lossy splitters, computed in each CTA from the splitting angle in
+// device memory: a differentiable angle is never read back to the host and
+// needs no separate kernels to build M or to take dL/dtheta.
 //
 // The backward runs in one pass over the output gradients gc, gd and the
 // forward inputs: the input gradients (M^H applied to the output gradients)
@@ -26,8 +28,42 @@ struct BsKernelArgs {
   long long obs;
   const float2* m;
   long long mbs;
+  const double* theta;      // splitter angle (kind > 0), per batch entry when tbs = 1
+  long long tbs;
+  int kind;
   int npix;
 };
+
+// R and T of the lossy symmetric splitter (optical_elements.py:376-383):
+// R = |sin t| - 0.01 |cos t|, T = 0.99 |cos t|, and their derivatives
+// (d|u| = sign(u) du, sign(0) = 0, as torch's and jax's abs).
+__host__ __device__ __forceinline__ void bs_rt(double t, double* R, double* T, double* dR, double* dT) {
+  const double s = sin(t), c = cos(t);
+  const double ss = (s > 0) - (s < 0), sc = (c > 0) - (c < 0);
+  *R = fabs(s) - 0.01 * fabs(c);
+  *T = 0.99 * fabs(c);
+  *dR = ss * c + 0.01 * sc * s;
+  *dT = -0.99 * sc * s;
+}
+
+// The splitter matrix of batch entry b: given (kind 0), or from the angle.
+__device__ __forceinline__ void bs_matrix(const BsKernelArgs& p, int b, float2 (&m)[4]) {
+  if (p.kind == XL_BS_MATRIX) {
+    const float2* q = p.m + (long long)b * p.mbs;
+    for (int i = 0; i < 4; ++i) m[i] = q[i];
+    return;
+  }
+  double R, T, dR, dT;
+  bs_rt(p.theta[(long long)b * p.tbs], &R, &T, &dR, &dT);
+  const float2 r = make_float2((float)R, 0.f), it = make_float2(0.f, (float)T), z = make_float2(0.f, 0.f);
+  if (p.kind == XL_BS_SYMMETRIC) {          // c = R a + iT b, d = iT a + R b
+    m[0] = r; m[1] = it; m[2] = it; m[3] = r;
+  } else if (p.kind == XL_BS_SINGLE_PORT0) { // c = R a, d = iT a
+    m[0] = r; m[1] = z; m[2] = it; m[3] = z;
+  } else {                                  // port 1: c = iT a, d = R a
+    m[0] = it; m[1] = z; m[2] = r; m[3] = z;
+  }
+}
 
 __device__ __forceinline__ float2 ld_or_zero(const float2* p, long long i) {
   return p ? p[i] : make_float2(0.f, 0.f);
@@ -35,7 +71,8 @@ __device__ __forceinline__ float2 ld_or_zero(const float2* p, long long i) {
 
 __global__ void __launch_bounds__(BS_THREADS) bs_apply_kernel(BsKernelArgs p) {
   const int b = blockIdx.y;
-  const float2* m = p.m + (long long)b * p.mbs;
+  float2 m[4];
+  bs_matrix(p, b, m);
   const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
   const long long ib0 = (long long)b * p.ibs[0], ib1 = (long long)b * p.ibs[1], ob = (long long)b * p.obs;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.npix; i += gridDim.x * blockDim.x) {
@@ -62,7 +99,8 @@ struct BsBackArgs {
 // (Re S00, Im S00, Re S01, Im S01, Re S10, Im S10, Re S11, Im S11).
 __global__ void __launch_bounds__(BS_THREADS) bs_backward_kernel(BsBackArgs p) {
   const int b = blockIdx.y;
-  const float2* m = p.f.m + (long long)b * p.f.mbs;
+  float2 m[4];
+  bs_matrix(p.f, b, m);
   const float2 m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
   const long long ib0 = (long long)b * p.f.ibs[0], ib1 = (long long)b * p.f.ibs[1];
   const long long gb = (long long)b * p.gbs, ob = (long long)b * p.ginbs;
@@ -111,6 +149,24 @@ __global__ void bs_finish_kernel(const double* __restrict__ partial, int nblk, i
   if (lane == 0) out[row] = (float)t;
 }
 
+// dL/dtheta per batch entry from S_ij = sum conj(g_i) in_j: sum_ij Re(dM_ij/dtheta S_ij).
+__global__ void bs_dtheta_kernel(const float2* __restrict__ S, const double* __restrict__ theta, long long tbs,
+                                 int kind, int batch, double* __restrict__ dtheta) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double R, T, dR, dT;
+  bs_rt(theta[(long long)b * tbs], &R, &T, &dR, &dT);
+  const float2* s = S + 4 * (long long)b;
+  double g;
+  if (kind == XL_BS_SYMMETRIC)
+    g = dR * ((double)s[0].x + s[3].x) - dT * ((double)s[1].y + s[2].y);
+  else if (kind == XL_BS_SINGLE_PORT0)
+    g = dR * s[0].x - dT * s[2].y;
+  else
+    g = -dT * s[0].y + dR * s[2].x;
+  dtheta[b] = g;
+}
+
 static int bs_blocks(int npix) {
   int nb = (npix + BS_THREADS * 4 - 1) / (BS_THREADS * 4);
   if (nb > 152 * 4) nb = 152 * 4;
@@ -119,7 +175,9 @@ static int bs_blocks(int npix) {
 
 static int bs_check(const XlBsArgs* a, const char* where) {
   if (!a || a->batch < 1 || a->batch > 65535 || a->ny < 1 || a->nx < 1 ||
-      (long long)a->ny * a->nx > 0x7fffffffLL || !a->m || !a->in[0][0] || !a->in[0][1] ||
+      (long long)a->ny * a->nx > 0x7fffffffLL || a->kind < XL_BS_MATRIX || a->kind > XL_BS_SINGLE_PORT1 ||
+      (a->kind == XL_BS_MATRIX && !a->m) || (a->kind != XL_BS_MATRIX && !a->theta) ||
+      (a->theta_bstride != 0 && a->theta_bstride != 1) || !a->in[0][0] || !a->in[0][1] ||
       (!a->in[1][0]) != (!a->in[1][1]) || a->in_bstride[0] < 0 || a->in_bstride[1] < 0 ||
       a->out_bstride < 0 || (a->m_bstride != 0 && a->m_bstride != 4)) {
     set_error("%s: bad arguments", where);
@@ -140,6 +198,9 @@ static BsKernelArgs bs_kernel_args(const XlBsArgs* a) {
   k.obs = a->out_bstride;
   k.m = (const float2*)a->m;
   k.mbs = a->m_bstride;
+  k.theta = a->theta;
+  k.tbs = a->theta_bstride;
+  k.kind = a->kind;
   k.npix = a->ny * a->nx;
   return k;
 }
@@ -163,9 +224,10 @@ extern "C" size_t xl_beam_splitter_work_bytes(int batch, int ny, int nx) {
 
 extern "C" int xl_beam_splitter_backward(void* stream, const XlBsArgs* a, const void* const* gout,
                                          long long gout_bstride, void* const* gin, long long gin_bstride,
-                                         void* s, void* work) {
+                                         void* s, void* work, void* dtheta) {
   if (int rc = bs_check(a, "xl_beam_splitter_backward")) return rc;
-  if (!gout || (s && !work) || gout_bstride < 0 || gin_bstride < 0) {
+  if (!gout || (s && !work) || gout_bstride < 0 || gin_bstride < 0 ||
+      (dtheta && (!s || a->kind == XL_BS_MATRIX))) {
     set_error("xl_beam_splitter_backward: bad arguments");
     return XL_EINVAL;
   }
@@ -191,6 +253,11 @@ extern "C" int xl_beam_splitter_backward(void* stream, const XlBsArgs* a, const 
     const int rows = a->batch * 8;
     bs_finish_kernel<<<(rows + 3) / 4, 128, 0, st>>>((const double*)work, nb, rows, (float*)s);
     XL_CHECK_LAUNCH("bs_finish_kernel");
+  }
+  if (dtheta) {
+    bs_dtheta_kernel<<<(a->batch + 127) / 128, 128, 0, st>>>((const float2*)s, a->theta, a->theta_bstride,
+                                                             a->kind, a->batch, (double*)dtheta);
+    XL_CHECK_LAUNCH("bs_dtheta_kernel");
   }
   return XL_OK;
 }

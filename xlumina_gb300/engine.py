@@ -1032,32 +1032,45 @@ def _bs_batch(a, b, m):
     return B, tuple(lead) if B > 1 else ()
 
 
-def _bs_args(a, b, m, ny, nx):
-    B, lead = _bs_batch(a, b, m)
+def _bs_args(a, b, m, ny, nx, kind=0):
+    """``m``: the complex (2, 2) / (B, 2, 2) matrix (kind XL_BS_MATRIX), or the
+    splitting angle(s) as a float64 device tensor of 1 or B values."""
+    if kind == _lib.XL_BS_MATRIX:
+        B, lead = _bs_batch(a, b, m)
+    else:
+        B, lead = _bs_batch(a, b, m.reshape(-1, 1, 1) if m.numel() > 1 else m.reshape(1, 1))
     pa, sa = _bs_port(a, B, ny, nx)
     pb, sb = _bs_port(b, B, ny, nx)
-    if m.dim() == 3 and m.shape[0] == 1:
-        m = m[0]
-    if m.dim() == 3 and m.shape[0] != B:
-        raise ValueError(f"{m.shape[0]} splitter matrices for a batch of {B}")
-    m = m.to(torch.complex64).contiguous()
     args = _lib.XlBsArgs()
-    args.batch, args.ny, args.nx = B, ny, nx
+    args.batch, args.ny, args.nx, args.kind = B, ny, nx, int(kind)
+    if kind == _lib.XL_BS_MATRIX:
+        if m.dim() == 3 and m.shape[0] == 1:
+            m = m[0]
+        if m.dim() == 3 and m.shape[0] != B:
+            raise ValueError(f"{m.shape[0]} splitter matrices for a batch of {B}")
+        m = m.to(torch.complex64).contiguous()
+        args.m = m.data_ptr()
+        args.m_bstride = 4 if m.dim() == 3 else 0
+    else:
+        m = m.detach().to(device=device(), dtype=torch.float64).reshape(-1).contiguous()
+        if m.numel() not in (1, B):
+            raise ValueError(f"{m.numel()} splitter angles for a batch of {B}")
+        args.theta = m.data_ptr()
+        args.theta_bstride = 1 if m.numel() > 1 else 0
     for j, port in enumerate((pa, pb)):
         for c in range(2):
             args.inp[j][c] = _ptr(port[c])
     args.in_bstride[0], args.in_bstride[1] = sa, sb
-    args.m = m.data_ptr()
-    args.m_bstride = 4 if m.dim() == 3 else 0
     return args, B, lead, (pa, pb, m)
 
 
-def beam_splitter(a, b, m):
+def beam_splitter(a, b, m, kind=0):
     """[c.Ex, c.Ey, d.Ex, d.Ey] = M [a; b] on the (Ex, Ey) planes (libxlgb).
     ``a``, ``b``: [Ex, Ey] tensors of shape (ny, nx) or (B, ny, nx) (``b`` may be
-    None); ``m``: complex device tensor (2, 2) or (B, 2, 2)."""
+    None); ``m``: complex device tensor (2, 2) or (B, 2, 2), or for the angle
+    kinds (XL_BS_SYMMETRIC, XL_BS_SINGLE_PORT0/1) the splitting angle(s)."""
     ny, nx = a[0].shape[-2:]
-    args, B, lead, keep = _bs_args(a, b, m, ny, nx)
+    args, B, lead, keep = _bs_args(a, b, m, ny, nx, kind)
     dev = keep[0][0].device
     outs = [torch.empty(lead + (ny, nx), dtype=torch.complex64, device=dev) for _ in range(4)]
     for i in range(2):
@@ -1068,11 +1081,12 @@ def beam_splitter(a, b, m):
     return outs
 
 
-def beam_splitter_backward(a, b, m, gouts, want_a=True, want_b=True, want_m=True):
-    """Gradients of ``beam_splitter``: (ga [Ex, Ey] or None, gb or None,
-    S (B, 2, 2) complex64 or None) with S_ij = sum conj(g_i) in_j, per batch entry."""
+def beam_splitter_backward(a, b, m, gouts, want_a=True, want_b=True, want_m=True, kind=0):
+    """Gradients of ``beam_splitter``: (ga [Ex, Ey] or None, gb or None, the
+    matrix's S (B, 2, 2) complex64 with S_ij = sum conj(g_i) in_j, or for the
+    angle kinds dL/dtheta (B,) float64; None when not wanted)."""
     ny, nx = a[0].shape[-2:]
-    args, B, lead, keep = _bs_args(a, b, m, ny, nx)
+    args, B, lead, keep = _bs_args(a, b, m, ny, nx, kind)
     dev = keep[0][0].device
     gs = [None if g is None else as_field(g).reshape((B, ny, nx) if B > 1 else (ny, nx)).contiguous()
           for g in gouts]
@@ -1086,10 +1100,11 @@ def beam_splitter_backward(a, b, m, gouts, want_a=True, want_b=True, want_m=True
         s = torch.empty((B, 2, 2), dtype=torch.complex64, device=dev)
         work = torch.empty(max(1, lib().xl_beam_splitter_work_bytes(B, ny, nx) // 8), dtype=torch.float64,
                            device=dev)
+    dth = torch.empty(B, dtype=torch.float64, device=dev) if (want_m and kind != _lib.XL_BS_MATRIX) else None
     gp = (ctypes.c_void_p * 4)(*[_ptr(g) for g in gs])
     ip = (ctypes.c_void_p * 4)(*[_ptr(g) for g in gin])
     _lib.check(lib().xl_beam_splitter_backward(stream_handle(), ctypes.byref(args), gp, ny * nx, ip, ny * nx,
-                                               _ptr(s), _ptr(work)), "xl_beam_splitter_backward")
+                                               _ptr(s), _ptr(work), _ptr(dth)), "xl_beam_splitter_backward")
     ga = gin[0:2] if want_a else None
     gb = gin[2:4] if (want_b and b is not None) else None
-    return ga, gb, s
+    return ga, gb, (dth if kind != _lib.XL_BS_MATRIX else s)

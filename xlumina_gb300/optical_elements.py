@@ -13,7 +13,7 @@ import time
 import numpy as np
 import torch
 
-from . import autograd, cm, engine, um  # noqa: F401  (units re-exported as in the reference)
+from . import _lib, autograd, cm, engine, um  # noqa: F401  (units re-exported as in the reference)
 from .toolbox import build_LCD_cell, rotate_mask  # noqa: F401
 from .vectorized_optics import VectorizedLight
 from .wave_optics import ScalarLight, _report
@@ -108,19 +108,6 @@ def _is_t(v):
     return isinstance(v, torch.Tensor)
 
 
-def _bs_loss_rt(theta):
-    """(R, T) of the lossy symmetric splitter: |sin|, |cos| less 1% of |cos|
-    (optical_elements.py:376-383)."""
-    if _is_t(theta):
-        th = theta.to(device=engine.device(), dtype=torch.float64)
-        T, R = torch.abs(torch.cos(th)), torch.abs(torch.sin(th))
-    else:
-        th = np.asarray(theta, dtype=np.float64)
-        T, R = np.abs(np.cos(th)), np.abs(np.sin(th))
-    noise = T * 0.01
-    return R - noise, T - noise
-
-
 def _bs_matrix(entries, like):
     """Complex 2x2 splitter matrix (row-major entries), on the device: a
     differentiable torch tensor when any entry is one, else a cached copy."""
@@ -135,27 +122,30 @@ def _bs_matrix(entries, like):
     return engine.device_array(m.reshape(np.shape(like) + (2, 2)), torch.complex64)
 
 
-def _i_times(v):
-    return torch.complex(torch.zeros_like(v), v) if _is_t(v) else 1j * v
-
-
-def _bs_apply(a, b, m):
+def _bs_apply(a, b, m, kind=0):
     """Mix the (Ex, Ey) of lights a, b (b may be None); outputs (c, d) with Ez zero."""
     pa = [a.Ex, a.Ey]
     pb = [b.Ex, b.Ey] if b is not None else None
-    cx, cy, dx, dy = autograd.beam_splitter(pa, pb, m)
+    cx, cy, dx, dy = autograd.beam_splitter(pa, pb, m, kind)
     c = VectorizedLight._wrap(a.x, a.y, a.wavelength, [cx, cy, None])
     d = VectorizedLight._wrap(a.x, a.y, a.wavelength, [dx, dy, None])
     return c, d
 
 
+def _bs_angle(theta):
+    """The splitting angle on the device (float64): a tensor as it is (its
+    gradient flows), a number from the constant cache."""
+    if _is_t(theta):
+        return theta
+    return engine.device_array(np.asarray(theta, dtype=np.float64).reshape(-1), torch.float64)
+
+
 def BS_symmetric(a, b, theta):
     """optical_elements.py:334-391: lossy symmetric beam splitter, c = R a + iT b,
     d = iT a + R b (R = |sin theta|, T = |cos theta|, both less 1% of T), as one
-    fused kernel; differentiable in the fields and in a tensor theta."""
-    R, T = _bs_loss_rt(theta)
-    iT = _i_times(T)
-    return _bs_apply(a, b, _bs_matrix([R, iT, iT, R], theta))
+    kernel that builds the matrix from the angle; differentiable in the fields
+    and in a tensor theta."""
+    return _bs_apply(a, b, _bs_angle(theta), _lib.XL_BS_SYMMETRIC)
 
 
 def bs_port0(a_Ex, a_Ey, c_Ex, c_Ey, d_Ex, d_Ey, T, R):
@@ -171,14 +161,8 @@ def bs_port1(a_Ex, a_Ey, c_Ex, c_Ey, d_Ex, d_Ey, T, R):
 def BS_symmetric_SI(a, theta, port=0):
     """optical_elements.py:411-460: single-input lossy splitter; port 0 gives
     c = R a, d = iT a, port 1 gives c = iT a, d = R a."""
-    R, T = _bs_loss_rt(theta)
-    iT = _i_times(T)
-    zero = 0.0
-    if int(port) == 0:
-        m = _bs_matrix([R, zero, iT, zero], theta)
-    else:
-        m = _bs_matrix([iT, zero, R, zero], theta)
-    return _bs_apply(a, None, m)
+    kind = _lib.XL_BS_SINGLE_PORT0 if int(port) == 0 else _lib.XL_BS_SINGLE_PORT1
+    return _bs_apply(a, None, _bs_angle(theta), kind)
 
 
 def BS(a1, a2, R, T, phase):
