@@ -154,7 +154,7 @@ def run_reference(args, budget_s=90.0):
     `budget_s` of work (at least 3); the line reports how many were timed."""
     from oracle import xlumina_ref as ref
     rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if rank != 0:      # under torchrun rank 0 alone runs the CPU reference
         return
     x, Ex, Ey, eta, theta, alpha, zs = make_inputs(1)
     t_w = time.perf_counter()
@@ -196,6 +196,52 @@ def cpu_baseline_sample(seconds=20.0):
                       f"scipy.fft workers={ref.WORKERS})"}
 
 
+# ---- replicas: under torchrun every rank runs the whole workload on its own
+# GPU (fields share nothing, so there is no data-path collective); timing is
+# bracketed by barriers and the whole-job rate is the units of all ranks over
+# the slowest rank's time.
+
+def dist_context():
+    """(rank, world size, local rank) of this process; initialises the process
+    group of a torchrun launch (NCCL with GPUs, gloo without)."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not dist.is_initialized():
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
+    return dist.get_rank(), dist.get_world_size(), local
+
+
+def replica_barrier():
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+        dist.barrier()
+
+
+def reduce_replicas(seconds, units):
+    """(the slowest rank's seconds, the units of all ranks)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(seconds), float(units)
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cpu")
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def run_gpu(args):
     import torch
 
@@ -203,10 +249,11 @@ def run_gpu(args):
     from xlumina_gb300 import optical_elements as oe
     from xlumina_gb300 import vectorized_optics as vo
 
-    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
-        print(json.dumps({"error": "this benchmark runs on one GPU only (--gpus 1)"}))
+    rank, world, local = dist_context()
+    if world != args.gpus:
+        print(json.dumps({"error": f"--gpus {args.gpus} but {world} process(es): launch one process per GPU"}))
         sys.exit(2)
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     B = args.batch
     x, Ex, Ey, eta, theta, alpha, zs = make_inputs(B)
@@ -225,7 +272,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
 
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    with ClockSampler(0) as clk:
+    with ClockSampler(local) as clk:
+        replica_barrier()
         torch.cuda.synchronize()
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
@@ -238,11 +286,13 @@ def run_gpu(args):
                 ev[k][s + 1].record(stream)
         t_end.record(stream)
         torch.cuda.synchronize()
+        replica_barrier()
         clk.mark_end()
-    total_ms = t_start.elapsed_time(t_end)
+    total_s, fields = reduce_replicas(t_start.elapsed_time(t_end) / 1e3, B * args.steps)
+    total_ms = total_s * 1e3
     stage_ms = [sum(ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps)) / args.steps
                 for s in range(3)]
-    value = B * args.steps / (total_ms / 1e3)
+    value = fields / total_s
 
     # roofline: algorithmic bytes per launch (B fields), per stage
     n2 = N * N
@@ -310,21 +360,24 @@ def run_gpu(args):
         e2e_step(i)
     torch.cuda.synchronize()
     ke = max(4, args.steps // 2)
+    replica_barrier()
     t0 = time.perf_counter()
     for i in range(ke):
         streams[i % 2].synchronize()   # the stream's host buffers are free again
         e2e_step(i)
     torch.cuda.synchronize()
-    e2e = B * ke / (time.perf_counter() - t0)
+    e2e_s, e2e_fields = reduce_replicas(time.perf_counter() - t0, B * ke)
+    e2e = e2e_fields / e2e_s
     h2d = (hosts[0]["Ex"].numel() + hosts[0]["Ey"].numel()) * 8 + \
         (hosts[0]["eta"].numel() + hosts[0]["theta"].numel()) * 4
     d2h = sum(hb.numel() for hb in hosts[0]["out"]) * 8
 
     line = {
-        "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "batch": B, "fields_per_step": B,
+        "config": {"workload": WORKLOAD, "batch": B, "fields_per_step": B * world,
+                   "parallelism": "replicas x%d (no data-path collective)" % world,
                    "l2": "inputs larger than L2 (%.2f GB of fields and masks per step)" %
                          ((Ex_d.numel() + Ey_d.numel()) * 8 / 1e9 + (eta_d.numel() + theta_d.numel()) * 4 / 1e9)},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -343,6 +396,10 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "spectrum_builds": engine.SPECTRA.builds,
     }
+    if world > 1:   # the single-GPU sections below are not replicated
+        if rank == 0:
+            print(json.dumps(line))
+        return
     if not args.no_fwd_bwd:
         del call, Ex_d, Ey_d, eta_d, theta_d, hosts
         torch.cuda.empty_cache()
