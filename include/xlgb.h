@@ -356,6 +356,30 @@ int xl_table_noise(void* stream, const XlNoiseArgs* args, const uint32_t* keys);
 /* The generator on the host: out = Philox4x32-10(counter[4], key[2]). */
 int xl_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out);
 
+/* ---- Optimiser ----------------------------------------------------------- */
+
+/* One AdamW step (torch.optim.AdamW's update, decoupled weight decay) over up
+ * to XL_ADAMW_MAX_TENSORS float32 tensors in one launch; `step` is the device
+ * step count after its increment (so the call can be recorded in a CUDA
+ * graph).  The optimisation tables' update (optax.adamw in the reference's
+ * experiments, e.g. experiments/hybrid_optimizer.py:33). */
+#define XL_ADAMW_MAX_TENSORS 32
+typedef struct {
+  float* p;
+  const float* g;
+  float* m;
+  float* v;
+  long long n;
+} XlAdamWTensor;
+typedef struct {
+  int count;
+  XlAdamWTensor t[XL_ADAMW_MAX_TENSORS];
+  float lr, beta1, beta2, eps, weight_decay;
+  const float* step;
+} XlAdamWArgs;
+
+int xl_adamw_step(void* stream, const XlAdamWArgs* args);
+
 /* ---- Losses ------------------------------------------------------------ */
 
 /* Intensity MSE, MSE_Intensity of loss_functions.py:137-149, per plane:

@@ -82,6 +82,20 @@ class XlNoiseArgs(ctypes.Structure):
                 ("amps", ctypes.c_void_p), ("wps", ctypes.c_void_p)]
 
 
+XL_ADAMW_MAX_TENSORS = 32
+
+
+class XlAdamWTensor(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_void_p), ("g", ctypes.c_void_p), ("m", ctypes.c_void_p), ("v", ctypes.c_void_p),
+                ("n", ctypes.c_longlong)]
+
+
+class XlAdamWArgs(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int), ("t", XlAdamWTensor * XL_ADAMW_MAX_TENSORS), ("lr", ctypes.c_float),
+                ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("eps", ctypes.c_float),
+                ("weight_decay", ctypes.c_float), ("step", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); every symbol include/xlgb.h declares.
 SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
@@ -143,6 +157,7 @@ SIGNATURES = {
     "xl_table_noise": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlNoiseArgs), ctypes.POINTER(ctypes.c_uint32)]),
     "xl_philox4x32_10": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                         ctypes.POINTER(ctypes.c_uint32)]),
+    "xl_adamw_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlAdamWArgs)]),
     "xl_apply_ops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                     ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

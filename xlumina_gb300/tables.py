@@ -19,6 +19,7 @@ import numpy as np
 import torch
 
 from . import loss_functions as lf
+from .optim import AdamW
 from . import optical_elements as oe
 from . import toolbox
 from .vectorized_optics import VectorizedLight
@@ -46,7 +47,7 @@ class FourFTable:
         self.phase2 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32),
                                       device=device).requires_grad_(True)
         # capturable: the step count lives on the device, so plans.CapturedStep can record a step
-        self.opt = torch.optim.AdamW([self.phase1, self.phase2], lr=0.05, capturable=capturable)
+        self.opt = AdamW([self.phase1, self.phase2], lr=0.05, capturable=capturable)
 
     def loss(self, inputs=None, target=None):
         inputs = self.inputs if inputs is None else inputs
@@ -96,7 +97,7 @@ class HighNATable:
                                      device=device).requires_grad_(True)
         self.phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
                                    device=device).requires_grad_(True)
-        self.opt = torch.optim.AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05, capturable=capturable)
+        self.opt = AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05, capturable=capturable)
 
     def loss(self):
         light = VectorizedLight(self.x, self.y, self.wavelength)
@@ -141,7 +142,7 @@ class VrsLcdTable:
         self.target = [0.01 * torch.randn((batch, n, n), dtype=torch.complex64, device=device, generator=g)
                        for _ in range(3)]
         self.alpha = float(rng.uniform(0, np.pi))
-        self.opt = torch.optim.AdamW([self.eta, self.theta], lr=0.05, capturable=capturable)
+        self.opt = AdamW([self.eta, self.theta], lr=0.05, capturable=capturable)
 
     def loss(self, fields=None):
         sl = slice(None) if fields is None else fields
@@ -191,7 +192,7 @@ class SharpFocusTable:
                                                dtype=torch.float32 if plane else torch.float64,
                                                device=device).requires_grad_(True))
         # capturable: the step count lives on the device, so plans.CapturedStep can record a step
-        self.opt = torch.optim.AdamW(self.params, lr=0.05, weight_decay=1e-4, capturable=capturable)
+        self.opt = AdamW(self.params, lr=0.05, weight_decay=1e-4, capturable=capturable)
 
     def loss(self):
         s = self.src
