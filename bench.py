@@ -405,6 +405,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         line["czt_high_na"] = run_czt()
         torch.cuda.empty_cache()
+        line["rs_plain_1024"] = run_rs_plain_config()
+        torch.cuda.empty_cache()
         line["fwd_bwd"] = run_fwd_bwd()
         torch.cuda.empty_cache()
         line["hybrid_sharp_focus"] = run_hybrid()
@@ -536,6 +538,40 @@ def run_fwd_bwd(steps=10, warmup=3):
                       "batch": B}
     torch.cuda.empty_cache()
     return out
+
+
+def run_rs_plain_config(batch=16, steps=20, warmup=3, seed=0):
+    """Scalar RS at 1024^2 (the reference's plain propagation case): 2 mm
+    window, 650 nm, Gaussian w0 = 200 um behind a per-field SLM phase
+    U[-pi, pi), z = 5 cm.  Batched (one call for `batch` fields, inputs
+    resident in HBM) and plain (one RS_propagation call per field)."""
+    import torch
+
+    from oracle import xlumina_ref as ref
+    from xlumina_gb300 import engine
+    from xlumina_gb300 import optical_elements as oe
+    from xlumina_gb300 import wave_optics as wo
+    n, wl, z = 1024, 0.650, 5.0e4
+    x, y = ref.space(1000.0, n)
+    src = wo.LightSource(x, y, wl)
+    src.gaussian_beam(w0=(200.0, 200.0), E0=1)
+    rng = np.random.default_rng(seed)
+    ph = torch.as_tensor(rng.uniform(-np.pi, np.pi, (batch, n, n)).astype(np.float32), device="cuda")
+    field = src.field.expand(batch, n, n)
+    call = engine.RsCall([field], x, y, wl, z, vector=False, pre=[engine.op_phase(ph)])
+    dt = _time_steps(call.run, steps, warmup)
+    light = wo.ScalarLight(x, y, wl)
+    light.field = src.field
+
+    def plain(i=[0]):
+        k = i[0] % batch
+        i[0] += 1
+        oe.SLM(light, ph[k], n)[0].RS_propagation(z)
+    dtp = _time_steps(plain, 2 * batch, 3)
+    alg = (112 + 4) * n * n          # bytes per field (4N^2: the phase mask)
+    return {"workload": "scalar RS 1024^2, 2 mm window, 650 nm, Gaussian w0 200 um, per-field SLM phase, z = 5 cm",
+            "batch": batch, "fields_per_s": batch / dt, "plain_fields_per_s": 1.0 / dtp,
+            "pipeline_gbs": batch * alg / dt / 1e9, "alg_bytes_per_field": alg}
 
 
 def run_hybrid(steps=5, warmup=2):
@@ -714,7 +750,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--only", choices=["czt", "hybrid"], default=None,
+    ap.add_argument("--only", choices=["czt", "hybrid", "rs1024"], default=None,
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
@@ -723,6 +759,9 @@ def main():
         return
     if args.only == "hybrid":
         print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only == "rs1024":
+        print(json.dumps({"rs_plain_1024": run_rs_plain_config(steps=args.steps, warmup=args.warmup)}))
         return
     if args.warmup < 3:
         args.warmup = 3
