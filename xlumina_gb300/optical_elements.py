@@ -23,9 +23,11 @@ _VECTOR = ('Vectorized light', 'Vectorized light source')
 
 
 def _phase_mask(phase, ny, nx):
-    """exp(i phase) materialised on the device (the mask an SLM returns)."""
-    ones = torch.ones((ny, nx), dtype=torch.complex64, device=engine.device())
-    return engine.apply_ops([ones], [engine.op_phase(phase)], ny, nx)[0]
+    """exp(i phase) materialised on the device (the mask an SLM returns), one
+    elementwise kernel."""
+    p = phase.detach() if isinstance(phase, torch.Tensor) else torch.as_tensor(phase, device=engine.device())
+    p = p.to(torch.float32)
+    return torch.polar(torch.ones((), dtype=torch.float32, device=p.device).expand_as(p), p)
 
 
 # ---------------------------------------------------------------- scalar --
