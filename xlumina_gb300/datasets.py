@@ -148,7 +148,7 @@ def _grid(n=1024, x_total=1500.0):
     from .toolbox import space
     x, y = space(x_total, n)
     dev = torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
-    X, Y = torch.meshgrid(torch.as_tensor(x, device=dev), torch.as_tensor(y, device=dev), indexing="xy")
+    X, Y = torch.meshgrid(torch.tensor(x, device=dev), torch.tensor(y, device=dev), indexing="xy")
     return X, Y
 
 

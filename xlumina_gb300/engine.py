@@ -104,10 +104,35 @@ def as_real_param(a, dev=None):
     return torch.as_tensor(arr, device=dev or device()).to(torch.float32).contiguous()
 
 
+_bytes_keys: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def array_key(a: np.ndarray) -> bytes:
+    """The bytes of a host grid array, as a cache key; remembered per array
+    object (a light's grid is shared by every light derived from it), so a
+    repeated call does not copy and hash the array again."""
+    k = id(a)
+    hit = _bytes_keys.get(k)
+    if hit is not None and hit[0] is a:
+        return hit[1]
+    b = a.tobytes()
+    with _LOCK:
+        _bytes_keys[k] = (a, b)       # the reference keeps the id valid
+        while len(_bytes_keys) > 256:
+            _bytes_keys.popitem(last=False)
+    return b
+
+
 def as_grid(a) -> np.ndarray:
+    """A grid axis as a read-only float64 host array (as the reference's
+    immutable jax arrays); an array that already is one is returned as it is."""
+    if isinstance(a, np.ndarray) and a.dtype == np.float64 and not a.flags.writeable:
+        return a
     if isinstance(a, torch.Tensor):
         a = a.detach().cpu().numpy()
-    return np.asarray(a, dtype=np.float64)
+    arr = np.array(a, dtype=np.float64)
+    arr.setflags(write=False)
+    return arr
 
 
 _grid_cache: "collections.OrderedDict" = collections.OrderedDict()
@@ -115,13 +140,13 @@ _grid_cache: "collections.OrderedDict" = collections.OrderedDict()
 
 def device_grid(a: np.ndarray) -> torch.Tensor:
     """float64 copy of a coordinate array on the device (cached by value)."""
-    key = (a.tobytes(), torch.cuda.current_device())
+    key = (array_key(a), torch.cuda.current_device())
     with _LOCK:
         t = _grid_cache.get(key)
         if t is not None:
             _grid_cache.move_to_end(key)
             return keep_for_capture(t)
-    t = torch.as_tensor(a, dtype=torch.float64, device=device())
+    t = torch.tensor(a, dtype=torch.float64, device=device())
     with _LOCK:
         _grid_cache[key] = t
         while len(_grid_cache) > 64:
@@ -156,7 +181,7 @@ def device_array(a, dtype) -> torch.Tensor:
         if t is not None:
             _array_cache.move_to_end(key)
             return keep_for_capture(t)
-    t = torch.as_tensor(arr, device=device()).to(dtype)
+    t = torch.tensor(arr, device=device()).to(dtype)
     with _LOCK:
         _array_cache[key] = t
         while len(_array_cache) > 256:
@@ -358,7 +383,7 @@ _highna_cache: "collections.OrderedDict" = collections.OrderedDict()
 
 def highna_coefficients(x, y, radius, f):
     """The lens's 6 per-pixel coefficient planes, cached by geometry (computed by libxlgb)."""
-    key = (x.tobytes(), y.tobytes(), float(radius), float(f), torch.cuda.current_device())
+    key = (array_key(x), array_key(y), float(radius), float(f), torch.cuda.current_device())
     with _LOCK:
         e = _highna_cache.get(key)
         if e is not None:
@@ -466,7 +491,7 @@ class SpectrumCache:
 
     @staticmethod
     def key(x, y, z, wavelength, dz=False):
-        return (x.tobytes(), y.tobytes(), float(z), float(wavelength), bool(dz), torch.cuda.current_device())
+        return (array_key(x), array_key(y), float(z), float(wavelength), bool(dz), torch.cuda.current_device())
 
     def get(self, x, y, z, wavelength, dz=False):
         """The transfer spectrum, or with ``dz`` the spectrum of its z-derivative."""
@@ -530,7 +555,7 @@ _offsets_cache: dict = {}
 
 def device_offsets(a: np.ndarray, P: int) -> torch.Tensor:
     """The wrapped impulse-response offsets of a grid axis on the device (cached)."""
-    key = (a.tobytes(), P, torch.cuda.current_device())
+    key = (array_key(a), P, torch.cuda.current_device())
     t = _offsets_cache.get(key)
     if t is None:
         t = device_array(rs_wrapped_offsets(a, P), torch.float64)
@@ -658,7 +683,7 @@ def rs_propagate(comps, x, y, wavelength, z, vector: bool, pre=(), post=()):
 
 def _mesh64(x, y):
     dev = device()
-    return torch.meshgrid(torch.as_tensor(x, device=dev), torch.as_tensor(y, device=dev), indexing="xy")
+    return torch.meshgrid(torch.tensor(x, device=dev), torch.tensor(y, device=dev), indexing="xy")
 
 
 def gaussian_field(x, y, wavelength, w0, E0=1.0, center=(0, 0), z_w0=(0, 0), alpha=0.0):

@@ -39,8 +39,8 @@ class _Grid:
     def _meshgrid(self):
         if self._XY is None:
             dev = engine.device()
-            xt = torch.as_tensor(self.x, device=dev)
-            yt = torch.as_tensor(self.y, device=dev)
+            xt = torch.tensor(self.x, device=dev)
+            yt = torch.tensor(self.y, device=dev)
             self._XY = torch.meshgrid(xt, yt, indexing="xy")
         return self._XY
 
