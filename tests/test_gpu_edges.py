@@ -73,3 +73,39 @@ def test_czt_small_grids(n, mx, my):
     yo = np.linspace(-4.0, 3.0, my)
     out = engine.czt_propagate([engine.as_field(f)], x, x, 0.5, 800.0, xo, yo, "scalar")[0].cpu().numpy()
     assert rel_l2(out, ref.czt(f, x, x, 0.5, 800.0, xo, yo)) < TOL
+
+
+def test_full_size_energy_and_adjoint_identity():
+    """Size-independent properties at the benchmark's 2048² size: RS conserves
+    the power of a beam well inside the window (the reference's
+    is_conserving_energy, toolbox.py:74-96; the FP64 oracle gives 1 - 1e-11
+    here), and <A u, v> = <u, A^H v> for a batch of VRS fields at two
+    distances."""
+    import torch
+
+    from xlumina_gb300 import engine, toolbox
+    from xlumina_gb300 import wave_optics as wo
+    n = 2048
+    x, y = ref.space(2000.0, n)
+    src = wo.LightSource(x, y, 0.65)
+    src.gaussian_beam(w0=(300.0, 300.0), E0=1)
+    out, _ = src.RS_propagation(5e4)
+    assert abs(toolbox.is_conserving_energy(src, out).item() - 1.0) < 1e-5
+
+    rng = np.random.default_rng(79)
+
+    def rnd(*s):
+        return torch.as_tensor((rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64),
+                               device="cuda")
+
+    def dot(a, b):
+        return complex(torch.sum(a.to(torch.complex128) * torch.conj(b.to(torch.complex128))).item())
+
+    zs = [1e4, 1e5]
+    ux, uy = rnd(2, n, n), rnd(2, n, n)
+    vs = [rnd(2, n, n) for _ in range(3)]
+    Au = engine.RsCall([ux, uy], x, y, 0.633, zs, True).run()
+    Ahv = engine.RsCall(vs, x, y, 0.633, zs, True, adjoint=True).run()
+    lhs = sum(dot(a, b) for a, b in zip(Au, vs))
+    rhs = dot(ux, Ahv[0]) + dot(uy, Ahv[1])
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
