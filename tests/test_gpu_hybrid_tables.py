@@ -109,3 +109,32 @@ def test_sharp_focus_table_gradients(setup):
         elif abs(got.item() - want.item()) > 1e-3 * abs(want.item()) + 2e-5 * top[k in dist]:
             bad.append((k, got.item(), want.item()))
     assert not bad, bad
+
+
+def test_checkpointed_tables_give_the_same_step():
+    """Activation checkpointing (wavefront edges of the sharp-focus table, the
+    focus of the high-NA table) gives the same gradients.  The deep table
+    keeps less at its peak; the one-focus table does not (its peak is the
+    chirp-z workspace, which the recomputation needs again)."""
+    import torch
+
+    from xlumina_gb300.tables import HighNATable, SharpFocusTable
+    for cls, kw in ((SharpFocusTable, dict(n=128, roi_n=48, seed=9)),
+                    (HighNATable, dict(n=256, roi_n=64, batch=4, seed=9))):
+        grads = []
+        peaks = []
+        for ck in (False, True):
+            t = cls(**kw, checkpoint=ck)
+            torch.cuda.synchronize()
+            torch.cuda.reset_peak_memory_stats()
+            base = torch.cuda.memory_allocated()
+            L = t.loss()
+            L.backward()
+            torch.cuda.synchronize()
+            peaks.append(torch.cuda.max_memory_allocated() - base)
+            params = t.params if hasattr(t, "params") else [t.eta, t.theta, t.alpha, t.phi]
+            grads.append([p.grad.detach().clone() for p in params])
+        for a, b in zip(*grads):
+            assert torch.allclose(a, b, rtol=1e-5, atol=1e-7)
+        if cls is SharpFocusTable:
+            assert peaks[1] < peaks[0], peaks

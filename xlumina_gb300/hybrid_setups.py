@@ -165,7 +165,23 @@ def _detect(lights, r, f, xout, yout):
     return _split_light(det, len(lights), tuple(l0.Ex.shape[:-2]))
 
 
-def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, yout):
+def _run_edges_checkpointed(jobs):
+    """_run_edges with activation checkpointing: the fields inside the
+    wavefront's edges (a building block's intermediate light, the batched
+    VRS's stacked inputs) are not kept for the backward; it recomputes them
+    from the wavefront's inputs (torch.utils.checkpoint, non-reentrant)."""
+    from torch.utils.checkpoint import checkpoint
+
+    from .vectorized_optics import VectorizedLight
+
+    def seg():
+        return tuple(t for light in _run_edges(jobs) for t in (light.Ex, light.Ey, light.Ez))
+    flat = checkpoint(seg, use_reentrant=False)
+    return [VectorizedLight._wrap(l.x, l.y, l.wavelength, list(flat[3 * k:3 * k + 3]))
+            for k, (_, l) in enumerate(jobs)]
+
+
+def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, yout, checkpoint=False):
     """Run a splitter grid.
 
     top[j] / left[i]: source lights entering splitters (0, j) from above and
@@ -176,7 +192,9 @@ def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, you
 
     The grid runs by wavefronts (the splitters with i + j = k depend only on
     wavefront k - 1): the free-space edges leaving a wavefront run as one
-    batched VRS, and the detectors as one batched focus."""
+    batched VRS, and the detectors as one batched focus.  ``checkpoint``
+    recomputes each wavefront's edges in the backward instead of keeping
+    their intermediate fields (deep tables, many noisy copies)."""
     rows, cols = len(thetas), len(thetas[0])
     a_in = {(0, j): top[j] for j in range(cols)}
     b_in = {(i, 0): left[i] for i in range(rows)}
@@ -196,7 +214,8 @@ def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, you
                 if (di, dj) == (i, j):
                     jobs.append((edge, c if port == "c" else d))
                     targets.append(("det", q))
-        for (kind, key), light in zip(targets, _run_edges(jobs)):
+        run = _run_edges_checkpointed if (checkpoint and torch.is_grad_enabled()) else _run_edges
+        for (kind, key), light in zip(targets, run(jobs)):
             if kind == "a":
                 a_in[key] = light
             elif kind == "b":
@@ -329,9 +348,10 @@ def batch_robust_discovery(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_param
     return I.transpose(0, 1)
 
 
-def hybrid_setup_sharp_focus(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9):
+def hybrid_setup_sharp_focus(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_params, distance_offset=8.9,
+                             checkpoint=False):
     """optical_elements.py:1503-1649: returns (stacked |Ez|^2 of the six
-    detectors, the detectors' lights)."""
+    detectors, the detectors' lights).  ``checkpoint``: see run_grid."""
     r, f, xout, yout = fixed_params[0:4]
     ph, eta, theta, z = _unpack_blocks(parameters, distance_offset)
     thetas = [_angle(parameters[18 + k]) for k in range(9)]
@@ -341,7 +361,7 @@ def hybrid_setup_sharp_focus(ls1, ls2, ls3, ls4, ls5, ls6, parameters, fixed_par
         return block(ph[b][0], ph[b][1], z1, eta[b], theta[b], z2)
     horizontal, vertical, outs = _sharp_focus_edges(ph, eta, theta, z, z4, z5, blk)
     dets = run_grid([ls1, ls2, ls3], [ls4, ls5, ls6], _grid_3x3(thetas), horizontal, vertical,
-                    _detectors(outs), r, f, xout, yout)
+                    _detectors(outs), r, f, xout, yout, checkpoint=checkpoint)
     return _ez_intensities(dets), dets
 
 

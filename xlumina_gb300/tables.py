@@ -81,8 +81,10 @@ def small_area_hybrid_batched(I):
 
 class HighNATable:
     def __init__(self, n=2048, roi_n=1024, batch=32, wavelength=0.650, half_width=2700.0, na=0.9,
-                 f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda", capturable=False):
+                 f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda", capturable=False,
+                 checkpoint=False):
         self.n, self.m, self.B = n, roi_n, batch
+        self.checkpoint = checkpoint
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
         self.wavelength, self.f, self.r = wavelength, f, na * f
@@ -99,13 +101,22 @@ class HighNATable:
                                    device=device).requires_grad_(True)
         self.opt = AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05, capturable=capturable)
 
-    def loss(self):
+    def _spot_intensity(self):
         light = VectorizedLight(self.x, self.y, self.wavelength)
         light.Ex = self.Ex.expand(self.B, self.n, self.n)
         light.Ey = self.Ey.expand(self.B, self.n, self.n)
         focus = oe.VCZT_objective_lens(oe.sSLM(oe.LCD(light, self.eta, self.theta), self.alpha, self.phi),
                                        self.r, self.f, self.xo, self.yo)
-        return small_area_hybrid_batched(torch.abs(focus.Ez) ** 2)
+        return torch.abs(focus.Ez) ** 2
+
+    def loss(self):
+        if self.checkpoint and torch.is_grad_enabled():
+            # the focal fields are recomputed in the backward instead of kept
+            from torch.utils.checkpoint import checkpoint
+            I = checkpoint(self._spot_intensity, use_reentrant=False)
+        else:
+            I = self._spot_intensity()
+        return small_area_hybrid_batched(I)
 
     def step(self):
         self.opt.zero_grad(set_to_none=True)
@@ -174,7 +185,8 @@ class SharpFocusTable:
     eight distances)."""
 
     def __init__(self, n=1024, roi_n=400, wavelength=0.635, half_width=2500.0, waist=1200.0, seed=2100,
-                 device="cuda", capturable=False):
+                 device="cuda", capturable=False, checkpoint=False):
+        self.checkpoint = checkpoint
         from .vectorized_optics import PolarizedLightSource
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(10.0, roi_n)
@@ -196,7 +208,7 @@ class SharpFocusTable:
 
     def loss(self):
         s = self.src
-        I, _ = oe.hybrid_setup_sharp_focus(s, s, s, s, s, s, self.params, self.fixed)
+        I, _ = oe.hybrid_setup_sharp_focus(s, s, s, s, s, s, self.params, self.fixed, checkpoint=self.checkpoint)
         return toolbox.softmin(lf.vectorized_loss_hybrid(I))
 
     def step(self):
