@@ -27,7 +27,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import cm
+from . import cm, engine
 
 # ------------------------------------------------------------ parameters --
 
@@ -135,7 +135,8 @@ def _run_edges(jobs):
     groups = {}
     for k, (edge, light) in enumerate(jobs):
         if _batchable(edge, light):
-            key = (light.x.tobytes(), light.y.tobytes(), float(light.wavelength), tuple(light.Ex.shape))
+            key = (engine.array_key(light.x), engine.array_key(light.y), float(light.wavelength),
+                   tuple(light.Ex.shape))
             groups.setdefault(key, []).append(k)
         else:
             out[k] = _run_edge(edge, light)
