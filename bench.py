@@ -162,10 +162,13 @@ def run_reference(args, budget_s=90.0):
     for _ in range(args.warmup):
         cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, zs[0])
     per_field = (time.perf_counter() - t_w) / max(1, args.warmup)
-    steps = max(3, min(args.steps, int(budget_s / max(per_field, 1e-3))))
+    steps = max(5, min(args.steps, int(budget_s / max(per_field, 1e-3))))
+    times = []
     t0 = time.perf_counter()
     for i in range(steps):
+        ts = time.perf_counter()
         cpu_vrs_field(ref, x, Ex, Ey, eta[0], theta[0], alpha, Z_SET[i % len(Z_SET)])
+        times.append(time.perf_counter() - ts)
     dt = time.perf_counter() - t0
     v = steps / dt
     cores = ref.WORKERS
@@ -173,6 +176,8 @@ def run_reference(args, budget_s=90.0):
             "steps": steps, "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic", "config": {"workload": WORKLOAD, "batch": 1},
+            "ms_per_field_p50": 1e3 * float(np.percentile(times, 50)),
+            "ms_per_field_p99": 1e3 * float(np.percentile(times, 99)),
             "cpu_baseline": {"value": v, "unit": "fields/s", "cores": cores, "kind": "port",
                              "sample": f"{steps} fields, one per step (capped at about {budget_s:.0f} s of work), "
                                        f"scipy.fft with {cores} workers"},
