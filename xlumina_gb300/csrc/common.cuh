@@ -208,6 +208,18 @@ struct GlobalParams {
 
 // Apply op number k of a program to the pixel's (Ex, Ey, Ez) (scalar fields
 // use e[0] only); its real parameters come from the reader pr(op, k, i, px).
+// The LCD retarder (delta = 0) from cos, sin of eta/2 and of theta:
+// a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2).
+__device__ __forceinline__ void lcd_apply_trig(float ch, float sh, float ct, float st, float2 (&e)[3]) {
+  const float c2 = ct * ct - st * st, s2 = 2.f * st * ct;
+  const float2 a = make_float2(ch, -sh * c2);
+  const float2 b = make_float2(0.f, -sh * s2);
+  const float2 d = make_float2(ch, sh * c2);
+  const float2 x = e[0], y = e[1];
+  e[0] = cadd(cmul(a, x), cmul(b, y));
+  e[1] = cadd(cmul(b, x), cmul(d, y));
+}
+
 template <class PR>
 __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3], const PixelCtx& px,
                                            const PR& pr) {
@@ -235,21 +247,12 @@ __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3]
       break;
     }
     case XL_OP_LCD: {  // general retarder with delta = 0 (eta, theta); Ez unchanged
-      float sh, ch, s2, c2;
-      float st, ct;
+      float sh, ch, st, ct;
       if (op.pmask & 1) phase_sincos(0.5f * pr(op, k, 0, px), &sh, &ch);
       else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
       if (op.pmask & 2) phase_sincos(pr(op, k, 1, px), &st, &ct);
       else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
-      // a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2)
-      c2 = ct * ct - st * st;
-      s2 = 2.f * st * ct;
-      const float2 a = make_float2(ch, -sh * c2);
-      const float2 b = make_float2(0.f, -sh * s2);
-      const float2 d = make_float2(ch, sh * c2);
-      const float2 x = e[0], y = e[1];
-      e[0] = cadd(cmul(a, x), cmul(b, y));
-      e[1] = cadd(cmul(b, x), cmul(d, y));
+      lcd_apply_trig(ch, sh, ct, st, e);
       break;
     }
     case XL_OP_LP: {  // linear polarizer at alpha; Ez set to zero
@@ -318,6 +321,25 @@ __device__ __forceinline__ void apply_prog(const XlProg& prog, float2 (&e)[3], c
 // dL/dp = Re(sum_c g_c conj(dy_c/dp)).
 __device__ __forceinline__ float re_gconj(float2 g, float2 d) { return g.x * d.x + g.y * d.y; }
 
+// Backward of lcd_apply_trig: parameter gradients into pg[0] (eta), pg[1]
+// (theta); g becomes J^H g (J symmetric: conj(J) g).
+__device__ __forceinline__ void lcd_bwd_trig(float ch, float sh, float ct, float st, const float2 (&e)[3],
+                                             float2 (&g)[3], float (&pg)[4]) {
+  const float c2 = ct * ct - st * st, s2 = 2.f * st * ct;
+  const float2 a = make_float2(ch, -sh * c2), bb = make_float2(0.f, -sh * s2), d = make_float2(ch, sh * c2);
+  // derivatives of the matrix entries
+  const float2 a_e = make_float2(-0.5f * sh, -0.5f * ch * c2), b_e = make_float2(0.f, -0.5f * ch * s2);
+  const float2 d_e = make_float2(-0.5f * sh, 0.5f * ch * c2);
+  const float2 a_t = make_float2(0.f, 2.f * sh * s2), b_t = make_float2(0.f, -2.f * sh * c2);
+  const float2 d_t = make_float2(0.f, -2.f * sh * s2);
+  const float2 x = e[0], y = e[1];
+  pg[0] += re_gconj(g[0], cadd(cmul(a_e, x), cmul(b_e, y))) + re_gconj(g[1], cadd(cmul(b_e, x), cmul(d_e, y)));
+  pg[1] += re_gconj(g[0], cadd(cmul(a_t, x), cmul(b_t, y))) + re_gconj(g[1], cadd(cmul(b_t, x), cmul(d_t, y)));
+  const float2 g0 = g[0], g1 = g[1];
+  g[0] = cadd(cmul(cconj(a), g0), cmul(cconj(bb), g1));
+  g[1] = cadd(cmul(cconj(bb), g0), cmul(cconj(d), g1));
+}
+
 __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
                                              const PixelCtx& px, float (&pg)[4]) {
   switch (op.kind) {
@@ -356,19 +378,7 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
       else { ch = op.dval[0]; sh = op.dval[1]; }
       if (op.pmask & 2) phase_sincos(op_param(op, 1, px), &st, &ct);
       else { ct = op.dval[2]; st = op.dval[3]; }
-      const float c2 = ct * ct - st * st, s2 = 2.f * st * ct;
-      const float2 a = make_float2(ch, -sh * c2), bb = make_float2(0.f, -sh * s2), d = make_float2(ch, sh * c2);
-      // derivatives of the matrix entries
-      const float2 a_e = make_float2(-0.5f * sh, -0.5f * ch * c2), b_e = make_float2(0.f, -0.5f * ch * s2);
-      const float2 d_e = make_float2(-0.5f * sh, 0.5f * ch * c2);
-      const float2 a_t = make_float2(0.f, 2.f * sh * s2), b_t = make_float2(0.f, -2.f * sh * c2);
-      const float2 d_t = make_float2(0.f, -2.f * sh * s2);
-      const float2 x = e[0], y = e[1];
-      pg[0] += re_gconj(g[0], cadd(cmul(a_e, x), cmul(b_e, y))) + re_gconj(g[1], cadd(cmul(b_e, x), cmul(d_e, y)));
-      pg[1] += re_gconj(g[0], cadd(cmul(a_t, x), cmul(b_t, y))) + re_gconj(g[1], cadd(cmul(b_t, x), cmul(d_t, y)));
-      const float2 g0 = g[0], g1 = g[1];   // J symmetric: J^H g = conj(J) g
-      g[0] = cadd(cmul(cconj(a), g0), cmul(cconj(bb), g1));
-      g[1] = cadd(cmul(cconj(bb), g0), cmul(cconj(d), g1));
+      lcd_bwd_trig(ch, sh, ct, st, e, g, pg);
       break;
     }
     case XL_OP_LP: {
