@@ -703,9 +703,7 @@ def run_serving(n_req=10000, seed=4000):
         lat.append(time.perf_counter() - t1)
     plain_rate = n_plain / (time.perf_counter() - t0)
 
-    rate = 0.8 * plain_rate * 1.5   # offered load: above the plain path's capacity, inside the batched one
     reqs = [make(i) for i in range(n_req)]
-    gaps = rng.exponential(1.0 / rate, n_req)
     from xlumina_gb300.autotune import BatchTuner
     srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2,
                  tuner=BatchTuner(candidates=(1, 2, 4, 8, 16), repeats=2))
@@ -715,6 +713,18 @@ def run_serving(n_req=10000, seed=4000):
         examples.setdefault((r.kind, len(r.x)), r)
     packing = srv.tune(list(examples.values()))
     t_tune = time.perf_counter() - t_tune
+    # capacity: a saturating burst (every request submitted at once)
+    n_sat = min(3000, n_req)
+    sat_reqs = [make(i) for i in range(n_sat)]
+    t0 = time.perf_counter()
+    sat = [srv.submit(r) for r in sat_reqs]
+    for f in sat:
+        f.result(timeout=600)
+    capacity = n_sat / (time.perf_counter() - t0)
+    srv.reset_stats()
+    # the Poisson stream at 80 % of that capacity
+    rate = 0.8 * capacity
+    gaps = rng.exponential(1.0 / rate, n_req)
     futs = [None] * n_req
 
     def client():
@@ -737,7 +747,8 @@ def run_serving(n_req=10000, seed=4000):
     st = srv.stats()
     return {"workload": "10,000 Poisson requests, sizes 256/512/1024/2048 (.4/.3/.2/.1), RS/VRS/CZT/grad, "
                         "z U[1,20] cm, HBM budget 150 GB",
-            "requests": n_req, "offered_req_per_s": rate, "served_req_per_s": n_req / wall,
+            "requests": n_req, "capacity_req_per_s": capacity, "offered_req_per_s": rate,
+            "offered_load": "80 % of the saturated capacity", "served_req_per_s": n_req / wall,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_batch": st["mean_batch"],
             "batch_packing": {f"{k[0]} {k[1]}^2": v for k, v in packing.items()}, "tuning_s": t_tune,
             "plain_req_per_s": plain_rate, "plain_p50_ms": float(np.percentile(np.asarray(lat) * 1e3, 50)),

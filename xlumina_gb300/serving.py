@@ -159,6 +159,13 @@ class Server:
             self._cv.notify()
         self._thread.join()
 
+    def reset_stats(self):
+        """Forget the latencies and counts recorded so far (e.g. after a warm-up)."""
+        with self._cv:
+            self.latencies = []
+            self.batches = 0
+            self.completed = 0
+
     def stats(self):
         lat = np.asarray(self.latencies) * 1e3
         if lat.size == 0:
