@@ -75,6 +75,10 @@ typedef struct {
 const char* xl_last_error(void);
 int xl_version(void);
 
+/* sizeof of the argument struct of that name ("XlCztArgs", ...), 0 if unknown:
+ * lets a binding check its mirrors of the structs against this build. */
+size_t xl_struct_size(const char* name);
+
 /* Number of bounded waits (on TMA-copy barriers) that ran out of iterations
  * since the last reset, on the current device; such a launch records the
  * event and returns without hanging, its output is not valid.  Synchronous. */
@@ -217,6 +221,13 @@ typedef struct {
                             ones (pre' = conj(post) L, g' = conj(g), post' = conj(pre) / L);
                             z, wavelength and cte as for the forward.  VCZT: 3 gradients in,
                             the Ez gradient folded into out[0], out[1]. */
+  /* Per-entry distances (XL_CZT_SCALAR and XL_CZT_VECTOR; NULL: every entry uses z).
+   * Entry b propagates over z_batch[b] (device float64) with its own chirp vectors,
+   * packed entry after entry: pre_x + b nx, g_x + b 2^log2_lx, post_x + b mx, and the
+   * same for y; cte_batch[b] (device complex64) replaces cte_re, cte_im (the adjoint
+   * conjugates it, as it does cte). */
+  const double* z_batch;
+  const void* cte_batch;
 } XlCztArgs;
 
 size_t xl_czt_work_bytes(int batch, int comps, int ny, int mx);
@@ -228,6 +239,36 @@ int xl_czt(void* stream, const XlCztArgs* args);
 
 /* One pass of xl_czt: 0 = prologue + x transform, 1 = y transform + epilogue. */
 int xl_czt_stage(void* stream, const XlCztArgs* args, int stage);
+
+/* Chirp vectors of a batch of distances, built on the device in float64 and
+ * stored as complex64, packed entry after entry as XlCztArgs.z_batch reads
+ * them.  Replaces the per-call host chirps of build_CZT_grid and
+ * Bluestein_method (wave_optics.py:299-331, 385-460) for CZT_jit
+ * (wave_optics.py:333-357) at many z: entry b has Dm = wavelength z[b] / dx,
+ * f1 = out0 + Dm/2, f2 = out1 + Dm/2 per axis and the factor
+ * cte[b] = z[b] dx dy wavelength.  The geometry is the forward's (input
+ * ny x nx, output my x mx, Bluestein lengths 2^log2_l >= m + M, at least 32);
+ * with adjoint = 1 the vectors are the adjoint set (pre' = conj(post) L,
+ * g' = conj(g), post' = conj(pre) / L, of lengths mx, 2^log2_lx, nx on x). */
+typedef struct {
+  int batch;
+  int ny, nx, my, mx;
+  int log2_lx, log2_ly;
+  int adjoint;
+  const double* z;           /* device float64, batch entries */
+  double wavelength, dx, dy;
+  double xout0, xout1;       /* first and last output coordinates */
+  double yout0, yout1;
+  void* pre_x;               /* complex64 outputs, batch x (nx | 2^log2_lx | mx), adjoint (mx | . | nx) */
+  void* g_x;
+  void* post_x;
+  void* pre_y;
+  void* g_y;
+  void* post_y;
+  void* cte;                 /* complex64, batch entries */
+} XlCztChirpArgs;
+
+int xl_czt_chirps(void* stream, const XlCztChirpArgs* args);
 
 /* ---- Elementwise ------------------------------------------------------ */
 

@@ -152,3 +152,34 @@ def test_noise_keys():
     assert (a == b).all() and not (a[0] == a[1]).all()
     chain = noise.keychain_optical_tables(7, 3)
     assert chain.shape == (3, 2) and chain[:, 1].tolist() == [7, 8, 9]
+
+
+def test_ctypes_mirrors_match_the_c_structs(lib):
+    """Every argument struct the binding mirrors has the size the library was built with."""
+    from xlumina_gb300 import _lib
+    names = ("XlOp", "XlProg", "XlRsArgs", "XlCztArgs", "XlCztChirpArgs", "XlBsArgs", "XlNoiseArgs",
+             "XlAdamWTensor", "XlAdamWArgs")
+    for name in names:
+        assert lib.xl_struct_size(name.encode()) == ctypes.sizeof(getattr(_lib, name)), name
+    assert lib.xl_struct_size(b"NoSuchStruct") == 0
+    src = open(os.path.join(ROOT, "include", "xlgb.h")).read()
+    assert set(re.findall(r"}\s*(Xl[A-Za-z]+)\s*;", src)) == set(names)
+
+
+def test_chirp_builder_argument_errors_without_gpu(lib):
+    from xlumina_gb300 import _lib
+    a = _lib.XlCztChirpArgs()
+    a.batch, a.ny, a.nx, a.my, a.mx, a.log2_lx, a.log2_ly = 2, 64, 64, 32, 32, 7, 7
+    assert lib.xl_czt_chirps(None, ctypes.byref(a)) == _lib.XL_EINVAL
+    assert b"null pointer" in lib.xl_last_error()
+    a.log2_lx = 6   # 64 < 64 + 32
+    assert lib.xl_czt_chirps(None, ctypes.byref(a)) == _lib.XL_EINVAL
+    assert b"Bluestein lengths" in lib.xl_last_error()
+    c = _lib.XlCztArgs()
+    c.batch, c.comps_in, c.comps_out, c.mode = 1, 1, 1, _lib.XL_CZT_PLAIN
+    c.ny, c.nx, c.my, c.mx, c.log2_lx, c.log2_ly = 64, 64, 32, 32, 7, 7
+    for f in ("pre_x", "g_x", "post_x", "pre_y", "g_y", "post_y", "work"):
+        setattr(c, f, 16)
+    c.z_batch = 16
+    assert lib.xl_czt(None, ctypes.byref(c)) == _lib.XL_EINVAL
+    assert b"per-entry distances" in lib.xl_last_error()

@@ -57,7 +57,19 @@ class XlCztArgs(ctypes.Structure):
                 ("cte_re", ctypes.c_double), ("cte_im", ctypes.c_double),
                 ("pre_x", ctypes.c_void_p), ("g_x", ctypes.c_void_p), ("post_x", ctypes.c_void_p),
                 ("pre_y", ctypes.c_void_p), ("g_y", ctypes.c_void_p), ("post_y", ctypes.c_void_p),
-                ("work", ctypes.c_void_p), ("pre", XlProg), ("adjoint", ctypes.c_int)]
+                ("work", ctypes.c_void_p), ("pre", XlProg), ("adjoint", ctypes.c_int),
+                ("z_batch", ctypes.c_void_p), ("cte_batch", ctypes.c_void_p)]
+
+
+class XlCztChirpArgs(ctypes.Structure):
+    _fields_ = [("batch", ctypes.c_int), ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("my", ctypes.c_int),
+                ("mx", ctypes.c_int), ("log2_lx", ctypes.c_int), ("log2_ly", ctypes.c_int),
+                ("adjoint", ctypes.c_int), ("z", ctypes.c_void_p), ("wavelength", ctypes.c_double),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("xout0", ctypes.c_double),
+                ("xout1", ctypes.c_double), ("yout0", ctypes.c_double), ("yout1", ctypes.c_double),
+                ("pre_x", ctypes.c_void_p), ("g_x", ctypes.c_void_p), ("post_x", ctypes.c_void_p),
+                ("pre_y", ctypes.c_void_p), ("g_y", ctypes.c_void_p), ("post_y", ctypes.c_void_p),
+                ("cte", ctypes.c_void_p)]
 
 
 class XlBsArgs(ctypes.Structure):
@@ -100,6 +112,7 @@ class XlAdamWArgs(ctypes.Structure):
 SIGNATURES = {
     "xl_last_error": (ctypes.c_char_p, []),
     "xl_version": (ctypes.c_int, []),
+    "xl_struct_size": (ctypes.c_size_t, [ctypes.c_char_p]),
     "xl_init": (ctypes.c_int, []),
     "xl_device_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
@@ -134,6 +147,7 @@ SIGNATURES = {
     "xl_czt_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_czt": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs)]),
     "xl_czt_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs), ctypes.c_int]),
+    "xl_czt_chirps": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztChirpArgs)]),
     "xl_ops_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

@@ -86,9 +86,15 @@ class RsPlan:
 
 
 class CztPlan:
-    """CZT (one component), VCZT, or the high-NA focus (lens op inside ``ops``)."""
+    """CZT (one component), VCZT, or the high-NA focus (lens op inside ``ops``).
+    ``z`` is one distance or one per batch entry; it is a constant here (the
+    distances that the reference's experiments optimise go through RS / VRS
+    propagation, which differentiates them)."""
 
     def __init__(self, x, y, wavelength, z, xout, yout, mode, ops, lens=None):
+        if isinstance(z, torch.Tensor) and z.requires_grad:
+            raise NotImplementedError("chirp-z propagation does not differentiate the distance; "
+                                      "pass z detached, or propagate with RS / VRS to optimise it")
         self.x, self.y, self.wavelength, self.z = x, y, wavelength, z
         self.xout, self.yout, self.mode, self.lens = xout, yout, mode, lens
         self.ops = list(ops or ())

@@ -2,6 +2,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <string.h>
 
 #include <mutex>
 #include <vector>
@@ -79,6 +80,24 @@ int ensure_init() {
 extern "C" const char* xl_last_error(void) { return xl::g_err; }
 
 extern "C" int xl_version(void) { return 100; }
+
+extern "C" size_t xl_struct_size(const char* name) {
+  if (!name) return 0;
+  struct Entry {
+    const char* name;
+    size_t size;
+  };
+  static const Entry sizes[] = {
+      {"XlOp", sizeof(XlOp)},           {"XlProg", sizeof(XlProg)},
+      {"XlRsArgs", sizeof(XlRsArgs)},   {"XlCztArgs", sizeof(XlCztArgs)},
+      {"XlCztChirpArgs", sizeof(XlCztChirpArgs)},
+      {"XlBsArgs", sizeof(XlBsArgs)},   {"XlNoiseArgs", sizeof(XlNoiseArgs)},
+      {"XlAdamWTensor", sizeof(XlAdamWTensor)}, {"XlAdamWArgs", sizeof(XlAdamWArgs)},
+  };
+  for (const Entry& e : sizes)
+    if (strcmp(e.name, name) == 0) return e.size;
+  return 0;
+}
 
 extern "C" int xl_init(void) { return xl::ensure_init(); }
 

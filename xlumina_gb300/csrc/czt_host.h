@@ -33,7 +33,14 @@ struct CztLaunch {
   const float2* post_y;  // my (includes 1/Ly)
   float2* work;          // B x cout x ny x mxp, column tiles of 2^lw
   XlProg pre;
+  const double* zb;      // per-entry distances (NULL: z for every entry); with them the
+  const float2* cteb;    // chirps are packed per entry and cteb[b] replaces cte
 };
+
+// Entry b's chirp vector: the shared one, or its slot in the per-entry packing.
+__device__ __forceinline__ const float2* czt_entry(const float2* v, const CztLaunch& p, int b, int len) {
+  return p.zb ? v + (long long)b * len : v;
+}
 
 // Column-tile width of the intermediate, set by the y transform's length 2^logl.
 inline int czt_tile_w(int logl) {

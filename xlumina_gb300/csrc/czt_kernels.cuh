@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
   const bool staged = st.n > 0;
   const bool fwd_phase = p.mode != XL_CZT_PLAIN;
   const bool vczt = p.mode == XL_CZT_VECTOR && !p.adjoint;
-  const float zf = (float)p.z;
+  constexpr int L = C::L;
 
   if (tid == 0 && staged) {
     mbar_init(mbar, 1);
@@ -105,6 +105,8 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
     const int b = grp / ngb;
     const int r0 = (grp - b * ngb) * C::G;
+    const double zd = p.zb ? p.zb[b] : p.z;
+    const float zf = (float)zd;
     if (staged) {
       if (!mbar_wait_bounded(mbar, phase)) ok = false;
       phase ^= 1u;
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
           e[2] = cscale(cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr)), zf / rr);
         }
         // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
-        float2 Fv = rs_kernel_value(p.x[n], p.y[r], p.z, p.inv_lambda, p.k);
+        float2 Fv = rs_kernel_value(p.x[n], p.y[r], zd, p.inv_lambda, p.k);
         if (p.adjoint) Fv = cconj(Fv);
 #pragma unroll
         for (int c = 0; c < 3; ++c) e[c] = cmul(e[c], Fv);
@@ -155,17 +157,18 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
       const bool act = live && c < p.cout;
       float2 v[16];
       const float2* src = post + (c < NC ? c * C::G + gi : 0) * nx;
+      const float2* pre_x = czt_entry(p.pre_x, p, b, nx);
       constexpr int MN = ZU ? C::H : 16;
 #pragma unroll
       for (int m = 0; m < MN; ++m) {
         const int i = j + m * C::T - p.ioff_x;
-        v[m] = (act && i >= 0 && i < nx) ? cmul(src[i], __ldg(p.pre_x + i)) : make_float2(0.f, 0.f);
+        v[m] = (act && i >= 0 && i < nx) ? cmul(src[i], __ldg(pre_x + i)) : make_float2(0.f, 0.f);
       }
 #pragma unroll
       for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
       block_fft_x<LOGL, 16, -1, ZU, true>(v, j, xch + line * C::XS, pass_tw<LOGL>());
       {
-        const float2* g = p.g_x;
+        const float2* g = czt_entry(p.g_x, p, b, L);
         asm volatile("" : "+l"(g) : : "memory");
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
@@ -173,10 +176,11 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
       block_fft_x<LOGL, 16, 1, false, true>(v, j, xch + line * C::XS, pass_tw<LOGL>());
       if (act) {
         float2* plane = p.work + ((long long)b * p.cout + c) * ny * p.mxp;
+        const float2* post_x = czt_entry(p.post_x, p, b, p.mx);
 #pragma unroll
         for (int m = 0; m < 16; ++m) {
           const int o = j + m * C::T - p.ooff_x;
-          if (o >= 0 && o < p.mx) plane[tiled_rt(r, o, ny, p.lw)] = cmul(v[m], __ldg(p.post_x + o));
+          if (o >= 0 && o < p.mx) plane[tiled_rt(r, o, ny, p.lw)] = cmul(v[m], __ldg(post_x + o));
         }
       }
     }
@@ -211,7 +215,16 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
   __syncthreads();
   float2* xb = xch + w * C::CXS;
   const bool fold = p.adjoint && p.mode == XL_CZT_VECTOR;
-  const float zf = (float)p.z;
+  const double zd = p.zb ? p.zb[b] : p.z;
+  const float zf = (float)zd;
+  const float2* pre_y = czt_entry(p.pre_y, p, b, ny);
+  const float2* g_y = czt_entry(p.g_y, p, b, C::L);
+  const float2* post_y = czt_entry(p.post_y, p, b, p.my);
+  float2 cte = p.cte;
+  if (p.cteb) {
+    cte = p.cteb[b];
+    if (p.adjoint) cte.y = -cte.y;
+  }
 #pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {
     const float2* tileT = p.work + ((long long)b * p.cout + c) * ny * p.mxp + (long long)t * ny * W + w;
@@ -220,13 +233,13 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
 #pragma unroll
     for (int m = 0; m < MN; ++m) {
       const int n = j + m * C::T - p.ioff_y;
-      v[m] = (live && n >= 0 && n < ny) ? cmul(tileT[(long long)n * W], __ldg(p.pre_y + n)) : make_float2(0.f, 0.f);
+      v[m] = (live && n >= 0 && n < ny) ? cmul(tileT[(long long)n * W], __ldg(pre_y + n)) : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
     block_fft_x<LOGL, 16, -1, ZU, false>(v, j, xb, stw);
     {
-      const float2* g = p.g_y;
+      const float2* g = g_y;
       asm volatile("" : "+l"(g));
 #pragma unroll
       for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
@@ -237,12 +250,12 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
     for (int m = 0; m < 16; ++m) {
       const int o = j + m * C::T - p.ooff_y;
       if (o < 0 || o >= p.my) continue;
-      float2 val = cmul(v[m], __ldg(p.post_y + o));
+      float2 val = cmul(v[m], __ldg(post_y + o));
       if (p.mode != XL_CZT_PLAIN) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
-        const float2 Fv = rs_kernel_value(p.xo[col], p.yo[o], p.z, p.inv_lambda, p.k);
+        const float2 Fv = rs_kernel_value(p.xo[col], p.yo[o], zd, p.inv_lambda, p.k);
         val = p.adjoint ? cmulc(val, Fv) : cmul(val, Fv);
       }
-      val = cmul(val, p.cte);
+      val = cmul(val, cte);
       const long long pix = (long long)b * p.obs + (long long)o * p.mx + col;
       if (fold && c == 2) {  // adjoint of Ez = (Ex X/r + Ey Y/r) z/r, vectorized_optics.py:341-344
         const float X = (float)p.xo[col], Y = (float)p.yo[o];

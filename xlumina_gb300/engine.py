@@ -729,6 +729,59 @@ def czt_grid(z, wavelength, xin, yin, xout, yout):
                 fx1=xout[0] + Dm / 2, fx2=xout[-1] + Dm / 2)
 
 
+def bluestein_length(m, M):
+    """The transform length of an m-point chirp-z onto M outputs: the
+    reference's np2 = next power of two >= m + M - 1 (wave_optics.py:373-383,
+    438), at least 32 here."""
+    if M < 2:
+        raise ValueError("chirp-z needs at least 2 output samples per axis")
+    mp = m + M - 1
+    L = int(2 ** int(np.ceil(np.log2(mp))))
+    if L == mp:
+        raise ValueError(f"m + M - 1 = {mp} is a power of two: the reference's Bluestein output slice "
+                         "(wave_optics.py:446) is one sample short for this size")
+    return max(L, 32)
+
+
+def entry_chirps(z, wavelength, x, y, xout, yout, adjoint=False):
+    """Chirp vectors and constant factors of a chirp-z at one distance per
+    batch entry, built on the device (float64, stored complex64) from the
+    device float64 distances ``z`` (B,): the per-entry form of
+    ``device_chirps`` for build_CZT_grid's Dm = lambda z / dx
+    (wave_optics.py:299-331).  Returns (Lx, Ly, pre_x, g_x, post_x, pre_y,
+    g_y, post_y, cte), packed entry after entry as XlCztArgs.z_batch reads
+    them; the vectors of ``adjoint`` calls are the adjoint set."""
+    L = lib()
+    B = int(z.numel())
+    nx, ny, mx, my = len(x), len(y), len(xout), len(yout)
+    Lx, Ly = bluestein_length(nx, mx), bluestein_length(ny, my)
+    ix, ox = (mx, nx) if adjoint else (nx, mx)
+    iy, oy = (my, ny) if adjoint else (ny, my)
+    sizes = [ix, Lx, ox, iy, Ly, oy, 1]
+    buf = torch.empty(B * sum(sizes), dtype=torch.complex64, device=z.device)
+    views, o = [], 0
+    for n in sizes:
+        views.append(buf[o:o + B * n])
+        o += B * n
+    a = _lib.XlCztChirpArgs()
+    a.batch, a.ny, a.nx, a.my, a.mx = B, ny, nx, my, mx
+    a.log2_lx, a.log2_ly = Lx.bit_length() - 1, Ly.bit_length() - 1
+    a.adjoint = 1 if adjoint else 0
+    a.z = z.data_ptr()
+    a.wavelength, a.dx, a.dy = float(wavelength), float(x[1] - x[0]), float(y[1] - y[0])
+    a.xout0, a.xout1, a.yout0, a.yout1 = float(xout[0]), float(xout[-1]), float(yout[0]), float(yout[-1])
+    (a.pre_x, a.g_x, a.post_x, a.pre_y, a.g_y, a.post_y, a.cte) = (v.data_ptr() for v in views)
+    _lib.check(L.xl_czt_chirps(stream_handle(), ctypes.byref(a)), "xl_czt_chirps")
+    return (Lx, Ly) + tuple(views)
+
+
+def _per_entry(z):
+    """True when ``z`` holds one distance per batch entry (a sequence or a 1-D tensor)."""
+    if isinstance(z, torch.Tensor):
+        return z.dim() >= 1
+    return isinstance(z, (list, tuple, np.ndarray)) and np.ndim(z) >= 1
+
+
 def bluestein_plan(m, f1, f2, Dm, M):
     """Chirp data of wave_optics.py:385-460 for an m-point input and M outputs, float64.
 
@@ -737,20 +790,14 @@ def bluestein_plan(m, f1, f2, Dm, M):
     post[l] = h[m-1+l] exp(-i 2 pi l_f (1/2 - m/2) / Dm) / L, where
     h[q] = W^((q-m+1)^2/2) with the complex power's principal branch.
     """
-    if M < 2:
-        raise ValueError("chirp-z needs at least 2 output samples per axis")
+    Lk = bluestein_length(m, M)
     D1 = f1 + (M * Dm + f2 - f1) / (2 * M)
     D2 = f2 + (M * Dm + f2 - f1) / (2 * M)
     mp = m + M - 1
-    L = int(2 ** int(np.ceil(np.log2(mp))))
-    if L == mp:
-        raise ValueError(f"m + M - 1 = {mp} is a power of two: the reference's Bluestein output slice "
-                         "(wave_optics.py:446) is one sample short for this size")
     A = np.exp(1j * 2 * np.pi * D1 / Dm)
     W = np.exp(-1j * 2 * np.pi * (D2 - D1) / (M * Dm))
     q = np.arange(-m + 1, max(M - 1, m - 1) + 1)
     h = W ** (q ** 2 / 2)
-    Lk = max(L, 32)
     g = np.fft.fft(1 / h[:mp + 1], Lk)
     pre = A ** (-np.arange(m)) * h[m - 1:2 * m - 1]
     lf = np.linspace(0, M - 1, M) / M * (D2 - D1) + D1
@@ -788,7 +835,9 @@ class CztCall:
 
     mode "scalar": wave_optics.py:233-263; "vczt": vectorized_optics.py:321-361;
     "high_na": optical_elements.py:600-638 (the lens op must be in ``pre``,
-    ``lens`` = (radius, f, sin_theta_max))."""
+    ``lens`` = (radius, f, sin_theta_max)).  ``z``: one distance, or one per
+    batch entry (a sequence or a 1-D tensor, kept on the device; the chirps
+    are then built there by ``entry_chirps``)."""
 
     def __init__(self, comps, x, y, wavelength, z, xout, yout, mode, pre=(), lens=None, outs=None,
                  adjoint=False):
@@ -800,6 +849,12 @@ class CztCall:
         lead = comps[0].shape[:-2]
         comps, B, ibs = batch_planes(comps, *comps[0].shape[-2:])
         dev = comps[0].device
+        zb = None
+        if mode != "high_na" and _per_entry(z):
+            zb = (z.detach() if isinstance(z, torch.Tensor) else torch.tensor(np.asarray(z, dtype=np.float64)))
+            zb = zb.to(device=dev, dtype=torch.float64).reshape(-1).contiguous()
+            if zb.numel() != B:
+                raise ValueError(f"{zb.numel()} distances for a batch of {B} fields")
         if mode == "high_na":
             r, f, s_max = lens
             Dm = f * wavelength * (nx - 1) / (2 * r)
@@ -807,13 +862,19 @@ class CztCall:
             cte = -(1j * s_max ** 2 / (f * wavelength))
             zz = 0.0
         else:
-            Dm = wavelength * z / (x[1] - x[0])
             cmode = _lib.XL_CZT_SCALAR if mode == "scalar" else _lib.XL_CZT_VECTOR
             cin, cout = (1, 1) if mode == "scalar" else ((3 if adjoint else 2), 3)
-            cte = z * (x[1] - x[0]) * (y[1] - y[0]) * wavelength
-            zz = float(z)
-        Lx, prex, gx, postx = device_chirps(nx, xout[0] + Dm / 2, xout[-1] + Dm / 2, Dm, mx, adjoint)
-        Ly, prey, gy, posty = device_chirps(ny, yout[0] + Dm / 2, yout[-1] + Dm / 2, Dm, my, adjoint)
+            if zb is None:
+                Dm = wavelength * z / (x[1] - x[0])
+                cte = z * (x[1] - x[0]) * (y[1] - y[0]) * wavelength
+                zz = float(z)
+        cteb = None
+        if zb is not None:
+            Lx, Ly, prex, gx, postx, prey, gy, posty, cteb = entry_chirps(zb, wavelength, x, y, xout, yout, adjoint)
+            cte, zz = 0.0, 0.0
+        else:
+            Lx, prex, gx, postx = device_chirps(nx, xout[0] + Dm / 2, xout[-1] + Dm / 2, Dm, mx, adjoint)
+            Ly, prey, gy, posty = device_chirps(ny, yout[0] + Dm / 2, yout[-1] + Dm / 2, Dm, my, adjoint)
         if adjoint:   # the call reads the forward's output plane and writes its input plane
             x, y, xout, yout = xout, yout, x, y
             ny, nx, my, mx = my, mx, ny, nx
@@ -838,10 +899,12 @@ class CztCall:
         a.pre_x, a.g_x, a.post_x = prex.data_ptr(), gx.data_ptr(), postx.data_ptr()
         a.pre_y, a.g_y, a.post_y = prey.data_ptr(), gy.data_ptr(), posty.data_ptr()
         a.work = work.data_ptr()
+        if zb is not None:
+            a.z_batch, a.cte_batch = zb.data_ptr(), cteb.data_ptr()
         fill_prog(a.pre, pre, ny, nx)
         self.args = a
         self.outs = outs
-        self._keep = (comps, work, prex, gx, postx, prey, gy, posty, gx_, gy_, gxo, gyo, list(pre or ()))
+        self._keep = (comps, work, prex, gx, postx, prey, gy, posty, gx_, gy_, gxo, gyo, list(pre or ()), zb, cteb)
 
     def run(self):
         _lib.check(lib().xl_czt(stream_handle(), ctypes.byref(self.args)), "xl_czt")

@@ -44,9 +44,9 @@ class Request:
     def key(self):
         k = (self.kind, len(self.y), len(self.x), float(self.x[0]), float(self.x[-1]), float(self.y[0]),
              float(self.y[-1]), float(self.wavelength))
-        if self.kind == "czt":
+        if self.kind == "czt":   # distances differ freely within a batch (per-entry chirps)
             k += (len(self.yout), len(self.xout), float(self.xout[0]), float(self.xout[-1]),
-                  float(self.yout[0]), float(self.yout[-1]), float(self.z))
+                  float(self.yout[0]), float(self.yout[-1]))
         return k
 
     def nbytes(self):
@@ -77,7 +77,8 @@ def run_batch(reqs):
         return [(o[0][i], o[1][i], o[2][i]) for i in range(len(reqs))]
     if r0.kind == "czt":
         f = torch.stack([r.fields[0] for r in reqs])
-        out = engine.czt_propagate([f], r0.x, r0.y, r0.wavelength, r0.z, r0.xout, r0.yout, "scalar")[0]
+        zc = zs if len(set(zs)) > 1 else r0.z   # one distance: the cached host chirps
+        out = engine.czt_propagate([f], r0.x, r0.y, r0.wavelength, zc, r0.xout, r0.yout, "scalar")[0]
         return [out[i] for i in range(len(reqs))]
     if r0.kind == "grad":
         with torch.enable_grad():
