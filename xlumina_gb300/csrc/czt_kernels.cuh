@@ -95,16 +95,19 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
     fence_mbar_init();
   }
   __syncthreads();
+  // row groups are taken batch entries fastest: CTAs that run together read the
+  // same rows of planes shared by the batch (the lens coefficients, shared
+  // masks), so those rows come from L2 after the first entry
   if (tid == 0 && staged && blockIdx.x < total) {
-    const int b = blockIdx.x / ngb, r0 = (blockIdx.x - b * ngb) * C::G;
+    const int b = blockIdx.x % p.B, r0 = (blockIdx.x / p.B) * C::G;
     stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
   }
 
   unsigned phase = 0;
   bool ok = true;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
-    const int b = grp / ngb;
-    const int r0 = (grp - b * ngb) * C::G;
+    const int b = grp % p.B;
+    const int r0 = (grp / p.B) * C::G;
     const double zd = p.zb ? p.zb[b] : p.z;
     const float zf = (float)zd;
     if (staged) {
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
     __syncthreads();   // every thread has read the stage and written its pixels
     if (tid == 0 && staged && grp + gridDim.x < total) {
       fence_proxy_async();
-      const int g = grp + gridDim.x, bn = g / ngb, rn = (g - bn * ngb) * C::G;
+      const int g = grp + gridDim.x, bn = g % p.B, rn = (g / p.B) * C::G;
       stage_rows(st, stage, mbar, bn, rn, min(C::G, ny - rn));
     }
     const int r = r0 + gi;
