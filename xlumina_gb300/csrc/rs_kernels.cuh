@@ -313,9 +313,11 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   float2* stw = smem + CW * C::CXS;    // NTW
   const int tid = threadIdx.x, lane = tid & 31;
   const int wc = lane % CW, j = (tid >> 5) * LPW + lane / CW;
-  const int t = blockIdx.x / (W / CW);                      // column tile
-  const int w = (blockIdx.x % (W / CW)) * CW + wc;          // column within the tile
-  const int b = blockIdx.y;
+  // batch entries fastest: the CTAs of one column tile run together and share
+  // its transfer-spectrum columns in L2
+  const int t = blockIdx.y / (W / CW);                      // column tile
+  const int w = (blockIdx.y % (W / CW)) * CW + wc;          // column within the tile
+  const int b = blockIdx.x;
   const int ny = p.ny;
   {
     const float2* g = pass_tw<C::LOGP>();
@@ -548,7 +550,7 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   } else if (stage == 1) {
     const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
-    rs_cols_conv<LOGQ><<<dim3(C::P / C::CW, p.B), C::COL_THREADS, sm, st>>>(p);
+    rs_cols_conv<LOGQ><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
     XL_CHECK_LAUNCH("rs_cols_conv");
   } else {
     const bool epi = p.post.nops > 0 || (p.adjoint && p.cout == 3);
