@@ -211,8 +211,10 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
     for (int i = tid; i < nx; i += blockDim.x) xf[i] = (float)p.x[i];
   __syncthreads();
 
+  // row groups are taken batch entries fastest: CTAs that run together read the
+  // same rows of the parameter planes a batch shares, which then come from L2
   auto issue = [&](int grp) {
-    const int b = grp / ngb, r0 = (grp - b * ngb) * C::G;
+    const int b = grp % p.B, r0 = (grp / p.B) * C::G;
     stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
   };
   if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
@@ -220,8 +222,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   unsigned phase = 0;
   bool ok = true;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
-    const int b = grp / ngb;
-    const int r0 = (grp - b * ngb) * C::G;
+    const int b = grp % p.B;
+    const int r0 = (grp / p.B) * C::G;
     if (staged) {
       if (!mbar_wait_bounded(mbar, phase)) ok = false;
       phase ^= 1u;
@@ -381,9 +383,9 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
   float2* xb = smem + line * C::XS;
   float2* post = smem + F::LINES * C::XS;     // COUT x G x nx (epilogue only)
 
-  auto load = [&](int grp, int c, float2 (&dst)[16]) {
-    const int b = grp / ngb;
-    int r = (grp - b * ngb) * C::G + gi;
+  auto load = [&](int grp, int c, float2 (&dst)[16]) {   // row groups batch entries fastest
+    const int b = grp % p.B;
+    int r = (grp / p.B) * C::G + gi;
     r = r < ny ? r : ny - 1;    // rows past the end load a valid row and discard it
     const float2* plane = p.work + ((long long)b * COUT + c) * ny * C::P;
     if constexpr (C::T % C::W == 0) {
@@ -399,8 +401,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, COUT>::THREADS, RowCfg<LOGQ, COUT
   float2 nxt[16];
   if (blockIdx.x < total) load(blockIdx.x, cg, nxt);
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
-    const int b = grp / ngb;
-    const int r0 = (grp - b * ngb) * C::G;
+    const int b = grp % p.B;
+    const int r0 = (grp / p.B) * C::G;
     const int r = r0 + gi;
     const bool live = r < ny;
     for (int c = cg; c < COUT; c += F::CG) {
