@@ -139,7 +139,7 @@ class ClockSampler:
 # DRAM bytes (read + write) per 2048^2 VRS field of each pass, from the ncu
 # capture summarised in profiles/rs_kernels_vrs2048.md (batch 2, scaled per
 # field; every field is an independent slice of the launch).
-NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 275.75e6, "rs_cols_conv": 521.35e6, "rs_rows_inv": 283.74e6}
+NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 276.15e6, "rs_cols_conv": 525.65e6, "rs_rows_inv": 283.60e6}
 
 
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
@@ -365,15 +365,21 @@ def run_gpu(args):
     for i in range(E2E_STREAMS):
         e2e_step(i)
     torch.cuda.synchronize()
+    # three consecutive timed segments of ke steps; the median is reported (the
+    # host link is shared with the rest of the machine and a single segment
+    # can catch a slow spell)
     ke = max(4, args.steps // 2)
-    replica_barrier()
-    t0 = time.perf_counter()
-    for i in range(ke):
-        streams[i % E2E_STREAMS].synchronize()   # the stream's host buffers are free again
-        e2e_step(i)
-    torch.cuda.synchronize()
-    e2e_s, e2e_fields = reduce_replicas(time.perf_counter() - t0, B * ke)
-    e2e = e2e_fields / e2e_s
+    segments = []
+    for _ in range(3):
+        replica_barrier()
+        t0 = time.perf_counter()
+        for i in range(ke):
+            streams[i % E2E_STREAMS].synchronize()   # the stream's host buffers are free again
+            e2e_step(i)
+        torch.cuda.synchronize()
+        e2e_s, e2e_fields = reduce_replicas(time.perf_counter() - t0, B * ke)
+        segments.append(e2e_fields / e2e_s)
+    e2e = float(np.median(segments))
     h2d = (hosts[0]["Ex"].numel() + hosts[0]["Ey"].numel()) * 8 + \
         (hosts[0]["eta"].numel() + hosts[0]["theta"].numel()) * 4
     d2h = sum(hb.numel() for hb in hosts[0]["out"]) * 8
@@ -397,7 +403,8 @@ def run_gpu(args):
         "stages_ms": dict(zip(names, stage_ms)),
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
-        "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "segments": segments, "steps_per_segment": ke},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
         "spectrum_builds": engine.SPECTRA.builds,
