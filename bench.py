@@ -137,9 +137,12 @@ class ClockSampler:
 
 
 # DRAM bytes (read + write) per 2048^2 VRS field of each pass, from the ncu
-# capture summarised in profiles/rs_kernels_vrs2048.md (batch 2, scaled per
-# field; every field is an independent slice of the launch).
-NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 276.15e6, "rs_cols_conv": 525.65e6, "rs_rows_inv": 283.60e6}
+# captures summarised in profiles/rs_kernels_vrs2048.md.  The column pass's
+# figure is from a capture of the bench's own launch (8 fields at 4 distances,
+# so pairs of fields share a transfer spectrum); the row passes' are from a
+# batch-2 capture scaled per field (every field is an independent slice of
+# those launches).
+NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 276.15e6, "rs_cols_conv": 478.88e6, "rs_rows_inv": 283.60e6}
 
 
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
@@ -397,7 +400,7 @@ def run_gpu(args):
                      "traffic": (NCU_TRAFFIC_PER_FIELD[names[dom]] * B
                                  if NCU_TRAFFIC_PER_FIELD[names[dom]] is not None else None),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "profiles/rs_kernels_vrs2048.md, scaled to the launch's fields",
+                                       "profiles/rs_kernels_vrs2048.md (the bench's own 8-field launch)",
                      "peak_source": peak_src,
                      "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
         "stages_ms": dict(zip(names, stage_ms)),
