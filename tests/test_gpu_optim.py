@@ -8,8 +8,10 @@ pytestmark = pytest.mark.gpu
 
 def _params(torch, seed):
     g = torch.Generator(device="cuda").manual_seed(seed)
-    shapes = [(256, 256), (3, 64, 64), (1000,), (1,)]
+    shapes = [(256, 256), (3, 64, 64), (1000,), (1003,), (1,)]   # 1003: four-wide body and a tail
     ps = [torch.randn(s, generator=g, device="cuda") for s in shapes]
+    # a view one element into its storage, not 16-byte aligned: the element-wise path
+    ps.append(torch.randn((1002,), generator=g, device="cuda")[1:].detach())
     ps.append(torch.randn((1,), generator=g, device="cuda", dtype=torch.float64))   # through torch's AdamW
     return [p.requires_grad_(True) for p in ps]
 
