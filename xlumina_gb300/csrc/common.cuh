@@ -340,13 +340,73 @@ __device__ __forceinline__ void lcd_bwd_trig(float ch, float sh, float ct, float
   g[1] = cadd(cmul(cconj(bb), g0), cmul(cconj(d), g1));
 }
 
-__device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
-                                             const PixelCtx& px, float (&pg)[4]) {
+// The sines and cosines an op's forward and backward need, so that a caller
+// that runs both (xl_ops_backward) evaluates them once: PHASE (c0, s0) of p0;
+// sSLM (c0, s0) of p0 and (c1, s1) of p1; LCD (c0, s0) of eta/2 and (c1, s1)
+// of theta; LP (c0, s0) of alpha.  Scalar parameters take the host's values.
+__device__ __forceinline__ float4 op_trig(const XlOp& op, const PixelCtx& px) {
+  float4 t = make_float4(1.f, 0.f, 1.f, 0.f);   // (c0, s0, c1, s1)
+  switch (op.kind) {
+    case XL_OP_PHASE:
+      phase_sincos(op_param(op, 0, px), &t.y, &t.x);
+      break;
+    case XL_OP_SSLM:
+    case XL_OP_SSLM_AMP:
+      phase_sincos(op_param(op, 0, px), &t.y, &t.x);
+      phase_sincos(op_param(op, 1, px), &t.w, &t.z);
+      break;
+    case XL_OP_LCD:
+      if (op.pmask & 1) phase_sincos(0.5f * op_param(op, 0, px), &t.y, &t.x);
+      else { t.x = op.dval[0]; t.y = op.dval[1]; }
+      if (op.pmask & 2) phase_sincos(op_param(op, 1, px), &t.w, &t.z);
+      else { t.z = op.dval[2]; t.w = op.dval[3]; }
+      break;
+    case XL_OP_LP:
+      if (op.pmask & 1) phase_sincos(op_param(op, 0, px), &t.y, &t.x);
+      else { t.x = op.sval[2]; t.y = op.sval[3]; }
+      break;
+    default:
+      break;
+  }
+  return t;
+}
+
+// apply_op with the trig of op_trig (the same arithmetic as apply_op_r).
+__device__ __forceinline__ void apply_op_t(const XlOp& op, const float4& t, float2 (&e)[3], const PixelCtx& px) {
+  switch (op.kind) {
+    case XL_OP_PHASE:
+      e[0] = cmul(e[0], make_float2(t.x, t.y));
+      break;
+    case XL_OP_SSLM:
+      e[0] = cmul(e[0], make_float2(t.x, t.y));
+      e[1] = cmul(e[1], make_float2(t.z, t.w));
+      break;
+    case XL_OP_SSLM_AMP:
+      e[0] = cscale(cmul(e[0], make_float2(t.x, t.y)), op_param(op, 2, px));
+      e[1] = cscale(cmul(e[1], make_float2(t.z, t.w)), op_param(op, 3, px));
+      break;
+    case XL_OP_LCD:
+      lcd_apply_trig(t.x, t.y, t.z, t.w, e);
+      break;
+    case XL_OP_LP: {
+      const float c = t.x, s = t.y;
+      const float2 x = e[0], y = e[1];
+      e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
+      e[1] = cadd(cscale(x, c * s), cscale(y, s * s));
+      e[2] = make_float2(0.f, 0.f);
+      break;
+    }
+    default:
+      apply_op(op, e, px);
+      break;
+  }
+}
+
+__device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, const float2 (&e)[3],
+                                               float2 (&g)[3], const PixelCtx& px, float (&pg)[4]) {
   switch (op.kind) {
     case XL_OP_PHASE: {
-      float s, c;
-      phase_sincos(op_param(op, 0, px), &s, &c);
-      const float2 ph = make_float2(c, s);
+      const float2 ph = make_float2(t.x, t.y);
       const float2 y = cmul(e[0], ph);
       pg[0] += re_gconj(g[0], make_float2(-y.y, y.x));   // dy/dphi = i y
       g[0] = cmulc(g[0], ph);
@@ -355,11 +415,8 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
     case XL_OP_SSLM:
     case XL_OP_SSLM_AMP: {
       const bool amp = op.kind == XL_OP_SSLM_AMP;
-      float s, c;
-      phase_sincos(op_param(op, 0, px), &s, &c);
-      const float2 p0 = make_float2(c, s);
-      phase_sincos(op_param(op, 1, px), &s, &c);
-      const float2 p1 = make_float2(c, s);
+      const float2 p0 = make_float2(t.x, t.y);
+      const float2 p1 = make_float2(t.z, t.w);
       const float a1 = amp ? op_param(op, 2, px) : 1.f, a2 = amp ? op_param(op, 3, px) : 1.f;
       const float2 u0 = cmul(e[0], p0), u1 = cmul(e[1], p1);   // before the amplitudes
       pg[0] += a1 * re_gconj(g[0], make_float2(-u0.y, u0.x));
@@ -372,19 +429,11 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
       g[1] = cscale(cmulc(g[1], p1), a2);
       break;
     }
-    case XL_OP_LCD: {
-      float sh, ch, st, ct;
-      if (op.pmask & 1) phase_sincos(0.5f * op_param(op, 0, px), &sh, &ch);
-      else { ch = op.dval[0]; sh = op.dval[1]; }
-      if (op.pmask & 2) phase_sincos(op_param(op, 1, px), &st, &ct);
-      else { ct = op.dval[2]; st = op.dval[3]; }
-      lcd_bwd_trig(ch, sh, ct, st, e, g, pg);
+    case XL_OP_LCD:
+      lcd_bwd_trig(t.x, t.y, t.z, t.w, e, g, pg);
       break;
-    }
     case XL_OP_LP: {
-      float s, c;
-      if (op.pmask & 1) phase_sincos(op_param(op, 0, px), &s, &c);
-      else { c = op.sval[2]; s = op.sval[3]; }
+      const float c = t.x, s = t.y;
       const float2 x = e[0], y = e[1];
       const float dcs = c * c - s * s, tcs = 2.f * c * s;
       pg[0] += re_gconj(g[0], cadd(cscale(x, -tcs), cscale(y, dcs))) +
@@ -425,6 +474,11 @@ __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3
     default:
       break;
   }
+}
+
+__device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
+                                             const PixelCtx& px, float (&pg)[4]) {
+  apply_op_bwd_t(op, op_trig(op, px), e, g, px, pg);
 }
 
 }  // namespace xl

@@ -58,6 +58,9 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
   constexpr int NS = XL_MAX_OPS * 4;
   constexpr int NT = 128;
   extern __shared__ float accm[];
+  // the trig of every op the forward recompute applies, for its backward
+  // (thread-private slots, so no barrier): evaluated once per pixel and entry
+  __shared__ float4 trig_s[KMAX - 1][NT];
   float* acc_s = accm;                              // NS x NT, when scalar_acc
   float* acc_p = accm + (scalar_acc ? NS * NT : 0); // NS x NT, when plane_acc
   const long long npix = (long long)p.ny * p.nx;
@@ -98,8 +101,13 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
         if (k < K) {
           st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
           if (k + 1 < K) {
-            if (k == hk) apply_highna(kc, e);
-            else apply_op(p.prog.ops[k], e, px);
+            if (k == hk) {
+              apply_highna(kc, e);
+            } else if (k < KMAX - 1) {
+              const float4 t = op_trig(p.prog.ops[k], px);
+              trig_s[k][tid] = t;
+              apply_op_t(p.prog.ops[k], t, e, px);
+            }
           }
         }
       }
@@ -115,6 +123,7 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
           float pg[4] = {0.f, 0.f, 0.f, 0.f};
           const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
           if (k == hk) apply_highna_bwd(kc, g);
+          else if (k + 1 < K && k < KMAX - 1) apply_op_bwd_t(op, trig_s[k][tid], ek, g, px, pg);
           else apply_op_bwd(op, ek, g, px, pg);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
