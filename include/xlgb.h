@@ -228,6 +228,13 @@ typedef struct {
    * conjugates it, as it does cte). */
   const double* z_batch;
   const void* cte_batch;
+  /* Optional (one distance only, scalar and vectorial modes): the transfer
+   * function evaluated once on this call's input plane (f_in, ny x nx) and
+   * output plane (f_out, my x mx), complex64 as xl_czt_transfer_plane writes
+   * it; NULL: evaluated per pixel in the kernels.  Both are the forward's
+   * H(z, X, Y) at the call's own coordinates (the adjoint conjugates). */
+  const void* f_in;
+  const void* f_out;
 } XlCztArgs;
 
 size_t xl_czt_work_bytes(int batch, int comps, int ny, int mx);
@@ -269,6 +276,14 @@ typedef struct {
 } XlCztChirpArgs;
 
 int xl_czt_chirps(void* stream, const XlCztChirpArgs* args);
+
+/* The RS impulse response H(z, X, Y) of wave_optics.py:291-297 on the grid
+ * (x, y) (device float64, nx and ny values), complex64, row-major ny x nx:
+ * the F and F0 planes of CZT_jit (wave_optics.py:339-341), computed as the
+ * chirp-z kernels compute them per pixel, for reuse by XlCztArgs.f_in /
+ * f_out when a geometry is propagated repeatedly. */
+int xl_czt_transfer_plane(void* stream, int ny, int nx, const double* x, const double* y, double z,
+                          double wavelength, void* out);
 
 /* ---- Elementwise ------------------------------------------------------ */
 

@@ -199,3 +199,34 @@ def test_phase_gradient_through_per_entry_czt():
         assert rel_l2(_np(g_all[b]), _np(g_one)) < 1e-5
     with pytest.raises(NotImplementedError):
         autograd.CztPlan(x, x, 0.633, torch.tensor(zs, device="cuda", requires_grad=True), xo, xo, "scalar", [])
+
+
+def test_transfer_planes_give_identical_results(torch_engine):
+    """The second call with a geometry reads F and F0 from cached planes
+    (xl_czt_transfer_plane); they hold the values the kernels compute per
+    pixel, so the result is bit-identical, forward and adjoint."""
+    torch, engine = torch_engine
+    rng = np.random.default_rng(16)
+    n, m = 96, 40
+    x, _ = ref.space(700.0, n)
+    xo, _ = ref.space(120.0, m)
+    f = torch.tensor(_field(rng, n, n, 3), device="cuda")
+    ey = torch.tensor(_field(rng, n, n, 3), device="cuda")
+    gs = [torch.tensor(_field(rng, m, m, 3), device="cuda") for _ in range(3)]
+    for z in (3.3e4, -2.1e4):
+        engine.TRANSFER_PLANES.clear()
+        b0 = engine.TRANSFER_PLANES.builds
+        first = engine.czt_propagate([f], x, x, 0.633, z, xo, xo, "scalar")[0]
+        assert engine.TRANSFER_PLANES.builds == b0            # first sight: evaluated in the kernels
+        second = engine.czt_propagate([f], x, x, 0.633, z, xo, xo, "scalar")[0]
+        assert engine.TRANSFER_PLANES.builds == b0 + 2        # F and F0 planes
+        assert torch.equal(first, second)
+        v1 = engine.czt_propagate([f, ey], x, x, 0.633, z, xo, xo, "vczt")
+        v2 = engine.czt_propagate([f, ey], x, x, 0.633, z, xo, xo, "vczt")
+        for a, b in zip(v1, v2):
+            assert torch.equal(a, b)
+        a1 = engine.CztCall(gs, x, x, 0.633, z, xo, xo, "vczt", adjoint=True).run()
+        a2 = engine.CztCall(gs, x, x, 0.633, z, xo, xo, "vczt", adjoint=True).run()
+        for a, b in zip(a1, a2):
+            assert torch.equal(a, b)
+        assert rel_l2(_np(second[1]), ref.czt(f[1].cpu().numpy().astype(np.complex128), x, x, 0.633, z, xo, xo)) < 1e-5

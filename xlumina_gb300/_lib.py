@@ -58,7 +58,8 @@ class XlCztArgs(ctypes.Structure):
                 ("pre_x", ctypes.c_void_p), ("g_x", ctypes.c_void_p), ("post_x", ctypes.c_void_p),
                 ("pre_y", ctypes.c_void_p), ("g_y", ctypes.c_void_p), ("post_y", ctypes.c_void_p),
                 ("work", ctypes.c_void_p), ("pre", XlProg), ("adjoint", ctypes.c_int),
-                ("z_batch", ctypes.c_void_p), ("cte_batch", ctypes.c_void_p)]
+                ("z_batch", ctypes.c_void_p), ("cte_batch", ctypes.c_void_p),
+                ("f_in", ctypes.c_void_p), ("f_out", ctypes.c_void_p)]
 
 
 class XlCztChirpArgs(ctypes.Structure):
@@ -148,6 +149,8 @@ SIGNATURES = {
     "xl_czt": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs)]),
     "xl_czt_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs), ctypes.c_int]),
     "xl_czt_chirps": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztChirpArgs)]),
+    "xl_czt_transfer_plane": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "xl_ops_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_longlong,

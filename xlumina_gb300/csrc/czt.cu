@@ -251,6 +251,10 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
     set_error("xl_czt: per-entry distances apply to the scalar and vectorial transforms only");
     return XL_EINVAL;
   }
+  if ((a->f_in || a->f_out) && (a->mode == XL_CZT_PLAIN || a->z_batch)) {
+    set_error("xl_czt: transfer planes apply to one distance in the scalar and vectorial modes");
+    return XL_EINVAL;
+  }
   if (!a->z_batch != !a->cte_batch) {
     set_error("xl_czt: z_batch and cte_batch go together");
     return XL_EINVAL;
@@ -293,6 +297,8 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
   p.pre = a->pre;
   p.zb = a->z_batch;
   p.cteb = (const float2*)a->cte_batch;
+  p.fin = (const float2*)a->f_in;
+  p.fout = (const float2*)a->f_out;
   cudaStream_t st = (cudaStream_t)stream;
   if (stage < 0 || stage == 0)
     if (int rc = dispatch_rows(st, p, llx)) return rc;

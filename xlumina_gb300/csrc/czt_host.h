@@ -35,6 +35,8 @@ struct CztLaunch {
   XlProg pre;
   const double* zb;      // per-entry distances (NULL: z for every entry); with them the
   const float2* cteb;    // chirps are packed per entry and cteb[b] replaces cte
+  const float2* fin;     // transfer function on the input plane (ny x nx), or NULL
+  const float2* fout;    // and on the output plane (my x mx), or NULL
 };
 
 // Entry b's chirp vector: the shared one, or its slot in the per-entry packing.

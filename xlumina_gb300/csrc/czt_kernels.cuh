@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
           e[2] = cscale(cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr)), zf / rr);
         }
         // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
-        float2 Fv = rs_kernel_value(p.x[n], p.y[r], zd, p.inv_lambda, p.k);
+        float2 Fv = p.fin ? p.fin[pix] : rs_kernel_value(p.x[n], p.y[r], zd, p.inv_lambda, p.k);
         if (p.adjoint) Fv = cconj(Fv);
 #pragma unroll
         for (int c = 0; c < 3; ++c) e[c] = cmul(e[c], Fv);
@@ -255,7 +255,8 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
       if (o < 0 || o >= p.my) continue;
       float2 val = cmul(v[m], __ldg(post_y + o));
       if (p.mode != XL_CZT_PLAIN) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
-        const float2 Fv = rs_kernel_value(p.xo[col], p.yo[o], zd, p.inv_lambda, p.k);
+        const float2 Fv = p.fout ? p.fout[(long long)o * p.mx + col]
+                                 : rs_kernel_value(p.xo[col], p.yo[o], zd, p.inv_lambda, p.k);
         val = p.adjoint ? cmulc(val, Fv) : cmul(val, Fv);
       }
       val = cmul(val, cte);

@@ -415,6 +415,37 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
   return XL_OK;
 }
 
+namespace xl {
+// The transfer function of the chirp-z prologue and epilogue on a whole grid,
+// evaluated by the same device function (rs_kernel_value) as the kernels.
+__global__ void __launch_bounds__(256) czt_transfer_plane_kernel(int ny, int nx, const double* __restrict__ x,
+                                                                 const double* __restrict__ y, double z,
+                                                                 double inv_lambda, float k, float2* out) {
+  const long long n = (long long)ny * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / nx), c = (int)(i - (long long)r * nx);
+    out[i] = rs_kernel_value(x[c], y[r], z, inv_lambda, k);
+  }
+}
+}  // namespace xl
+
+extern "C" int xl_czt_transfer_plane(void* stream, int ny, int nx, const double* x, const double* y, double z,
+                                     double wavelength, void* out) {
+  if (ny < 1 || nx < 1 || !x || !y || !out || !(wavelength > 0)) {
+    set_error("xl_czt_transfer_plane: bad arguments");
+    return XL_EINVAL;
+  }
+  if (int rc = ensure_init()) return rc;
+  const long long n = (long long)ny * nx;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  czt_transfer_plane_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      ny, nx, x, y, z, 1.0 / wavelength, (float)(2.0 * M_PI / wavelength), (float2*)out);
+  XL_CHECK_LAUNCH("czt_transfer_plane_kernel");
+  return XL_OK;
+}
+
 extern "C" int xl_highna_coefficients(void* stream, int ny, int nx, const double* x, const double* y,
                                       double radius, double f, void* out) {
   if (ny < 1 || nx < 1 || !x || !y || !out || !(radius > 0) || !(f > 0)) {

@@ -830,6 +830,72 @@ def device_chirps(m, f1, f2, Dm, M, adjoint=False):
     return v
 
 
+class TransferPlaneCache:
+    """The chirp-z transfer function F = H(z, X, Y) (wave_optics.py:339-341)
+    on whole grids, keyed by (grid, z, wavelength); LRU, bounded in bytes.
+
+    A geometry is evaluated per pixel inside the kernels the first time it is
+    seen and gets a plane the second time, so a table propagated every step
+    reads F from memory while a distance used once (a serving request) costs
+    no extra pass.  Planes are never built during graph capture."""
+
+    def __init__(self, max_bytes=2 << 30):
+        self.max_bytes = max_bytes
+        self._d: "collections.OrderedDict" = collections.OrderedDict()
+        self._seen: "collections.OrderedDict" = collections.OrderedDict()
+        self._bytes = 0
+        self.builds = 0
+
+    @staticmethod
+    def _key(x, y, z, wavelength):
+        return (array_key(x), array_key(y), float(z), float(wavelength), torch.cuda.current_device())
+
+    def pair(self, x, y, xout, yout, z, wavelength):
+        """(F on the input grid, F0 on the output grid), or (None, None) while the
+        geometry has not been seen before (or during graph capture, unless built)."""
+        kin, kout = self._key(x, y, z, wavelength), self._key(xout, yout, z, wavelength)
+        with _LOCK:
+            built = kin in self._d and kout in self._d
+            seen = all(k in self._d or k in self._seen for k in (kin, kout))
+            if not built and (not seen or torch.cuda.is_current_stream_capturing()):
+                for k in (kin, kout):
+                    self._seen[k] = True
+                while len(self._seen) > 4096:
+                    self._seen.popitem(last=False)
+                return None, None
+        return self._plane(kin, x, y, z, wavelength), self._plane(kout, xout, yout, z, wavelength)
+
+    def _plane(self, k, x, y, z, wavelength):
+        with _LOCK:
+            e = self._d.get(k)
+            if e is not None:
+                self._d.move_to_end(k)
+        if e is not None:
+            return e.use()
+        ny, nx = len(y), len(x)
+        t = torch.empty((ny, nx), dtype=torch.complex64, device=device())
+        _lib.check(lib().xl_czt_transfer_plane(stream_handle(), ny, nx, device_grid(x).data_ptr(),
+                                               device_grid(y).data_ptr(), float(z), float(wavelength),
+                                               t.data_ptr()), "xl_czt_transfer_plane")
+        with _LOCK:
+            self._d[k] = _Built(t)
+            self._bytes += t.numel() * 8
+            self.builds += 1
+            while self._bytes > self.max_bytes and len(self._d) > 2:
+                _, old = self._d.popitem(last=False)
+                self._bytes -= old.t.numel() * 8
+        return t
+
+    def clear(self):
+        with _LOCK:
+            self._d.clear()
+            self._seen.clear()
+            self._bytes = 0
+
+
+TRANSFER_PLANES = TransferPlaneCache()
+
+
 class CztCall:
     """One prepared chirp-z launch (scalar CZT, VCZT, or the high-NA focus).
 
@@ -899,12 +965,20 @@ class CztCall:
         a.pre_x, a.g_x, a.post_x = prex.data_ptr(), gx.data_ptr(), postx.data_ptr()
         a.pre_y, a.g_y, a.post_y = prey.data_ptr(), gy.data_ptr(), posty.data_ptr()
         a.work = work.data_ptr()
+        fin = fout = None
         if zb is not None:
             a.z_batch, a.cte_batch = zb.data_ptr(), cteb.data_ptr()
+        elif cmode != _lib.XL_CZT_PLAIN:
+            # F on the call's input plane and F0 on its output plane (for the
+            # adjoint the grids are already swapped)
+            fin, fout = TRANSFER_PLANES.pair(x, y, xout, yout, zz, wavelength)
+            if fin is not None:
+                a.f_in, a.f_out = fin.data_ptr(), fout.data_ptr()
         fill_prog(a.pre, pre, ny, nx)
         self.args = a
         self.outs = outs
-        self._keep = (comps, work, prex, gx, postx, prey, gy, posty, gx_, gy_, gxo, gyo, list(pre or ()), zb, cteb)
+        self._keep = (comps, work, prex, gx, postx, prey, gy, posty, gx_, gy_, gxo, gyo, list(pre or ()), zb, cteb,
+                      fin, fout)
 
     def run(self):
         _lib.check(lib().xl_czt(stream_handle(), ctypes.byref(self.args)), "xl_czt")
