@@ -112,3 +112,25 @@ def test_high_na_focus_full_size(xl):
     exp = ref.vczt_objective_lens(Ex1, Ey1, x, y, 0.650, r, f, xo, yo)
     for o, e in zip((out.Ex, out.Ey, out.Ez), exp):
         assert rel_l2(_np(o), e) < TOL
+
+
+def test_high_na_lens_odd_grid_keeps_the_reference_nan(xl):
+    """optical_elements.py:538 divides by rho: on an odd grid the centre pixel
+    (rho = 0) is NaN in every component, in the reference and here; every
+    other pixel matches the oracle."""
+    wo, vo, oe = xl
+    n = 33
+    x, y = ref.space(500.0, n)
+    rng = np.random.default_rng(33)
+    Ex = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    Ey = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    light = vo.VectorizedLight(x, y, 0.65)
+    light.Ex, light.Ey = Ex.astype(np.complex64), Ey.astype(np.complex64)
+    E, _ = oe.high_NA_objective_lens(light, 400.0, 400.0 / 0.9)
+    got = _np(E)
+    want = np.asarray(ref.high_na_lens(Ex.astype(np.complex64).astype(np.complex128),
+                                       Ey.astype(np.complex64).astype(np.complex128), x, y, 400.0, 400.0 / 0.9)[0])
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    assert np.isnan(got[:, n // 2, n // 2]).all() and np.isnan(got).sum() == 3
+    ok = ~np.isnan(want)
+    assert rel_l2(got[ok], want[ok]) < 1e-6
