@@ -321,6 +321,21 @@ def main(ref_root):
               hna_grid=np.array(hg, dtype=np.float64), plain=plain, bluestein=blu, theta=th, phi=phv, G=Gv,
               lens_helper=lens_h)
 
+        # 16. Jones matrices, the scalar SLM phase and the single-input splitter ports.
+        al, phs, et, ths, de, a1s, a2s = 0.37, -1.1, 2.3, 0.81, 0.6, 0.7, 0.45
+        ph_plane = rng.uniform(-np.pi, np.pi, (12, 12))
+        aEx = rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))
+        aEy = rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))
+        zero = np.zeros((8, 8), dtype=np.complex128)
+        T, R = 0.83, 0.51
+        p0 = oe.bs_port0(aEx, aEy, zero, zero, zero, zero, T, R)
+        p1 = oe.bs_port1(aEx, aEy, zero, zero, zero, zero, T, R)
+        _save("jones", alpha=al, phi=phs, eta=et, theta=ths, delta=de, a1=a1s, a2=a2s,
+              lp=oe.jones_LP(al), retarder=oe.jones_general_retarder(et, ths, de), sslm=oe.jones_sSLM(al, phs),
+              sslm_amp=oe.jones_sSLM_with_amplitude(al, phs, a1s, a2s), lcd=oe.jones_LCD(et, ths),
+              phase_plane=ph_plane, slm_phase=oe.phase_scalar_SLM(ph_plane), aEx=aEx, aEy=aEy, T=T, R=R,
+              port0=np.stack(p0), port1=np.stack(p1))
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))
