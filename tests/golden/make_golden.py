@@ -336,6 +336,17 @@ def main(ref_root):
               phase_plane=ph_plane, slm_phase=oe.phase_scalar_SLM(ph_plane), aEx=aEx, aEy=aEy, T=T, R=R,
               port0=np.stack(p0), port1=np.stack(p1))
 
+        # 17. amplitude and phase losses, per component, and the hybrid area loss over a stack.
+        import types
+        a3 = rng.standard_normal((3, 20, 20)) + 1j * rng.standard_normal((3, 20, 20))
+        b3 = rng.standard_normal((3, 20, 20)) + 1j * rng.standard_normal((3, 20, 20))
+        la = types.SimpleNamespace(Ex=a3[0], Ey=a3[1], Ez=a3[2])
+        lb = types.SimpleNamespace(Ex=b3[0], Ey=b3[1], Ez=b3[2])
+        I6 = np.abs(rng.standard_normal((6, 20, 20))) ** 3
+        _save("losses_more", a3=a3, b3=b3, mse_amplitude=lf.MSE_Amplitude(a3[0], b3[0]),
+              mse_phase=lf.MSE_Phase(a3[0], b3[0]), vmse_amplitude=lf.vMSE_Amplitude(la, lb),
+              vmse_phase=lf.vMSE_Phase(la, lb), I6=I6, loss_hybrid=lf.vectorized_loss_hybrid(I6))
+
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

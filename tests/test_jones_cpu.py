@@ -1,8 +1,11 @@
-"""The Jones matrix constructors (optical_elements.py:109-180), the scalar
-SLM phase (:76-85) and the single-input splitter ports (:393-409) against
-the golden fixture made from the reference's own source.  These build 2x2
-matrices and small arrays on the host, so they run without a GPU.
-Bars: complex64 matrices 1e-6, float64 arrays 1e-12."""
+"""The host-side pieces of the API against golden fixtures made from the
+reference's own source: the Jones matrix constructors
+(optical_elements.py:109-180), the scalar SLM phase (:76-85), the
+single-input splitter ports (:393-409), and the amplitude, phase and area
+losses (loss_functions.py:42-135).  They build 2x2 matrices and reduce small
+arrays on the host, so they run without a GPU.
+Bars: complex64 matrices 1e-6, float64 values 1e-12 (the area loss 1e-9
+relative)."""
 import numpy as np
 
 from oracle import xlumina_ref as ref
@@ -45,3 +48,24 @@ def test_scalar_slm_phase_and_splitter_ports():
     for fn, key in ((oe.bs_port0, "port0"), (oe.bs_port1, "port1")):
         out = np.stack(fn(g["aEx"], g["aEy"], z, z, z, z, T, R))
         assert np.abs(out - g[key]).max() < 1e-12, key
+
+
+def test_amplitude_phase_and_area_losses_match_the_reference():
+    """MSE_Amplitude, MSE_Phase (loss_functions.py:109-135), their per-component
+    forms vMSE_Amplitude, vMSE_Phase (:61-91) and vectorized_loss_hybrid
+    (:42-50) on host tensors against the reference's outputs (float64)."""
+    import types
+
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    g = golden("losses_more")
+    a3, b3 = torch.as_tensor(g["a3"]), torch.as_tensor(g["b3"])
+    assert abs(float(lf.MSE_Amplitude(a3[0], b3[0])) - float(g["mse_amplitude"])) < 1e-12
+    assert abs(float(lf.MSE_Phase(a3[0], b3[0])) - float(g["mse_phase"])) < 1e-12
+    la = types.SimpleNamespace(Ex=a3[0], Ey=a3[1], Ez=a3[2])
+    lb = types.SimpleNamespace(Ex=b3[0], Ey=b3[1], Ez=b3[2])
+    assert np.abs(lf.vMSE_Amplitude(la, lb).numpy() - g["vmse_amplitude"]).max() < 1e-12
+    assert np.abs(lf.vMSE_Phase(la, lb).numpy() - g["vmse_phase"]).max() < 1e-12
+    got = lf.vectorized_loss_hybrid(torch.as_tensor(g["I6"])).numpy()
+    assert np.abs(got - g["loss_hybrid"]).max() < 1e-9 * np.abs(g["loss_hybrid"]).max()
