@@ -279,6 +279,19 @@ def run_gpu(args):
         for s in range(3):
             call.stage(s)
     torch.cuda.synchronize()
+    # the column pass's kernel variant, chosen by measurement on this launch
+    from xlumina_gb300 import _lib
+    from xlumina_gb300.autotune import VariantTuner, cuda_event_timer
+    col_logp = engine.rs_logq(N, N) + 1
+    if args.col_variant is None:
+        tuned = VariantTuner(repeats=5).best_variant(_lib.XL_PASS_RS_COLS, col_logp,
+                                                      cuda_event_timer(lambda: call.stage(1)), force=True)
+    else:   # a fixed variant (profiling one kernel)
+        _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, col_logp, args.col_variant))
+        tuned = {"variant": args.col_variant, "ms": {}}
+    for s in range(3):
+        call.stage(s)
+    torch.cuda.synchronize()
 
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     with ClockSampler(local) as clk:
@@ -298,6 +311,18 @@ def run_gpu(args):
         replica_barrier()
         clk.mark_end()
     total_s, fields = reduce_replicas(t_start.elapsed_time(t_end) / 1e3, B * args.steps)
+    step_ms = np.asarray([ev[k][0].elapsed_time(ev[k][3]) for k in range(args.steps)])
+    # the timed output against the FP64 oracle: fields 0 (z = 1 cm) and 3 (z = 20 cm)
+    # of the last timed step (rank 0)
+    parity = None
+    if rank == 0 and not args.no_parity:
+        from oracle import xlumina_ref as ref
+        parity = {"what": "fields of the last timed step against the FP64 oracle (complex64 Ex, Ey, Ez)"}
+        for b in (0, 3):
+            exp = cpu_vrs_field(ref, x, Ex, Ey, eta[b], theta[b], alpha, zs[b])
+            errs = [_rel_l2(call.outs[c][b].cpu().numpy(), exp[c]) for c in range(3)]
+            parity[f"field{b}_z{zs[b] / 1e4:g}cm"] = dict(zip(("Ex", "Ey", "Ez"), errs))
+        parity["max"] = max(max(v.values()) for k, v in parity.items() if k.startswith("field"))
     total_ms = total_s * 1e3
     stage_ms = [sum(ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps)) / args.steps
                 for s in range(3)]
@@ -403,7 +428,17 @@ def run_gpu(args):
                                        "profiles/rs_kernels_vrs2048.md (the bench's own 8-field launch)",
                      "peak_source": peak_src,
                      "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
+        "rel_l2": parity,
+        "latency": {"step_ms_p50": float(np.percentile(step_ms, 50)),
+                    "step_ms_p99": float(np.percentile(step_ms, 99)),
+                    "ms_per_field_p50": float(np.percentile(step_ms / B, 50)),
+                    "ms_per_field_p99": float(np.percentile(step_ms / B, 99)),
+                    "how": "CUDA events around each timed step of B fields; a field's latency is its step's"},
         "stages_ms": dict(zip(names, stage_ms)),
+        "column_pass_variant": {"chosen": tuned["variant"], "transform_length": 1 << col_logp,
+                                "ms_per_launch": {str(k): v for k, v in tuned["ms"].items()},
+                                "variants": "0 one line per thread; 1 two lines per thread (packed FP32), "
+                                            "pairs interleaved in warps; 2 packed, pairs in barrier groups"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -434,7 +469,7 @@ def run_gpu(args):
     print(json.dumps(line))
 
 
-def run_czt(batch=8, steps=20, warmup=3):
+def run_czt(batch=8, steps=20, warmup=3, check=True):
     """The high-NA objective-lens focus (VCZT_objective_lens, optical_elements.py:600-638):
     2048^2 (Ex, Ey) behind a per-pixel LCD and sSLM -> lens -> 1024^2 focal ROI
     (Ex, Ey, Ez), forward, `batch` fields per launch; per-kernel times from
@@ -478,7 +513,16 @@ def run_czt(batch=8, steps=20, warmup=3):
     # write 3 n m complex64; columns read 3 n m and write 3 m^2
     rows_b = 8 * n * n + 3 * n * m * 8 + (16 + 8 + 24) * n * n / batch
     cols_b = 3 * n * m * 8 + 3 * m * m * 8
+    err = None
+    if check:   # field 0 of the last timed launch against the FP64 oracle
+        from oracle import xlumina_ref as ref
+        ax, ay = ref.lcd(src.astype(np.complex128), np.zeros((n, n)), eta.cpu().numpy().astype(np.float64),
+                         theta.cpu().numpy().astype(np.float64))
+        ax, ay = ref.sslm(ax, ay, alpha[0].cpu().numpy().astype(np.float64), phi[0].cpu().numpy().astype(np.float64))
+        exp = ref.vczt_objective_lens(ax, ay, x, y, 0.650, r, f, xo, yo)
+        err = max(_rel_l2(call.outs[c][0].cpu().numpy(), exp[c]) for c in range(3))
     return {"workload": "high-NA focus 2048^2 -> 1024^2 ROI (2 um), LCD + sSLM + lens fused, Ez derived, forward",
+            "rel_l2": err,
             "batch": batch, "fields_per_s": batch / ((rows + cols) / 1e3),
             "czt_rows_ms": rows, "czt_cols_ms": cols,
             "czt_rows_gbs": batch * rows_b / (rows / 1e3) / 1e9, "czt_cols_gbs": batch * cols_b / (cols / 1e3) / 1e9}
@@ -499,10 +543,51 @@ def _time_steps(fn, steps, warmup):
     return s.elapsed_time(e) / 1e3 / steps
 
 
+def _rel_l2(a, b):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def oracle_four_f_intensity(t, b):
+    """Table b of a FourFTable through the FP64 oracle: its normalised output intensity."""
+    from oracle import xlumina_ref as ref
+    inp, _, p1, p2 = t.entry(b)
+    u = ref.slm(inp, p1)[0]
+    u = ref.rs_propagate(u, t.x, t.y, t.wavelength, t.f)
+    u = u * ref.lens_mask(t.x, t.y, t.wavelength, t.lens_r, (t.f, t.f))
+    u = ref.czt(u, t.x, t.y, t.wavelength, t.f, t.xo, t.yo)
+    u = ref.slm(u, p2)[0]
+    I = np.abs(ref.czt(u, t.xo, t.yo, t.wavelength, t.f, t.xo, t.yo)) ** 2
+    return I / np.sum(I)
+
+
+def oracle_high_na_intensity(t, b):
+    """Table b of a HighNATable through the FP64 oracle: its focal |Ez|^2."""
+    from oracle import xlumina_ref as ref
+    eta, theta, alpha, phi = t.entry(b)
+    Ex = t.Ex.cpu().numpy().astype(np.complex128)
+    ax, ay = ref.lcd(Ex, np.zeros_like(Ex), eta, theta)
+    ax, ay = ref.sslm(ax, ay, alpha, phi)
+    return np.abs(ref.vczt_objective_lens(ax, ay, t.x, t.y, t.wavelength, t.r, t.f, t.xo, t.yo)[2]) ** 2
+
+
+def _peak_step_bytes(step):
+    """Device memory in use at the peak of one step, above what was allocated before it."""
+    import torch
+    torch.cuda.synchronize()
+    base = torch.cuda.memory_allocated()
+    torch.cuda.reset_peak_memory_stats()
+    step()
+    torch.cuda.synchronize()
+    return int(torch.cuda.max_memory_allocated() - base)
+
+
 def run_fwd_bwd(steps=10, warmup=3):
     """fwd+bwd optimisation steps through the hand-written adjoints: the batched
     form (one step over the whole batch, eager and replayed from a captured
-    CUDA graph) and the plain form (one table or field per call)."""
+    CUDA graph) and the plain form (one table or field per call).  Each row
+    states the rel-L2 of one timed table's output against the FP64 oracle."""
     import torch
 
     from xlumina_gb300.plans import CapturedStep
@@ -532,26 +617,49 @@ def run_fwd_bwd(steps=10, warmup=3):
 
     t4 = FourFTable()
     dt = _time_steps(t4.step, steps, warmup)
-    single = lambda i=[0]: t4.step(t4.inputs[i[0] % t4.B:i[0] % t4.B + 1], t4.target[i[0] % t4.B:i[0] % t4.B + 1])  # noqa: E731
+    single = lambda i=[0]: t4.step(tables=slice(i[0] % t4.B, i[0] % t4.B + 1))  # noqa: E731
     dt1 = _time_steps(single, t4.B, 2)
     B = t4.B
+    with torch.no_grad():
+        err4 = _rel_l2(t4.intensities()[0].cpu().numpy(), oracle_four_f_intensity(t4, 0))
     del t4
     torch.cuda.empty_cache()
     cap = captured_rate(lambda: FourFTable(capturable=True), steps)
-    out["four_f"] = {"workload": "4f table 16 x 1024^2 (SLM1 -> RS 25 cm -> lens -> CZT 512^2 ROI -> SLM2 -> CZT), "
-                                 "532 nm, normalised intensity MSE, AdamW",
+    out["four_f"] = {"workload": "4f step, 16 independent tables (own seed: input mask, 10 % binary target, "
+                                 "SLM1 1024^2 and SLM2 512^2 phases U[-pi, pi)), 1024^2 -> RS 25 cm -> lens -> "
+                                 "CZT 512^2 ROI -> SLM2 -> CZT, 532 nm, normalised intensity MSE, AdamW",
                      "steps_per_s": 1.0 / dt, "tables_per_s": B / dt, "captured_steps_per_s": cap,
-                     "captured_tables_per_s": B * cap, "plain_tables_per_s": 1.0 / dt1, "batch": B}
-    th = HighNATable()
-    dt = _time_steps(th.step, max(2, steps // 2), 2)
-    B = th.B
-    del th
-    torch.cuda.empty_cache()
-    cap = captured_rate(lambda: HighNATable(capturable=True), max(2, steps // 2))
-    out["high_na"] = {"workload": "high-NA table 32 x 2048^2 -> 1024^2 focal ROI (2 um), 650 nm, NA 0.9, f 3 mm, "
-                                  "LCD + sSLM, Ez spot loss, AdamW", "steps_per_s": 1.0 / dt,
-                      "tables_per_s": B / dt, "captured_steps_per_s": cap, "captured_tables_per_s": B * cap,
-                      "batch": B}
+                     "captured_tables_per_s": B * cap, "plain_tables_per_s": 1.0 / dt1, "batch": B,
+                     "rel_l2": {"what": "table 0's normalised output intensity after the timed steps, "
+                                        "against the FP64 oracle", "value": err4}}
+
+    # high-NA: the configured form keeps no focal field for the backward
+    # (activation checkpointing: the focus is recomputed); the row also times
+    # the form that keeps them, with each form's peak memory
+    hrow = {}
+    for ck in (True, False):
+        th = HighNATable(checkpoint=ck)
+        dt = _time_steps(th.step, max(2, steps // 2), 2)
+        peak = _peak_step_bytes(th.step)
+        if ck:
+            with torch.no_grad():
+                errh = _rel_l2(th._spot_intensity()[0].cpu().numpy(), oracle_high_na_intensity(th, 0))
+        B = th.B
+        del th
+        torch.cuda.empty_cache()
+        hrow[ck] = (dt, peak)
+    cap = captured_rate(lambda: HighNATable(capturable=True, checkpoint=True), max(2, steps // 2))
+    out["high_na"] = {"workload": "high-NA step, 32 tables with their own per-pixel LCD (eta, theta) and sSLM "
+                                  "(alpha, phi) planes U[0, 2 pi), 2048^2 -> VCZT objective lens (NA 0.9, f 3 mm) "
+                                  "-> 1024^2 focal ROI (2 um), 650 nm, Ez spot loss, AdamW, activation "
+                                  "checkpointing of the focal fields",
+                      "steps_per_s": 1.0 / hrow[True][0], "tables_per_s": B / hrow[True][0],
+                      "captured_steps_per_s": cap, "captured_tables_per_s": B * cap, "batch": B,
+                      "peak_step_bytes": hrow[True][1],
+                      "without_checkpointing": {"steps_per_s": 1.0 / hrow[False][0],
+                                                "peak_step_bytes": hrow[False][1]},
+                      "rel_l2": {"what": "table 0's focal |Ez|^2 after the timed steps, against the FP64 oracle",
+                                 "value": errh}}
     torch.cuda.empty_cache()
     return out
 
@@ -585,7 +693,10 @@ def run_rs_plain_config(batch=16, steps=20, warmup=3, seed=0):
         oe.SLM(light, ph[k], n)[0].RS_propagation(z)
     dtp = _time_steps(plain, 2 * batch, 3)
     alg = (112 + 4) * n * n          # bytes per field (4N^2: the phase mask)
-    return {"workload": "scalar RS 1024^2, 2 mm window, 650 nm, Gaussian w0 200 um, per-field SLM phase, z = 5 cm",
+    exp = ref.rs_propagate(ref.slm(ref.gaussian_beam(x, y, wl, (200.0, 200.0)), ph[0].cpu().numpy())[0],
+                           x, y, wl, z)
+    err = _rel_l2(call.outs[0][0].cpu().numpy(), exp)
+    return {"rel_l2": err, "workload": "scalar RS 1024^2, 2 mm window, 650 nm, Gaussian w0 200 um, per-field SLM phase, z = 5 cm",
             "batch": batch, "fields_per_s": batch / dt, "plain_fields_per_s": 1.0 / dtp,
             "pipeline_gbs": batch * alg / dt / 1e9, "alg_bytes_per_field": alg}
 
@@ -777,12 +888,16 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--col-variant", type=int, default=None,
+                    help="use this column-pass kernel variant instead of measuring them all")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the timed outputs")
     ap.add_argument("--only", choices=["czt", "hybrid", "rs1024"], default=None,
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
     if args.only == "czt":
-        print(json.dumps({"czt_high_na": run_czt(batch=args.batch, steps=args.steps, warmup=args.warmup)}))
+        print(json.dumps({"czt_high_na": run_czt(batch=args.batch, steps=args.steps, warmup=args.warmup,
+                                                  check=False)}))
         return
     if args.only == "hybrid":
         print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))

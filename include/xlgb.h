@@ -88,6 +88,29 @@ int xl_device_timeouts(unsigned int* count, int reset);
  * before the first launch (every entry point calls it lazily as well). */
 int xl_init(void);
 
+/* ---- kernel variants ----------------------------------------------------
+ * Some passes have several kernels for one transform length (thread shape,
+ * columns per thread, barrier grouping).  All variants of a pass give the
+ * same results to float32 rounding; which one is fastest is measured per
+ * GPU by the package's autotuner, which selects it here.  The choice is
+ * process-wide and read at every launch.  No counterpart in the reference:
+ * its transforms are XLA's (wave_optics.py:281-289, 385-460). */
+enum {
+  XL_PASS_RS_COLS = 0,   /* RS / VRS column pass (forward FFT, spectrum, inverse FFT) */
+  XL_PASS_CZT_ROWS = 1,  /* chirp-z x transform over rows */
+  XL_PASS_CZT_COLS = 2,  /* chirp-z y transform over column tiles */
+  XL_PASS_RS_ROWS = 3,   /* RS / VRS forward and inverse row passes */
+  XL_NUM_PASSES = 4
+};
+/* Variants available for `pass` at transform length 2^log2_len (>= 1; 0 if
+ * the pass or length is unknown).  Variant 0 is the one-line-per-thread
+ * kernel; higher numbers are the packed two-line kernels. */
+int xl_kernel_variant_count(int pass, int log2_len);
+/* Select variant `variant` (< the count) for later launches. */
+int xl_set_kernel_variant(int pass, int log2_len, int variant);
+/* The variant launches use now (negative XL_E* code for a bad argument). */
+int xl_get_kernel_variant(int pass, int log2_len);
+
 /* ---- Rayleigh-Sommerfeld (RS / VRS) ----------------------------------- */
 
 /* The spectrum of dH/dz, the z-derivative of the same impulse response
@@ -174,10 +197,14 @@ int xl_rs_stage(void* stream, const XlRsArgs* args, int stage);
  * ignored: the workspace is a fixed device array of
  * XL_RS_NOALLOC_MAX_WORK_BYTES inside the library, held on every GPU that
  * loads it until exit.  Calls needing more scratch than that
- * (xl_rs_work_bytes) fail with XL_EINVAL.  The first call on a device looks
- * up the array's address (and uploads the twiddle tables if no other entry
- * point has); make that first call before any stream capture.  All calls
- * share the array: calls whose work overlaps on the GPU race. */
+ * (xl_rs_work_bytes) fail with XL_EINVAL.  The array is created on a device
+ * by the device's set-up: xl_init(), or the first call of any entry point
+ * there.  A host that hands device memory to its own pool calls xl_init() on
+ * each device before reserving it; that set-up (or the first call) must also
+ * come before any stream capture.  The stream must belong to the current
+ * device (XL_EINVAL otherwise).  All calls share the array and it keeps the
+ * last call's contents: calls whose work overlaps on the GPU (other streams,
+ * other host threads) race. */
 #define XL_RS_NOALLOC_MAX_WORK_BYTES (64ull << 20)
 int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* args);
 

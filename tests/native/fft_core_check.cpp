@@ -4,6 +4,7 @@
 #include <cmath>
 #include <vector>
 #include "../../xlumina_gb300/csrc/fft_core.cuh"
+#include "../../xlumina_gb300/csrc/fft_pair.cuh"
 
 using namespace xl;
 
@@ -126,4 +127,65 @@ extern "C" int fft_core_check_zu(int logn, int dir, const float* in, float* out)
 
 extern "C" int fft_core_check(int logn, int dir, const float* in, float* out) {
   return dir < 0 ? dispatch<-1>(logn, in, out) : dispatch<1>(logn, in, out);
+}
+
+// ---- the two-line (packed) engine of fft_pair.cuh: two lines a, b at once ----
+struct PRegs { cpair v[16]; };
+
+template <int LOGN, int DIR, bool ZU, int P>
+static void emu_p(std::vector<PRegs>& V, f4* sm, const f4* stw) {
+  using S = FftShape<LOGN, 16>;
+  for (int j = 0; j < S::T; ++j) pfft_pass<LOGN, P, DIR, ZU && P == 0, false>(V[j].v, j, sm, stw, 0);
+  if constexpr (P < S::NPASS - 1) {
+    for (int j = 0; j < S::T; ++j) pfft_gather<LOGN>(V[j].v, j, sm);
+    emu_p<LOGN, DIR, false, P + 1>(V, sm, stw);
+  }
+}
+
+template <int LOGN, int DIR>
+static void run_p(const float* a, const float* b, float* oa, float* ob, int zu) {
+  using S = FftShape<LOGN, 16>;
+  std::vector<float2> tw(S::N);
+  for (int q = 0; q < S::N; ++q) {
+    double ang = 2.0 * M_PI * q / S::N;
+    tw[q] = make_float2((float)std::cos(ang), (float)-std::sin(ang));
+  }
+  std::vector<f4> stw(FftTw<LOGN, 16>::SIZE), sm(S::SMEM);
+  for (int i = 0; i < FftTw<LOGN, 16>::SIZE; ++i) stw[i] = pair_tw(pass_twiddle_entry<LOGN, 16>(i, tw.data()));
+  std::vector<PRegs> V(S::T);
+  for (int j = 0; j < S::T; ++j)
+    for (int m = 0; m < 16; ++m) {
+      const int n = j + m * S::T;
+      V[j].v[m] = p_from2(make_float2(a[2 * n], a[2 * n + 1]), make_float2(b[2 * n], b[2 * n + 1]));
+    }
+  if (zu) emu_p<LOGN, DIR, true, 0>(V, sm.data(), stw.data());
+  else emu_p<LOGN, DIR, false, 0>(V, sm.data(), stw.data());
+  for (int j = 0; j < S::T; ++j)
+    for (int m = 0; m < 16; ++m) {
+      const int n = j + m * S::T;
+      const float2 x = p_lo(V[j].v[m]), y = p_hi(V[j].v[m]);
+      oa[2 * n] = x.x; oa[2 * n + 1] = x.y;
+      ob[2 * n] = y.x; ob[2 * n + 1] = y.y;
+    }
+}
+
+template <int DIR>
+static int dispatch_p(int logn, const float* a, const float* b, float* oa, float* ob, int zu) {
+  switch (logn) {
+    case 5: run_p<5, DIR>(a, b, oa, ob, zu); return 0;
+    case 6: run_p<6, DIR>(a, b, oa, ob, zu); return 0;
+    case 7: run_p<7, DIR>(a, b, oa, ob, zu); return 0;
+    case 8: run_p<8, DIR>(a, b, oa, ob, zu); return 0;
+    case 9: run_p<9, DIR>(a, b, oa, ob, zu); return 0;
+    case 10: run_p<10, DIR>(a, b, oa, ob, zu); return 0;
+    case 11: run_p<11, DIR>(a, b, oa, ob, zu); return 0;
+    case 12: run_p<12, DIR>(a, b, oa, ob, zu); return 0;
+    case 13: run_p<13, DIR>(a, b, oa, ob, zu); return 0;
+  }
+  return -1;
+}
+
+// Two lines through the packed engine; zu: their upper halves are zero and not read.
+extern "C" int fft_pair_check(int logn, int dir, int zu, const float* a, const float* b, float* oa, float* ob) {
+  return dir < 0 ? dispatch_p<-1>(logn, a, b, oa, ob, zu) : dispatch_p<1>(logn, a, b, oa, ob, zu);
 }

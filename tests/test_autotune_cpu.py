@@ -39,3 +39,29 @@ def test_large_fields_pack_one(tmp_path):
     # the GPU is full with one request: time grows linearly with the batch
     t = BatchTuner(path=str(tmp_path / "t.json"), device_name="dev", candidates=(1, 2, 4), repeats=1)
     assert t.best_batch(("vrs", 2048, 2048), lambda b: 5e-4 * b) == 1
+
+
+def test_variant_tuner_picks_fastest_and_caches(tmp_path):
+    from xlumina_gb300.autotune import VariantTuner
+    selected = {}
+    times = {0: 2.0e-3, 1: 1.2e-3, 2: 1.5e-3}
+    t = VariantTuner(path=str(tmp_path / "v.json"), device_name="GB300", repeats=2,
+                     count=lambda p, l: 3, select=lambda p, l, v: selected.__setitem__((p, l), v))
+    calls = []
+
+    def measure():
+        v = selected[(0, 12)]
+        calls.append(v)
+        return times[v]
+
+    r = t.best_variant(0, 12, measure)
+    assert r["variant"] == 1 and selected[(0, 12)] == 1 and not r["cached"]
+    assert set(calls) == {0, 1, 2}
+    n = len(calls)
+    t2 = VariantTuner(path=str(tmp_path / "v.json"), device_name="GB300",
+                      count=lambda p, l: 3, select=lambda p, l, v: selected.__setitem__((p, l), v))
+    selected[(0, 12)] = 0
+    r2 = t2.best_variant(0, 12, measure)
+    assert r2 == {"variant": 1, "ms": {}, "cached": True} and selected[(0, 12)] == 1 and len(calls) == n
+    # forced: measured again
+    assert t2.best_variant(0, 12, measure, force=True)["variant"] == 1 and len(calls) > n

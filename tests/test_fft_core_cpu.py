@@ -18,6 +18,7 @@ def fftlib(tmp_path_factory):
     lib.fft_core_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.fft_core_check_stw.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.fft_core_check_zu.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.fft_pair_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4
     return lib
 
 
@@ -54,3 +55,28 @@ def test_zero_padded_fft_matches_numpy(fftlib, logn, direction):
     ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
     err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
     assert err < 2e-7 * logn, err
+
+
+@pytest.mark.parametrize("logn", range(5, 14))
+@pytest.mark.parametrize("direction", [-1, 1])
+@pytest.mark.parametrize("pruned", [False, True])
+def test_pair_fft_matches_numpy(fftlib, logn, direction, pruned):
+    """The packed two-line engine (fft_pair.cuh): two independent lines per
+    thread, each against numpy, with and without the pruned first pass."""
+    n = 1 << logn
+    rng = np.random.default_rng(300 + logn + 20 * pruned)
+    a = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    b = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    ga, gb = a.copy(), b.copy()
+    if pruned:
+        a[n // 2:] = 0
+        b[n // 2:] = 0
+        ga[n // 2:] = 1e30   # never read
+        gb[n // 2:] = -1e30
+    oa, ob = np.empty_like(a), np.empty_like(b)
+    assert fftlib.fft_pair_check(logn, direction, int(pruned), ga.ctypes.data, gb.ctypes.data,
+                                 oa.ctypes.data, ob.ctypes.data) == 0
+    for x, out in ((a, oa), (b, ob)):
+        ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
+        err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+        assert err < 2e-7 * logn, err

@@ -1,0 +1,103 @@
+"""Every kernel variant of a pass gives the oracle's result: the packed
+two-line column pass (interleaved and in barrier groups) against the
+one-line kernel and the FP64 oracle, for the transform lengths that have it
+(1024, 2048 and 4096 points: fields of 257..2048 per side).
+
+Tolerance: relative L2 <= 1e-5 against the oracle (the path's bar); the
+variants agree with each other to float32 rounding (<= 1e-6).
+"""
+import numpy as np
+import pytest
+
+from oracle import xlumina_ref as ref
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _np(t):
+    return t.detach().cpu().numpy().astype(np.complex128)
+
+
+@pytest.fixture
+def variants():
+    """(set, count) for the RS column pass; restores the selection afterwards."""
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    saved = {l: lib.xl_get_kernel_variant(_lib.XL_PASS_RS_COLS, l) for l in range(10, 13)}
+
+    def select(log2_len, v):
+        _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, log2_len, v), "xl_set_kernel_variant")
+
+    yield select, lambda l: lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, l)
+    for l, v in saved.items():
+        select(l, v)
+
+
+def test_variant_table_bounds():
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 3
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
+    assert lib.xl_kernel_variant_count(99, 12) == 0
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 3) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
+    assert lib.xl_get_kernel_variant(-1, 12) == _lib.XL_EINVAL
+
+
+@pytest.mark.parametrize("n,vector", [(300, True), (1000, False), (1024, True), (2048, False)])
+def test_rs_column_variants_match_oracle(variants, n, vector):
+    import torch
+
+    from xlumina_gb300 import engine
+    select, count = variants
+    logp = engine.rs_logq(n, n) + 1
+    assert count(logp) == 3
+    x, y = ref.space(1000.0, n)
+    rng = np.random.default_rng(n + vector)
+    Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
+    Ey = 0.5 * ref.gaussian_beam(x, y, 0.633, (250.0, 250.0)) * np.exp(1j * rng.uniform(-1, 1, (n, n)))
+    z = 3.0e4
+    comps = [torch.as_tensor(Ex.astype(np.complex64), device="cuda")]
+    if vector:
+        comps.append(torch.as_tensor(Ey.astype(np.complex64), device="cuda"))
+        exp = ref.vrs_propagate(Ex.astype(np.complex64), Ey.astype(np.complex64), x, y, 0.633, z)
+    else:
+        exp = [ref.rs_propagate(Ex.astype(np.complex64), x, y, 0.633, z)]
+    outs = []
+    for v in range(3):
+        select(logp, v)
+        got = engine.rs_propagate(comps, x, y, 0.633, z, vector=vector)
+        torch.cuda.synchronize()
+        outs.append([_np(g) for g in got])
+        for g, e in zip(outs[-1], exp):
+            assert rel_l2(g, e) < TOL, (v, rel_l2(g, e))
+    for v in (1, 2):
+        for g, g0 in zip(outs[v], outs[0]):
+            assert rel_l2(g, g0) < 1e-6, v
+
+
+@pytest.mark.parametrize("v", [1, 2])
+def test_rs_column_variants_adjoint_and_batch(variants, v):
+    """The adjoint (conjugate spectrum) and a batch with a distance per entry
+    through a packed variant equal the one-line kernel's results."""
+    import torch
+
+    from xlumina_gb300 import engine
+    select, _ = variants
+    n = 700
+    x, y = ref.space(600.0, n)
+    rng = np.random.default_rng(77)
+    E = torch.as_tensor((rng.standard_normal((3, 2, n, n)) + 1j * rng.standard_normal((3, 2, n, n)))
+                        .astype(np.complex64), device="cuda")
+    zs = [1e4, 2e4, 5e4]
+    logp = engine.rs_logq(n, n) + 1
+    res = {}
+    for var in (0, v):
+        select(logp, var)
+        fwd = engine.rs_propagate([E[:, 0], E[:, 1]], x, y, 0.6, zs, vector=True)
+        adj = engine.RsCall([E[:, 0], E[:, 1], E[:, 0]], x, y, 0.6, zs, vector=True, adjoint=True).run()
+        res[var] = [_np(t) for t in fwd] + [_np(t) for t in adj]
+    for a, b in zip(res[v], res[0]):
+        assert rel_l2(a, b) < 1e-6

@@ -20,6 +20,8 @@ XL_MAX_OPS = 8
 XL_MAX_SIDE = 4096
 XL_RS_NOALLOC_MAX_WORK_BYTES = 64 << 20
 
+XL_PASS_RS_COLS, XL_PASS_CZT_ROWS, XL_PASS_CZT_COLS, XL_PASS_RS_ROWS = range(4)
+
 OP_NONE, OP_PHASE, OP_SSLM, OP_SSLM_AMP, OP_LCD, OP_LP, OP_SEPMASK, OP_CMUL, OP_HIGHNA = range(9)
 
 
@@ -115,6 +117,9 @@ SIGNATURES = {
     "xl_version": (ctypes.c_int, []),
     "xl_struct_size": (ctypes.c_size_t, [ctypes.c_char_p]),
     "xl_init": (ctypes.c_int, []),
+    "xl_kernel_variant_count": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "xl_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "xl_get_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "xl_device_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_spectrum_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),

@@ -108,3 +108,81 @@ class BatchTuner:
             except OSError:
                 pass   # a read-only cache location still tunes, for this process
         return b
+
+
+class VariantTuner:
+    """Kernel variant of a pass chosen by measurement, per GPU model.
+
+    The library has several kernels for some passes at one transform length
+    (the one-line column pass and the packed two-line ones, interleaved in
+    the warps or in barrier groups); they agree to float32 rounding and differ
+    in speed by GPU and workload shape.  ``best_variant(pass_id, log2_len,
+    measure)`` times every variant with ``measure()`` (seconds of one launch,
+    device work included) and selects the fastest in the library
+    (``xl_set_kernel_variant``); the choice is cached with the batch packings,
+    keyed by device model, pass and length, so later processes select it
+    without measuring.  ``count`` / ``select`` default to the library's entry
+    points and can be replaced (tests without a GPU)."""
+
+    def __init__(self, path: str | None = None, device_name: str | None = None, repeats: int = 5,
+                 count=None, select=None):
+        self._tuner = BatchTuner(path=path, device_name=device_name)
+        self.repeats = int(repeats)
+        self._count = count
+        self._select = select
+
+    def _lib_count(self, pass_id, log2_len):
+        from . import engine
+        return int(engine.lib().xl_kernel_variant_count(int(pass_id), int(log2_len)))
+
+    def _lib_select(self, pass_id, log2_len, v):
+        from . import _lib, engine
+        _lib.check(engine.lib().xl_set_kernel_variant(int(pass_id), int(log2_len), int(v)), "xl_set_kernel_variant")
+
+    def count(self, pass_id, log2_len) -> int:
+        return (self._count or self._lib_count)(pass_id, log2_len)
+
+    def select(self, pass_id, log2_len, v) -> None:
+        (self._select or self._lib_select)(pass_id, log2_len, v)
+
+    def best_variant(self, pass_id: int, log2_len: int, measure, force: bool = False) -> dict:
+        """{"variant": v, "ms": {v: median ms}} (``ms`` empty on a cache hit);
+        ``force`` measures even when the choice is cached."""
+        cls = ("variant", int(pass_id), int(log2_len))
+        n = self.count(pass_id, log2_len)
+        with self._tuner._lock:
+            hit = self._tuner.cached(cls)
+        if hit is not None and not force and int(hit["variant"]) < n:
+            self.select(pass_id, log2_len, int(hit["variant"]))
+            return {"variant": int(hit["variant"]), "ms": {}, "cached": True}
+        ms = {}
+        for v in range(n):
+            self.select(pass_id, log2_len, v)
+            measure()                                   # warm-up (smem carve-out, caches)
+            ms[v] = 1e3 * statistics.median(measure() for _ in range(self.repeats))
+        best = min(ms, key=ms.get)
+        self.select(pass_id, log2_len, best)
+        with self._tuner._lock:
+            self._tuner._cache.setdefault(self._tuner.device_name, {})[self._tuner.class_key(cls)] = {
+                "variant": best, "ms": {str(k): v for k, v in ms.items()}, "when": time.time()}
+            try:
+                self._tuner.save()
+            except OSError:
+                pass
+        return {"variant": best, "ms": ms, "cached": False}
+
+
+def cuda_event_timer(fn):
+    """measure() for VariantTuner: seconds of one call of ``fn`` on the
+    current stream, from CUDA events around it."""
+    import torch
+
+    def measure():
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        e.synchronize()
+        return s.elapsed_time(e) / 1e3
+    return measure

@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -75,7 +76,50 @@ int ensure_init() {
   return XL_OK;
 }
 
+// ---- kernel variants per (pass, transform length) ----
+// Available variants: the one-line kernel (0) everywhere; the packed two-line
+// column pass, interleaved (1) or in barrier groups (2), for 1024..4096-point
+// RS transforms.
+static int variant_count(int pass, int log2_len) {
+  if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
+  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 12) return 3;
+  return 1;
+}
+static std::atomic<int> g_variant[XL_NUM_PASSES][14];
+
+static bool variants_defaults() {
+  for (int l = 10; l <= 12; ++l) g_variant[XL_PASS_RS_COLS][l] = 1;
+  return true;
+}
+static const bool g_variants_ready = variants_defaults();
+
+int kernel_variant(int pass, int log2_len) {
+  if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 0 || log2_len > 13) return 0;
+  return g_variant[pass][log2_len].load(std::memory_order_relaxed);
+}
+
 }  // namespace xl
+
+extern "C" int xl_kernel_variant_count(int pass, int log2_len) { return xl::variant_count(pass, log2_len); }
+
+extern "C" int xl_set_kernel_variant(int pass, int log2_len, int variant) {
+  const int n = xl::variant_count(pass, log2_len);
+  if (n == 0 || variant < 0 || variant >= n) {
+    xl::set_error("xl_set_kernel_variant: pass %d at length 2^%d has %d variant(s), got %d", pass, log2_len, n,
+                  variant);
+    return XL_EINVAL;
+  }
+  xl::g_variant[pass][log2_len].store(variant, std::memory_order_relaxed);
+  return XL_OK;
+}
+
+extern "C" int xl_get_kernel_variant(int pass, int log2_len) {
+  if (xl::variant_count(pass, log2_len) == 0) {
+    xl::set_error("xl_get_kernel_variant: unknown pass %d or length 2^%d", pass, log2_len);
+    return XL_EINVAL;
+  }
+  return xl::kernel_variant(pass, log2_len);
+}
 
 extern "C" const char* xl_last_error(void) { return xl::g_err; }
 

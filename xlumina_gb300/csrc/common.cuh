@@ -7,7 +7,7 @@
 #include <stdint.h>
 
 #include "fft_core.cuh"
-#include "xl_types.h"
+#include "xlgb.h"
 
 namespace xl {
 

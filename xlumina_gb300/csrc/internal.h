@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
-#include "xl_types.h"
+#include "xlgb.h"
 
 namespace xl {
 
@@ -12,6 +12,10 @@ namespace xl {
 void set_error(const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* where);
 int ensure_init();  // uploads twiddle tables to the current device once
+
+// The kernel variant selected for a pass at transform length 2^log2_len
+// (xl_set_kernel_variant; defined in capi.cu).
+int kernel_variant(int pass, int log2_len);
 
 inline int ilog2_ceil(long long v) {
   int l = 0;

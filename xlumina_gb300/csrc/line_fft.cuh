@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fft_pair.cuh"
 #include "internal.h"
 
 namespace xl {
@@ -39,11 +40,14 @@ __host__ __device__ constexpr int ptw_off(int logp) {
 constexpr int PTW_TOTAL = ptw_off(14);
 
 static __device__ float2 g_ptw[PTW_TOTAL];
+// the same tables in the two-line engine's form, (wr, wr, wi, wi) per entry
+static __device__ float4 g_ptw4[PTW_TOTAL];
 
 template <int LOGP> __device__ __forceinline__ const float2* pass_tw() {
   static_assert(ptw_size(LOGP) == FftTw<LOGP, 16>::SIZE, "pass table size");
   return g_ptw + ptw_off(LOGP);
 }
+template <int LOGP> __device__ __forceinline__ const float4* pass_tw4() { return g_ptw4 + ptw_off(LOGP); }
 
 // Address of (row r, column col) in a column-tiled plane with `rows` rows:
 // element (r, col) at ((col / W) rows + r) W + col % W.
@@ -170,7 +174,10 @@ static cudaError_t line_tu_tables(const float2* host) {
   if (e != cudaSuccess) return e;
   std::vector<float2> ptw(PTW_TOTAL, make_float2(1.f, 0.f));
   fill_pass_tables<5>(ptw, host);
-  return cudaMemcpyToSymbol(g_ptw, ptw.data(), sizeof(g_ptw));
+  if ((e = cudaMemcpyToSymbol(g_ptw, ptw.data(), sizeof(g_ptw))) != cudaSuccess) return e;
+  std::vector<float4> ptw4(PTW_TOTAL);
+  for (int i = 0; i < PTW_TOTAL; ++i) ptw4[i] = pair_tw(ptw[i]);
+  return cudaMemcpyToSymbol(g_ptw4, ptw4.data(), sizeof(g_ptw4));
 }
 
 static cudaError_t line_tu_timeouts(unsigned int* count, int reset) {

@@ -204,25 +204,29 @@ static float2* g_noalloc_ptr[256];
 
 // Device address of the scratch array for the current device.  The array's
 // name in host code is only a stand-in for the symbol, so the address is
-// looked up once per device, with that device current.
-static int noalloc_scratch(float2** out) {
+// looked up once per device, with that device current.  The lookup also
+// loads this file's device module, which is when the runtime allocates the
+// array.
+static cudaError_t noalloc_lookup(float2** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetDevice");
-  if (dev < 0 || dev >= 256) {
-    set_error("xl_rs_propagate_noalloc: device index %d out of range", dev);
-    return XL_EINVAL;
-  }
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_rs_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetSymbolAddress");
+    if ((e = cudaGetSymbolAddress(&p, g_rs_noalloc_scratch)) != cudaSuccess) return e;
     g_noalloc_ptr[dev] = (float2*)p;
   }
-  *out = g_noalloc_ptr[dev];
-  return XL_OK;
+  if (out) *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
 }
+
+// Run at every device's set-up (xl_init, or the first call of any entry
+// point), so that the array exists from then on: a host that hands the rest
+// of device memory to its own pool afterwards still has it.
+static cudaError_t noalloc_setup(const float2*) { return noalloc_lookup(nullptr); }
+static const bool g_noalloc_registered = register_device_tables(&noalloc_setup, nullptr);
 
 extern "C" int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* a) {
   if (!a) {
@@ -242,8 +246,19 @@ extern "C" int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* a) {
               need, (unsigned long long)XL_RS_NOALLOC_MAX_WORK_BYTES);
     return XL_EINVAL;
   }
+  if (int rc = ensure_init()) return rc;
+  int dev = 0, sdev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetDevice");
+  if ((e = cudaStreamGetDevice((cudaStream_t)stream, &sdev)) != cudaSuccess)
+    return cuda_fail(e, "xl_rs_propagate_noalloc: cudaStreamGetDevice");
+  if (sdev != dev) {
+    set_error("xl_rs_propagate_noalloc: the stream belongs to device %d, the current device is %d", sdev, dev);
+    return XL_EINVAL;
+  }
   float2* scratch = nullptr;
-  if (int rc = noalloc_scratch(&scratch)) return rc;
+  if ((e = noalloc_lookup(&scratch)) != cudaSuccess)
+    return cuda_fail(e, "xl_rs_propagate_noalloc: cudaGetSymbolAddress");
   XlRsArgs b = *a;
   b.work = scratch;
   return rs_run(stream, &b, -1);

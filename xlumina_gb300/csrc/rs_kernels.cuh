@@ -362,6 +362,90 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   }
 }
 
+// Column pass on the packed two-line engine (fft_pair.cuh): each thread
+// transforms two adjacent columns of the CTA's CW at once, so every butterfly
+// instruction works on both, and loads, stores and exchanges move the two
+// columns' elements as one 16-byte access.  NG = CW / 2 column pairs per CTA.
+// GROUPED: pair g is a group of T threads (whole warps) with its own named
+// barrier, so the groups drift apart and one group's loads overlap another's
+// arithmetic; otherwise the pairs interleave in the lanes of every warp (a
+// warp load covers whole 32-byte sectors) under one CTA barrier.
+template <int LOGQ, bool GROUPED> struct RsColPair {
+  using C = RsCfg<LOGQ>;
+  static constexpr int NG = C::CW / 2;
+  static constexpr int THREADS = NG * C::T;
+  // pair buffers offset by 8 / NG slots mod 8 when the pairs share a warp, so
+  // that one quarter-warp's 16-byte accesses fall in distinct banks
+  static constexpr int XSP = C::XS + (GROUPED ? 0 : 8 / NG);
+  static constexpr size_t SMEM = ((size_t)NG * XSP + C::NTW) * 16;
+  static constexpr int MINB = (512 / THREADS) > 1 ? (512 / THREADS) : 1;   // at most 128 registers
+  static_assert(C::CW % 2 == 0 && C::T % 32 == 0, "two-line column pass shape");
+  static_assert(GROUPED || (32 % NG == 0 && C::T % (32 / NG) == 0), "interleaved lanes");
+};
+
+template <int LOGQ, bool GROUPED>
+__global__ void __launch_bounds__(RsColPair<LOGQ, GROUPED>::THREADS, RsColPair<LOGQ, GROUPED>::MINB)
+    rs_cols_conv_p(const __grid_constant__ RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  using K = RsColPair<LOGQ, GROUPED>;
+  constexpr int W = C::W, CW = C::CW, NG = K::NG;
+  extern __shared__ __align__(16) float4 smem4[];
+  float4* stw = smem4 + NG * K::XSP;   // NTW pair twiddles
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int pr = GROUPED ? tid / C::T : lane % NG;
+  const int j = GROUPED ? tid % C::T : (tid >> 5) * (32 / NG) + lane / NG;
+  const int t = blockIdx.y / (W / CW);                       // column tile
+  const int w = (blockIdx.y % (W / CW)) * CW + 2 * pr;       // first column of the pair within the tile
+  const int b = blockIdx.x;
+  const int ny = p.ny;
+  {
+    const float4* g = pass_tw4<C::LOGP>();
+    for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
+  }
+  __syncthreads();
+  const int kx = t * W + w;
+  const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
+  const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+  float4* xb = smem4 + pr * K::XSP;
+  using Sync = typename std::conditional<GROUPED, GroupSync, CtaSync>::type;
+  Sync sync;
+  if constexpr (GROUPED) sync = GroupSync{1 + pr, C::T};
+#pragma unroll 1
+  for (int c = 0; c < p.cout; ++c) {
+    float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+    cpair v[16];
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      v[m] = n < ny ? p_from(*(const float4*)(tile + (long long)n * W)) : pz();
+    }
+#pragma unroll
+    for (int m = C::H; m < 16; ++m) v[m] = pz();
+    block_pfft<C::LOGP, -1, true, false>(v, j, xb, stw, sync);
+    const float2* sp = spec;
+    asm volatile("" : "+l"(sp));
+    if (p.adjoint) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const float4 s = __ldg((const float4*)(sp + (long long)(j + m * C::T) * C::SW));
+        v[m] = pmul_pp<true>(v[m], make_float2(s.x, s.z), make_float2(s.y, s.w));
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const float4 s = __ldg((const float4*)(sp + (long long)(j + m * C::T) * C::SW));
+        v[m] = pmul_pp<false>(v[m], make_float2(s.x, s.z), make_float2(s.y, s.w));
+      }
+    }
+    block_pfft<C::LOGP, 1, false, false>(v, j, xb, stw, sync);
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      if (n < ny) *(float4*)(tile + (long long)n * W) = p_to(v[m]);
+    }
+  }
+}
+
 // Inverse row pass: inverse P-point FFT per row and component, crop to nx
 // columns (the last pass computes only the surviving half), optional fused
 // epilogue program (or, for the VRS adjoint, the fold of the Ez gradient into
@@ -541,6 +625,17 @@ static int launch_rows_inv(cudaStream_t s, const RsLaunch& p) {
   return XL_OK;
 }
 
+template <int LOGQ, bool GROUPED>
+static int launch_cols_pair(cudaStream_t st, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  using K = RsColPair<LOGQ, GROUPED>;
+  cudaError_t e = allow_smem(rs_cols_conv_p<LOGQ, GROUPED>, K::SMEM);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv_p smem");
+  rs_cols_conv_p<LOGQ, GROUPED><<<dim3(p.B, C::P / C::CW), K::THREADS, K::SMEM, st>>>(p);
+  XL_CHECK_LAUNCH("rs_cols_conv_p");
+  return XL_OK;
+}
+
 template <int LOGQ>
 static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   using C = RsCfg<LOGQ>;
@@ -550,6 +645,11 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     if (p.cin == 2) return launch_rows_fwd<LOGQ, 2>(st, p);
     return launch_rows_fwd<LOGQ, 3>(st, p);
   } else if (stage == 1) {
+    const int var = kernel_variant(XL_PASS_RS_COLS, C::LOGP);
+    if constexpr (LOGQ >= 9 && LOGQ <= 11) {
+      if (var == 1) return launch_cols_pair<LOGQ, false>(st, p);
+      if (var == 2) return launch_cols_pair<LOGQ, true>(st, p);
+    }
     const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
     if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
     rs_cols_conv<LOGQ><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);

@@ -27,45 +27,83 @@ from .wave_optics import LightSource
 
 
 class FourFTable:
+    """A batch of B 4f tables.  ``independent`` (the default): every table has
+    its own seed, hence its own input mask, binary target and pair of SLM
+    phase planes (phase1 (B, n, n), phase2 (B, m, m)), so the step optimises B
+    independent parameter sets at once.  ``independent=False``: the B input
+    masks share one pair of SLM planes, the structure of
+    experiments/four_f_optical_table.py:36-127 (a batch of inputs through one
+    setup)."""
+
     def __init__(self, n=1024, roi_n=512, batch=16, wavelength=0.532, half_width=1500.0, f=2.5e5,
-                 roi_half_width=1000.0, waist=1200.0, seed=2000, device="cuda", capturable=False):
+                 roi_half_width=1000.0, waist=1200.0, seed=2000, device="cuda", capturable=False,
+                 independent=True):
         self.n, self.m, self.B, self.f = n, roi_n, batch, f
+        self.independent = independent
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
         self.wavelength = wavelength
         self.lens_r = (half_width, half_width)
-        rng = np.random.default_rng(seed)
         src = LightSource(self.x, self.y, wavelength)
         src.gaussian_beam(w0=(waist, waist), E0=1)
-        masks = (rng.uniform(0, 1, (batch, n, n)) > 0.5).astype(np.float32)
+        if independent:
+            seeds = [np.random.default_rng(seed + b) for b in range(batch)]
+            masks = np.stack([(r.uniform(0, 1, (n, n)) > 0.5).astype(np.float32) for r in seeds])
+            tgt = np.stack([(r.uniform(0, 1, (roi_n, roi_n)) < 0.1).astype(np.float32) for r in seeds])
+            p1 = np.stack([r.uniform(-np.pi, np.pi, (n, n)).astype(np.float32) for r in seeds])
+            p2 = np.stack([r.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32) for r in seeds])
+        else:
+            rng = np.random.default_rng(seed)
+            masks = (rng.uniform(0, 1, (batch, n, n)) > 0.5).astype(np.float32)
+            tgt = (rng.uniform(0, 1, (batch, roi_n, roi_n)) < 0.1).astype(np.float32)
+            p1 = rng.uniform(-np.pi, np.pi, (n, n)).astype(np.float32)
+            p2 = rng.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32)
         self.inputs = src.field[None] * torch.as_tensor(masks, device=device)
-        tgt = (rng.uniform(0, 1, (batch, roi_n, roi_n)) < 0.1).astype(np.float32)
         tgt /= tgt.sum(axis=(-2, -1), keepdims=True)
         self.target = torch.as_tensor(tgt, device=device)
-        self.phase1 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (n, n)).astype(np.float32),
-                                      device=device).requires_grad_(True)
-        self.phase2 = torch.as_tensor(rng.uniform(-np.pi, np.pi, (roi_n, roi_n)).astype(np.float32),
-                                      device=device).requires_grad_(True)
+        self.phase1 = torch.as_tensor(p1, device=device).requires_grad_(True)
+        self.phase2 = torch.as_tensor(p2, device=device).requires_grad_(True)
         # capturable: the step count lives on the device, so plans.CapturedStep can record a step
         self.opt = AdamW([self.phase1, self.phase2], lr=0.05, capturable=capturable)
 
-    def loss(self, inputs=None, target=None):
-        inputs = self.inputs if inputs is None else inputs
-        target = self.target if target is None else target
+    def entry(self, b):
+        """The inputs, target and SLM planes of table b (float64 / complex128
+        host arrays), for checking one table against the oracle."""
+        def host(t):
+            return t.detach().cpu().numpy().astype(np.float64)
+        p1 = self.phase1[b] if self.independent else self.phase1
+        p2 = self.phase2[b] if self.independent else self.phase2
+        return (self.inputs[b].detach().cpu().numpy().astype(np.complex128), host(self.target[b]),
+                host(p1), host(p2))
+
+    def intensities(self, inputs=None, tables=None):
+        """The output intensities of the tables, each normalised to sum 1
+        (B, m, m).  ``tables``: a slice of the batch."""
+        sl = slice(None) if tables is None else tables
+        inputs = self.inputs[sl] if inputs is None else inputs
+        p1 = self.phase1[sl] if self.independent else self.phase1
+        p2 = self.phase2[sl] if self.independent else self.phase2
         light = LightSource(self.x, self.y, self.wavelength)
         light.field = inputs
-        l1, _ = oe.SLM(light, self.phase1, self.n)
+        l1, _ = oe.SLM(light, p1, self.n)
         l2, _ = l1.RS_propagation(self.f)
         l3, _ = oe.lens(l2, self.lens_r, (self.f, self.f))
         l4 = l3.CZT(self.f, self.xo, self.yo)
-        l5, _ = oe.SLM(l4, self.phase2, self.m)
+        l5, _ = oe.SLM(l4, p2, self.m)
         I = torch.abs(l5.CZT(self.f).field) ** 2
-        I = I / torch.sum(I, dim=(-2, -1), keepdim=True)
+        return I / torch.sum(I, dim=(-2, -1), keepdim=True)
+
+    def loss(self, inputs=None, target=None, tables=None):
+        """Mean over the tables of the normalised intensity MSE
+        (experiments/four_f_optical_table.py:129-141)."""
+        sl = slice(None) if tables is None else tables
+        target = self.target[sl] if target is None else target
+        I = self.intensities(inputs, tables)
         return torch.mean(torch.sum((I - target) ** 2, dim=(-2, -1)) / (self.m * self.m))
 
-    def step(self, inputs=None, target=None):
+    def step(self, inputs=None, target=None, tables=None):
         self.opt.zero_grad(set_to_none=True)
-        L = self.loss(inputs, target)
+        L = self.loss(inputs, target, tables)
         L.backward()
         self.opt.step()
         return L
@@ -80,9 +118,18 @@ def small_area_hybrid_batched(I):
 
 
 class HighNATable:
+    """B high-NA focusing tables, each with its own parameter set: an LCD
+    (eta, theta) and an sSLM (alpha, phi), per-pixel float32 planes drawn
+    U[0, 2 pi) (B, n, n each), in front of a VCZT objective lens; the loss is
+    the Ez spot-size loss (small_area_hybrid) averaged over the tables.
+    ``shared_lcd``: one LCD setting for the whole batch instead (the sharp-
+    focus table's structure).  ``checkpoint``: the focal fields are not kept
+    for the backward; it recomputes them from the parameters (the
+    intermediate fields of a table are then never stored)."""
+
     def __init__(self, n=2048, roi_n=1024, batch=32, wavelength=0.650, half_width=2700.0, na=0.9,
                  f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda", capturable=False,
-                 checkpoint=False):
+                 checkpoint=False, shared_lcd=False):
         self.n, self.m, self.B = n, roi_n, batch
         self.checkpoint = checkpoint
         self.x, self.y = toolbox.space(half_width, n)
@@ -93,13 +140,22 @@ class HighNATable:
         src.gaussian_beam(w0=(waist, waist), E0=1)
         self.Ex = src.field
         self.Ey = torch.zeros_like(src.field)
-        self.eta = torch.full((n, n), float(rng.uniform(0, 2 * np.pi)), device=device).requires_grad_(True)
-        self.theta = torch.full((n, n), float(rng.uniform(0, 2 * np.pi)), device=device).requires_grad_(True)
-        self.alpha = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
-                                     device=device).requires_grad_(True)
-        self.phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, (batch, n, n)).astype(np.float32),
+
+        def planes(lead):
+            return torch.as_tensor(rng.uniform(0, 2 * np.pi, lead + (n, n)).astype(np.float32),
                                    device=device).requires_grad_(True)
+        lcd_lead = () if shared_lcd else (batch,)
+        self.eta, self.theta = planes(lcd_lead), planes(lcd_lead)
+        self.alpha, self.phi = planes((batch,)), planes((batch,))
         self.opt = AdamW([self.eta, self.theta, self.alpha, self.phi], lr=0.05, capturable=capturable)
+
+    def entry(self, b):
+        """Table b's parameter planes (float64 host arrays), for checking one
+        table against the oracle."""
+        def host(t):
+            return t.detach().cpu().numpy().astype(np.float64)
+        e, t = (self.eta, self.theta) if self.eta.dim() == 2 else (self.eta[b], self.theta[b])
+        return host(e), host(t), host(self.alpha[b]), host(self.phi[b])
 
     def _spot_intensity(self):
         light = VectorizedLight(self.x, self.y, self.wavelength)
