@@ -438,7 +438,10 @@ def run_gpu(args):
         "column_pass_variant": {"chosen": tuned["variant"], "transform_length": 1 << col_logp,
                                 "ms_per_launch": {str(k): v for k, v in tuned["ms"].items()},
                                 "variants": "0 one line per thread; 1 two lines per thread (packed FP32), "
-                                            "pairs interleaved in warps; 2 packed, pairs in barrier groups"},
+                                            "pairs interleaved in warps; 2 packed, pairs in barrier groups; "
+                                            "3 one line per thread with L2 prefetch; 4 packed interleaved "
+                                            "with L2 and register prefetch; 5 one line per thread, two "
+                                            "barrier groups; 6 one line per thread, two CTAs per SM"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

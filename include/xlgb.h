@@ -84,6 +84,23 @@ size_t xl_struct_size(const char* name);
  * event and returns without hanging, its output is not valid.  Synchronous. */
 int xl_device_timeouts(unsigned int* count, int reset);
 
+/* Non-blocking check for kernel errors: *flag = 1 if a kernel of this
+ * library had a bounded wait run out (its output is not valid) since the
+ * last clear, on any device, else 0.  Kernels raise a word in mapped host
+ * memory, so no device synchronisation is needed; work still queued is not
+ * reflected, so read it after synchronising with the launches of interest.
+ * clear != 0 resets the word.  The Python package checks it at the start of
+ * every propagation call and after every synchronising step, and raises
+ * (XL_ETIMEOUT). */
+int xl_device_status(unsigned int* flag, int clear);
+
+/* Limit of the kernels' bounded waits on their TMA copies, in ns, on the
+ * current device (default 1e9, one second).  0 makes every such wait give up
+ * at once: a test setting that takes the timeout path (the kernel lets its
+ * copy in flight land, raises the status word and returns) without a fault
+ * or a hang. */
+int xl_set_wait_limit(unsigned long long ns);
+
 /* Upload the twiddle tables to the current device.  Called once per device
  * before the first launch (every entry point calls it lazily as well). */
 int xl_init(void);
@@ -207,6 +224,16 @@ int xl_rs_stage(void* stream, const XlRsArgs* args, int stage);
  * other host threads) race. */
 #define XL_RS_NOALLOC_MAX_WORK_BYTES (64ull << 20)
 int xl_rs_propagate_noalloc(void* stream, const XlRsArgs* args);
+
+/* ---- Bare line transforms ----------------------------------------------
+ * Unnormalised complex64 FFTs of `lines` contiguous lines of 2^log2_len
+ * points (line l at in + l * 2^log2_len), forward (dir = -1: sum x[n]
+ * e^{-2 pi i n k / L}) or inverse (dir = +1, no 1/L), in -> out.  In place
+ * (in == out) for log2_len >= 5.  log2_len 0..13.  Replaces the
+ * jnp.fft.fft / jnp.fft.ifft calls of the reference's Bluestein helpers
+ * compute_fft and Bluestein_method (wave_optics.py:385-460, :401, :406,
+ * :408); the propagators fuse their transforms instead. */
+int xl_fft_lines(void* stream, int log2_len, long long lines, int dir, const void* in, void* out);
 
 /* ---- Chirp-z (CZT / VCZT / high-NA focus) ----------------------------- */
 
@@ -389,6 +416,36 @@ int xl_beam_splitter_backward(void* stream, const XlBsArgs* args, const void* co
  * a fixed order (work: xl_mse_intensity_work_bytes(planes, npix)). */
 int xl_re_inner(void* stream, int planes, long long npix, const void* a, long long a_pstride, const void* b,
                 long long b_pstride, void* work, void* out);
+
+/* ---- Fused loss epilogues (planes of npix pixels; complex_in = 1: the
+ * planes are complex64 fields and the intensity |u|^2 is formed in the
+ * kernel; 0: float32 intensities; in_pstride in elements).  Two reduction
+ * passes with float64 block partials summed in a fixed order, so repeated
+ * calls give identical results.  work: xl_loss_work_bytes(planes, npix),
+ * which the forward fills with the statistics its gradient reads (keep it
+ * between the two calls).  loss: planes float32 values (device).  Gradients
+ * take the upstream gradient per plane (gloss, device float32) and write gin
+ * (contiguous planes): for a complex input torch's convention 2 dL/d conj(u)
+ * = 2 dL/dI u. */
+size_t xl_loss_work_bytes(int planes, long long npix);
+
+/* small_area_hybrid (loss_functions.py:24-40) per plane: In = I / (sum I +
+ * 1e-8), mask = In > 0.7 max In, loss = sum mask / (sum mask In + 1e-8)
+ * (vectorized_loss_hybrid, :42-50, is the planes > 1 form). */
+int xl_area_loss(void* stream, int planes, long long npix, int complex_in, const void* in, long long in_pstride,
+                 void* work, float* loss);
+int xl_area_loss_grad(void* stream, int planes, long long npix, int complex_in, const void* in,
+                      long long in_pstride, const void* work, const float* gloss, void* gin);
+
+/* The 4f table's normalised intensity MSE (experiments/four_f_optical_table.py:
+ * 129-141) per plane: In = I / sum I, loss = sum (In - T)^2 / npix, against
+ * float32 target planes (target_pstride elements apart; 0: one target). */
+int xl_norm_intensity_mse(void* stream, int planes, long long npix, int complex_in, const void* in,
+                          long long in_pstride, const float* target, long long target_pstride, void* work,
+                          float* loss);
+int xl_norm_intensity_mse_grad(void* stream, int planes, long long npix, int complex_in, const void* in,
+                               long long in_pstride, const float* target, long long target_pstride,
+                               const void* work, const float* gloss, void* gin);
 
 /* The distance gradient through the VRS Ez derivation (vectorized_optics.py:258-261):
  * out[b] = sum_i Re(conj(gez_i) dEz_i/dz), dEz/dz = -(Ex X + Ey Y) z / r^3, for

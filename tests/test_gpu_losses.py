@@ -66,3 +66,97 @@ def test_vmse_intensity_and_broadcast_target():
     got_b = lf.MSE_Intensity(u.Ex, t)
     exp_b = torch.sum((torch.abs(u.Ex) ** 2 - torch.abs(t) ** 2) ** 2, dim=(-2, -1)) / (n * n)
     assert rel_l2(got_b.cpu().numpy(), exp_b.cpu().numpy()) < 1e-5
+
+
+def test_area_loss_golden():
+    """The fused small_area_hybrid and vectorized_loss_hybrid against the
+    reference's own values (losses.npz, losses_more.npz)."""
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    g = golden("losses")
+    v = lf.small_area_hybrid(torch.as_tensor(g["I"].astype(np.float32), device="cuda"))
+    assert v.shape == () and abs(float(v) - float(g["small_area"])) <= 1e-5 * abs(float(g["small_area"]))
+    g2 = golden("losses_more")
+    got = lf.vectorized_loss_hybrid(torch.as_tensor(g2["I6"].astype(np.float32), device="cuda"))
+    assert rel_l2(got.cpu().numpy(), g2["loss_hybrid"]) < 1e-5
+
+
+def _spots(rng, B, n):
+    """Smooth focal spots with noise: a clear maximum and a mask of a few hundred pixels."""
+    X, Y = np.meshgrid(np.linspace(-1, 1, n), np.linspace(-1, 1, n))
+    f = np.stack([np.exp(-((X - 0.1 * b) ** 2 + Y ** 2) / 0.02) * (1 + 0.3 * rng.standard_normal((n, n)))
+                  for b in range(B)])
+    return (f * np.exp(1j * rng.uniform(-np.pi, np.pi, (B, n, n)))).astype(np.complex64)
+
+
+def test_area_loss_fused_from_fields_values_and_gradients():
+    """Area loss of |Ez|^2 formed in the kernel, per plane, against torch
+    autograd of the reference formula in complex128 (same masks)."""
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    from xlumina_gb300.tables import small_area_hybrid_batched
+    rng = np.random.default_rng(21)
+    B, n = 4, 128
+    e0 = torch.as_tensor(_spots(rng, B, n), device="cuda")
+    w = torch.as_tensor(rng.uniform(0.5, 2.0, B).astype(np.float32), device="cuda")
+    e = e0.clone().requires_grad_(True)
+    L = lf.small_area_hybrid_field(e)
+    assert L.shape == (B,)
+    (L * w).sum().backward()
+    er = e0.to(torch.complex128).requires_grad_(True)
+    Ir = torch.abs(er) ** 2
+    In = Ir / (torch.sum(Ir, dim=(-2, -1), keepdim=True) + 1e-8)
+    mask = (In > 0.7 * torch.amax(In, dim=(-2, -1), keepdim=True)).double()
+    Lr = torch.sum(mask, dim=(-2, -1)) / (torch.sum(mask * In, dim=(-2, -1)) + 1e-8)
+    (Lr * w.double()).sum().backward()
+    assert rel_l2(L.detach().cpu().numpy(), Lr.detach().cpu().numpy()) < 1e-5
+    assert rel_l2(e.grad.cpu().numpy(), er.grad.cpu().numpy()) < 1e-4
+    # the mean over planes equals the torch batched form, and repeats exactly
+    I = torch.abs(e0) ** 2
+    assert float(torch.mean(lf.small_area_hybrid_field(e0))) == pytest.approx(
+        float(small_area_hybrid_batched(I)), rel=1e-5)
+    assert torch.equal(lf.small_area_hybrid_field(e0), lf.small_area_hybrid_field(e0))
+
+
+def test_area_loss_on_intensities_gradient():
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    rng = np.random.default_rng(22)
+    I0 = torch.as_tensor(np.abs(_spots(rng, 3, 96)) ** 2, device="cuda")
+    I = I0.clone().requires_grad_(True)
+    lf.vectorized_loss_hybrid(I).sum().backward()
+    Ir = I0.double().requires_grad_(True)
+    In = Ir / (torch.sum(Ir, dim=(-2, -1), keepdim=True) + 1e-8)
+    mask = (In > 0.7 * torch.amax(In, dim=(-2, -1), keepdim=True)).double()
+    (torch.sum(mask, dim=(-2, -1)) / (torch.sum(mask * In, dim=(-2, -1)) + 1e-8)).sum().backward()
+    assert rel_l2(I.grad.cpu().numpy(), Ir.grad.cpu().numpy()) < 1e-4
+
+
+@pytest.mark.parametrize("shared_target", [False, True])
+def test_normalised_intensity_mse_values_and_gradients(shared_target):
+    """The 4f loss (experiments/four_f_optical_table.py:129-141) fused, against
+    torch autograd of the formula in complex128."""
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    rng = np.random.default_rng(23 + shared_target)
+    B, m = 3, 80
+    u0 = torch.as_tensor((rng.standard_normal((B, m, m)) + 1j * rng.standard_normal((B, m, m))).astype(np.complex64),
+                         device="cuda")
+    t = (rng.uniform(0, 1, (m, m) if shared_target else (B, m, m)) < 0.1).astype(np.float32)
+    t /= t.sum(axis=(-2, -1), keepdims=True)
+    tg = torch.as_tensor(t, device="cuda")
+    w = torch.as_tensor(rng.uniform(0.5, 2.0, B).astype(np.float32), device="cuda")
+    u = u0.clone().requires_grad_(True)
+    L = lf.normalized_intensity_mse(u, tg)
+    (L * w).sum().backward()
+    ur = u0.to(torch.complex128).requires_grad_(True)
+    Ir = torch.abs(ur) ** 2
+    Ir = Ir / torch.sum(Ir, dim=(-2, -1), keepdim=True)
+    Lr = torch.sum((Ir - tg.double()) ** 2, dim=(-2, -1)) / (m * m)
+    (Lr * w.double()).sum().backward()
+    assert rel_l2(L.detach().cpu().numpy(), Lr.detach().cpu().numpy()) < 1e-5
+    assert rel_l2(u.grad.cpu().numpy(), ur.grad.cpu().numpy()) < 1e-4

@@ -1,6 +1,7 @@
 """Every kernel variant of a pass gives the oracle's result: the packed
-two-line column pass (interleaved and in barrier groups) against the
-one-line kernel and the FP64 oracle, for the transform lengths that have it
+two-line column pass (interleaved, in barrier groups, with prefetching) and
+the prefetching one-line kernel against the one-line kernel and the FP64
+oracle, for the transform lengths that have it
 (1024, 2048 and 4096 points: fields of 257..2048 per side).
 
 Tolerance: relative L2 <= 1e-5 against the oracle (the path's bar); the
@@ -38,10 +39,10 @@ def variants():
 def test_variant_table_bounds():
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 3
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 7
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(99, 12) == 0
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 3) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 7) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
     assert lib.xl_get_kernel_variant(-1, 12) == _lib.XL_EINVAL
 
@@ -53,7 +54,8 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     from xlumina_gb300 import engine
     select, count = variants
     logp = engine.rs_logq(n, n) + 1
-    assert count(logp) == 3
+    nv = count(logp)
+    assert nv == 7
     x, y = ref.space(1000.0, n)
     rng = np.random.default_rng(n + vector)
     Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
@@ -66,19 +68,19 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     else:
         exp = [ref.rs_propagate(Ex.astype(np.complex64), x, y, 0.633, z)]
     outs = []
-    for v in range(3):
+    for v in range(nv):
         select(logp, v)
         got = engine.rs_propagate(comps, x, y, 0.633, z, vector=vector)
         torch.cuda.synchronize()
         outs.append([_np(g) for g in got])
         for g, e in zip(outs[-1], exp):
             assert rel_l2(g, e) < TOL, (v, rel_l2(g, e))
-    for v in (1, 2):
+    for v in range(1, nv):
         for g, g0 in zip(outs[v], outs[0]):
             assert rel_l2(g, g0) < 1e-6, v
 
 
-@pytest.mark.parametrize("v", [1, 2])
+@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6])
 def test_rs_column_variants_adjoint_and_batch(variants, v):
     """The adjoint (conjugate spectrum) and a batch with a distance per entry
     through a packed variant equal the one-line kernel's results."""

@@ -121,6 +121,8 @@ SIGNATURES = {
     "xl_set_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_get_kernel_variant": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "xl_device_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
+    "xl_device_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
+    "xl_set_wait_limit": (ctypes.c_int, [ctypes.c_ulonglong]),
     "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_spectrum_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_transfer_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
@@ -150,6 +152,8 @@ SIGNATURES = {
     "xl_rs_propagate": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
     "xl_rs_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs), ctypes.c_int]),
     "xl_rs_propagate_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlRsArgs)]),
+    "xl_fft_lines": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
     "xl_czt_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_czt": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs)]),
     "xl_czt_stage": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlCztArgs), ctypes.c_int]),
@@ -170,6 +174,19 @@ SIGNATURES = {
     "xl_mse_intensity_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
                                              ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_loss_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
+    "xl_area_loss": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_area_loss_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
+    "xl_norm_intensity_mse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
+                                             ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_norm_intensity_mse_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                                  ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                                  ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
     "xl_beam_splitter": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlBsArgs)]),
     "xl_beam_splitter_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "xl_beam_splitter_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XlBsArgs),
@@ -190,7 +207,11 @@ _lib = None
 
 
 class XlError(RuntimeError):
-    """A libxlgb entry point returned an error code."""
+    """A libxlgb entry point returned an error code (``code``: the XL_E* value)."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
 
 
 def load(path: str = LIB):
@@ -214,4 +235,21 @@ def load(path: str = LIB):
 def check(rc: int, what: str = "") -> None:
     if rc != XL_OK:
         msg = _lib.xl_last_error().decode() if _lib is not None else ""
-        raise XlError(f"{what or 'libxlgb'} failed with code {rc}: {msg}")
+        raise XlError(f"{what or 'libxlgb'} failed with code {rc}: {msg}", rc)
+
+
+def check_device_status(clear: bool = True) -> None:
+    """Raise XlError (code XL_ETIMEOUT) if a kernel had a bounded wait run out
+    since the last check: that launch returned without its data and its output
+    is not valid.  Reads a word the kernels write in mapped host memory, so it
+    costs no device synchronisation; launches still queued are covered by a
+    later check.  ``clear``: reset the word when raising."""
+    if _lib is None:
+        return
+    flag = ctypes.c_uint(0)
+    check(_lib.xl_device_status(ctypes.byref(flag), 0), "xl_device_status")
+    if flag.value:
+        if clear:
+            _lib.xl_device_status(ctypes.byref(flag), 1)
+        raise XlError("a libxlgb kernel's bounded wait on its input copies ran out (about one second); "
+                      "the output of that launch is not valid", XL_ETIMEOUT)

@@ -219,6 +219,47 @@ def mse_intensity(a, b):
     return _MseIntensity.apply(a, b)
 
 
+class _AreaLoss(torch.autograd.Function):
+    """small_area_hybrid per plane (fused passes of libxlgb) with the
+    hand-written gradient seeded per plane."""
+
+    @staticmethod
+    def forward(ctx, x):
+        out, work = engine.area_loss(x)
+        ctx.save_for_backward(x, work)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        x, work = ctx.saved_tensors
+        return engine.area_loss_grad(x, work, g).reshape(x.shape)
+
+
+def area_loss(x):
+    """Per-plane small_area_hybrid of intensities, or of |x|^2 for a complex field."""
+    return _AreaLoss.apply(x)
+
+
+class _NormIntensityMse(torch.autograd.Function):
+    """The 4f normalised intensity MSE per plane with the hand-written gradient."""
+
+    @staticmethod
+    def forward(ctx, x, target):
+        out, work = engine.norm_intensity_mse(x, target)
+        ctx.save_for_backward(x, target, work)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        x, target, work = ctx.saved_tensors
+        return engine.norm_intensity_mse_grad(x, target, work, g).reshape(x.shape), None
+
+
+def norm_intensity_mse(x, target):
+    """Per-plane normalised intensity MSE of intensities, or of |x|^2 for a complex field."""
+    return _NormIntensityMse.apply(x, target)
+
+
 def _sum_to(g, shape):
     """Sum a per-batch gradient down to a broadcast input's shape."""
     if g is None or tuple(g.shape) == tuple(shape):

@@ -32,6 +32,7 @@ static bool g_init_dev[256];
 struct DeviceTables {
   TableUpload upload;
   TimeoutCounter timeouts;
+  StatusSetup status;
 };
 
 static std::vector<DeviceTables>& registry() {
@@ -39,9 +40,41 @@ static std::vector<DeviceTables>& registry() {
   return r;
 }
 
-bool register_device_tables(TableUpload upload, TimeoutCounter timeouts) {
-  registry().push_back({upload, timeouts});
+bool register_device_tables(TableUpload upload, TimeoutCounter timeouts, StatusSetup status) {
+  registry().push_back({upload, timeouts, status});
   return true;
+}
+
+// The status word kernels raise when a bounded wait runs out: one word of
+// mapped (zero-copy) pinned host memory for the process, so that the host
+// reads it without synchronising the device.  Allocated at the first device
+// set-up; null if mapped host memory is unavailable (the counters remain).
+static unsigned int* g_status_host = nullptr;
+static unsigned int* g_status_dev = nullptr;
+static unsigned long long g_wait_limit[256];
+
+static cudaError_t status_word() {
+  if (g_status_host) return cudaSuccess;
+  void* h = nullptr;
+  cudaError_t e = cudaHostAlloc(&h, sizeof(unsigned int), cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e != cudaSuccess) return e;
+  *(volatile unsigned int*)h = 0u;
+  void* d = nullptr;
+  if ((e = cudaHostGetDevicePointer(&d, h, 0)) != cudaSuccess) {
+    cudaFreeHost(h);
+    return e;
+  }
+  g_status_host = (unsigned int*)h;
+  g_status_dev = (unsigned int*)d;
+  return cudaSuccess;
+}
+
+// Point every unit's kernels at the status word and set their wait limit (current device).
+static cudaError_t set_status_all(unsigned long long limit_ns) {
+  for (const DeviceTables& t : registry())
+    if (t.status)
+      if (cudaError_t e = t.status(g_status_dev, limit_ns)) return e;
+  return cudaSuccess;
 }
 
 // Twiddle tables for S = 1, 2, 4, ..., XL_MAX_FFT at offset S: e^{-2 pi i q / S},
@@ -72,26 +105,45 @@ int ensure_init() {
   const float2* h = host_twiddles().data();
   for (const DeviceTables& t : registry())
     if ((e = t.upload(h)) != cudaSuccess) return cuda_fail(e, "upload device tables");
+  if ((e = status_word()) != cudaSuccess) return cuda_fail(e, "status word (mapped host memory)");
+  g_wait_limit[dev] = kDefaultWaitLimitNs;
+  if ((e = set_status_all(g_wait_limit[dev])) != cudaSuccess) return cuda_fail(e, "device status set-up");
   g_init_dev[dev] = true;
   return XL_OK;
 }
 
+int set_wait_limit(unsigned long long ns) {
+  if (int rc = ensure_init()) return rc;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if ((e = set_status_all(ns)) != cudaSuccess) return cuda_fail(e, "xl_set_wait_limit");
+  g_wait_limit[dev] = ns;
+  return XL_OK;
+}
+
+int read_status(unsigned int* flag, int clear) {
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  *flag = g_status_host ? *(volatile unsigned int*)g_status_host : 0u;
+  if (clear && g_status_host) *(volatile unsigned int*)g_status_host = 0u;
+  return XL_OK;
+}
+
 // ---- kernel variants per (pass, transform length) ----
-// Available variants: the one-line kernel (0) everywhere; the packed two-line
-// column pass, interleaved (1) or in barrier groups (2), for 1024..4096-point
-// RS transforms.
+// Available variants: the one-line kernel (0) everywhere; for 1024..4096-point
+// RS transforms the packed two-line column pass, interleaved (1) or in
+// barrier groups (2), the one-line kernel with L2 prefetch (3), the
+// interleaved packed one with L2 and register prefetch (4), and the one-line
+// kernel with prefetch in two barrier groups (5) or in CTAs of half the
+// columns, two per SM (6).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
-  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 12) return 3;
+  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 12) return 7;
   return 1;
 }
 static std::atomic<int> g_variant[XL_NUM_PASSES][14];
 
-static bool variants_defaults() {
-  for (int l = 10; l <= 12; ++l) g_variant[XL_PASS_RS_COLS][l] = 1;
-  return true;
-}
-static const bool g_variants_ready = variants_defaults();
 
 int kernel_variant(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 0 || log2_len > 13) return 0;
@@ -144,6 +196,16 @@ extern "C" size_t xl_struct_size(const char* name) {
 }
 
 extern "C" int xl_init(void) { return xl::ensure_init(); }
+
+extern "C" int xl_device_status(unsigned int* flag, int clear) {
+  if (!flag) {
+    xl::set_error("xl_device_status: null output");
+    return XL_EINVAL;
+  }
+  return xl::read_status(flag, clear);
+}
+
+extern "C" int xl_set_wait_limit(unsigned long long ns) { return xl::set_wait_limit(ns); }
 
 extern "C" int xl_device_timeouts(unsigned int* count, int reset) {
   if (!count) {

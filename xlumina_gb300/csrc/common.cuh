@@ -543,21 +543,48 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
       : "memory");
 }
 
+// Bring `bytes` (a multiple of 16, 16-byte aligned start) of global memory
+// into L2 ahead of use (one thread; no registers or shared memory held).
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
 
-// Bounded wait for phase `phase` of the barrier: gives up after about a
-// second of wall time and returns false (the caller records the error and
-// carries on without the data; it never spins forever).
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* mbar, unsigned phase) {
+// ---- bounded waits and the error status they report ----
+// Each translation unit has its own copies (filled at device set-up):
+// a count of waits that ran out, the wait limit, and the device address of a
+// word in mapped host memory that a kernel sets when one of its waits runs
+// out, so that the host sees the event without synchronising.
+static __device__ unsigned int g_line_timeouts;
+static __device__ unsigned long long g_wait_limit_ns = 1000000000ull;
+static __device__ unsigned int* g_status_word;
+constexpr unsigned long long kDrainLimitNs = 1000000000ull;
+
+// Bounded wait for phase `phase` of the barrier: gives up after `limit_ns`
+// of wall time and returns false (it never spins forever).  A limit of 0
+// gives up without waiting (the test setting of xl_set_wait_limit).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* mbar, unsigned phase,
+                                                  unsigned long long limit_ns = kDrainLimitNs) {
+  if (limit_ns == 0) return false;
   if (mbar_try_wait(mbar, phase)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
     if (mbar_try_wait(mbar, phase)) return true;
-    if (global_ns() - t0 > 1000000000ull) return false;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+// A wait ran out: count it and raise the host-visible status word.
+__device__ __forceinline__ void record_timeout() {
+  atomicAdd(&g_line_timeouts, 1u);
+  if (g_status_word) {
+    *(volatile unsigned int*)g_status_word = 1u;
+    __threadfence_system();
   }
 }
 

@@ -104,14 +104,20 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
   }
 
   unsigned phase = 0;
-  bool ok = true;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
     const int b = grp % p.B;
     const int r0 = (grp / p.B) * C::G;
     const double zd = p.zb ? p.zb[b] : p.z;
     const float zf = (float)zd;
     if (staged) {
-      if (!mbar_wait_bounded(mbar, phase)) ok = false;
+      const bool got = mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
+      if (__syncthreads_or(!got)) {   // every thread takes this branch or none does
+        // the copy may still be in flight: let it land, record the event and
+        // leave without issuing another (the launch's output is not valid)
+        mbar_wait_bounded(mbar, phase);
+        if (tid == 0) record_timeout();
+        return;
+      }
       phase ^= 1u;
     }
     // prologue over the row group's pixels
@@ -187,10 +193,6 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
         }
       }
     }
-  }
-  if (!ok && tid == 0) {
-    atomicAdd(&g_line_timeouts, 1u);
-    mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
   }
 }
 

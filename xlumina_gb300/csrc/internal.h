@@ -12,6 +12,9 @@ namespace xl {
 void set_error(const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* where);
 int ensure_init();  // uploads twiddle tables to the current device once
+constexpr unsigned long long kDefaultWaitLimitNs = 1000000000ull;   // bounded waits: one second
+int set_wait_limit(unsigned long long ns);       // xl_set_wait_limit (current device)
+int read_status(unsigned int* flag, int clear);  // xl_device_status
 
 // The kernel variant selected for a pass at transform length 2^log2_len
 // (xl_set_kernel_variant; defined in capi.cu).
@@ -40,8 +43,11 @@ inline cudaError_t allow_smem(K kernel, size_t bytes) {
 // (whole-program compilation, one device module per unit).  It registers,
 // from a static initialiser, the function that fills them from the host
 // twiddles and, optionally, a reader of its device timeout counter.
+// A unit with bounded waits also registers the setter of its status word
+// pointer and wait limit.
 using TableUpload = cudaError_t (*)(const float2* host_twiddles);
 using TimeoutCounter = cudaError_t (*)(unsigned int* count, int reset);
-bool register_device_tables(TableUpload upload, TimeoutCounter timeouts);
+using StatusSetup = cudaError_t (*)(unsigned int* status_word, unsigned long long wait_limit_ns);
+bool register_device_tables(TableUpload upload, TimeoutCounter timeouts, StatusSetup status = nullptr);
 
 }  // namespace xl

@@ -100,9 +100,6 @@ __device__ __forceinline__ void stage_rows(const RowStage& st, unsigned char* st
   }
 }
 
-// Bounded waits that ran out, counted per translation unit (read by xl_device_timeouts).
-static __device__ unsigned int g_line_timeouts;
-
 // Which planes to stage: every input component and every per-pixel parameter
 // plane of the fused program whose rows are 16-byte aligned, while the stage
 // fits next to `fixed_smem` bytes of other shared memory.
@@ -187,6 +184,12 @@ static cudaError_t line_tu_timeouts(unsigned int* count, int reset) {
   return cudaMemcpyToSymbol(g_line_timeouts, &zero, sizeof(unsigned int));
 }
 
-static const bool line_tu_registered = register_device_tables(&line_tu_tables, &line_tu_timeouts);
+static cudaError_t line_tu_status(unsigned int* word, unsigned long long limit_ns) {
+  cudaError_t e = cudaMemcpyToSymbol(g_status_word, &word, sizeof(word));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(g_wait_limit_ns, &limit_ns, sizeof(limit_ns));
+}
+
+static const bool line_tu_registered = register_device_tables(&line_tu_tables, &line_tu_timeouts, &line_tu_status);
 
 }  // namespace xl

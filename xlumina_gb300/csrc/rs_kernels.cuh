@@ -220,12 +220,18 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
 
   unsigned phase = 0;
-  bool ok = true;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
     const int b = grp % p.B;
     const int r0 = (grp / p.B) * C::G;
     if (staged) {
-      if (!mbar_wait_bounded(mbar, phase)) ok = false;
+      const bool got = mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
+      if (__syncthreads_or(!got)) {   // every thread takes this branch or none does
+        // the copy may still be in flight: let it land, record the event and
+        // leave without issuing another (the launch's output is not valid)
+        mbar_wait_bounded(mbar, phase);
+        if (tid == 0) record_timeout();
+        return;
+      }
       phase ^= 1u;
     }
     // prologue over the row group's pixels
@@ -292,12 +298,6 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
       }
     }
   }
-  if (!ok) {
-    if (tid == 0) {
-      atomicAdd(&g_line_timeouts, 1u);
-      mbar_wait_bounded(mbar, phase);   // a copy may still be in flight
-    }
-  }
 }
 
 // Column pass, in place on one tile of W spectrum columns: FFT along y of the
@@ -305,7 +305,10 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 // (conjugate for the adjoint), inverse FFT, keep the ny surviving rows.
 // A CTA takes CW columns of a tile; lanes interleave them, so every warp
 // access is one contiguous run of CW columns.
-template <int LOGQ>
+// L2 prefetch (PF): the CTA's spectrum columns at the start, and the next
+// component's column tile while this one is transformed, so that their loads
+// meet L2 rather than DRAM latency.
+template <int LOGQ, bool PF>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
     rs_cols_conv(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
@@ -330,9 +333,13 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
   const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
   float2* xb = xch + wc * C::CXS;
+  if (PF && tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
 #pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {
     float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+    if (PF && tid == 0 && c + 1 < p.cout)
+      l2_prefetch(p.work + ((long long)b * p.cout + c + 1) * ny * C::P + (long long)t * ny * W,
+                  (unsigned)(ny * W * 8));
     float2 v[16];
 #pragma unroll
     for (int m = 0; m < C::H; ++m) {
@@ -362,6 +369,81 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   }
 }
 
+// One-line column pass in other CTA shapes: CWK columns per CTA (CWK = CW:
+// one CTA per SM; CWK = CW / 2: two), split into NGRP groups of CWK / NGRP
+// columns with their own named barriers, so that groups (or co-resident CTAs)
+// in different phases overlap one's exchanges with another's arithmetic.
+// With L2 prefetch of the spectrum and of the next component's tile.
+template <int LOGQ, int CWK, int NGRP> struct RsColShape {
+  using C = RsCfg<LOGQ>;
+  static constexpr int CWG = CWK / NGRP;                  // columns per group
+  static constexpr int THREADS = CWK * C::T;
+  static constexpr int MINB = (1024 / THREADS) > 1 ? (1024 / THREADS) : 1;
+  static constexpr int XSK = C::XS + (CWG >= 8 ? 0 : 16 / CWG);
+  static constexpr size_t SMEM = ((size_t)CWK * XSK + C::NTW) * sizeof(float2);
+  static_assert(C::CW % CWK == 0 && CWK % NGRP == 0 && (CWG * C::T) % 32 == 0, "column CTA shape");
+};
+
+template <int LOGQ, int CWK, int NGRP>
+__global__ void __launch_bounds__(RsColShape<LOGQ, CWK, NGRP>::THREADS, RsColShape<LOGQ, CWK, NGRP>::MINB)
+    rs_cols_conv_g(const __grid_constant__ RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  using K = RsColShape<LOGQ, CWK, NGRP>;
+  constexpr int W = C::W, CWG = K::CWG, LPW = 32 / CWG;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* stw = smem + CWK * K::XSK;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int grp = tid / (CWG * C::T), gtid = tid % (CWG * C::T);
+  const int wc = lane % CWG, j = (gtid >> 5) * LPW + lane / CWG;
+  const int t = blockIdx.y / (W / CWK);
+  const int w = (blockIdx.y % (W / CWK)) * CWK + grp * CWG + wc;
+  const int b = blockIdx.x;
+  const int ny = p.ny;
+  {
+    const float2* g = pass_tw<C::LOGP>();
+    for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
+  }
+  __syncthreads();
+  const int kx = t * W + w;
+  const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
+  const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+  float2* xb = smem + (grp * CWG + wc) * K::XSK;
+  using Sync = typename std::conditional<(NGRP > 1), GroupSync, CtaSync>::type;
+  Sync sync;
+  if constexpr (NGRP > 1) sync = GroupSync{1 + grp, CWG * C::T};
+  if (tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
+#pragma unroll 1
+  for (int c = 0; c < p.cout; ++c) {
+    const long long tbase = ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W;
+    float2* tile = p.work + tbase + w;
+    if (tid == 0 && c + 1 < p.cout) l2_prefetch(p.work + tbase + (long long)ny * C::P, (unsigned)(ny * W * 8));
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      v[m] = n < ny ? tile[(long long)n * W] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw, sync);
+    const float2* sp = spec;
+    asm volatile("" : "+l"(sp));
+    if (p.adjoint) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+    }
+    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw, sync);
+#pragma unroll
+    for (int m = 0; m < C::H; ++m) {
+      const int n = j + m * C::T;
+      if (n < ny) tile[(long long)n * W] = v[m];
+    }
+  }
+}
+
 // Column pass on the packed two-line engine (fft_pair.cuh): each thread
 // transforms two adjacent columns of the CTA's CW at once, so every butterfly
 // instruction works on both, and loads, stores and exchanges move the two
@@ -383,7 +465,10 @@ template <int LOGQ, bool GROUPED> struct RsColPair {
   static_assert(GROUPED || (32 % NG == 0 && C::T % (32 / NG) == 0), "interleaved lanes");
 };
 
-template <int LOGQ, bool GROUPED>
+// PF: L2 prefetch as in rs_cols_conv; RP: the next component's inputs are
+// loaded into registers at the start of this component's transforms, so their
+// latency is spent under the arithmetic.
+template <int LOGQ, bool GROUPED, bool PF = false, bool RP = false>
 __global__ void __launch_bounds__(RsColPair<LOGQ, GROUPED>::THREADS, RsColPair<LOGQ, GROUPED>::MINB)
     rs_cols_conv_p(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
@@ -410,14 +495,35 @@ __global__ void __launch_bounds__(RsColPair<LOGQ, GROUPED>::THREADS, RsColPair<L
   using Sync = typename std::conditional<GROUPED, GroupSync, CtaSync>::type;
   Sync sync;
   if constexpr (GROUPED) sync = GroupSync{1 + pr, C::T};
-#pragma unroll 1
-  for (int c = 0; c < p.cout; ++c) {
-    float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
-    cpair v[16];
+  auto tile_of = [&](int c) {
+    return p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+  };
+  auto load_in = [&](int c, float4 (&dst)[C::H]) {
+    const float2* tl = tile_of(c);
 #pragma unroll
     for (int m = 0; m < C::H; ++m) {
       const int n = j + m * C::T;
-      v[m] = n < ny ? p_from(*(const float4*)(tile + (long long)n * W)) : pz();
+      dst[m] = n < ny ? *(const float4*)(tl + (long long)n * W) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  if (PF && tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
+  float4 nxt[RP ? C::H : 1];
+  if constexpr (RP) load_in(0, nxt);
+#pragma unroll 1
+  for (int c = 0; c < p.cout; ++c) {
+    float2* tile = tile_of(c);
+    if (PF && tid == 0 && c + 1 < p.cout) l2_prefetch(tile_of(c + 1) - w, (unsigned)(ny * W * 8));
+    cpair v[16];
+    if constexpr (RP) {
+#pragma unroll
+      for (int m = 0; m < C::H; ++m) v[m] = p_from(nxt[m]);
+      if (c + 1 < p.cout) load_in(c + 1, nxt);
+    } else {
+#pragma unroll
+      for (int m = 0; m < C::H; ++m) {
+        const int n = j + m * C::T;
+        v[m] = n < ny ? p_from(*(const float4*)(tile + (long long)n * W)) : pz();
+      }
     }
 #pragma unroll
     for (int m = C::H; m < 16; ++m) v[m] = pz();
@@ -625,14 +731,36 @@ static int launch_rows_inv(cudaStream_t s, const RsLaunch& p) {
   return XL_OK;
 }
 
-template <int LOGQ, bool GROUPED>
+template <int LOGQ, bool GROUPED, bool PF = false, bool RP = false>
 static int launch_cols_pair(cudaStream_t st, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
   using K = RsColPair<LOGQ, GROUPED>;
-  cudaError_t e = allow_smem(rs_cols_conv_p<LOGQ, GROUPED>, K::SMEM);
+  cudaError_t e = allow_smem(rs_cols_conv_p<LOGQ, GROUPED, PF, RP>, K::SMEM);
   if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv_p smem");
-  rs_cols_conv_p<LOGQ, GROUPED><<<dim3(p.B, C::P / C::CW), K::THREADS, K::SMEM, st>>>(p);
+  rs_cols_conv_p<LOGQ, GROUPED, PF, RP><<<dim3(p.B, C::P / C::CW), K::THREADS, K::SMEM, st>>>(p);
   XL_CHECK_LAUNCH("rs_cols_conv_p");
+  return XL_OK;
+}
+
+template <int LOGQ, int CWK, int NGRP>
+static int launch_cols_g(cudaStream_t st, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  using K = RsColShape<LOGQ, CWK, NGRP>;
+  cudaError_t e = allow_smem(rs_cols_conv_g<LOGQ, CWK, NGRP>, K::SMEM);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv_g smem");
+  rs_cols_conv_g<LOGQ, CWK, NGRP><<<dim3(p.B, C::P / CWK), K::THREADS, K::SMEM, st>>>(p);
+  XL_CHECK_LAUNCH("rs_cols_conv_g");
+  return XL_OK;
+}
+
+template <int LOGQ, bool PF>
+static int launch_cols(cudaStream_t st, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
+  cudaError_t e = allow_smem(rs_cols_conv<LOGQ, PF>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
+  rs_cols_conv<LOGQ, PF><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
+  XL_CHECK_LAUNCH("rs_cols_conv");
   return XL_OK;
 }
 
@@ -649,11 +777,12 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     if constexpr (LOGQ >= 9 && LOGQ <= 11) {
       if (var == 1) return launch_cols_pair<LOGQ, false>(st, p);
       if (var == 2) return launch_cols_pair<LOGQ, true>(st, p);
+      if (var == 3) return launch_cols<LOGQ, true>(st, p);
+      if (var == 4) return launch_cols_pair<LOGQ, false, true, true>(st, p);
+      if (var == 5) return launch_cols_g<LOGQ, C::CW, 2>(st, p);
+      if (var == 6) return launch_cols_g<LOGQ, C::CW / 2, 1>(st, p);
     }
-    const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
-    if ((e = allow_smem(rs_cols_conv<LOGQ>, sm)) != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
-    rs_cols_conv<LOGQ><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
-    XL_CHECK_LAUNCH("rs_cols_conv");
+    return launch_cols<LOGQ, false>(st, p);
   } else {
     const bool epi = p.post.nops > 0 || (p.adjoint && p.cout == 3);
     if (p.cout == 1) return epi ? launch_rows_inv<LOGQ, 1, true>(st, p) : launch_rows_inv<LOGQ, 1, false>(st, p);

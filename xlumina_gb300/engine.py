@@ -667,10 +667,13 @@ class RsCall:
         self._keep = (comps, specs, spec_ptrs, spec_index, work, zt, list(pre or ()), list(post or ()))
 
     def run(self):
+        _lib.check_device_status()     # an earlier launch's wait that ran out is reported here
         _lib.check(lib().xl_rs_propagate(stream_handle(), ctypes.byref(self.args)), "xl_rs_propagate")
         return self.outs
 
     def stage(self, s: int):
+        if s == 0:
+            _lib.check_device_status()
         _lib.check(lib().xl_rs_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_rs_stage")
 
 
@@ -981,10 +984,13 @@ class CztCall:
                       fin, fout)
 
     def run(self):
+        _lib.check_device_status()     # an earlier launch's wait that ran out is reported here
         _lib.check(lib().xl_czt(stream_handle(), ctypes.byref(self.args)), "xl_czt")
         return self.outs
 
     def stage(self, s: int):
+        if s == 0:
+            _lib.check_device_status()
         _lib.check(lib().xl_czt_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_czt_stage")
 
 
@@ -1270,3 +1276,72 @@ def beam_splitter_backward(a, b, m, gouts, want_a=True, want_b=True, want_m=True
     ga = gin[0:2] if want_a else None
     gb = gin[2:4] if (want_b and b is not None) else None
     return ga, gb, (dth if kind != _lib.XL_BS_MATRIX else s)
+
+
+# ------------------------------------------------------ fused loss epilogues --
+
+def _loss_planes(t: torch.Tensor):
+    """(contiguous planes, count, plane stride, complex?) of a (..., ny, nx)
+    complex64 field or float32 intensity."""
+    cplx = t.is_complex()
+    t = (t.to(torch.complex64) if cplx else t.to(torch.float32)).contiguous()
+    ny, nx = t.shape[-2:]
+    return t, t.numel() // (ny * nx), ny * nx, cplx
+
+
+def area_loss(x: torch.Tensor):
+    """small_area_hybrid per plane (loss_functions.py:24-40) of intensities
+    or, for a complex field, of its intensity |x|^2, in two fused passes.
+    Returns (losses of shape x.shape[:-2], the work buffer its gradient needs)."""
+    t, n, ps, cplx = _loss_planes(x)
+    L = lib()
+    work = torch.empty(max(1, L.xl_loss_work_bytes(n, ps) // 8), dtype=torch.float64, device=t.device)
+    out = torch.empty(n, dtype=torch.float32, device=t.device)
+    _lib.check(L.xl_area_loss(stream_handle(), n, ps, int(cplx), t.data_ptr(), ps, work.data_ptr(), out.data_ptr()),
+               "xl_area_loss")
+    return out.reshape(x.shape[:-2]), work
+
+
+def area_loss_grad(x: torch.Tensor, work: torch.Tensor, g: torch.Tensor) -> torch.Tensor:
+    t, n, ps, cplx = _loss_planes(x)
+    g = g.to(device=t.device, dtype=torch.float32).reshape(-1).contiguous()
+    gin = torch.empty(t.shape, dtype=t.dtype, device=t.device)
+    _lib.check(lib().xl_area_loss_grad(stream_handle(), n, ps, int(cplx), t.data_ptr(), ps, work.data_ptr(),
+                                       g.data_ptr(), gin.data_ptr()), "xl_area_loss_grad")
+    return gin
+
+
+def _target_planes(target: torch.Tensor, ny, nx, n):
+    tg = target.to(torch.float32)
+    if tg.numel() == ny * nx:
+        return tg.reshape(ny, nx).contiguous(), 0
+    if tg.numel() != n * ny * nx:
+        raise ValueError(f"target of shape {tuple(target.shape)} does not match {n} planes of {ny}x{nx}")
+    return tg.contiguous(), ny * nx
+
+
+def norm_intensity_mse(x: torch.Tensor, target: torch.Tensor):
+    """The 4f tables' normalised intensity MSE per plane
+    (experiments/four_f_optical_table.py:129-141): In = I / sum I,
+    sum((In - T)^2) / npix.  Returns (losses, work buffer)."""
+    t, n, ps, cplx = _loss_planes(x)
+    ny, nx = t.shape[-2:]
+    tg, tps = _target_planes(target, ny, nx, n)
+    L = lib()
+    work = torch.empty(max(1, L.xl_loss_work_bytes(n, ps) // 8), dtype=torch.float64, device=t.device)
+    out = torch.empty(n, dtype=torch.float32, device=t.device)
+    _lib.check(L.xl_norm_intensity_mse(stream_handle(), n, ps, int(cplx), t.data_ptr(), ps, tg.data_ptr(), tps,
+                                       work.data_ptr(), out.data_ptr()), "xl_norm_intensity_mse")
+    return out.reshape(x.shape[:-2]), work
+
+
+def norm_intensity_mse_grad(x, target, work, g):
+    t, n, ps, cplx = _loss_planes(x)
+    ny, nx = t.shape[-2:]
+    tg, tps = _target_planes(target, ny, nx, n)
+    g = g.to(device=t.device, dtype=torch.float32).reshape(-1).contiguous()
+    gin = torch.empty(t.shape, dtype=t.dtype, device=t.device)
+    _lib.check(lib().xl_norm_intensity_mse_grad(stream_handle(), n, ps, int(cplx), t.data_ptr(), ps, tg.data_ptr(),
+                                                tps, work.data_ptr(), g.data_ptr(), gin.data_ptr()),
+               "xl_norm_intensity_mse_grad")
+    return gin

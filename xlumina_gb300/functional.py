@@ -9,15 +9,16 @@ The propagators run on the library's kernels: a grid is rebuilt from the
 spacings and output grids passed in (the transfer function depends on
 coordinate differences only), and the stacked (3, N, N) forms run as a
 batch of three fields.  ``Bluestein_method`` and ``compute_fft``, the
-one-axis building blocks, are evaluated with device FFTs (cuFFT through
-torch); the propagators do not use them.
+one-axis building blocks, keep the reference's float64 chirps and run their
+transforms on the library's complex64 line FFTs (xl_fft_lines); the
+propagators do not use them.
 """
 from __future__ import annotations
 
 import numpy as np
 import torch
 
-from . import engine
+from . import _lib, engine
 
 
 def _axis(n, d):
@@ -88,19 +89,42 @@ def compute_np2(x):
     return 2 ** (np.ceil(np.log2(x))).astype(int)
 
 
+def fft_lines(a: torch.Tensor, n: int, dim: int, inverse: bool = False) -> torch.Tensor:
+    """The n-point FFT (n a power of two, up to 8192) of ``a`` along ``dim``,
+    zero-padded or cropped to n as jnp.fft.fft(a, n, axis) does; unnormalised
+    forward, or inverse with the 1/n of jnp.fft.ifft.  Runs in complex64 on the
+    library's line transforms (xl_fft_lines) and returns complex128."""
+    n = int(n)
+    logn = int(np.log2(n))
+    if 1 << logn != n or logn > 13:
+        raise ValueError(f"FFT length must be a power of two up to 8192, got {n}")
+    a = torch.movedim(a, dim, -1)
+    m = a.shape[-1]
+    lines = a.reshape(-1, m)
+    buf = torch.zeros((lines.shape[0], n), dtype=torch.complex64, device=a.device)
+    buf[:, :min(m, n)] = lines[:, :min(m, n)].to(torch.complex64)
+    out = buf if logn >= 5 else torch.empty_like(buf)
+    _lib.check(engine.lib().xl_fft_lines(engine.stream_handle(), logn, buf.shape[0], 1 if inverse else -1,
+                                         buf.data_ptr(), out.data_ptr()), "xl_fft_lines")
+    res = out.to(torch.complex128)
+    if inverse:
+        res = res / n
+    return torch.movedim(res.reshape(a.shape[:-1] + (n,)), -1, dim)
+
+
 def compute_fft(x, D1, D2, Dm, m, n, mp, M_out, np2):
     """wave_optics.py:385-410: Bluestein's convolution along axis 0 of an (m, n)
-    array (length-np2 device FFTs); returns (b, h)."""
+    array (length-np2 transforms on the library's line FFTs); returns (b, h)."""
     dev = engine.device()
     x = torch.as_tensor(np.asarray(x) if not isinstance(x, torch.Tensor) else x, device=dev).to(torch.complex128)
     A = np.exp(1j * 2 * np.pi * D1 / Dm)
     W = np.exp(-1j * 2 * np.pi * (D2 - D1) / (M_out * Dm))
     kk = np.arange(-m + 1, max(M_out - 1, m - 1) + 1, dtype=np.float64)
     h = torch.as_tensor(W ** (kk ** 2 / 2), device=dev)
-    ft = torch.fft.fft(1 / h[:mp + 1], int(np2))
+    ft = fft_lines(1 / h[:mp + 1], np2, 0)
     b = torch.as_tensor(A ** (-np.arange(m, dtype=np.float64)), device=dev) * h[m - 1:2 * m - 1]
-    B = torch.fft.fft(x * b[:, None], int(np2), dim=0)
-    return torch.fft.ifft(B * ft[:, None], dim=0), h
+    B = fft_lines(x * b[:, None], np2, 0)
+    return fft_lines(B * ft[:, None], np2, 0, inverse=True), h
 
 
 def Bluestein_method(x, f1, f2, Dm, M_out):

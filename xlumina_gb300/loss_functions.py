@@ -11,16 +11,36 @@ def _t(a):
 
 
 def small_area_hybrid(detected_intensity):
-    """loss_functions.py:24-40: area above 0.7*max over the enclosed normalised intensity."""
+    """loss_functions.py:24-40: area above 0.7*max over the enclosed normalised
+    intensity, in two fused libxlgb passes with a hand-written gradient (a
+    CUDA tensor; other inputs go through torch)."""
     I = _t(detected_intensity)
+    if I.is_cuda:
+        return autograd.area_loss(I)
     In = I / (torch.sum(I) + 1e-08)
     mask = (In > 0.7 * torch.max(In)).to(In.dtype)
     return torch.sum(mask) / (torch.sum(mask * In) + 1e-08)
 
 
 def vectorized_loss_hybrid(detected_intensities):
-    """loss_functions.py:42-50."""
-    return torch.stack([small_area_hybrid(i) for i in _t(detected_intensities)])
+    """loss_functions.py:42-50: small_area_hybrid of every plane (one fused launch on the GPU)."""
+    I = _t(detected_intensities)
+    if I.is_cuda:
+        return autograd.area_loss(I)
+    return torch.stack([small_area_hybrid(i) for i in I])
+
+
+def small_area_hybrid_field(field):
+    """small_area_hybrid of |field|^2 per plane, the intensity formed inside
+    the fused kernels (no intensity tensor; the gradient goes to the field)."""
+    return autograd.area_loss(field)
+
+
+def normalized_intensity_mse(field, target):
+    """The 4f tables' loss per plane (experiments/four_f_optical_table.py:129-141):
+    In = |field|^2 / sum |field|^2, sum((In - target)^2) / npix, fused, with
+    the gradient to the field."""
+    return autograd.norm_intensity_mse(field, target)
 
 
 def MSE_Intensity(input_light, target_light):

@@ -23,6 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
+from . import _lib
 from . import autograd, engine
 
 
@@ -196,10 +197,18 @@ class Server:
             ev, reqs, results, nb, _ = item
             self._bytes -= nb
             now = time.perf_counter()
+            try:   # a kernel wait that ran out: the batch's results are not valid
+                _lib.check_device_status()
+                err = None
+            except _lib.XlError as e:
+                err = e
             for r, res in zip(reqs, results):
                 self.latencies.append(now - r.t_arrival)
                 self.completed += 1
-                r.future.set_result(res)
+                if err is None:
+                    r.future.set_result(res)
+                else:
+                    r.future.set_exception(err)
         return bool(done)
 
     def _take_batch(self):

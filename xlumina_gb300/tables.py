@@ -79,6 +79,11 @@ class FourFTable:
     def intensities(self, inputs=None, tables=None):
         """The output intensities of the tables, each normalised to sum 1
         (B, m, m).  ``tables``: a slice of the batch."""
+        I = torch.abs(self.output_field(inputs, tables)) ** 2
+        return I / torch.sum(I, dim=(-2, -1), keepdim=True)
+
+    def output_field(self, inputs=None, tables=None):
+        """The tables' output fields (B, m, m) (a slice of the batch with ``tables``)."""
         sl = slice(None) if tables is None else tables
         inputs = self.inputs[sl] if inputs is None else inputs
         p1 = self.phase1[sl] if self.independent else self.phase1
@@ -90,16 +95,15 @@ class FourFTable:
         l3, _ = oe.lens(l2, self.lens_r, (self.f, self.f))
         l4 = l3.CZT(self.f, self.xo, self.yo)
         l5, _ = oe.SLM(l4, p2, self.m)
-        I = torch.abs(l5.CZT(self.f).field) ** 2
-        return I / torch.sum(I, dim=(-2, -1), keepdim=True)
+        return l5.CZT(self.f).field
 
     def loss(self, inputs=None, target=None, tables=None):
         """Mean over the tables of the normalised intensity MSE
-        (experiments/four_f_optical_table.py:129-141)."""
+        (experiments/four_f_optical_table.py:129-141), fused into two
+        reduction passes over the output fields with a hand-written gradient."""
         sl = slice(None) if tables is None else tables
         target = self.target[sl] if target is None else target
-        I = self.intensities(inputs, tables)
-        return torch.mean(torch.sum((I - target) ** 2, dim=(-2, -1)) / (self.m * self.m))
+        return torch.mean(lf.normalized_intensity_mse(self.output_field(inputs, tables), target))
 
     def step(self, inputs=None, target=None, tables=None):
         self.opt.zero_grad(set_to_none=True)
@@ -157,22 +161,29 @@ class HighNATable:
         e, t = (self.eta, self.theta) if self.eta.dim() == 2 else (self.eta[b], self.theta[b])
         return host(e), host(t), host(self.alpha[b]), host(self.phi[b])
 
-    def _spot_intensity(self):
+    def _focal_ez(self):
         light = VectorizedLight(self.x, self.y, self.wavelength)
         light.Ex = self.Ex.expand(self.B, self.n, self.n)
         light.Ey = self.Ey.expand(self.B, self.n, self.n)
         focus = oe.VCZT_objective_lens(oe.sSLM(oe.LCD(light, self.eta, self.theta), self.alpha, self.phi),
                                        self.r, self.f, self.xo, self.yo)
-        return torch.abs(focus.Ez) ** 2
+        return focus.Ez
+
+    def _spot_intensity(self):
+        return torch.abs(self._focal_ez()) ** 2
+
+    def _table_losses(self):
+        # the area loss of |Ez|^2 in two fused passes, gradient to Ez
+        return lf.small_area_hybrid_field(self._focal_ez())
 
     def loss(self):
         if self.checkpoint and torch.is_grad_enabled():
             # the focal fields are recomputed in the backward instead of kept
             from torch.utils.checkpoint import checkpoint
-            I = checkpoint(self._spot_intensity, use_reentrant=False)
+            losses = checkpoint(self._table_losses, use_reentrant=False)
         else:
-            I = self._spot_intensity()
-        return small_area_hybrid_batched(I)
+            losses = self._table_losses()
+        return torch.mean(losses)
 
     def step(self):
         self.opt.zero_grad(set_to_none=True)
