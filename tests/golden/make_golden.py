@@ -348,5 +348,38 @@ def main(ref_root):
               vmse_phase=lf.vMSE_Phase(la, lb), I6=I6, loss_hybrid=lf.vectorized_loss_hybrid(I6))
 
 
+    # 18. host helpers: build_CZT_grid and the minimum trustworthy RS / VRS
+    # distances (get_RS_minimum_z / get_VRS_minimum_z print the value and
+    # return None; the printed number is captured).
+    from xlumina import wave_optics as wo
+
+    def printed(fn):
+        buf = io.StringIO()
+        with contextlib.redirect_stdout(buf):
+            ret = fn()
+        return ret, float(buf.getvalue().split(":")[-1])
+
+    grids = []
+    for (z, wl, nin, hin, nxo, nyo, hxo, hyo) in ((2500.0, 0.6, 36, 140.0, 24, 20, 30.0, 20.0),
+                                                   (5.0e4, 0.532, 64, 750.0, 32, 32, 400.0, 400.0)):
+        xin, yin = tb.space(hin, nin)
+        xo, yo = np.linspace(-hxo, hxo, nxo), np.linspace(-hyo, hyo, nyo)
+        cnx, cny, cdx, cdy, Xo, Yo, Dm, fy1, fy2, fx1, fx2 = wo.build_CZT_grid(z, wl, xin, yin, xo, yo)
+        grids.append(dict(z=z, wl=wl, xin=xin, yin=yin, xo=xo, yo=yo, scal=np.array(
+            [cnx, cny, cdx, cdy, Dm, fy1, fy2, fx1, fx2], dtype=np.float64), Xo=Xo, Yo=Yo))
+    minz = []
+    for (h, n, wl, nidx, qf) in ((150.0, 64, 0.65, 1, 1), (1000.0, 1024, 0.633, 1, 2), (500.0, 128, 0.532, 1.5, 1),
+                                 (5.0, 16, 0.6, 1, 1), (0.5, 64, 0.6, 1, 1)):
+        xx, yy = tb.space(h, n)
+        sl = ScalarLight(xx, yy, wl)
+        ret_s, zs = printed(lambda: sl.get_RS_minimum_z(n=nidx, quality_factor=qf))
+        vl = VectorizedLight(xx, yy, wl)
+        ret_v, zv = printed(lambda: vl.get_VRS_minimum_z(n=nidx, quality_factor=qf))
+        assert ret_s is None and ret_v is None
+        minz.append((h, n, wl, nidx, qf, zs, zv))
+    _save("host_helpers", **{f"g{i}_{k}": v for i, g in enumerate(grids) for k, v in g.items()},
+          minz=np.array(minz, dtype=np.float64))
+
+
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XLUMINA_REF", ""))

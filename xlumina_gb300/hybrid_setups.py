@@ -166,20 +166,29 @@ def _detect(lights, r, f, xout, yout):
     return _split_light(det, len(lights), tuple(l0.Ex.shape[:-2]))
 
 
-def _run_edges_checkpointed(jobs):
-    """_run_edges with activation checkpointing: the fields inside the
-    wavefront's edges (a building block's intermediate light, the batched
-    VRS's stacked inputs) are not kept for the backward; it recomputes them
-    from the wavefront's inputs (torch.utils.checkpoint, non-reentrant)."""
-    from torch.utils.checkpoint import checkpoint
+def _flatten_lights(lights):
+    """(tensors, spec) of a list of lights (None kept as None): each light as
+    its (Ex, Ey, Ez) planes, for a checkpointed segment's inputs / outputs."""
+    flat, spec = [], []
+    for light in lights:
+        if light is None:
+            spec.append(None)
+            continue
+        spec.append((light.x, light.y, light.wavelength))
+        flat += [light.Ex, light.Ey, light.Ez]
+    return flat, spec
 
+
+def _unflatten_lights(flat, spec):
     from .vectorized_optics import VectorizedLight
-
-    def seg():
-        return tuple(t for light in _run_edges(jobs) for t in (light.Ex, light.Ey, light.Ez))
-    flat = checkpoint(seg, use_reentrant=False)
-    return [VectorizedLight._wrap(l.x, l.y, l.wavelength, list(flat[3 * k:3 * k + 3]))
-            for k, (_, l) in enumerate(jobs)]
+    out, i = [], 0
+    for sp in spec:
+        if sp is None:
+            out.append(None)
+            continue
+        out.append(VectorizedLight._wrap(sp[0], sp[1], sp[2], list(flat[i:i + 3])))
+        i += 3
+    return out
 
 
 def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, yout, checkpoint=False):
@@ -194,13 +203,17 @@ def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, you
     The grid runs by wavefronts (the splitters with i + j = k depend only on
     wavefront k - 1): the free-space edges leaving a wavefront run as one
     batched VRS, and the detectors as one batched focus.  ``checkpoint``
-    recomputes each wavefront's edges in the backward instead of keeping
-    their intermediate fields (deep tables, many noisy copies)."""
+    (False, True, an int K or a checkpointing.CheckpointPolicy) stores only
+    the inputs of every K-th wavefront, within a memory budget if the policy
+    has one, and recomputes the others' fields in the backward."""
+    from .checkpointing import CheckpointPolicy
     rows, cols = len(thetas), len(thetas[0])
+    nwf = rows + cols - 1
     a_in = {(0, j): top[j] for j in range(cols)}
     b_in = {(i, 0): left[i] for i in range(rows)}
     det_in = [None] * len(detectors)
-    for k in range(rows + cols - 1):
+
+    def wavefront(k, a_in, b_in, det_in):
         cells = [(i, k - i) for i in range(rows) if 0 <= k - i < cols]
         jobs, targets = [], []
         for i, j in cells:
@@ -215,14 +228,56 @@ def run_grid(top, left, thetas, horizontal, vertical, detectors, r, f, xout, you
                 if (di, dj) == (i, j):
                     jobs.append((edge, c if port == "c" else d))
                     targets.append(("det", q))
-        run = _run_edges_checkpointed if (checkpoint and torch.is_grad_enabled()) else _run_edges
-        for (kind, key), light in zip(targets, run(jobs)):
+        for (kind, key), light in zip(targets, _run_edges(jobs)):
             if kind == "a":
                 a_in[key] = light
             elif kind == "b":
                 b_in[key] = light
             else:
                 det_in[key] = light
+
+    policy = CheckpointPolicy.coerce(checkpoint)
+    if policy is None or not torch.is_grad_enabled():
+        for k in range(nwf):
+            wavefront(k, a_in, b_in, det_in)
+        return _detect(det_in, r, f, xout, yout)
+
+    from torch.utils.checkpoint import checkpoint as torch_checkpoint
+    # output lights per wavefront, for the budget estimate
+    n_out = [sum((j + 1 < cols) + (i + 1 < rows) + sum((di, dj) == (i, j) for di, dj, _, _ in detectors)
+                 for i in range(rows) for j in [k - i] if 0 <= j < cols) for k in range(nwf)]
+    src = next(l for l in list(top) + list(left) if l is not None)
+    light_bytes = 3 * src.Ex.numel() * src.Ex.element_size()
+    for k0, k1, ck in policy.segments(n_out, light_bytes):
+        if not ck:
+            for k in range(k0, k1):
+                wavefront(k, a_in, b_in, det_in)
+            continue
+        # the segment's state: the lights entering wavefronts >= k0 and the detectors so far
+        a_keys = sorted(key for key in a_in if sum(key) >= k0)
+        b_keys = sorted(key for key in b_in if sum(key) >= k0)
+        flat_in, spec_in = _flatten_lights([a_in[q] for q in a_keys] + [b_in[q] for q in b_keys] + det_in)
+        out_spec = {}
+
+        def seg(*flat, a_keys=a_keys, b_keys=b_keys, spec_in=spec_in, k0=k0, k1=k1, out_spec=out_spec):
+            lights = _unflatten_lights(flat, spec_in)
+            sa = dict(zip(a_keys, lights[:len(a_keys)]))
+            sb = dict(zip(b_keys, lights[len(a_keys):len(a_keys) + len(b_keys)]))
+            sd = list(lights[len(a_keys) + len(b_keys):])
+            for k in range(k0, k1):
+                wavefront(k, sa, sb, sd)
+            ka = sorted(key for key in sa if sum(key) >= k1)
+            kb = sorted(key for key in sb if sum(key) >= k1)
+            fo, so = _flatten_lights([sa[q] for q in ka] + [sb[q] for q in kb] + sd)
+            out_spec.update(ka=ka, kb=kb, spec=so)
+            return tuple(fo)
+
+        flat_out = torch_checkpoint(seg, *flat_in, use_reentrant=False)
+        lights = _unflatten_lights(flat_out, out_spec["spec"])
+        na, nb = len(out_spec["ka"]), len(out_spec["kb"])
+        a_in = dict(zip(out_spec["ka"], lights[:na]))
+        b_in = dict(zip(out_spec["kb"], lights[na:na + nb]))
+        det_in = list(lights[na + nb:])
     return _detect(det_in, r, f, xout, yout)
 
 
