@@ -136,13 +136,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(inside)}
 
 
-# DRAM bytes (read + write) per 2048^2 VRS field of each pass, from the ncu
-# captures summarised in profiles/rs_kernels_vrs2048.md.  The column pass's
-# figure is from a capture of the bench's own launch (8 fields at 4 distances,
-# so pairs of fields share a transfer spectrum); the row passes' are from a
-# batch-2 capture scaled per field (every field is an independent slice of
-# those launches).
+# DRAM bytes (read + write) per 2048^2 VRS field of each pass, measured by
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum, one replay pass).  The
+# column pass's figure is from a capture of this benchmark's own 8-field
+# launch (4 distances, so pairs of fields share a transfer spectrum) with
+# NCU_TRAFFIC_COMMAND below; the row passes' from a batch-2 capture (--batch 2)
+# scaled per field (every field is an independent slice of those launches).
+# The column-pass variants move the same bytes (within 2 % at batch 2).
 NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 276.15e6, "rs_cols_conv": 478.88e6, "rs_rows_inv": 283.60e6}
+NCU_TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum "
+                       "--clock-control none -k regex:rs_cols -s 1 -c 1 python bench.py --steps 10 --warmup 3 "
+                       "--no-cpu-baseline --no-fwd-bwd --no-serving")
 
 
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
@@ -424,8 +428,8 @@ def run_gpu(args):
                      "frac": achieved / peak,
                      "traffic": (NCU_TRAFFIC_PER_FIELD[names[dom]] * B
                                  if NCU_TRAFFIC_PER_FIELD[names[dom]] is not None else None),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "profiles/rs_kernels_vrs2048.md (the bench's own 8-field launch)",
+                     "traffic_source": "ncu capture of this benchmark's own 8-field launch, "
+                                       "dram__bytes_read.sum + dram__bytes_write.sum: " + NCU_TRAFFIC_COMMAND,
                      "peak_source": peak_src,
                      "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
         "rel_l2": parity,
@@ -441,7 +445,8 @@ def run_gpu(args):
                                             "pairs interleaved in warps; 2 packed, pairs in barrier groups; "
                                             "3 one line per thread with L2 prefetch; 4 packed interleaved "
                                             "with L2 and register prefetch; 5 one line per thread, two "
-                                            "barrier groups; 6 one line per thread, two CTAs per SM"},
+                                            "barrier groups; 6 one line per thread, two CTAs per SM; 7 as 5 with "
+                                            "the groups started half a component apart"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -417,6 +417,17 @@ int xl_beam_splitter_backward(void* stream, const XlBsArgs* args, const void* co
 int xl_re_inner(void* stream, int planes, long long npix, const void* a, long long a_pstride, const void* b,
                 long long b_pstride, void* work, void* out);
 
+/* Per-plane MSE of kind 0 intensity (= xl_mse_intensity), 1 amplitude
+ * sum (|a| - |b|)^2 / npix (MSE_Amplitude, loss_functions.py:109-121) or
+ * 2 phase sum (arg a - arg b)^2 / npix (MSE_Phase, :123-135; vMSE_* at
+ * :61-107 are the per-component forms); work and out as xl_mse_intensity.
+ * The gradient takes gloss per plane and writes ga and / or gb (torch's
+ * convention for complex tensors; zero where |a| or |b| is zero). */
+int xl_plane_mse(void* stream, int kind, int planes, long long npix, const void* a, long long a_pstride,
+                 const void* b, long long b_pstride, void* work, void* out);
+int xl_plane_mse_grad(void* stream, int kind, int planes, long long npix, const void* a, long long a_pstride,
+                      const void* b, long long b_pstride, const void* gloss, void* ga, void* gb);
+
 /* ---- Fused loss epilogues (planes of npix pixels; complex_in = 1: the
  * planes are complex64 fields and the intensity |u|^2 is formed in the
  * kernel; 0: float32 intensities; in_pstride in elements).  Two reduction

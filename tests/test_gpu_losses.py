@@ -160,3 +160,36 @@ def test_normalised_intensity_mse_values_and_gradients(shared_target):
     (Lr * w.double()).sum().backward()
     assert rel_l2(L.detach().cpu().numpy(), Lr.detach().cpu().numpy()) < 1e-5
     assert rel_l2(u.grad.cpu().numpy(), ur.grad.cpu().numpy()) < 1e-4
+
+
+def test_amplitude_and_phase_mse_golden_and_gradients():
+    """MSE_Amplitude / MSE_Phase and their per-component forms fused on the
+    device: against the reference's values (losses_more.npz) and torch
+    autograd of the formulas in complex128."""
+    import torch
+
+    import xlumina_gb300.loss_functions as lf
+    from xlumina_gb300.vectorized_optics import VectorizedLight
+    g = golden("losses_more")
+    a3 = torch.as_tensor(g["a3"].astype(np.complex64), device="cuda")
+    b3 = torch.as_tensor(g["b3"].astype(np.complex64), device="cuda")
+    assert float(lf.MSE_Amplitude(a3[0], b3[0])) == pytest.approx(float(g["mse_amplitude"]), rel=1e-5)
+    assert float(lf.MSE_Phase(a3[0], b3[0])) == pytest.approx(float(g["mse_phase"]), rel=1e-5)
+    x = np.linspace(-10, 10, 20)
+    la, lb = VectorizedLight(x, x, 0.5), VectorizedLight(x, x, 0.5)
+    la.Ex, la.Ey, la.Ez = a3[0], a3[1], a3[2]
+    lb.Ex, lb.Ey, lb.Ez = b3[0], b3[1], b3[2]
+    assert rel_l2(lf.vMSE_Amplitude(la, lb).cpu().numpy(), g["vmse_amplitude"]) < 1e-5
+    assert rel_l2(lf.vMSE_Phase(la, lb).cpu().numpy(), g["vmse_phase"]) < 1e-5
+    rng = np.random.default_rng(31)
+    w = torch.as_tensor(rng.uniform(0.5, 2.0, 3).astype(np.float32), device="cuda")
+    for fn, ref_fn in ((lf.MSE_Amplitude, lambda u, v: (torch.abs(u) - torch.abs(v)) ** 2),
+                       (lf.MSE_Phase, lambda u, v: (torch.angle(u) - torch.angle(v)) ** 2)):
+        a = a3.clone().requires_grad_(True)
+        b = b3.clone().requires_grad_(True)
+        (fn(a, b) * w).sum().backward()
+        ar = a3.to(torch.complex128).requires_grad_(True)
+        br = b3.to(torch.complex128).requires_grad_(True)
+        (torch.sum(ref_fn(ar, br), dim=(-2, -1)) / 400 * w.double()).sum().backward()
+        assert rel_l2(a.grad.cpu().numpy(), ar.grad.cpu().numpy()) < 1e-4
+        assert rel_l2(b.grad.cpu().numpy(), br.grad.cpu().numpy()) < 1e-4

@@ -39,10 +39,10 @@ def variants():
 def test_variant_table_bounds():
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 7
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 8
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(99, 12) == 0
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 7) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 8) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
     assert lib.xl_get_kernel_variant(-1, 12) == _lib.XL_EINVAL
 
@@ -55,7 +55,7 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     select, count = variants
     logp = engine.rs_logq(n, n) + 1
     nv = count(logp)
-    assert nv == 7
+    assert nv == 8
     x, y = ref.space(1000.0, n)
     rng = np.random.default_rng(n + vector)
     Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
@@ -80,7 +80,7 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
             assert rel_l2(g, g0) < 1e-6, v
 
 
-@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6, 7])
 def test_rs_column_variants_adjoint_and_batch(variants, v):
     """The adjoint (conjugate spectrum) and a batch with a distance per entry
     through a packed variant equal the one-line kernel's results."""

@@ -174,6 +174,12 @@ SIGNATURES = {
     "xl_mse_intensity_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
                                              ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "xl_plane_mse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p,
+                                    ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                    ctypes.c_void_p]),
+    "xl_plane_mse_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_longlong,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "xl_loss_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "xl_area_loss": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p]),

@@ -198,25 +198,26 @@ def apply_ops(base, ops, ny, nx):
 
 
 class _MseIntensity(torch.autograd.Function):
-    """Intensity MSE per plane with the hand-written gradient of libxlgb."""
+    """Intensity (amplitude, phase) MSE per plane with the hand-written gradient of libxlgb."""
 
     @staticmethod
-    def forward(ctx, a, b):
+    def forward(ctx, a, b, kind="intensity"):
         ctx.save_for_backward(a, b)
-        return engine.mse_intensity(a, b)
+        ctx.kind = kind
+        return engine.mse_intensity(a, b, kind)
 
     @staticmethod
     def backward(ctx, g):
         a, b = ctx.saved_tensors
         want_a, want_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
-        ga, gb = engine.mse_intensity_grad(a, b, g, want_a, want_b)
+        ga, gb = engine.mse_intensity_grad(a, b, g, want_a, want_b, ctx.kind)
         if gb is not None and tuple(b.shape) != tuple(gb.shape):   # a broadcast target
             gb = gb.reshape((-1,) + tuple(b.shape[-2:])).sum(0).reshape(b.shape)
-        return ga, gb
+        return ga, gb, None
 
 
-def mse_intensity(a, b):
-    return _MseIntensity.apply(a, b)
+def mse_intensity(a, b, kind="intensity"):
+    return _MseIntensity.apply(a, b, kind)
 
 
 class _AreaLoss(torch.autograd.Function):

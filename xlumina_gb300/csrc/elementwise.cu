@@ -192,7 +192,9 @@ __global__ void highna_plane_kernel(int ny, int nx, XlOp op, float* out) {
 constexpr int MSE_THREADS = 256;
 
 // Per-plane reductions of a pixel function f(a_i, b_i): KIND 0 the intensity
-// MSE term (|a|^2 - |b|^2)^2, KIND 1 the real inner product Re(conj(a) b).
+// MSE term (|a|^2 - |b|^2)^2, KIND 1 the real inner product Re(conj(a) b),
+// KIND 2 the amplitude term (|a| - |b|)^2, KIND 3 the phase term
+// (arg a - arg b)^2 (loss_functions.py:109-135).
 template <int KIND>
 __global__ void __launch_bounds__(MSE_THREADS) plane_sum_partial(const float2* __restrict__ a, long long aps,
                                                                  const float2* __restrict__ b, long long bps,
@@ -207,8 +209,14 @@ __global__ void __launch_bounds__(MSE_THREADS) plane_sum_partial(const float2* _
     if (KIND == 0) {
       const float d = (u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y);
       acc = fmaf(d, d, acc);
-    } else {
+    } else if (KIND == 1) {
       acc = fmaf(u.x, v.x, fmaf(u.y, v.y, acc));
+    } else if (KIND == 2) {
+      const float d = hypotf(u.x, u.y) - hypotf(v.x, v.y);
+      acc = fmaf(d, d, acc);
+    } else {
+      const float d = atan2f(u.y, u.x) - atan2f(v.y, v.x);
+      acc = fmaf(d, d, acc);
     }
   }
   __shared__ float red[MSE_THREADS / 32];
@@ -251,6 +259,41 @@ __global__ void mse_int_grad(const float2* __restrict__ a, long long aps, const 
     const float d = s * ((u.x * u.x + u.y * u.y) - (v.x * v.x + v.y * v.y));
     if (ga) ga[(long long)plane * npix + i] = make_float2(d * u.x, d * u.y);
     if (gb) gb[(long long)plane * npix + i] = make_float2(-d * v.x, -d * v.y);
+  }
+}
+
+// Gradients of the amplitude (KIND 2) and phase (KIND 3) MSE per plane with
+// upstream gradient g[p] (torch's convention, 2 dL/d conj):
+// amplitude: ga = 2 g (|a| - |b|) a / (|a| npix), gb = -2 g (|a| - |b|) b / (|b| npix);
+// phase: ga = 2 g (arg a - arg b) i a / (|a|^2 npix), gb the same with -i b / |b|^2;
+// zero where |a| (|b|) is zero, as torch's abs and angle give.
+template <int KIND>
+__global__ void amp_phase_grad(const float2* __restrict__ a, long long aps, const float2* __restrict__ b,
+                               long long bps, long long npix, const float* __restrict__ g, float two_inv_n,
+                               float2* __restrict__ ga, float2* __restrict__ gb) {
+  const int plane = blockIdx.y;
+  a += (long long)plane * aps;
+  b += (long long)plane * bps;
+  const float s = g[plane] * two_inv_n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 u = a[i], v = b[i];
+    float2 ru, rv;
+    if (KIND == 2) {
+      const float au = hypotf(u.x, u.y), av = hypotf(v.x, v.y);
+      const float d = s * (au - av);
+      const float fu = au > 0.f ? d / au : 0.f, fv = av > 0.f ? -d / av : 0.f;
+      ru = make_float2(fu * u.x, fu * u.y);
+      rv = make_float2(fv * v.x, fv * v.y);
+    } else {
+      const float d = s * (atan2f(u.y, u.x) - atan2f(v.y, v.x));
+      const float nu = u.x * u.x + u.y * u.y, nv = v.x * v.x + v.y * v.y;
+      const float fu = nu > 0.f ? d / nu : 0.f, fv = nv > 0.f ? -d / nv : 0.f;
+      ru = make_float2(-fu * u.y, fu * u.x);
+      rv = make_float2(-fv * v.y, fv * v.x);
+    }
+    if (ga) ga[(long long)plane * npix + i] = ru;
+    if (gb) gb[(long long)plane * npix + i] = rv;
   }
 }
 
@@ -532,6 +575,59 @@ extern "C" int xl_mse_intensity_grad(void* stream, int planes, long long npix, c
       (const float2*)a, a_pstride, (const float2*)b, b_pstride, npix, (const float*)gloss,
       (float)(4.0 / (double)npix), (float2*)ga, (float2*)gb);
   XL_CHECK_LAUNCH("mse_int_grad");
+  return XL_OK;
+}
+
+extern "C" int xl_plane_mse(void* stream, int kind, int planes, long long npix, const void* a, long long a_pstride,
+                            const void* b, long long b_pstride, void* work, void* out) {
+  if (kind < 0 || kind > 2) {
+    set_error("xl_plane_mse: kind must be 0 (intensity), 1 (amplitude) or 2 (phase), got %d", kind);
+    return XL_EINVAL;
+  }
+  if (kind == 0) return xl_mse_intensity(stream, planes, npix, a, a_pstride, b, b_pstride, work, out);
+  if (planes < 1 || planes > 65535 || npix < 1 || !a || !b || !work || !out) {
+    set_error("xl_plane_mse: bad arguments");
+    return XL_EINVAL;
+  }
+  const int nb = mse_blocks(npix);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 1)
+    plane_sum_partial<2><<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
+                                                                    b_pstride, npix, (double*)work);
+  else
+    plane_sum_partial<3><<<dim3(nb, planes), MSE_THREADS, 0, st>>>((const float2*)a, a_pstride, (const float2*)b,
+                                                                    b_pstride, npix, (double*)work);
+  XL_CHECK_LAUNCH("plane_sum_partial");
+  mse_int_finish<<<(planes + 3) / 4, 128, 0, st>>>((const double*)work, nb, planes, 1.0 / (double)npix,
+                                                    (float*)out);
+  XL_CHECK_LAUNCH("mse_int_finish");
+  return XL_OK;
+}
+
+extern "C" int xl_plane_mse_grad(void* stream, int kind, int planes, long long npix, const void* a,
+                                 long long a_pstride, const void* b, long long b_pstride, const void* gloss, void* ga,
+                                 void* gb) {
+  if (kind < 0 || kind > 2) {
+    set_error("xl_plane_mse_grad: kind must be 0 (intensity), 1 (amplitude) or 2 (phase), got %d", kind);
+    return XL_EINVAL;
+  }
+  if (kind == 0) return xl_mse_intensity_grad(stream, planes, npix, a, a_pstride, b, b_pstride, gloss, ga, gb);
+  if (planes < 1 || planes > 65535 || npix < 1 || !a || !b || !gloss || (!ga && !gb)) {
+    set_error("xl_plane_mse_grad: bad arguments");
+    return XL_EINVAL;
+  }
+  long long nblk = (npix + 255) / 256;
+  if (nblk > 152 * 8) nblk = 152 * 8;
+  const dim3 grid((unsigned)nblk, planes);
+  const float tn = (float)(2.0 / (double)npix);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 1)
+    amp_phase_grad<2><<<grid, 256, 0, st>>>((const float2*)a, a_pstride, (const float2*)b, b_pstride, npix,
+                                            (const float*)gloss, tn, (float2*)ga, (float2*)gb);
+  else
+    amp_phase_grad<3><<<grid, 256, 0, st>>>((const float2*)a, a_pstride, (const float2*)b, b_pstride, npix,
+                                            (const float*)gloss, tn, (float2*)ga, (float2*)gb);
+  XL_CHECK_LAUNCH("amp_phase_grad");
   return XL_OK;
 }
 

@@ -384,7 +384,11 @@ template <int LOGQ, int CWK, int NGRP> struct RsColShape {
   static_assert(C::CW % CWK == 0 && CWK % NGRP == 0 && (CWG * C::T) % 32 == 0, "column CTA shape");
 };
 
-template <int LOGQ, int CWK, int NGRP>
+// STAGGER (two groups): group 1 starts its first component only once group 0
+// has finished that component's forward transform, so that the groups run
+// half a component apart and one's loads and exchanges meet the other's
+// arithmetic instead of its own.
+template <int LOGQ, int CWK, int NGRP, bool STAGGER = false>
 __global__ void __launch_bounds__(RsColShape<LOGQ, CWK, NGRP>::THREADS, RsColShape<LOGQ, CWK, NGRP>::MINB)
     rs_cols_conv_g(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
@@ -412,6 +416,9 @@ __global__ void __launch_bounds__(RsColShape<LOGQ, CWK, NGRP>::THREADS, RsColSha
   Sync sync;
   if constexpr (NGRP > 1) sync = GroupSync{1 + grp, CWG * C::T};
   if (tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
+  if constexpr (STAGGER && NGRP == 2) {
+    if (grp == 1) asm volatile("bar.sync 3, %0;" ::"r"(K::THREADS) : "memory");
+  }
 #pragma unroll 1
   for (int c = 0; c < p.cout; ++c) {
     const long long tbase = ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W;
@@ -426,6 +433,9 @@ __global__ void __launch_bounds__(RsColShape<LOGQ, CWK, NGRP>::THREADS, RsColSha
 #pragma unroll
     for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
     block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw, sync);
+    if constexpr (STAGGER && NGRP == 2) {
+      if (grp == 0 && c == 0) asm volatile("bar.arrive 3, %0;" ::"r"(K::THREADS) : "memory");
+    }
     const float2* sp = spec;
     asm volatile("" : "+l"(sp));
     if (p.adjoint) {
@@ -742,13 +752,13 @@ static int launch_cols_pair(cudaStream_t st, const RsLaunch& p) {
   return XL_OK;
 }
 
-template <int LOGQ, int CWK, int NGRP>
+template <int LOGQ, int CWK, int NGRP, bool STAGGER = false>
 static int launch_cols_g(cudaStream_t st, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
   using K = RsColShape<LOGQ, CWK, NGRP>;
-  cudaError_t e = allow_smem(rs_cols_conv_g<LOGQ, CWK, NGRP>, K::SMEM);
+  cudaError_t e = allow_smem(rs_cols_conv_g<LOGQ, CWK, NGRP, STAGGER>, K::SMEM);
   if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv_g smem");
-  rs_cols_conv_g<LOGQ, CWK, NGRP><<<dim3(p.B, C::P / CWK), K::THREADS, K::SMEM, st>>>(p);
+  rs_cols_conv_g<LOGQ, CWK, NGRP, STAGGER><<<dim3(p.B, C::P / CWK), K::THREADS, K::SMEM, st>>>(p);
   XL_CHECK_LAUNCH("rs_cols_conv_g");
   return XL_OK;
 }
@@ -781,6 +791,7 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
       if (var == 4) return launch_cols_pair<LOGQ, false, true, true>(st, p);
       if (var == 5) return launch_cols_g<LOGQ, C::CW, 2>(st, p);
       if (var == 6) return launch_cols_g<LOGQ, C::CW / 2, 1>(st, p);
+      if (var == 7) return launch_cols_g<LOGQ, C::CW, 2, true>(st, p);
     }
     return launch_cols<LOGQ, false>(st, p);
   } else {

@@ -1047,8 +1047,12 @@ def _planes(t: torch.Tensor):
     return t, n, ny * nx
 
 
-def mse_intensity(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
-    """sum((|a|^2 - |b|^2)^2) / npix over the last two dims (libxlgb, fixed-order sums)."""
+MSE_KINDS = {"intensity": 0, "amplitude": 1, "phase": 2}
+
+
+def mse_intensity(a: torch.Tensor, b: torch.Tensor, kind: str = "intensity") -> torch.Tensor:
+    """sum((|a|^2 - |b|^2)^2) / npix over the last two dims (libxlgb, fixed-order
+    sums); ``kind`` "amplitude": (|a| - |b|)^2, "phase": (arg a - arg b)^2."""
     a = as_field(a)
     b = as_field(b)
     ny, nx = a.shape[-2:]
@@ -1065,12 +1069,12 @@ def mse_intensity(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     L = lib()
     work = torch.empty(max(1, L.xl_mse_intensity_work_bytes(na, npix) // 8), dtype=torch.float64, device=a.device)
     out = torch.empty(na, dtype=torch.float32, device=a.device)
-    _lib.check(L.xl_mse_intensity(stream_handle(), na, npix, av.data_ptr(), aps, bv.data_ptr(), bps,
-                                  work.data_ptr(), out.data_ptr()), "xl_mse_intensity")
+    _lib.check(L.xl_plane_mse(stream_handle(), MSE_KINDS[kind], na, npix, av.data_ptr(), aps, bv.data_ptr(), bps,
+                              work.data_ptr(), out.data_ptr()), "xl_plane_mse")
     return out.reshape(a.shape[:-2])
 
 
-def mse_intensity_grad(a, b, g, want_a=True, want_b=False):
+def mse_intensity_grad(a, b, g, want_a=True, want_b=False, kind: str = "intensity"):
     """Gradients of ``mse_intensity`` for the upstream gradient ``g`` (shape a.shape[:-2])."""
     a = as_field(a)
     b = as_field(b)
@@ -1083,8 +1087,8 @@ def mse_intensity_grad(a, b, g, want_a=True, want_b=False):
     g = g.to(device=a.device, dtype=torch.float32).reshape(-1).contiguous()
     ga = torch.empty(a.shape, dtype=torch.complex64, device=a.device) if want_a else None
     gb = torch.empty(a.shape, dtype=torch.complex64, device=a.device) if want_b else None
-    _lib.check(lib().xl_mse_intensity_grad(stream_handle(), na, ny * nx, av.data_ptr(), aps, bv.data_ptr(), bps,
-                                           g.data_ptr(), _ptr(ga), _ptr(gb)), "xl_mse_intensity_grad")
+    _lib.check(lib().xl_plane_mse_grad(stream_handle(), MSE_KINDS[kind], na, ny * nx, av.data_ptr(), aps,
+                                       bv.data_ptr(), bps, g.data_ptr(), _ptr(ga), _ptr(gb)), "xl_plane_mse_grad")
     return ga, gb
 
 
