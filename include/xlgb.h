@@ -51,11 +51,14 @@ enum {
   XL_OP_SEPMASK = 6,   /* separable mask colfac[col]*rowfac[row] with FP64 pupil test
                           (thin lens, :678-703); sval[0] != 0 zeroes Ez (vector lens) */
   XL_OP_CMUL = 7,      /* multiply all components by a complex64 plane ptr[0] */
-  XL_OP_HIGHNA = 8     /* high-NA objective lens, optical_elements.py:515-594: ptr[0], ptr[1]
+  XL_OP_HIGHNA = 8,    /* high-NA objective lens, optical_elements.py:515-594: ptr[0], ptr[1]
                           float64 x, y; dval[0] radius, dval[1] focal length, dval[2]
                           sin(theta_max), dval[3] 1/radius^2; Ez derived from Ex, Ey, output
                           (Ex, Ey, Ez).  ptr[2] (optional): the 6 coefficient planes from
                           xl_highna_coefficients, plane stride pbstride (ny*nx) */
+  XL_OP_HIGHNA_EZ = 9  /* the same lens keeping only its Ez row: e0 = K20 Ex + K21 Ey, e1 = e2 = 0
+                          (the focus a loss of |Ez|^2 alone needs, small_area_hybrid on the
+                          Ez detector, hybrid_sharp_optical_table.py); same parameters */
 };
 
 typedef struct {

@@ -65,3 +65,14 @@ def test_variant_tuner_picks_fastest_and_caches(tmp_path):
     assert r2 == {"variant": 1, "ms": {}, "cached": True} and selected[(0, 12)] == 1 and len(calls) == n
     # forced: measured again
     assert t2.best_variant(0, 12, measure, force=True)["variant"] == 1 and len(calls) > n
+
+
+def test_latency_bound_limits_the_batch(tmp_path):
+    """With a bound on the launch time the tuner gives up throughput for latency."""
+    t = BatchTuner(path=str(tmp_path / "l.json"), device_name="dev", candidates=(1, 2, 4, 8, 16), repeats=1)
+    measure = lambda b: 1e-3 + 1e-3 * b   # noqa: E731  (throughput keeps rising with the batch)
+    assert t.best_batch(("vrs", 1024, 1024), measure) == 16
+    assert t.best_batch(("vrs", 1024, 1024), measure, max_launch_s=5.5e-3) == 4
+    assert t.best_batch(("vrs", 1024, 1024), measure, max_launch_s=1e-4) == 1   # none fits: the smallest
+    # cached per bound
+    assert t.best_batch(("vrs", 1024, 1024), lambda b: 1.0, max_launch_s=5.5e-3) == 4

@@ -134,3 +134,37 @@ def test_high_na_lens_odd_grid_keeps_the_reference_nan(xl):
     assert np.isnan(got[:, n // 2, n // 2]).all() and np.isnan(got).sum() == 3
     ok = ~np.isnan(want)
     assert rel_l2(got[ok], want[ok]) < 1e-6
+
+
+def test_ez_only_focus_matches_the_full_focus_and_its_gradients():
+    """VCZT_objective_lens_ez (the lens's Ez row, one transformed component)
+    gives the full focus's Ez, and the same gradients of an Ez loss with
+    respect to the fields and the mask parameters in front of the lens."""
+    import torch
+
+    import xlumina_gb300.optical_elements as oe
+    import xlumina_gb300.vectorized_optics as vo
+    n, m = 192, 64
+    x, y = ref.space(1500.0, n)
+    xo, yo = ref.space(2.0, m)
+    rng = np.random.default_rng(88)
+    Ex0 = (ref.gaussian_beam(x, y, 0.65, (800.0, 800.0)) * np.exp(1j * rng.uniform(0, 1, (n, n))))
+    res = []
+    for ez_only in (False, True):
+        light = vo.VectorizedLight(x, y, 0.65)
+        ex = torch.as_tensor(Ex0.astype(np.complex64), device="cuda").requires_grad_(True)
+        light.Ex, light.Ey = ex, 0.3 * ex.detach()
+        a = torch.as_tensor(rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32), device="cuda")
+        a = a if not res else res[0][3].detach().clone()
+        a.requires_grad_(True)
+        eta = torch.full((n, n), 0.7, device="cuda", requires_grad=True)
+        lit = oe.sSLM(oe.LCD(light, eta, 0.4), a, a)
+        ez = (oe.VCZT_objective_lens_ez(lit, 1800.0, 2000.0, xo, yo) if ez_only
+              else oe.VCZT_objective_lens(lit, 1800.0, 2000.0, xo, yo).Ez)
+        w = torch.as_tensor(rng.uniform(0, 1, (m, m)).astype(np.float32), device="cuda") if not res else res[0][4]
+        (w * torch.abs(ez) ** 2).sum().backward()
+        res.append((ez.detach(), ex.grad, eta.grad, a, w, a.grad))
+    (e0, gx0, ge0, _, _, ga0), (e1, gx1, ge1, _, _, ga1) = res
+    assert rel_l2(_np(e1), _np(e0)) < 1e-6
+    for g1, g0 in ((gx1, gx0), (ge1, ge0), (ga1, ga0)):
+        assert rel_l2(g1.cpu().numpy(), g0.cpu().numpy()) < 1e-5

@@ -22,7 +22,7 @@ XL_RS_NOALLOC_MAX_WORK_BYTES = 64 << 20
 
 XL_PASS_RS_COLS, XL_PASS_CZT_ROWS, XL_PASS_CZT_COLS, XL_PASS_RS_ROWS = range(4)
 
-OP_NONE, OP_PHASE, OP_SSLM, OP_SSLM_AMP, OP_LCD, OP_LP, OP_SEPMASK, OP_CMUL, OP_HIGHNA = range(9)
+OP_NONE, OP_PHASE, OP_SSLM, OP_SSLM_AMP, OP_LCD, OP_LP, OP_SEPMASK, OP_CMUL, OP_HIGHNA, OP_HIGHNA_EZ = range(10)
 
 
 class XlOp(ctypes.Structure):

@@ -109,8 +109,11 @@ class CztPlan:
                               self.mode, pre=self.ops, lens=self.lens).run()
 
     def adjoint(self, grads):
-        return engine.CztCall(list(grads), self.x, self.y, self.wavelength, self.z, self.xout, self.yout,
-                              self.mode, lens=self.lens, adjoint=True).run()
+        g = engine.CztCall(list(grads), self.x, self.y, self.wavelength, self.z, self.xout, self.yout,
+                           self.mode, lens=self.lens, adjoint=True).run()
+        if self.mode == "high_na_ez":   # the program's (Ex, Ey) inputs: Ey's output row is zero
+            g = [g[0], torch.zeros_like(g[0])]
+        return g
 
 
 def _z_tensor(plan):

@@ -4,7 +4,8 @@ For a class of requests (kind and grid side), the tuner times batched
 launches of 1, 2, 4, ... requests and keeps the smallest batch whose
 throughput (requests per second) is within ``tolerance`` of the best one:
 packing more requests into one launch past that point adds latency to the
-first of them and no throughput.  A small field leaves most SMs idle, so its
+first of them and no throughput.  With a latency bound (seconds per
+launch), only batches whose launch fits in it are candidates.  A small field leaves most SMs idle, so its
 class packs many requests per launch; a 2048^2 field fills the GPU alone.
 
 Choices are cached on disk as JSON, per GPU model and class, so the
@@ -79,30 +80,42 @@ class BatchTuner:
     def cached(self, cls):
         return self._cache.get(self.device_name, {}).get(self.class_key(cls))
 
-    def choose(self, rates: dict) -> int:
-        """Smallest candidate within the tolerance of the best requests/s."""
+    def choose(self, rates: dict, launch_s: dict | None = None, max_launch_s: float | None = None) -> int:
+        """Smallest candidate within the tolerance of the best requests/s,
+        among those whose launch takes at most ``max_launch_s`` (a request
+        waits for its whole batch, so this bounds the latency batching adds);
+        the smallest candidate if none is that fast."""
+        if max_launch_s is not None and launch_s is not None:
+            ok = {b: r for b, r in rates.items() if launch_s[b] <= max_launch_s}
+            if not ok:
+                return int(min(rates))
+            rates = ok
         best = max(rates.values())
         for b in sorted(rates):
             if rates[b] >= (1.0 - self.tolerance) * best:
                 return int(b)
         return int(max(rates, key=rates.get))
 
-    def best_batch(self, cls, measure, max_batch: int | None = None) -> int:
+    def best_batch(self, cls, measure, max_batch: int | None = None, max_launch_s: float | None = None) -> int:
+        """``max_launch_s``: a latency bound, seconds per batched launch (None: throughput alone)."""
+        key = tuple(cls) + (("launch<=", float(max_launch_s)),) if max_launch_s is not None else tuple(cls)
         with self._lock:
-            hit = self.cached(cls)
+            hit = self.cached(key)
         if hit is not None:
             b = int(hit["batch"])
             return min(b, max_batch) if max_batch else b
         cands = [c for c in self.candidates if not max_batch or c <= max_batch] or [1]
-        rates = {}
+        rates, launch = {}, {}
         for b in cands:
             measure(b)                                     # warm-up (spectra, caches)
             ts = [measure(b) for _ in range(self.repeats)]
-            rates[b] = b / max(statistics.median(ts), 1e-9)
-        b = self.choose(rates)
+            launch[b] = statistics.median(ts)
+            rates[b] = b / max(launch[b], 1e-9)
+        b = self.choose(rates, launch, max_launch_s)
         with self._lock:
-            self._cache.setdefault(self.device_name, {})[self.class_key(cls)] = {
-                "batch": b, "rates": {str(k): v for k, v in rates.items()}, "when": time.time()}
+            self._cache.setdefault(self.device_name, {})[self.class_key(key)] = {
+                "batch": b, "rates": {str(k): v for k, v in rates.items()},
+                "launch_ms": {str(k): 1e3 * v for k, v in launch.items()}, "when": time.time()}
             try:
                 self.save()
             except OSError:

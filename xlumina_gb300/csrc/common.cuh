@@ -191,6 +191,22 @@ __device__ __forceinline__ void apply_highna_bwd(const float (&kc)[6], float2 (&
   g[2] = make_float2(0.f, 0.f);
 }
 
+// The lens's Ez row alone (XL_OP_HIGHNA_EZ) and its backward: only e0
+// depends on the input, gEx = K20 g0, gEy = K21 g0.
+__device__ __forceinline__ void apply_highna_ez(const float (&kc)[6], float2 (&e)[3]) {
+  const float2 ex = e[0], ey = e[1];
+  e[0] = cadd(cscale(ex, kc[4]), cscale(ey, kc[5]));
+  e[1] = make_float2(0.f, 0.f);
+  e[2] = make_float2(0.f, 0.f);
+}
+
+__device__ __forceinline__ void apply_highna_ez_bwd(const float (&kc)[6], float2 (&g)[3]) {
+  const float2 g0 = g[0];
+  g[0] = cscale(g0, kc[4]);
+  g[1] = cscale(g0, kc[5]);
+  g[2] = make_float2(0.f, 0.f);
+}
+
 __device__ __forceinline__ float op_param(const XlOp& op, int i, const PixelCtx& px) {
   if (op.pmask & (1 << i)) {
     const float* p = (const float*)op.ptr[i];
@@ -294,6 +310,12 @@ __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3]
       float kc[6];
       highna_coeffs(op, px, kc);
       apply_highna(kc, e);
+      break;
+    }
+    case XL_OP_HIGHNA_EZ: {  // the lens's Ez row alone
+      float kc[6];
+      highna_coeffs(op, px, kc);
+      apply_highna_ez(kc, e);
       break;
     }
     default:
@@ -469,6 +491,12 @@ __device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, 
       float kc[6];
       highna_coeffs(op, px, kc);
       apply_highna_bwd(kc, g);
+      break;
+    }
+    case XL_OP_HIGHNA_EZ: {
+      float kc[6];
+      highna_coeffs(op, px, kc);
+      apply_highna_ez_bwd(kc, g);
       break;
     }
     default:

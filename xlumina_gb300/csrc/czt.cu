@@ -227,7 +227,8 @@ static int czt_run(void* stream, const XlCztArgs* a, int stage) {
                         (a->mode == XL_CZT_VECTOR && !a->adjoint && a->comps_in == 2 && a->comps_out == 3) ||
                         (a->mode == XL_CZT_VECTOR && a->adjoint && a->comps_in == 3 && a->comps_out == 3) ||
                         (a->mode == XL_CZT_PLAIN && a->comps_in >= 1 && a->comps_in <= 3 &&
-                         a->comps_out >= a->comps_in && a->comps_out <= 3);
+                         a->comps_out >= 1 && a->comps_out <= 3 &&
+                         (a->comps_out >= a->comps_in || a->pre.nops > 0));   // a program may fold components
   if (!ok_modes) {
     set_error("xl_czt: mode %d with comps %d -> %d is not supported", a->mode, a->comps_in, a->comps_out);
     return XL_EINVAL;

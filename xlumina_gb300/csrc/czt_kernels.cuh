@@ -109,17 +109,10 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
     const int r0 = (grp / p.B) * C::G;
     const double zd = p.zb ? p.zb[b] : p.z;
     const float zf = (float)zd;
-    if (staged) {
-      const bool got = mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
-      if (__syncthreads_or(!got)) {   // every thread takes this branch or none does
-        // the copy may still be in flight: let it land, record the event and
-        // leave without issuing another (the launch's output is not valid)
-        mbar_wait_bounded(mbar, phase);
-        if (tid == 0) record_timeout();
-        return;
-      }
-      phase ^= 1u;
-    }
+    // a wait that runs out is acted on at the barrier after the prologue
+    // (the prologue then works on stale data, and the launch's output is not
+    // valid), so that no extra barrier is taken per row group
+    const bool got = !staged || mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
     // prologue over the row group's pixels
     for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
       const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
@@ -152,7 +145,16 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
 #pragma unroll
       for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
     }
-    __syncthreads();   // every thread has read the stage and written its pixels
+    // every thread has read the stage and written its pixels; every thread
+    // takes the timeout branch or none does
+    if (__syncthreads_or(!got)) {
+      // the copy may still be in flight: let it land, record the event and
+      // leave without issuing another
+      mbar_wait_bounded(mbar, phase);
+      if (tid == 0) record_timeout();
+      return;
+    }
+    phase ^= 1u;
     if (tid == 0 && staged && grp + gridDim.x < total) {
       fence_proxy_async();
       const int g = grp + gridDim.x, bn = g % p.B, rn = (g / p.B) * C::G;

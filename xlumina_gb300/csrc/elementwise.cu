@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
       PixelCtx px0{row, col, i, 0};
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
-        if (k < K && hk < 0 && p.prog.ops[k].kind == XL_OP_HIGHNA) {
+        if (k < K && hk < 0 && (p.prog.ops[k].kind == XL_OP_HIGHNA || p.prog.ops[k].kind == XL_OP_HIGHNA_EZ)) {
           highna_coeffs(p.prog.ops[k], px0, kc);
           hk = k;
         }
@@ -102,7 +102,8 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
           st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
           if (k + 1 < K) {
             if (k == hk) {
-              apply_highna(kc, e);
+              if (p.prog.ops[k].kind == XL_OP_HIGHNA) apply_highna(kc, e);
+              else apply_highna_ez(kc, e);
             } else if (k < KMAX - 1) {
               const float4 t = op_trig(p.prog.ops[k], px);
               trig_s[k][tid] = t;
@@ -122,7 +123,10 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
           const XlOp& op = p.prog.ops[k];
           float pg[4] = {0.f, 0.f, 0.f, 0.f};
           const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
-          if (k == hk) apply_highna_bwd(kc, g);
+          if (k == hk) {
+            if (op.kind == XL_OP_HIGHNA) apply_highna_bwd(kc, g);
+            else apply_highna_ez_bwd(kc, g);
+          }
           else if (k + 1 < K && k < KMAX - 1) apply_op_bwd_t(op, trig_s[k][tid], ek, g, px, pg);
           else apply_op_bwd(op, ek, g, px, pg);
 #pragma unroll

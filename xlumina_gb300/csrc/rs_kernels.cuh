@@ -223,17 +223,10 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
     const int b = grp % p.B;
     const int r0 = (grp / p.B) * C::G;
-    if (staged) {
-      const bool got = mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
-      if (__syncthreads_or(!got)) {   // every thread takes this branch or none does
-        // the copy may still be in flight: let it land, record the event and
-        // leave without issuing another (the launch's output is not valid)
-        mbar_wait_bounded(mbar, phase);
-        if (tid == 0) record_timeout();
-        return;
-      }
-      phase ^= 1u;
-    }
+    // a wait that runs out is acted on at the barrier after the prologue
+    // (the prologue then works on stale data, and the launch's output is not
+    // valid), so that no extra barrier is taken per row group
+    const bool got = !staged || mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
     // prologue over the row group's pixels
     {
       int last = -1;
@@ -267,7 +260,16 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
         for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
       }
     }
-    __syncthreads();   // every thread has read the stage and written its pixels
+    // every thread has read the stage and written its pixels; every thread
+    // takes the timeout branch or none does
+    if (__syncthreads_or(!got)) {
+      // the copy may still be in flight: let it land, record the event and
+      // leave without issuing another
+      mbar_wait_bounded(mbar, phase);
+      if (tid == 0) record_timeout();
+      return;
+    }
+    phase ^= 1u;
     if (tid == 0 && staged && grp + gridDim.x < total) {
       fence_proxy_async();
       issue(grp + gridDim.x);

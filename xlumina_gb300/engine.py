@@ -402,11 +402,13 @@ def highna_coefficients(x, y, radius, f):
     return t
 
 
-def op_high_na(x, y, radius, f):
-    """optical_elements.py:515-594 as one per-pixel op (returns the op and sin(theta_max))."""
+def op_high_na(x, y, radius, f, ez_only=False):
+    """optical_elements.py:515-594 as one per-pixel op (returns the op and
+    sin(theta_max)); ``ez_only``: the lens's Ez row alone (one output
+    component), for a focus whose Ex and Ey nothing reads."""
     s_max = radius / np.sqrt(radius ** 2 + f ** 2)
     coef = highna_coefficients(x, y, radius, f)
-    op = JonesOp(_lib.OP_HIGHNA, ptrs=[device_grid(x), device_grid(y), coef],
+    op = JonesOp(_lib.OP_HIGHNA_EZ if ez_only else _lib.OP_HIGHNA, ptrs=[device_grid(x), device_grid(y), coef],
                  dval=[radius, f, s_max, 1.0 / (radius * radius)])
     return op, s_max
 
@@ -904,7 +906,8 @@ class CztCall:
 
     mode "scalar": wave_optics.py:233-263; "vczt": vectorized_optics.py:321-361;
     "high_na": optical_elements.py:600-638 (the lens op must be in ``pre``,
-    ``lens`` = (radius, f, sin_theta_max)).  ``z``: one distance, or one per
+    ``lens`` = (radius, f, sin_theta_max)); "high_na_ez": the same focus of the
+    Ez component alone (``pre`` ends with the lens's Ez-row op, one output).  ``z``: one distance, or one per
     batch entry (a sequence or a 1-D tensor, kept on the device; the chirps
     are then built there by ``entry_chirps``)."""
 
@@ -919,15 +922,18 @@ class CztCall:
         comps, B, ibs = batch_planes(comps, *comps[0].shape[-2:])
         dev = comps[0].device
         zb = None
-        if mode != "high_na" and _per_entry(z):
+        if mode not in ("high_na", "high_na_ez") and _per_entry(z):
             zb = (z.detach() if isinstance(z, torch.Tensor) else torch.tensor(np.asarray(z, dtype=np.float64)))
             zb = zb.to(device=dev, dtype=torch.float64).reshape(-1).contiguous()
             if zb.numel() != B:
                 raise ValueError(f"{zb.numel()} distances for a batch of {B} fields")
-        if mode == "high_na":
+        if mode in ("high_na", "high_na_ez"):
             r, f, s_max = lens
             Dm = f * wavelength * (nx - 1) / (2 * r)
-            cmode, cin, cout = _lib.XL_CZT_PLAIN, (3 if adjoint else len(comps)), 3
+            if mode == "high_na":
+                cmode, cin, cout = _lib.XL_CZT_PLAIN, (3 if adjoint else len(comps)), 3
+            else:
+                cmode, cin, cout = _lib.XL_CZT_PLAIN, (1 if adjoint else len(comps)), 1
             cte = -(1j * s_max ** 2 / (f * wavelength))
             zz = 0.0
         else:

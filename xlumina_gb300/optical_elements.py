@@ -218,6 +218,26 @@ def VCZT_objective_lens(input_field, r, f, xout, yout):
     return VectorizedLight._wrap(xout, yout, input_field.wavelength, outs)
 
 
+def VCZT_objective_lens_ez(input_field, r, f, xout, yout):
+    """The Ez component of VCZT_objective_lens (optical_elements.py:600-638)
+    alone, as a tensor: the lens's Ez row fused into the first chirp-z pass
+    and one transformed component instead of three.  A loss that reads only
+    the focal Ez (the Ez spot size of hybrid_sharp_optical_table.py) needs no
+    more; jax's jit drops the unread Ex and Ey of the reference's focus the
+    same way."""
+    xout = engine.as_grid(xout)
+    yout = engine.as_grid(yout)
+    op, s_max = engine.op_high_na(input_field.x, input_field.y, r, f, ez_only=True)
+    E = input_field._base(2)
+    ops = input_field._ops + [op]
+    if autograd.needs_grad(E, ops):
+        plan = autograd.CztPlan(input_field.x, input_field.y, input_field.wavelength, None, xout, yout,
+                                "high_na_ez", ops, lens=(r, f, s_max))
+        return autograd.fused_propagate(plan, E, 1)[0]
+    return engine.czt_propagate(E, input_field.x, input_field.y, input_field.wavelength, None, xout, yout,
+                                mode="high_na_ez", pre=ops, lens=(r, f, s_max))[0]
+
+
 # ------------------------------------------------------- general elements --
 
 def circular_mask(X, Y, r):

@@ -102,12 +102,17 @@ def request_class(r: Request):
 
 class Server:
     """``tuner`` (an ``autotune.BatchTuner``): the batch size per request class
-    comes from it once the class is tuned (``tune``), else ``max_batch``."""
+    comes from it once the class is tuned (``tune``), else ``max_batch``.
+    ``max_launch_ms``: the tuner keeps only batch sizes whose launch takes at
+    most this long, which bounds the latency that batching adds to a request
+    (None: throughput alone)."""
 
-    def __init__(self, hbm_budget_bytes=150e9, max_batch=16, streams=2, device=None, tuner=None):
+    def __init__(self, hbm_budget_bytes=150e9, max_batch=16, streams=2, device=None, tuner=None,
+                 max_launch_ms=None):
         self.budget = float(hbm_budget_bytes)
         self.max_batch = int(max_batch)
         self.tuner = tuner
+        self.max_launch_s = None if max_launch_ms is None else float(max_launch_ms) / 1e3
         self._caps = {}
         self.device = device or engine.device()
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(streams)]
@@ -138,7 +143,7 @@ class Server:
                 torch.cuda.synchronize()
                 return time.perf_counter() - t0
 
-            out[cls] = self._caps[cls] = self.tuner.best_batch(cls, measure, self.max_batch)
+            out[cls] = self._caps[cls] = self.tuner.best_batch(cls, measure, self.max_batch, self.max_launch_s)
         return out
 
     def batch_cap(self, r: Request) -> int:

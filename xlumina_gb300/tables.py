@@ -129,13 +129,17 @@ class HighNATable:
     ``shared_lcd``: one LCD setting for the whole batch instead (the sharp-
     focus table's structure).  ``checkpoint``: the focal fields are not kept
     for the backward; it recomputes them from the parameters (the
-    intermediate fields of a table are then never stored)."""
+    intermediate fields of a table are then never stored).  ``ez_only``
+    (default): the focus computes the Ez component alone, the only one the
+    loss reads (VCZT_objective_lens_ez); False runs the full three-component
+    focus and takes its Ez."""
 
     def __init__(self, n=2048, roi_n=1024, batch=32, wavelength=0.650, half_width=2700.0, na=0.9,
                  f=3000.0, roi_half_width=1.0, waist=1500.0, seed=3000, device="cuda", capturable=False,
-                 checkpoint=False, shared_lcd=False):
+                 checkpoint=False, shared_lcd=False, ez_only=True):
         self.n, self.m, self.B = n, roi_n, batch
         self.checkpoint = checkpoint
+        self.ez_only = ez_only
         self.x, self.y = toolbox.space(half_width, n)
         self.xo, self.yo = toolbox.space(roi_half_width, roi_n)
         self.wavelength, self.f, self.r = wavelength, f, na * f
@@ -165,9 +169,10 @@ class HighNATable:
         light = VectorizedLight(self.x, self.y, self.wavelength)
         light.Ex = self.Ex.expand(self.B, self.n, self.n)
         light.Ey = self.Ey.expand(self.B, self.n, self.n)
-        focus = oe.VCZT_objective_lens(oe.sSLM(oe.LCD(light, self.eta, self.theta), self.alpha, self.phi),
-                                       self.r, self.f, self.xo, self.yo)
-        return focus.Ez
+        masked = oe.sSLM(oe.LCD(light, self.eta, self.theta), self.alpha, self.phi)
+        if self.ez_only:
+            return oe.VCZT_objective_lens_ez(masked, self.r, self.f, self.xo, self.yo)
+        return oe.VCZT_objective_lens(masked, self.r, self.f, self.xo, self.yo).Ez
 
     def _spot_intensity(self):
         return torch.abs(self._focal_ez()) ** 2
