@@ -841,7 +841,11 @@ def run_serving(n_req=10000, seed=4000):
 
     def serve(max_launch_ms, rate=None):
         """Tune, measure the capacity with a saturating burst, then serve the
-        Poisson stream at ``rate`` (default 80 % of that capacity)."""
+        Poisson stream at ``rate`` (default 80 % of that capacity).  Each run
+        serves fresh copies of the requests (a request's future completes once)."""
+        import dataclasses
+        from concurrent.futures import Future
+        stream = [dataclasses.replace(r, future=Future()) for r in reqs]
         srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2,
                      tuner=BatchTuner(candidates=(1, 2, 4, 8, 16), repeats=2), max_launch_ms=max_launch_ms)
         t_tune = time.perf_counter()
@@ -861,7 +865,7 @@ def run_serving(n_req=10000, seed=4000):
 
         def client():
             t = time.perf_counter()
-            for i, r in enumerate(reqs):
+            for i, r in enumerate(stream):
                 t += gaps[i]
                 d = t - time.perf_counter()
                 if d > 0:
@@ -910,7 +914,7 @@ def main():
     ap.add_argument("--col-variant", type=int, default=None,
                     help="use this column-pass kernel variant instead of measuring them all")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the timed outputs")
-    ap.add_argument("--only", choices=["czt", "hybrid", "rs1024"], default=None,
+    ap.add_argument("--only", choices=["czt", "hybrid", "rs1024", "highna_step", "fourf_step"], default=None,
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
@@ -920,6 +924,15 @@ def main():
         return
     if args.only == "hybrid":
         print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only in ("highna_step", "fourf_step"):
+        import torch
+
+        from xlumina_gb300.tables import FourFTable, HighNATable
+        t = HighNATable(checkpoint=True) if args.only == "highna_step" else FourFTable()
+        dt = _time_steps(t.step, args.steps, args.warmup)
+        torch.cuda.synchronize()
+        print(json.dumps({args.only: {"steps_per_s": 1.0 / dt, "tables_per_s": t.B / dt, "batch": t.B}}))
         return
     if args.only == "rs1024":
         print(json.dumps({"rs_plain_1024": run_rs_plain_config(steps=args.steps, warmup=args.warmup)}))

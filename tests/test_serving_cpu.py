@@ -37,3 +37,17 @@ def test_request_class_is_kind_and_size():
     assert request_class(_req("czt", 1e4)) == ("czt", 64, 64)
     assert request_class(_req("rs", 2e4, n=128)) == ("rs", 128, 128)
     assert np.isfinite(_req("vrs", 1e4).nbytes())
+
+
+def test_a_served_request_cannot_be_resubmitted():
+    """A request's future completes once; submitting it again is refused on
+    the client side (the scheduler thread never sees it)."""
+    import numpy as np
+    import pytest
+
+    from xlumina_gb300.serving import Request, Server
+    r = Request("rs", [], np.zeros(4), np.zeros(4), 0.5, 1.0)
+    r.future.set_result(None)
+    srv = Server.__new__(Server)     # the client-side check needs no device
+    with pytest.raises(ValueError):
+        Server.submit(srv, r)

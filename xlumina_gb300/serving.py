@@ -151,6 +151,9 @@ class Server:
 
     # -- client side
     def submit(self, req: Request) -> Future:
+        if req.future.done():
+            raise ValueError("this request was served already (its future is done): submit a copy "
+                             "(dataclasses.replace(req, future=Future()))")
         if req.nbytes() > self.budget:
             req.future.set_exception(MemoryError("request larger than the HBM budget"))
             return req.future
