@@ -914,6 +914,8 @@ def main():
     ap.add_argument("--col-variant", type=int, default=None,
                     help="use this column-pass kernel variant instead of measuring them all")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the timed outputs")
+    ap.add_argument("--czt-rows-variant", type=int, default=None,
+                    help="use this chirp-z row-pass kernel variant (all transform lengths)")
     ap.add_argument("--only", choices=["czt", "hybrid", "rs1024", "highna_step", "fourf_step"], default=None,
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
@@ -925,6 +927,10 @@ def main():
     if args.only == "hybrid":
         print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))
         return
+    if args.czt_rows_variant is not None:
+        from xlumina_gb300 import _lib, engine
+        for lg in range(5, 14):
+            _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, args.czt_rows_variant))
     if args.only in ("highna_step", "fourf_step"):
         import torch
 

@@ -123,8 +123,8 @@ enum {
   XL_NUM_PASSES = 4
 };
 /* Variants available for `pass` at transform length 2^log2_len (>= 1; 0 if
- * the pass or length is unknown).  Variant 0 is the one-line-per-thread
- * kernel; higher numbers are the packed two-line kernels. */
+ * the pass or length is unknown).  Variant 0 is the default kernel shape;
+ * the others are the alternatives the autotuner measures against it. */
 int xl_kernel_variant_count(int pass, int log2_len);
 /* Select variant `variant` (< the count) for later launches. */
 int xl_set_kernel_variant(int pass, int log2_len, int variant);

@@ -41,6 +41,7 @@ def test_variant_table_bounds():
     lib = engine.lib()
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 8
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 3
     assert lib.xl_kernel_variant_count(99, 12) == 0
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 8) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
@@ -103,3 +104,40 @@ def test_rs_column_variants_adjoint_and_batch(variants, v):
         res[var] = [_np(t) for t in fwd] + [_np(t) for t in adj]
     for a, b in zip(res[v], res[0]):
         assert rel_l2(a, b) < 1e-6
+
+
+@pytest.mark.parametrize("v", [1, 2])
+def test_czt_row_variants_match(v):
+    """The chirp-z x transform with its stage capped for two CTAs per SM (1)
+    or unstaged (2) gives the default kernel's result: a VCZT behind an LCD
+    and the Ez-only high-NA focus behind an sSLM."""
+    import torch
+
+    import xlumina_gb300.optical_elements as oe
+    import xlumina_gb300.vectorized_optics as vo
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    n, m = 512, 128
+    x, y = ref.space(1500.0, n)
+    xo, yo = ref.space(300.0, m)
+    rng = np.random.default_rng(99)
+    E = torch.as_tensor((rng.standard_normal((2, n, n)) + 1j * rng.standard_normal((2, n, n))).astype(np.complex64),
+                        device="cuda")
+    eta = torch.as_tensor(rng.uniform(0, 6, (n, n)).astype(np.float32), device="cuda")
+    logl = [lg for lg in range(5, 14)]
+    saved = {lg: lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg) for lg in logl}
+    res = {}
+    try:
+        for var in (0, v):
+            for lg in logl:
+                _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, var))
+            light = vo.VectorizedLight(x, y, 0.6)
+            light.Ex, light.Ey = E[0], E[1]
+            a = oe.VCZT_objective_lens_ez(oe.sSLM(light, eta, eta), 1800.0, 2000.0, xo, yo)
+            b = oe.LCD(light, eta, 0.3).VCZT(2.0e4, xo, yo)
+            res[var] = [_np(a), _np(b.Ex), _np(b.Ey), _np(b.Ez)]
+    finally:
+        for lg, s in saved.items():
+            lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, s)
+    for got, exp in zip(res[v], res[0]):
+        assert rel_l2(got, exp) < 1e-6

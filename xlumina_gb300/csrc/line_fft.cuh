@@ -102,10 +102,11 @@ __device__ __forceinline__ void stage_rows(const RowStage& st, unsigned char* st
 
 // Which planes to stage: every input component and every per-pixel parameter
 // plane of the fused program whose rows are 16-byte aligned, while the stage
-// fits next to `fixed_smem` bytes of other shared memory.
+// fits next to `fixed_smem` bytes of other shared memory within `cap` (the
+// CTA's shared memory, barrier included; a smaller cap leaves room for more
+// CTAs per SM, the planes that do not fit are read from global memory).
 static inline void plan_row_stage(int cin, const float2* const* in, long long ibs, int nx, const XlProg& prog,
-                                  int G, size_t fixed_smem, RowStage& st) {
-  const size_t cap = 226 * 1024;   // the CTA's shared memory, barrier included
+                                  int G, size_t fixed_smem, RowStage& st, size_t cap = 226 * 1024) {
   st.n = 0;
   st.row_bytes = 0;
   for (int c = 0; c < 3; ++c) st.fld[c] = -1;
