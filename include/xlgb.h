@@ -359,7 +359,8 @@ int xl_highna_coefficients(void* stream, int ny, int nx, const double* x, const 
  * program's input planes and `gout` the gradient of its output (torch
  * convention for complex tensors, 2 dL/d conj(y)); `gin` receives the
  * gradient of the input (in[1], in[2] may be NULL for planes that are zero,
- * e.g. the Ez a propagator derives itself).  pgrad[op*4 + i] (XL_MAX_OPS*4 entries, NULL skips)
+ * e.g. the Ez a propagator derives itself; gout[1], gout[2] may be NULL for
+ * output planes whose gradient is zero).  pgrad[op*4 + i] (XL_MAX_OPS*4 entries, NULL skips)
  * receives dL/dp for parameter i of op: a float32 plane for a per-pixel
  * parameter (summed over the batch when the parameter is shared by it), or
  * one float64 accumulator that the call adds into for a scalar parameter. */

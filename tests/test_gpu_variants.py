@@ -108,8 +108,9 @@ def test_rs_column_variants_adjoint_and_batch(variants, v):
 
 @pytest.mark.parametrize("v", [1, 2])
 def test_czt_row_variants_match(v):
-    """The chirp-z x transform with its stage capped for two CTAs per SM (1)
-    or unstaged (2) gives the default kernel's result: a VCZT behind an LCD
+    """The chirp-z x transform with every plane staged for one CTA per SM
+    (1) or unstaged (2) gives the default kernel's result (the stage capped
+    for two CTAs per SM): a VCZT behind an LCD
     and the Ez-only high-NA focus behind an sSLM."""
     import torch
 

@@ -111,8 +111,8 @@ class CztPlan:
     def adjoint(self, grads):
         g = engine.CztCall(list(grads), self.x, self.y, self.wavelength, self.z, self.xout, self.yout,
                            self.mode, lens=self.lens, adjoint=True).run()
-        if self.mode == "high_na_ez":   # the program's (Ex, Ey) inputs: Ey's output row is zero
-            g = [g[0], torch.zeros_like(g[0])]
+        if self.mode == "high_na_ez":   # the program's outputs (e0, e1): e1's gradient is zero
+            g = [g[0], None]
         return g
 
 

@@ -137,8 +137,8 @@ int read_status(unsigned int* flag, int clear) {
 // interleaved packed one with L2 and register prefetch (4), and the one-line
 // kernel with prefetch in two barrier groups (5) or in CTAs of half the
 // columns, two per SM (6), and the two groups of (5) started half a
-// component apart (7).  The chirp-z x transform: every plane staged that
-// fits one CTA per SM (0), the stage capped for two CTAs per SM (1), no
+// component apart (7).  The chirp-z x transform: the stage capped for two
+// CTAs per SM (0), every plane staged that fits one CTA per SM (1), no
 // staging (2).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;

@@ -115,8 +115,8 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
       float2 g[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       const long long go = (long long)b * p.gbs + i;
       g[0] = p.gout[0][go];
-      if (p.C > 1) g[1] = p.gout[1][go];
-      if (p.C > 2) g[2] = p.gout[2][go];
+      if (p.C > 1 && p.gout[1]) g[1] = p.gout[1][go];
+      if (p.C > 2 && p.gout[2]) g[2] = p.gout[2][go];
 #pragma unroll
       for (int k = KMAX - 1; k >= 0; --k) {
         if (k < K) {
@@ -425,7 +425,7 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
     p.in[c] = c < comps ? (const float2*)in[c] : nullptr;
     p.gout[c] = c < comps ? (const float2*)gout[c] : nullptr;
     p.gin[c] = c < comps ? (float2*)gin[c] : nullptr;
-    if (c < comps && ((!p.in[c] && c == 0) || !p.gout[c])) {
+    if (c == 0 && (!p.in[0] || !p.gout[0])) {
       set_error("xl_ops_backward: null plane %d", c);
       return XL_EINVAL;
     }

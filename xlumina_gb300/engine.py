@@ -434,7 +434,8 @@ def apply_ops(comps, ops, ny, nx):
 
 def ops_backward(base, gout, ops, ny, nx, want_input=True):
     """Backward of a Jones program.  ``base``: the program's input planes (None
-    for a plane that is zero); ``gout``: gradients of its output planes.
+    for a plane that is zero); ``gout``: gradients of its output planes (None
+    after the first for a plane whose gradient is zero: it is not read).
     Returns (input gradients, {(op, slot): parameter gradient})."""
     L = lib()
     C = len(gout)
@@ -468,7 +469,7 @@ def ops_backward(base, gout, ops, ny, nx, want_input=True):
     prog = _lib.XlProg()
     fill_prog(prog, ops, ny, nx)
     inp = (ctypes.c_void_p * 3)(*[(b.data_ptr() if b is not None else 0) for b in base] + [0] * (3 - len(base)))
-    go = (ctypes.c_void_p * 3)(*[g.data_ptr() for g in gout] + [0] * (3 - C))
+    go = (ctypes.c_void_p * 3)(*[(g.data_ptr() if g is not None else 0) for g in gout] + [0] * (3 - C))
     gi = (ctypes.c_void_p * 3)(*[(g.data_ptr() if g is not None else 0) for g in gin] + [0] * (3 - C))
     _lib.check(L.xl_ops_backward(stream_handle(), B, C, ny, nx, inp, ibs, go, ny * nx, gi, ny * nx,
                                  ctypes.byref(prog), pgrad), "xl_ops_backward")
