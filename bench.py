@@ -447,7 +447,8 @@ def run_gpu(args):
                                             "3 one line per thread with L2 prefetch; 4 packed interleaved "
                                             "with L2 and register prefetch; 5 one line per thread, two "
                                             "barrier groups; 6 one line per thread, two CTAs per SM; 7 as 5 with "
-                                            "the groups started half a component apart"},
+                                            "the groups started half a component apart; 8 (4096 points) "
+                                            "radix-64, 64 elements per thread, one exchange per transform"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

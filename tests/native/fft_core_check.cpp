@@ -5,6 +5,7 @@
 #include <vector>
 #include "../../xlumina_gb300/csrc/fft_core.cuh"
 #include "../../xlumina_gb300/csrc/fft_pair.cuh"
+#include "../../xlumina_gb300/csrc/fft64.cuh"
 
 using namespace xl;
 
@@ -188,4 +189,72 @@ static int dispatch_p(int logn, const float* a, const float* b, float* oa, float
 // Two lines through the packed engine; zu: their upper halves are zero and not read.
 extern "C" int fft_pair_check(int logn, int dir, int zu, const float* a, const float* b, float* oa, float* ob) {
   return dir < 0 ? dispatch_p<-1>(logn, a, b, oa, ob, zu) : dispatch_p<1>(logn, a, b, oa, ob, zu);
+}
+
+// ---- the radix-64 4096-point engine of fft64.cuh: 64 threads of 64 elements ----
+struct R64 { float2 v[64]; };
+
+// One 4096-point transform (zin: the upper half of the input is zero and not
+// read; zout: only outputs 0..2047 are produced, the rest of out is untouched).
+template <int DIR, bool ZIN, bool ZOUT>
+static void run_64(const float* in, float* out) {
+  std::vector<float2> tw(4096), stw(4096), xb(F64_XS);
+  for (int q = 0; q < 4096; ++q) {
+    const double ang = 2.0 * M_PI * q / 4096;
+    tw[q] = make_float2((float)std::cos(ang), (float)-std::sin(ang));
+  }
+  for (int i = 0; i < 4096; ++i) stw[i] = f64_twiddle_entry(i, tw.data());
+  std::vector<R64> V(64);
+  for (int j = 0; j < 64; ++j)
+    for (int m = 0; m < (ZIN ? 32 : 64); ++m) {
+      const int n = j + 64 * m;
+      V[j].v[m] = make_float2(in[2 * n], in[2 * n + 1]);
+    }
+  for (int j = 0; j < 64; ++j) {
+    f64_pass0<DIR, ZIN>(V[j].v);
+    f64_write<DIR>(V[j].v, j, xb.data(), stw.data());
+  }
+  for (int j = 0; j < 64; ++j) f64_pass1<DIR, ZOUT>(V[j].v, j, xb.data());
+  for (int j = 0; j < 64; ++j)
+    for (int m = 0; m < (ZOUT ? 32 : 64); ++m) {
+      const int n = j + 64 * m;
+      out[2 * n] = V[j].v[m].x;
+      out[2 * n + 1] = V[j].v[m].y;
+    }
+}
+
+template <int DIR>
+static void run_64d(int zin, int zout, const float* in, float* out) {
+  if (zin && zout) run_64<DIR, true, true>(in, out);
+  else if (zin) run_64<DIR, true, false>(in, out);
+  else if (zout) run_64<DIR, false, true>(in, out);
+  else run_64<DIR, false, false>(in, out);
+}
+
+extern "C" int fft64_check(int dir, int zin, int zout, const float* in, float* out) {
+  if (dir < 0) run_64d<-1>(zin, zout, in, out);
+  else run_64d<1>(zin, zout, in, out);
+  return 0;
+}
+
+// Exchange slots of the radix-64 engine for four interleaved lines (lane =
+// 4 (j % 8) + line): for each half-warp access of the pass-0 writes and the
+// pass-1 gathers, the number of distinct 8-byte bank pairs (16 when free of
+// conflicts); returns the minimum over all accesses.
+extern "C" int fft64_min_banks() {
+  int worst = 16;
+  for (int j0 = 0; j0 < 64; j0 += 8)
+    for (int half = 0; half < 2; ++half)
+      for (int i = 0; i < 64; ++i)
+        for (int phase = 0; phase < 2; ++phase) {
+          bool seen[16] = {false};
+          int distinct = 0;
+          for (int l = 0; l < 16; ++l) {
+            const int line = l & 3, j = j0 + half * 4 + (l >> 2);
+            const int slot = line * F64_XB + (phase == 0 ? F64_ROW * j + i : F64_ROW * i + j);
+            if (!seen[slot & 15]) { seen[slot & 15] = true; ++distinct; }
+          }
+          if (distinct < worst) worst = distinct;
+        }
+  return worst;
 }

@@ -19,6 +19,7 @@ def fftlib(tmp_path_factory):
     lib.fft_core_check_stw.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.fft_core_check_zu.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.fft_pair_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4
+    lib.fft64_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     return lib
 
 
@@ -80,3 +81,32 @@ def test_pair_fft_matches_numpy(fftlib, logn, direction, pruned):
         ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
         err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
         assert err < 2e-7 * logn, err
+
+
+@pytest.mark.parametrize("direction", [-1, 1])
+@pytest.mark.parametrize("zin,zout", [(False, False), (True, False), (False, True), (True, True)])
+def test_radix64_fft_matches_numpy(fftlib, direction, zin, zout):
+    """The radix-64 4096-point engine (fft64.cuh): 64 threads of 64 elements,
+    one exchange; pruned input (upper half zero, never read) and pruned output
+    (only the lower half produced)."""
+    n = 4096
+    rng = np.random.default_rng(500 + direction + 3 * zin + 7 * zout)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    g = x.copy()
+    if zin:
+        x[n // 2:] = 0
+        g[n // 2:] = 1e30   # never read
+    out = np.full_like(x, 7.0)
+    assert fftlib.fft64_check(direction, int(zin), int(zout), g.ctypes.data, out.ctypes.data) == 0
+    ref = np.fft.fft(x.astype(np.complex128)) if direction < 0 else np.fft.ifft(x.astype(np.complex128)) * n
+    keep = n // 2 if zout else n
+    err = np.linalg.norm(out[:keep] - ref[:keep]) / np.linalg.norm(ref[:keep])
+    assert err < 2e-7 * 12, err
+    if zout:
+        assert np.all(out[keep:] == 7.0)
+
+
+def test_radix64_exchange_is_conflict_free(fftlib):
+    """Every half-warp write and gather of the radix-64 exchange (four lines
+    interleaved in the lanes) touches 16 distinct 8-byte bank pairs."""
+    assert fftlib.fft64_min_banks() == 16

@@ -22,14 +22,22 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture
 def zero_wait():
+    """Every bounded wait gives up at once; the chirp-z row pass stages every
+    plane that fits (kernel variant 1), so that its rows are waited for at
+    every transform length."""
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
     flag, n = ctypes.c_uint(0), ctypes.c_uint(0)
     lib.xl_device_status(ctypes.byref(flag), 1)
     lib.xl_device_timeouts(ctypes.byref(n), 1)
+    saved = {lg: lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg) for lg in range(5, 14)}
+    for lg in saved:
+        _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, 1), "xl_set_kernel_variant")
     _lib.check(lib.xl_set_wait_limit(0), "xl_set_wait_limit")
     yield lib
     _lib.check(lib.xl_set_wait_limit(10 ** 9), "xl_set_wait_limit")
+    for lg, v in saved.items():
+        _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, v), "xl_set_kernel_variant")
     lib.xl_device_status(ctypes.byref(flag), 1)
     lib.xl_device_timeouts(ctypes.byref(n), 1)
 

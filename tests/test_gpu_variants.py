@@ -1,8 +1,8 @@
 """Every kernel variant of a pass gives the oracle's result: the packed
-two-line column pass (interleaved, in barrier groups, with prefetching) and
-the prefetching one-line kernel against the one-line kernel and the FP64
-oracle, for the transform lengths that have it
-(1024, 2048 and 4096 points: fields of 257..2048 per side).
+two-line column pass (interleaved, in barrier groups, with prefetching), the
+prefetching one-line kernel and, at 4096 points, the radix-64 kernel against
+the one-line kernel and the FP64 oracle, for the transform lengths that have
+them (1024, 2048 and 4096 points: fields of 257..2048 per side).
 
 Tolerance: relative L2 <= 1e-5 against the oracle (the path's bar); the
 variants agree with each other to float32 rounding (<= 1e-6).
@@ -39,11 +39,13 @@ def variants():
 def test_variant_table_bounds():
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 8
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 9
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 8
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 3
     assert lib.xl_kernel_variant_count(99, 12) == 0
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 8) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 9) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 8) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
     assert lib.xl_get_kernel_variant(-1, 12) == _lib.XL_EINVAL
 
@@ -56,7 +58,7 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     select, count = variants
     logp = engine.rs_logq(n, n) + 1
     nv = count(logp)
-    assert nv == 8
+    assert nv == (9 if logp == 12 else 8)
     x, y = ref.space(1000.0, n)
     rng = np.random.default_rng(n + vector)
     Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
@@ -81,15 +83,16 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
             assert rel_l2(g, g0) < 1e-6, v
 
 
-@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6, 7, 8])
 def test_rs_column_variants_adjoint_and_batch(variants, v):
     """The adjoint (conjugate spectrum) and a batch with a distance per entry
-    through a packed variant equal the one-line kernel's results."""
+    through a variant equal the one-line kernel's results (the radix-64
+    variant 8 exists for 4096-point transforms only: fields of 1025..2048)."""
     import torch
 
     from xlumina_gb300 import engine
     select, _ = variants
-    n = 700
+    n = 1100 if v == 8 else 700
     x, y = ref.space(600.0, n)
     rng = np.random.default_rng(77)
     E = torch.as_tensor((rng.standard_normal((3, 2, n, n)) + 1j * rng.standard_normal((3, 2, n, n)))

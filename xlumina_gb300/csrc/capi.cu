@@ -137,12 +137,15 @@ int read_status(unsigned int* flag, int clear) {
 // interleaved packed one with L2 and register prefetch (4), and the one-line
 // kernel with prefetch in two barrier groups (5) or in CTAs of half the
 // columns, two per SM (6), and the two groups of (5) started half a
-// component apart (7).  The chirp-z x transform: the stage capped for two
+// component apart (7); for 4096-point transforms also the radix-64 column
+// pass (8: two passes of 64 elements per thread, one exchange per
+// transform).  The chirp-z x transform: the stage capped for two
 // CTAs per SM (0), every plane staged that fits one CTA per SM (1), no
 // staging (2).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
-  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 12) return 8;
+  if (pass == XL_PASS_RS_COLS && log2_len == 12) return 9;
+  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 11) return 8;
   if (pass == XL_PASS_CZT_ROWS && log2_len >= 5) return 3;
   return 1;
 }

@@ -285,13 +285,15 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   using C = CztCfg<LOGL>;
   using F = CztRowCfg<LOGL, NC>;
   const size_t fixed = ((size_t)(F::LINES * C::XS + NC * C::G * p.nx) * 8 + 15) / 16 * 16;
-  // kernel variant: 0 cap the stage so that two CTAs fit per SM (where the
-  // registers allow two: the one-component transforms); 1 stage every plane
+  // kernel variant: 0 cap the stage so that two CTAs fit per SM where the
+  // registers allow two (the one-component transforms; three components keep
+  // one CTA per SM and stage every plane that fits); 1 stage every plane
   // that fits one CTA per SM; 2 stage nothing (all planes read from global
   // memory, as many CTAs as the registers allow).  Measured on the Ez-only
   // high-NA step (32 x 2048^2): 1354 (0), 1138 (1), 1348 (2) tables/s.
   const int var = kernel_variant(XL_PASS_CZT_ROWS, LOGL);
-  const size_t cap = var == 0 ? (size_t)(227 * 1024) / 2 - 1024 : var == 1 ? (size_t)226 * 1024 : 0;
+  const size_t one_cta = (size_t)226 * 1024, two_cta = (size_t)(227 * 1024) / 2 - 1024;
+  const size_t cap = var == 0 ? (NC == 1 ? two_cta : one_cta) : var == 1 ? one_cta : 0;
   RowStage st;
   plan_row_stage(p.cin, p.in, p.ibs, p.nx, p.pre, C::G, fixed, st, cap);
   const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;

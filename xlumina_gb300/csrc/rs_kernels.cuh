@@ -35,6 +35,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "fft64.cuh"
 #include "line_fft.cuh"
 #include "rs_host.h"
 
@@ -367,6 +368,80 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
     for (int m = 0; m < C::H; ++m) {
       const int n = j + m * C::T;
       if (n < ny) tile[(long long)n * W] = v[m];
+    }
+  }
+}
+
+// Column pass at P = 4096 with the radix-64 engine (fft64.cuh): 64 threads
+// per column hold 64 elements each, so a transform has one exchange instead
+// of two and the CTA (4 columns, 256 threads, one per SM) runs four barriers
+// per component instead of eight.  Persistent: each CTA builds the pass-0
+// twiddle table once and walks (batch entry, column group) units batch
+// entries fastest, as the one-line kernel's grid does.
+template <int LOGQ>
+__global__ void __launch_bounds__(256, 1) rs_cols_conv64(const __grid_constant__ RsLaunch p) {
+  using C = RsCfg<LOGQ>;
+  static_assert(C::P == 4096 && C::CW == 4, "radix-64 column pass: P = 4096, 4 columns per CTA");
+  constexpr int W = C::W, CW = C::CW;
+  extern __shared__ __align__(16) float2 smem[];
+  float2* xch = smem;                    // CW lines, F64_XB slots apart
+  float2* stw = smem + CW * F64_XB;      // 4096: w4096^(j k) at k * 64 + j
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int wc = lane & 3, j = (tid >> 5) * 8 + (lane >> 2);
+  {
+    const float2* g = tw_table(12);
+    for (int i = tid; i < 4096; i += 256) stw[i] = f64_twiddle_entry(i, g);
+  }
+  float2* xb = xch + wc * F64_XB;
+  const int ny = p.ny;
+  const int units = p.B * (C::P / CW);
+#pragma unroll 1
+  for (int u = blockIdx.x; u < units; u += gridDim.x) {
+    const int b = u % p.B, grp = u / p.B;
+    const int t = grp / (W / CW);                      // column tile
+    const int w = (grp % (W / CW)) * CW + wc;          // column within the tile
+    const int kx = t * W + w;
+    const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
+    const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+#pragma unroll 1
+    for (int c = 0; c < p.cout; ++c) {
+      float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+      float2 v[64];
+#pragma unroll
+      for (int m = 0; m < 32; ++m) {
+        const int n = j + 64 * m;
+        v[m] = n < ny ? tile[(long long)n * W] : make_float2(0.f, 0.f);
+      }
+      f64_pass0<-1, true>(v);
+      __syncthreads();   // the previous transform's gathers are done (and the table is built)
+      f64_write<-1>(v, j, xb, stw);
+      __syncthreads();
+      f64_pass1<-1, false>(v, j, xb);
+      const float2* sp = spec;
+      asm volatile("" : "+l"(sp));
+      if (p.adjoint) {
+#pragma unroll
+        for (int m = 0; m < 64; ++m) {
+          v[m] = cmulc(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
+          if (m % 16 == 15) XL_ORDER();
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < 64; ++m) {
+          v[m] = cmul(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
+          if (m % 16 == 15) XL_ORDER();
+        }
+      }
+      f64_pass0<1, false>(v);
+      __syncthreads();
+      f64_write<1>(v, j, xb, stw);
+      __syncthreads();
+      f64_pass1<1, true>(v, j, xb);
+#pragma unroll
+      for (int m = 0; m < 32; ++m) {
+        const int n = j + 64 * m;
+        if (n < ny) tile[(long long)n * W] = v[m];
+      }
     }
   }
 }
@@ -765,6 +840,18 @@ static int launch_cols_g(cudaStream_t st, const RsLaunch& p) {
   return XL_OK;
 }
 
+template <int LOGQ>
+static int launch_cols64(cudaStream_t st, const RsLaunch& p) {
+  using C = RsCfg<LOGQ>;
+  const size_t sm = (size_t)(C::CW * F64_XB + 4096) * sizeof(float2);
+  cudaError_t e = allow_smem(rs_cols_conv64<LOGQ>, sm);
+  if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv64 smem");
+  const int grid = persistent_grid(rs_cols_conv64<LOGQ>, 256, sm, p.B * (C::P / C::CW));
+  rs_cols_conv64<LOGQ><<<grid, 256, sm, st>>>(p);
+  XL_CHECK_LAUNCH("rs_cols_conv64");
+  return XL_OK;
+}
+
 template <int LOGQ, bool PF>
 static int launch_cols(cudaStream_t st, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
@@ -794,6 +881,9 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
       if (var == 5) return launch_cols_g<LOGQ, C::CW, 2>(st, p);
       if (var == 6) return launch_cols_g<LOGQ, C::CW / 2, 1>(st, p);
       if (var == 7) return launch_cols_g<LOGQ, C::CW, 2, true>(st, p);
+    }
+    if constexpr (LOGQ == 11) {
+      if (var == 8) return launch_cols64<LOGQ>(st, p);
     }
     return launch_cols<LOGQ, false>(st, p);
   } else {
