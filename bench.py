@@ -915,6 +915,8 @@ def main():
     ap.add_argument("--col-variant", type=int, default=None,
                     help="use this column-pass kernel variant instead of measuring them all")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the timed outputs")
+    ap.add_argument("--step-batch", type=int, default=None,
+                    help="tables per step for --only highna_step / fourf_step (default: the workload's)")
     ap.add_argument("--czt-rows-variant", type=int, default=None,
                     help="use this chirp-z row-pass kernel variant (all transform lengths)")
     ap.add_argument("--only", choices=["czt", "hybrid", "rs1024", "highna_step", "fourf_step"], default=None,
@@ -936,7 +938,8 @@ def main():
         import torch
 
         from xlumina_gb300.tables import FourFTable, HighNATable
-        t = HighNATable(checkpoint=True) if args.only == "highna_step" else FourFTable()
+        kw = {"batch": args.step_batch} if args.step_batch else {}
+        t = HighNATable(checkpoint=True, **kw) if args.only == "highna_step" else FourFTable(**kw)
         dt = _time_steps(t.step, args.steps, args.warmup)
         torch.cuda.synchronize()
         print(json.dumps({args.only: {"steps_per_s": 1.0 / dt, "tables_per_s": t.B / dt, "batch": t.B}}))

@@ -104,6 +104,16 @@ int xl_device_status(unsigned int* flag, int clear);
  * or a hang. */
 int xl_set_wait_limit(unsigned long long ns);
 
+/* Device address of page-locked host memory (cudaHostAlloc'd, or
+ * registered with cudaHostRegister) that the current device can reach
+ * directly: *dev = the pointer kernels use.  XL_EINVAL for any other pointer
+ * (pageable or device memory).  Output planes of xl_rs_propagate may be such
+ * host memory: the last pass then stores the propagated field straight over
+ * the host link, with no separate device-to-host copy (the reference returns
+ * device arrays that a caller copies with jax.device_get / np.asarray,
+ * wave_optics.py:281-297). */
+int xl_host_mapped(const void* host, void** dev);
+
 /* Upload the twiddle tables to the current device.  Called once per device
  * before the first launch (every entry point calls it lazily as well). */
 int xl_init(void);

@@ -42,7 +42,7 @@ def test_variant_table_bounds():
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 9
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 8
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 3
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 4
     assert lib.xl_kernel_variant_count(99, 12) == 0
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 9) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 8) == _lib.XL_EINVAL
@@ -109,12 +109,12 @@ def test_rs_column_variants_adjoint_and_batch(variants, v):
         assert rel_l2(a, b) < 1e-6
 
 
-@pytest.mark.parametrize("v", [1, 2])
+@pytest.mark.parametrize("v", [1, 2, 3])
 def test_czt_row_variants_match(v):
     """The chirp-z x transform with every plane staged for one CTA per SM
-    (1) or unstaged (2) gives the default kernel's result (the stage capped
-    for two CTAs per SM): a VCZT behind an LCD
-    and the Ez-only high-NA focus behind an sSLM."""
+    (1), unstaged (2) or with registers for two CTAs per SM (3) gives the
+    default kernel's result (the stage capped for two CTAs per SM): a VCZT
+    behind an LCD and the Ez-only high-NA focus behind an sSLM."""
     import torch
 
     import xlumina_gb300.optical_elements as oe

@@ -123,6 +123,7 @@ SIGNATURES = {
     "xl_device_timeouts": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "xl_device_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint), ctypes.c_int]),
     "xl_set_wait_limit": (ctypes.c_int, [ctypes.c_ulonglong]),
+    "xl_host_mapped": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "xl_rs_spectrum_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_spectrum_work_bytes": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "xl_rs_transfer_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,

@@ -67,9 +67,10 @@ __device__ __forceinline__ long long tiled_rt(int r, int col, int rows, int lw) 
 
 // x transform.  NC: components per row (1, or 3 for VCZT and the high-NA
 // focus; a plain transform of 2 components runs as 3 with the third idle).
-// ZU: the input window lies in the first half of the line.
-template <int LOGL, int NC, bool ZU>
-__global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, NC>::MINB)
+// ZU: the input window lies in the first half of the line.  MB: resident
+// CTAs per SM the registers are sized for (0: CztRowCfg's MINB).
+template <int LOGL, int NC, bool ZU, int MB = 0>
+__global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRowCfg<LOGL, NC>::MINB)
     czt_rows(const __grid_constant__ CztLaunch p, const __grid_constant__ RowStage st) {
   using C = CztCfg<LOGL>;
   using F = CztRowCfg<LOGL, NC>;
@@ -98,9 +99,10 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
   // row groups are taken batch entries fastest: CTAs that run together read the
   // same rows of planes shared by the batch (the lens coefficients, shared
   // masks), so those rows come from L2 after the first entry
-  if (tid == 0 && staged && blockIdx.x < total) {
+  if (tid == 0 && blockIdx.x < total) {
     const int b = blockIdx.x % p.B, r0 = (blockIdx.x / p.B) * C::G;
-    stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
+    if (staged) stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
+    prefetch_rows(st, b, r0, min(C::G, ny - r0));
   }
 
   unsigned phase = 0;
@@ -155,10 +157,13 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, CztRowCfg<LOGL, 
       return;
     }
     phase ^= 1u;
-    if (tid == 0 && staged && grp + gridDim.x < total) {
-      fence_proxy_async();
+    if (tid == 0 && grp + gridDim.x < total) {
       const int g = grp + gridDim.x, bn = g % p.B, rn = (g / p.B) * C::G;
-      stage_rows(st, stage, mbar, bn, rn, min(C::G, ny - rn));
+      if (staged) {
+        fence_proxy_async();
+        stage_rows(st, stage, mbar, bn, rn, min(C::G, ny - rn));
+      }
+      prefetch_rows(st, bn, rn, min(C::G, ny - rn));
     }
     const int r = r0 + gi;
     const bool live = r < ny;
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
 // ---------------------------------------------------------------------------
 // Launch code.
 
-template <int LOGL, int NC, bool ZU>
+template <int LOGL, int NC, bool ZU, int MB = 0>
 static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   using C = CztCfg<LOGL>;
   using F = CztRowCfg<LOGL, NC>;
@@ -289,11 +294,17 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   // registers allow two (the one-component transforms; three components keep
   // one CTA per SM and stage every plane that fits); 1 stage every plane
   // that fits one CTA per SM; 2 stage nothing (all planes read from global
-  // memory, as many CTAs as the registers allow).  Measured on the Ez-only
-  // high-NA step (32 x 2048^2): 1354 (0), 1138 (1), 1348 (2) tables/s.
+  // memory, as many CTAs as the registers allow); 3 as 0 with the registers
+  // sized for two CTAs per SM instead of three (MB = 2: no spills).
+  // Measured on the Ez-only high-NA step (32 x 2048^2): 1354 (0), 1138 (1),
+  // 1348 (2) tables/s.
   const int var = kernel_variant(XL_PASS_CZT_ROWS, LOGL);
+  constexpr int MB2 = 512 / F::THREADS;   // two CTAs of 256 threads
+  if constexpr (NC == 1 && MB == 0 && MB2 >= 1 && MB2 < F::MINB) {
+    if (var == 3) return launch_czt_rows<LOGL, NC, ZU, MB2>(s, p);
+  }
   const size_t one_cta = (size_t)226 * 1024, two_cta = (size_t)(227 * 1024) / 2 - 1024;
-  const size_t cap = var == 0 ? (NC == 1 ? two_cta : one_cta) : var == 1 ? one_cta : 0;
+  const size_t cap = (var == 0 || var == 3) ? (NC == 1 ? two_cta : one_cta) : var == 1 ? one_cta : 0;
   RowStage st;
   plan_row_stage(p.cin, p.in, p.ibs, p.nx, p.pre, C::G, fixed, st, cap);
   const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;
@@ -301,11 +312,11 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
     set_error("czt: input row of %d columns too long for shared memory", p.nx);
     return XL_EUNSUPPORTED;
   }
-  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU>, sm);
+  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU, MB>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "czt_rows smem");
   const int total = p.B * ((p.ny + C::G - 1) / C::G);
-  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU>, F::THREADS, sm, total);
-  czt_rows<LOGL, NC, ZU><<<grid, F::THREADS, sm, s>>>(p, st);
+  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU, MB>, F::THREADS, sm, total);
+  czt_rows<LOGL, NC, ZU, MB><<<grid, F::THREADS, sm, s>>>(p, st);
   XL_CHECK_LAUNCH("czt_rows");
   return XL_OK;
 }

@@ -60,6 +60,7 @@ __device__ __forceinline__ long long tiled(int r, int col, int rows) {
 // XL_ROW_STREAMS planes (input components and per-pixel parameter planes of
 // the fused program), each copied G rows at a time ----
 #define XL_ROW_STREAMS 8
+#define XL_ROW_PREFETCH 4
 struct RowStream {
   const char* src;      // row 0 of batch entry 0
   long long bstride;    // bytes between batch entries (0: shared by the batch)
@@ -72,6 +73,10 @@ struct RowStage {
   RowStream s[XL_ROW_STREAMS];
   int fld[3];                  // stage offset of input component c, -1: read from global memory
   int prm[XL_MAX_OPS][4];      // stage offset of parameter plane i of op k, -1: global memory
+  // planes the prologue reads from global memory (not staged, or the lens
+  // coefficient planes), prefetched into L2 one row group ahead
+  int npf;
+  RowStream pf[XL_ROW_PREFETCH];   // soff unused
 };
 
 // Per-pixel parameters of the fused program, from the stage when the plane is
@@ -97,6 +102,15 @@ __device__ __forceinline__ void stage_rows(const RowStage& st, unsigned char* st
     const RowStream& q = st.s[s];
     bulk_copy_g2s(stage + q.soff, q.src + (long long)b * q.bstride + (long long)r0 * q.row_bytes,
                   (unsigned)(rows * q.row_bytes), mbar);
+  }
+}
+
+// Prefetch into L2 the rows of group (batch b, rows r0 .. r0 + rows - 1) of
+// the planes the prologue reads from global memory (one thread).
+__device__ __forceinline__ void prefetch_rows(const RowStage& st, int b, int r0, int rows) {
+  for (int s = 0; s < st.npf; ++s) {
+    const RowStream& q = st.pf[s];
+    l2_prefetch(q.src + (long long)b * q.bstride + (long long)r0 * q.row_bytes, (unsigned)(rows * q.row_bytes));
   }
 }
 
@@ -127,11 +141,35 @@ static inline void plan_row_stage(int cin, const float2* const* in, long long ib
     st.row_bytes += row_bytes;
     return o;
   };
-  for (int c = 0; c < cin && c < 3; ++c) st.fld[c] = add(in[c], ibs * 8, nx * 8);
+  // planes left in global memory: prefetched into L2 where the bulk prefetch
+  // allows it (16-byte aligned rows)
+  st.npf = 0;
+  auto prefetch = [&](const void* src, long long bstride_bytes, int row_bytes) {
+    if (st.npf >= XL_ROW_PREFETCH || !src) return;
+    if (((uintptr_t)src % 16) || (bstride_bytes % 16) || (row_bytes % 16)) return;
+    RowStream& q = st.pf[st.npf++];
+    q.src = (const char*)src;
+    q.bstride = bstride_bytes;
+    q.row_bytes = row_bytes;
+    q.soff = 0;
+  };
+  for (int c = 0; c < cin && c < 3; ++c) {
+    st.fld[c] = add(in[c], ibs * 8, nx * 8);
+    if (st.fld[c] < 0) prefetch(in[c], ibs * 8, nx * 8);
+  }
   for (int k = 0; k < prog.nops; ++k) {
     const XlOp& op = prog.ops[k];
     for (int i = 0; i < 4; ++i)
-      if (op.pmask & (1 << i)) st.prm[k][i] = add(op.ptr[i], op.pbstride * 4, nx * 4);
+      if (op.pmask & (1 << i)) {
+        st.prm[k][i] = add(op.ptr[i], op.pbstride * 4, nx * 4);
+        if (st.prm[k][i] < 0) prefetch(op.ptr[i], op.pbstride * 4, nx * 4);
+      }
+    // the lens's precomputed coefficient planes (6 x ny x nx float32, shared
+    // by the batch): the Ez row's two, or all six
+    if ((op.kind == XL_OP_HIGHNA || op.kind == XL_OP_HIGHNA_EZ) && op.ptr[2]) {
+      const char* cp = (const char*)op.ptr[2];
+      for (int q = op.kind == XL_OP_HIGHNA_EZ ? 4 : 0; q < 6; ++q) prefetch(cp + q * op.pbstride * 4, 0, nx * 4);
+    }
   }
 }
 

@@ -216,9 +216,10 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   // same rows of the parameter planes a batch shares, which then come from L2
   auto issue = [&](int grp) {
     const int b = grp % p.B, r0 = (grp / p.B) * C::G;
-    stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
+    if (staged) stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
+    prefetch_rows(st, b, r0, min(C::G, ny - r0));
   };
-  if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
+  if (tid == 0 && blockIdx.x < total) issue(blockIdx.x);
 
   unsigned phase = 0;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
@@ -271,8 +272,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
       return;
     }
     phase ^= 1u;
-    if (tid == 0 && staged && grp + gridDim.x < total) {
-      fence_proxy_async();
+    if (tid == 0 && grp + gridDim.x < total) {
+      if (staged) fence_proxy_async();
       issue(grp + gridDim.x);
     }
     const int r = r0 + gi;

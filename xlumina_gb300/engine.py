@@ -589,12 +589,29 @@ def build_rs_spectra_device(x, y, zd: torch.Tensor, wavelength, dz=False) -> tor
     return spec
 
 
+def out_pointer(t, shape):
+    """Address the kernels write an output plane to: a CUDA tensor's data, or
+    page-locked host memory (a pinned CPU tensor) reached over the host link,
+    which saves the device-to-host copy of a result wanted on the host."""
+    if t.dtype != torch.complex64 or tuple(t.shape) != tuple(shape) or not t.is_contiguous():
+        raise ValueError(f"output must be a contiguous complex64 tensor of shape {tuple(shape)}, "
+                         f"got {t.dtype} {tuple(t.shape)}")
+    if t.is_cuda:
+        return t.data_ptr()
+    if t.device.type != "cpu" or not t.is_pinned():
+        raise ValueError("an output on the host must be pinned (page-locked) memory")
+    dev = ctypes.c_void_p()
+    _lib.check(lib().xl_host_mapped(ctypes.c_void_p(t.data_ptr()), ctypes.byref(dev)), "xl_host_mapped")
+    return dev.value
+
+
 class RsCall:
     """One prepared RS / VRS launch: arguments, outputs and the buffers they point at.
 
     ``comps`` are complex64 CUDA tensors of shape (ny, nx) or (B, ny, nx);
     ``z`` is a float or a sequence of B floats (one transfer spectrum per
-    distinct value, from the cache)."""
+    distinct value, from the cache).  ``outs``: the output planes to write,
+    CUDA tensors or pinned host tensors (see ``out_pointer``)."""
 
     def __init__(self, comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None, work=None,
                  adjoint=False, dz=False, want_ez=False, spectra=None):
@@ -648,7 +665,7 @@ class RsCall:
         for i, c in enumerate(comps):
             a.inp[i] = c.data_ptr()
         for i, o in enumerate(outs):
-            a.out[i] = o.data_ptr()
+            a.out[i] = out_pointer(o, tuple(lead) + (ny, nx))
         a.in_bstride = ibs
         a.out_bstride = ny * nx
         if vector:
@@ -680,9 +697,10 @@ class RsCall:
         _lib.check(lib().xl_rs_stage(stream_handle(), ctypes.byref(self.args), int(s)), "xl_rs_stage")
 
 
-def rs_propagate(comps, x, y, wavelength, z, vector: bool, pre=(), post=()):
-    """Scalar RS (comps = [field]) or VRS (comps = [Ex, Ey]); returns 1 or 3 tensors."""
-    return RsCall(comps, x, y, wavelength, z, vector, pre, post).run()
+def rs_propagate(comps, x, y, wavelength, z, vector: bool, pre=(), post=(), outs=None):
+    """Scalar RS (comps = [field]) or VRS (comps = [Ex, Ey]); returns 1 or 3 tensors
+    (``outs``, if given: CUDA or pinned host tensors written in place)."""
+    return RsCall(comps, x, y, wavelength, z, vector, pre, post, outs=outs).run()
 
 
 # ---------------------------------------------------------------- sources --

@@ -76,17 +76,25 @@ class VectorizedLight(_Grid):
 
     draw_intensity_profile = draw
 
-    def VRS_propagation(self, z):
-        """vectorized_optics.py:244-284: Ez derived from Ex, Ey; returns (light, quality_factor)."""
+    def VRS_propagation(self, z, out=None):
+        """vectorized_optics.py:244-284: Ez derived from Ex, Ey; returns (light, quality_factor).
+
+        ``out``: optional (Ex, Ey, Ez) planes to write the result into, CUDA
+        tensors or pinned host tensors; a result wanted on the host is then
+        stored there by the last pass, with no device-to-host copy (not for a
+        propagation that needs gradients)."""
         tic = time.perf_counter()
         zv, _ = engine.z_values(z)
         qf = engine.quality_factor(self.x, self.y, self.wavelength, zv)
         E = self._base(2)
         if autograd.needs_grad(E, self._ops, z):
+            if out is not None:
+                raise ValueError("out= is for propagations without gradients")
             plan = autograd.RsPlan(self.x, self.y, self.wavelength, z, True, self._ops)
             Ex, Ey, Ez = autograd.fused_propagate(plan, E, 3)
         else:
-            Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, zv, vector=True, pre=self._ops)
+            Ex, Ey, Ez = engine.rs_propagate(E, self.x, self.y, self.wavelength, zv, vector=True, pre=self._ops,
+                                             outs=None if out is None else list(out))
         _report("VRS", tic)
         return VectorizedLight._wrap(self.x, self.y, self.wavelength, [Ex, Ey, Ez]), qf
 
