@@ -150,6 +150,38 @@ NCU_TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
                        "--no-cpu-baseline --no-fwd-bwd --no-serving")
 
 
+def host_link_rates(dev, nbytes=256 << 20, reps=4):
+    """Copy rates (GB/s) between pinned host memory and the device: each
+    direction alone and both at once on two streams."""
+    import torch
+    d = torch.empty(nbytes // 8, dtype=torch.complex64, device=dev)
+    d2 = torch.empty_like(d)
+    h = torch.empty(nbytes // 8, dtype=torch.complex64).pin_memory()
+    h2 = torch.empty_like(h).pin_memory()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def rate(fn, moved):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return moved * reps / (time.perf_counter() - t0) / 1e9
+
+    def both():
+        with torch.cuda.stream(s1):
+            h.copy_(d, non_blocking=True)
+        with torch.cuda.stream(s2):
+            d2.copy_(h2, non_blocking=True)
+        s1.synchronize()
+        s2.synchronize()
+
+    return {"d2h_gbs": rate(lambda: h.copy_(d, non_blocking=True), nbytes),
+            "h2d_gbs": rate(lambda: d.copy_(h, non_blocking=True), nbytes),
+            "duplex_gbs": rate(both, 2 * nbytes)}
+
+
 def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
     """One field of the workload through the FP64 CPU restatement."""
     ax, ay = ref.lcd(Ex, Ey, eta.astype(np.float64), theta.astype(np.float64))
@@ -416,6 +448,12 @@ def run_gpu(args):
     h2d = (hosts[0]["Ex"].numel() + hosts[0]["Ey"].numel()) * 8 + \
         (hosts[0]["eta"].numel() + hosts[0]["theta"].numel()) * 4
     d2h = sum(hb.numel() for hb in hosts[0]["out"]) * 8
+    link = host_link_rates(dev)
+    # the fields/s the copies alone allow: each direction at its own rate, and
+    # both together at the duplex rate
+    link_s = max(d2h / (link["d2h_gbs"] * 1e9), h2d / (link["h2d_gbs"] * 1e9),
+                 (d2h + h2d) / (link["duplex_gbs"] * 1e9))
+    link["bound_fields_per_s"] = B / link_s
 
     line = {
         "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": args.steps,
@@ -452,7 +490,10 @@ def run_gpu(args):
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "segments": segments, "steps_per_segment": ke},
+                "segments": segments, "steps_per_segment": ke,
+                "host_link": dict(link, how="pinned-memory copies of 256 MiB, one stream per direction, "
+                                            "timed outside the timed region; bound = B / the longest of "
+                                            "the step's copies at these rates")},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
         "spectrum_builds": engine.SPECTRA.builds,

@@ -222,8 +222,6 @@ struct GlobalParams {
   }
 };
 
-// Apply op number k of a program to the pixel's (Ex, Ey, Ez) (scalar fields
-// use e[0] only); its real parameters come from the reader pr(op, k, i, px).
 // The LCD retarder (delta = 0) from cos, sin of eta/2 and of theta:
 // a = ch - i sh (c^2 - s^2), b = c = -i sh 2 s c, d = ch + i sh (c^2 - s^2).
 __device__ __forceinline__ void lcd_apply_trig(float ch, float sh, float ct, float st, float2 (&e)[3]) {
@@ -236,91 +234,114 @@ __device__ __forceinline__ void lcd_apply_trig(float ch, float sh, float ct, flo
   e[1] = cadd(cmul(b, x), cmul(d, y));
 }
 
+// Op k of a program applied to one pixel's (Ex, Ey, Ez) (scalar fields use
+// e[0] only), its kind a compile-time constant; its real parameters come from
+// the reader pr(op, k, i, px).
+template <int KIND, class PR>
+__device__ __forceinline__ void apply_kind(const XlOp& op, int k, float2 (&e)[3], const PixelCtx& px,
+                                           const PR& pr) {
+  if constexpr (KIND == XL_OP_PHASE) {  // scalar SLM: field * e^{i phi}
+    float s, c;
+    phase_sincos(pr(op, k, 0, px), &s, &c);
+    e[0] = cmul(e[0], make_float2(c, s));
+  } else if constexpr (KIND == XL_OP_SSLM) {  // diag(e^{i a}, e^{i p}); Ez unchanged
+    float s, c;
+    phase_sincos(pr(op, k, 0, px), &s, &c);
+    e[0] = cmul(e[0], make_float2(c, s));
+    phase_sincos(pr(op, k, 1, px), &s, &c);
+    e[1] = cmul(e[1], make_float2(c, s));
+  } else if constexpr (KIND == XL_OP_SSLM_AMP) {  // diag(A1 e^{i a}, A2 e^{i p}); Ez unchanged
+    float s, c;
+    phase_sincos(pr(op, k, 0, px), &s, &c);
+    e[0] = cscale(cmul(e[0], make_float2(c, s)), pr(op, k, 2, px));
+    phase_sincos(pr(op, k, 1, px), &s, &c);
+    e[1] = cscale(cmul(e[1], make_float2(c, s)), pr(op, k, 3, px));
+  } else if constexpr (KIND == XL_OP_LCD) {  // general retarder with delta = 0 (eta, theta); Ez unchanged
+    float sh, ch, st, ct;
+    if (op.pmask & 1) phase_sincos(0.5f * pr(op, k, 0, px), &sh, &ch);
+    else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
+    if (op.pmask & 2) phase_sincos(pr(op, k, 1, px), &st, &ct);
+    else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
+    lcd_apply_trig(ch, sh, ct, st, e);
+  } else if constexpr (KIND == XL_OP_LP) {  // linear polarizer at alpha; Ez set to zero
+    float s, c;
+    if (op.pmask & 1) phase_sincos(pr(op, k, 0, px), &s, &c);
+    else { c = op.sval[2]; s = op.sval[3]; }   // scalar alpha: cos, sin from the host
+    const float2 x = e[0], y = e[1];
+    e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
+    e[1] = cadd(cscale(x, c * s), cscale(y, s * s));
+    e[2] = make_float2(0.f, 0.f);
+  } else if constexpr (KIND == XL_OP_SEPMASK) {  // separable complex mask ax[col]*ay[row] with an FP64 pupil test
+    // ptr[0]: float2 colfac[nx]; ptr[1]: float2 rowfac[ny];
+    // ptr[2], ptr[3]: double pupil terms (col, row); pupil = (tc + tr < 1) if present.
+    const float2 fc = ((const float2*)op.ptr[0])[px.col];
+    const float2 fr = ((const float2*)op.ptr[1])[px.row];
+    float2 m = cmul(fc, fr);
+    if (op.ptr[2]) {
+      const double tc = ((const double*)op.ptr[2])[px.col];
+      const double tr = ((const double*)op.ptr[3])[px.row];
+      if (!(tc + tr < 1.0)) m = make_float2(0.f, 0.f);
+    }
+    e[0] = cmul(e[0], m);
+    e[1] = cmul(e[1], m);
+    if (op.sval[0] != 0.f) e[2] = make_float2(0.f, 0.f);  // vector lens drops Ez
+    else e[2] = cmul(e[2], m);
+  } else if constexpr (KIND == XL_OP_CMUL) {  // multiply every component by a per-pixel complex array
+    const float2* p = (const float2*)op.ptr[0];
+    const float2 m = p[(long long)px.batch * op.pbstride + px.pix];
+    e[0] = cmul(e[0], m);
+    e[1] = cmul(e[1], m);
+    e[2] = cmul(e[2], m);
+  } else if constexpr (KIND == XL_OP_HIGHNA) {  // optical_elements.py:528-594
+    float kc[6];
+    highna_coeffs(op, px, kc);
+    apply_highna(kc, e);
+  } else if constexpr (KIND == XL_OP_HIGHNA_EZ) {  // the lens's Ez row alone
+    float kc[6];
+    highna_coeffs(op, px, kc);
+    apply_highna_ez(kc, e);
+  }
+}
+
+// The switch over an op's kind, with BODY(K) run for the kind K.
+#define XL_OP_SWITCH(kind, BODY)                          \
+  switch (kind) {                                         \
+    case XL_OP_PHASE: BODY(XL_OP_PHASE) break;            \
+    case XL_OP_SSLM: BODY(XL_OP_SSLM) break;              \
+    case XL_OP_SSLM_AMP: BODY(XL_OP_SSLM_AMP) break;      \
+    case XL_OP_LCD: BODY(XL_OP_LCD) break;                \
+    case XL_OP_LP: BODY(XL_OP_LP) break;                  \
+    case XL_OP_SEPMASK: BODY(XL_OP_SEPMASK) break;        \
+    case XL_OP_CMUL: BODY(XL_OP_CMUL) break;              \
+    case XL_OP_HIGHNA: BODY(XL_OP_HIGHNA) break;          \
+    case XL_OP_HIGHNA_EZ: BODY(XL_OP_HIGHNA_EZ) break;    \
+    default: break;                                       \
+  }
+
+// Apply op number k of a program to one pixel.
 template <class PR>
 __device__ __forceinline__ void apply_op_r(const XlOp& op, int k, float2 (&e)[3], const PixelCtx& px,
                                            const PR& pr) {
-  switch (op.kind) {
-    case XL_OP_PHASE: {  // scalar SLM: field * e^{i phi}
-      float s, c;
-      phase_sincos(pr(op, k, 0, px), &s, &c);
-      e[0] = cmul(e[0], make_float2(c, s));
-      break;
-    }
-    case XL_OP_SSLM: {  // diag(e^{i a}, e^{i p}); Ez unchanged
-      float s, c;
-      phase_sincos(pr(op, k, 0, px), &s, &c);
-      e[0] = cmul(e[0], make_float2(c, s));
-      phase_sincos(pr(op, k, 1, px), &s, &c);
-      e[1] = cmul(e[1], make_float2(c, s));
-      break;
-    }
-    case XL_OP_SSLM_AMP: {  // diag(A1 e^{i a}, A2 e^{i p}); Ez unchanged
-      float s, c;
-      phase_sincos(pr(op, k, 0, px), &s, &c);
-      e[0] = cscale(cmul(e[0], make_float2(c, s)), pr(op, k, 2, px));
-      phase_sincos(pr(op, k, 1, px), &s, &c);
-      e[1] = cscale(cmul(e[1], make_float2(c, s)), pr(op, k, 3, px));
-      break;
-    }
-    case XL_OP_LCD: {  // general retarder with delta = 0 (eta, theta); Ez unchanged
-      float sh, ch, st, ct;
-      if (op.pmask & 1) phase_sincos(0.5f * pr(op, k, 0, px), &sh, &ch);
-      else { ch = op.dval[0]; sh = op.dval[1]; }   // scalar eta: cos, sin of eta/2 from the host
-      if (op.pmask & 2) phase_sincos(pr(op, k, 1, px), &st, &ct);
-      else { ct = op.dval[2]; st = op.dval[3]; }   // scalar theta
-      lcd_apply_trig(ch, sh, ct, st, e);
-      break;
-    }
-    case XL_OP_LP: {  // linear polarizer at alpha; Ez set to zero
-      float s, c;
-      if (op.pmask & 1) phase_sincos(pr(op, k, 0, px), &s, &c);
-      else { c = op.sval[2]; s = op.sval[3]; }   // scalar alpha: cos, sin from the host
-      const float2 x = e[0], y = e[1];
-      e[0] = cadd(cscale(x, c * c), cscale(y, c * s));
-      e[1] = cadd(cscale(x, c * s), cscale(y, s * s));
-      e[2] = make_float2(0.f, 0.f);
-      break;
-    }
-    case XL_OP_SEPMASK: {  // separable complex mask ax[col]*ay[row] with an FP64 pupil test
-      // ptr[0]: float2 colfac[nx]; ptr[1]: float2 rowfac[ny];
-      // ptr[2], ptr[3]: double pupil terms (col, row); pupil = (tc + tr < 1) if present.
-      const float2 fc = ((const float2*)op.ptr[0])[px.col];
-      const float2 fr = ((const float2*)op.ptr[1])[px.row];
-      float2 m = cmul(fc, fr);
-      if (op.ptr[2]) {
-        const double tc = ((const double*)op.ptr[2])[px.col];
-        const double tr = ((const double*)op.ptr[3])[px.row];
-        if (!(tc + tr < 1.0)) m = make_float2(0.f, 0.f);
-      }
-      e[0] = cmul(e[0], m);
-      e[1] = cmul(e[1], m);
-      if (op.sval[0] != 0.f) e[2] = make_float2(0.f, 0.f);  // vector lens drops Ez
-      else e[2] = cmul(e[2], m);
-      break;
-    }
-    case XL_OP_CMUL: {  // multiply every component by a per-pixel complex array
-      const float2* p = (const float2*)op.ptr[0];
-      const float2 m = p[(long long)px.batch * op.pbstride + px.pix];
-      e[0] = cmul(e[0], m);
-      e[1] = cmul(e[1], m);
-      e[2] = cmul(e[2], m);
-      break;
-    }
-    case XL_OP_HIGHNA: {  // optical_elements.py:528-594
-      float kc[6];
-      highna_coeffs(op, px, kc);
-      apply_highna(kc, e);
-      break;
-    }
-    case XL_OP_HIGHNA_EZ: {  // the lens's Ez row alone
-      float kc[6];
-      highna_coeffs(op, px, kc);
-      apply_highna_ez(kc, e);
-      break;
-    }
-    default:
-      break;
-  }
+#define XL_ONE_(K) apply_kind<K>(op, k, e, px, pr);
+  XL_OP_SWITCH(op.kind, XL_ONE_)
+#undef XL_ONE_
+}
+
+// Apply op number k to NPX pixels at once: the kind is dispatched once, and
+// the pixels' loads and arithmetic are independent, so they overlap.
+template <int NPX, class PR>
+__device__ __forceinline__ void apply_op_vec(const XlOp& op, int k, float2 (&e)[NPX][3], const PixelCtx (&px)[NPX],
+                                             const PR (&pr)[NPX]) {
+#define XL_VEC_(K)                                            \
+  _Pragma("unroll") for (int q = 0; q < NPX; ++q) apply_kind<K>(op, k, e[q], px[q], pr[q]);
+  XL_OP_SWITCH(op.kind, XL_VEC_)
+#undef XL_VEC_
+}
+
+template <int NPX, class PR>
+__device__ __forceinline__ void apply_prog_vec(const XlProg& prog, float2 (&e)[NPX][3], const PixelCtx (&px)[NPX],
+                                               const PR (&pr)[NPX]) {
+  for (int i = 0; i < prog.nops; ++i) apply_op_vec<NPX>(prog.ops[i], i, e, px, pr);
 }
 
 template <class PR>

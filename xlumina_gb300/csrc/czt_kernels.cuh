@@ -28,6 +28,8 @@
 
 #include <math.h>
 
+#include <type_traits>
+
 #include "czt_host.h"
 #include "line_fft.cuh"
 
@@ -115,37 +117,57 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRow
     // (the prologue then works on stale data, and the launch's output is not
     // valid), so that no extra barrier is taken per row group
     const bool got = !staged || mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
-    // prologue over the row group's pixels
-    for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
-      const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
-      if (r >= ny) break;
-      const long long pix = (long long)r * nx + n;
-      float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    // prologue over the row group's pixels; in CTAs of up to 256 threads, four
+    // per thread at a time while four remain, then one: each op of the program
+    // is dispatched once for the four, and their loads and arithmetic overlap
+    const int lim = min(C::G, ny - r0) * nx;
+    auto chunk = [&](auto npx, int base) {
+      constexpr int NPX = decltype(npx)::value;
+      float2 e[NPX][3];
+      PixelCtx px[NPX];
+      StagedParams pr[NPX];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (c < p.cin) {
-          const int fo = st.fld[c];
-          e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+      for (int q = 0; q < NPX; ++q) {
+        const int idx = base + q * F::THREADS;
+        const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
+        const long long pix = (long long)r * nx + n;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          e[q][c] = make_float2(0.f, 0.f);
+          if (c < p.cin) {
+            const int fo = st.fld[c];
+            e[q][c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+          }
         }
+        px[q] = PixelCtx{r, n, pix, b};
+        pr[q] = StagedParams{stage, &st, g2, nx, n};
       }
-      if (p.pre.nops) {
-        PixelCtx px{r, n, pix, b};
-        apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
-      }
-      if (fwd_phase) {
-        if (vczt) {  // vectorized_optics.py:340-344
-          const float X = (float)p.x[n], Y = (float)p.y[r];
-          const float rr = sqrtf(X * X + Y * Y + zf * zf);
-          e[2] = cscale(cadd(cscale(e[0], X / rr), cscale(e[1], Y / rr)), zf / rr);
+      if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
+#pragma unroll
+      for (int q = 0; q < NPX; ++q) {
+        const int r = px[q].row, n = px[q].col;
+        if (fwd_phase) {
+          if (vczt) {  // vectorized_optics.py:340-344
+            const float X = (float)p.x[n], Y = (float)p.y[r];
+            const float rr = sqrtf(X * X + Y * Y + zf * zf);
+            e[q][2] = cscale(cadd(cscale(e[q][0], X / rr), cscale(e[q][1], Y / rr)), zf / rr);
+          }
+          // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
+          float2 Fv = p.fin ? p.fin[px[q].pix] : rs_kernel_value(p.x[n], p.y[r], zd, p.inv_lambda, p.k);
+          if (p.adjoint) Fv = cconj(Fv);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) e[q][c] = cmul(e[q][c], Fv);
         }
-        // wave_optics.py:341 (F on the input plane); the adjoint applies conj(F0) here
-        float2 Fv = p.fin ? p.fin[pix] : rs_kernel_value(p.x[n], p.y[r], zd, p.inv_lambda, p.k);
-        if (p.adjoint) Fv = cconj(Fv);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) e[c] = cmul(e[c], Fv);
+        for (int c = 0; c < NC; ++c) post[(c * C::G + (r - r0)) * nx + n] = e[q][c];
       }
-#pragma unroll
-      for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
+    };
+    {
+      int base = tid;
+      if constexpr (F::THREADS <= 256) {   // CTAs of 768 threads ran slower with it
+        for (; base + 3 * F::THREADS < lim; base += 4 * F::THREADS) chunk(std::integral_constant<int, 4>{}, base);
+      }
+      for (; base < lim; base += F::THREADS) chunk(std::integral_constant<int, 1>{}, base);
     }
     // every thread has read the stage and written its pixels; every thread
     // takes the timeout branch or none does

@@ -229,38 +229,53 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
     // (the prologue then works on stale data, and the launch's output is not
     // valid), so that no extra barrier is taken per row group
     const bool got = !staged || mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
-    // prologue over the row group's pixels
+    // prologue over the row group's pixels; in CTAs of up to 256 threads, four
+    // per thread at a time while four remain, then one: each op of the program
+    // is dispatched once for the four, and their loads and arithmetic overlap
     {
-      int last = -1;
-      float Y = 0.f, z2 = 0.f;
-      for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
-        const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
-        if (r >= ny) break;
-        const long long pix = (long long)r * nx + n;
-        float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      const int lim = min(C::G, ny - r0) * nx;
+      const float zb = MODE == 2 ? (float)p.z[b] : 0.f;
+      auto chunk = [&](auto npx, int base) {
+        constexpr int NPX = decltype(npx)::value;
+        float2 e[NPX][3];
+        PixelCtx px[NPX];
+        StagedParams pr[NPX];
 #pragma unroll
-        for (int c = 0; c < CIN; ++c) {
-          const int fo = st.fld[c];
-          e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
-        }
-        if (p.pre.nops) {
-          PixelCtx px{r, n, pix, b};
-          apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
-        }
-        if constexpr (MODE == 2) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
-          if (g2 != last) {
-            last = g2;
-            Y = (float)p.y[r];
-            const float zb = (float)p.z[b];
-            z2 = Y * Y + zb * zb;
+        for (int q = 0; q < NPX; ++q) {
+          const int idx = base + q * F::THREADS;
+          const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
+          const long long pix = (long long)r * nx + n;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            e[q][c] = make_float2(0.f, 0.f);
+            if (c < CIN) {
+              const int fo = st.fld[c];
+              e[q][c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+            }
           }
-          const float X = xf[n];
-          const float inv = rsqrtf(X * X + z2);
-          e[2] = cadd(cscale(e[0], X * inv), cscale(e[1], Y * inv));
+          px[q] = PixelCtx{r, n, pix, b};
+          pr[q] = StagedParams{stage, &st, g2, nx, n};
         }
+        if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
 #pragma unroll
-        for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
+        for (int q = 0; q < NPX; ++q) {
+          const int r = px[q].row, n = px[q].col;
+          if constexpr (MODE == 2) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
+            const float Y = (float)p.y[r];
+            const float z2 = Y * Y + zb * zb;
+            const float X = xf[n];
+            const float inv = rsqrtf(X * X + z2);
+            e[q][2] = cadd(cscale(e[q][0], X * inv), cscale(e[q][1], Y * inv));
+          }
+#pragma unroll
+          for (int c = 0; c < NC; ++c) post[(c * C::G + (r - r0)) * nx + n] = e[q][c];
+        }
+      };
+      int base = tid;
+      if constexpr (F::THREADS <= 256) {   // CTAs of 768 threads ran slower with it
+        for (; base + 3 * F::THREADS < lim; base += 4 * F::THREADS) chunk(std::integral_constant<int, 4>{}, base);
       }
+      for (; base < lim; base += F::THREADS) chunk(std::integral_constant<int, 1>{}, base);
     }
     // every thread has read the stage and written its pixels; every thread
     // takes the timeout branch or none does
