@@ -387,9 +387,11 @@ __device__ __forceinline__ void lcd_bwd_trig(float ch, float sh, float ct, float
 // that runs both (xl_ops_backward) evaluates them once: PHASE (c0, s0) of p0;
 // sSLM (c0, s0) of p0 and (c1, s1) of p1; LCD (c0, s0) of eta/2 and (c1, s1)
 // of theta; LP (c0, s0) of alpha.  Scalar parameters take the host's values.
-__device__ __forceinline__ float4 op_trig(const XlOp& op, const PixelCtx& px) {
+// The kind is passed apart from the op so that a kernel specialised for a
+// fixed program folds the switches below (the generic callers pass op.kind).
+__device__ __forceinline__ float4 op_trig(int kind, const XlOp& op, const PixelCtx& px) {
   float4 t = make_float4(1.f, 0.f, 1.f, 0.f);   // (c0, s0, c1, s1)
-  switch (op.kind) {
+  switch (kind) {
     case XL_OP_PHASE:
       phase_sincos(op_param(op, 0, px), &t.y, &t.x);
       break;
@@ -413,10 +415,12 @@ __device__ __forceinline__ float4 op_trig(const XlOp& op, const PixelCtx& px) {
   }
   return t;
 }
+__device__ __forceinline__ float4 op_trig(const XlOp& op, const PixelCtx& px) { return op_trig(op.kind, op, px); }
 
 // apply_op with the trig of op_trig (the same arithmetic as apply_op_r).
-__device__ __forceinline__ void apply_op_t(const XlOp& op, const float4& t, float2 (&e)[3], const PixelCtx& px) {
-  switch (op.kind) {
+__device__ __forceinline__ void apply_op_t(int kind, const XlOp& op, const float4& t, float2 (&e)[3],
+                                           const PixelCtx& px) {
+  switch (kind) {
     case XL_OP_PHASE:
       e[0] = cmul(e[0], make_float2(t.x, t.y));
       break;
@@ -444,10 +448,13 @@ __device__ __forceinline__ void apply_op_t(const XlOp& op, const float4& t, floa
       break;
   }
 }
+__device__ __forceinline__ void apply_op_t(const XlOp& op, const float4& t, float2 (&e)[3], const PixelCtx& px) {
+  apply_op_t(op.kind, op, t, e, px);
+}
 
-__device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, const float2 (&e)[3],
+__device__ __forceinline__ void apply_op_bwd_t(int kind, const XlOp& op, const float4& t, const float2 (&e)[3],
                                                float2 (&g)[3], const PixelCtx& px, float (&pg)[4]) {
-  switch (op.kind) {
+  switch (kind) {
     case XL_OP_PHASE: {
       const float2 ph = make_float2(t.x, t.y);
       const float2 y = cmul(e[0], ph);
@@ -457,7 +464,7 @@ __device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, 
     }
     case XL_OP_SSLM:
     case XL_OP_SSLM_AMP: {
-      const bool amp = op.kind == XL_OP_SSLM_AMP;
+      const bool amp = kind == XL_OP_SSLM_AMP;
       const float2 p0 = make_float2(t.x, t.y);
       const float2 p1 = make_float2(t.z, t.w);
       const float a1 = amp ? op_param(op, 2, px) : 1.f, a2 = amp ? op_param(op, 3, px) : 1.f;
@@ -525,9 +532,18 @@ __device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, 
   }
 }
 
+__device__ __forceinline__ void apply_op_bwd_t(const XlOp& op, const float4& t, const float2 (&e)[3],
+                                               float2 (&g)[3], const PixelCtx& px, float (&pg)[4]) {
+  apply_op_bwd_t(op.kind, op, t, e, g, px, pg);
+}
+
+__device__ __forceinline__ void apply_op_bwd(int kind, const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
+                                             const PixelCtx& px, float (&pg)[4]) {
+  apply_op_bwd_t(kind, op, op_trig(kind, op, px), e, g, px, pg);
+}
 __device__ __forceinline__ void apply_op_bwd(const XlOp& op, const float2 (&e)[3], float2 (&g)[3],
                                              const PixelCtx& px, float (&pg)[4]) {
-  apply_op_bwd_t(op, op_trig(op, px), e, g, px, pg);
+  apply_op_bwd(op.kind, op, e, g, px, pg);
 }
 
 }  // namespace xl

@@ -1,5 +1,7 @@
 // Stand-alone per-pixel kernels: a Jones program applied outside a
 // propagator (masks whose result the caller reads directly).
+#include <initializer_list>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -53,18 +55,35 @@ struct OpsBwdLaunch {
 // shared memory holds, [slot][thread] so that a warp's accesses fall in
 // distinct banks: the scalar-parameter partial sums (when any scalar
 // gradient is asked for), then the shared-plane batch sums (when needed).
-template <int KMAX>
+//
+// FK: the program's op kinds fixed at compile time (FixedKinds<...>, for the
+// programs the tables run), so that the per-op switches fold and the trig
+// stays in registers; FixedKinds<> reads them from the program.
+template <int... KS> struct FixedKinds {
+  static constexpr int n = 0;
+  __device__ static constexpr int at(int) { return XL_OP_NONE; }
+};
+template <int K0, int... KR> struct FixedKinds<K0, KR...> {
+  static constexpr int n = 1 + sizeof...(KR);
+  __device__ static constexpr int at(int k) { return k == 0 ? K0 : FixedKinds<KR...>::at(k - 1); }
+};
+
+template <int KMAX, class FK = FixedKinds<>>
 __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p, int scalar_acc, int plane_acc) {
   constexpr int NS = XL_MAX_OPS * 4;
   constexpr int NT = 128;
+  constexpr bool FIXED = FK::n > 0;
+  static_assert(!FIXED || FK::n == KMAX, "a fixed program unrolls to its length");
   extern __shared__ float accm[];
   // the trig of every op the forward recompute applies, for its backward
-  // (thread-private slots, so no barrier): evaluated once per pixel and entry
-  __shared__ float4 trig_s[KMAX - 1][NT];
+  // (thread-private slots, so no barrier): evaluated once per pixel and entry.
+  // A fixed program keeps it in registers instead.
+  __shared__ float4 trig_s[FIXED ? 1 : KMAX - 1][NT];
   float* acc_s = accm;                              // NS x NT, when scalar_acc
   float* acc_p = accm + (scalar_acc ? NS * NT : 0); // NS x NT, when plane_acc
   const long long npix = (long long)p.ny * p.nx;
-  const int K = p.prog.nops;
+  const int K = FIXED ? FK::n : p.prog.nops;
+  auto kind = [&](int k) { return FIXED ? FK::at(k) : p.prog.ops[k].kind; };
   const int tid = threadIdx.x;
   const int b_lo = gridDim.y > 1 ? blockIdx.y : 0;
   const int b_hi = gridDim.y > 1 ? blockIdx.y + 1 : p.B;
@@ -82,7 +101,7 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
       PixelCtx px0{row, col, i, 0};
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
-        if (k < K && hk < 0 && (p.prog.ops[k].kind == XL_OP_HIGHNA || p.prog.ops[k].kind == XL_OP_HIGHNA_EZ)) {
+        if (k < K && hk < 0 && (kind(k) == XL_OP_HIGHNA || kind(k) == XL_OP_HIGHNA_EZ)) {
           highna_coeffs(p.prog.ops[k], px0, kc);
           hk = k;
         }
@@ -90,6 +109,7 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
     for (int b = b_lo; b < b_hi; ++b) {
       PixelCtx px{row, col, i, b};
       float2 st[KMAX][3];
+      float4 trig_r[KMAX];
       float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       const long long off = (long long)b * p.ibs + i;
       e[0] = p.in[0][off];
@@ -102,12 +122,13 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
           st[k][0] = e[0]; st[k][1] = e[1]; st[k][2] = e[2];
           if (k + 1 < K) {
             if (k == hk) {
-              if (p.prog.ops[k].kind == XL_OP_HIGHNA) apply_highna(kc, e);
+              if (kind(k) == XL_OP_HIGHNA) apply_highna(kc, e);
               else apply_highna_ez(kc, e);
             } else if (k < KMAX - 1) {
-              const float4 t = op_trig(p.prog.ops[k], px);
-              trig_s[k][tid] = t;
-              apply_op_t(p.prog.ops[k], t, e, px);
+              const float4 t = op_trig(kind(k), p.prog.ops[k], px);
+              if constexpr (FIXED) trig_r[k] = t;
+              else trig_s[FIXED ? 0 : k][tid] = t;
+              apply_op_t(kind(k), p.prog.ops[k], t, e, px);
             }
           }
         }
@@ -124,11 +145,12 @@ __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p,
           float pg[4] = {0.f, 0.f, 0.f, 0.f};
           const float2 ek[3] = {st[k][0], st[k][1], st[k][2]};
           if (k == hk) {
-            if (op.kind == XL_OP_HIGHNA) apply_highna_bwd(kc, g);
+            if (kind(k) == XL_OP_HIGHNA) apply_highna_bwd(kc, g);
             else apply_highna_ez_bwd(kc, g);
           }
-          else if (k + 1 < K && k < KMAX - 1) apply_op_bwd_t(op, trig_s[k][tid], ek, g, px, pg);
-          else apply_op_bwd(op, ek, g, px, pg);
+          else if (k + 1 < K && k < KMAX - 1)
+            apply_op_bwd_t(kind(k), op, FIXED ? trig_r[k] : trig_s[FIXED ? 0 : k][tid], ek, g, px, pg);
+          else apply_op_bwd(kind(k), op, ek, g, px, pg);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             void* dst = p.pgrad[k * 4 + q];
@@ -447,17 +469,47 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
     set_error("xl_ops_backward: plane too large");
     return XL_EINVAL;
   }
-  int blocks = (int)((npix + 127) / 128);
+  const long long need = (npix + 127) / 128;
   // without batch sums, one thread per pixel and batch entry (grid.y = batch)
   const int gy = (plane_acc || batch > 65535) ? 1 : batch;
-  const int cap = gy > 1 ? (152 * 16 + gy - 1) / gy : 152 * 16;
-  if (blocks > cap) blocks = cap;
-  if (blocks < 1) blocks = 1;
   const size_t sm = (size_t)(scalar_acc + plane_acc) * XL_MAX_OPS * 4 * 128 * sizeof(float);
-  if (prog->nops <= 4)
-    ops_backward_kernel<4><<<dim3(blocks, gy), 128, sm, (cudaStream_t)stream>>>(p, scalar_acc, plane_acc);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 152;
+  // one wave: the CTAs that fit on the device at once (the pixel loop strides
+  // over the rest), so that no second, partly empty wave follows
+  auto grid_for = [&](auto kernel) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, sm) != cudaSuccess || per_sm < 1)
+      per_sm = 4;
+    long long bx = ((long long)per_sm * sms + gy - 1) / gy;
+    if (bx > need) bx = need;
+    if (bx < 1) bx = 1;
+    return dim3((unsigned)bx, gy);
+  };
+  // programs the tables and the benchmarks run get a kernel with their op
+  // kinds fixed; any other program takes the generic one
+  auto is = [&](std::initializer_list<int> ks) {
+    if ((int)ks.size() != prog->nops) return false;
+    int k = 0;
+    for (int v : ks)
+      if (prog->ops[k++].kind != v) return false;
+    return true;
+  };
+  cudaStream_t s = (cudaStream_t)stream;
+  auto run = [&](auto kernel) { kernel<<<grid_for(kernel), 128, sm, s>>>(p, scalar_acc, plane_acc); };
+  if (is({XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA_EZ}))
+    run(ops_backward_kernel<3, FixedKinds<XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA_EZ>>);
+  else if (is({XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA}))
+    run(ops_backward_kernel<3, FixedKinds<XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA>>);
+  else if (is({XL_OP_LCD, XL_OP_LP}))
+    run(ops_backward_kernel<2, FixedKinds<XL_OP_LCD, XL_OP_LP>>);
+  else if (is({XL_OP_PHASE}))
+    run(ops_backward_kernel<1, FixedKinds<XL_OP_PHASE>>);
+  else if (prog->nops <= 4)
+    run(ops_backward_kernel<4>);
   else
-    ops_backward_kernel<XL_MAX_OPS><<<dim3(blocks, gy), 128, sm, (cudaStream_t)stream>>>(p, scalar_acc, plane_acc);
+    run(ops_backward_kernel<XL_MAX_OPS>);
   XL_CHECK_LAUNCH("ops_backward_kernel");
   return XL_OK;
 }

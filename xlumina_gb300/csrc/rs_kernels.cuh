@@ -216,10 +216,9 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   // same rows of the parameter planes a batch shares, which then come from L2
   auto issue = [&](int grp) {
     const int b = grp % p.B, r0 = (grp / p.B) * C::G;
-    if (staged) stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
-    prefetch_rows(st, b, r0, min(C::G, ny - r0));
+    stage_rows(st, stage, mbar, b, r0, min(C::G, ny - r0));
   };
-  if (tid == 0 && blockIdx.x < total) issue(blockIdx.x);
+  if (tid == 0 && staged && blockIdx.x < total) issue(blockIdx.x);
 
   unsigned phase = 0;
   for (int grp = blockIdx.x; grp < total; grp += gridDim.x) {
@@ -229,12 +228,50 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
     // (the prologue then works on stale data, and the launch's output is not
     // valid), so that no extra barrier is taken per row group
     const bool got = !staged || mbar_wait_bounded(mbar, phase, g_wait_limit_ns);
-    // prologue over the row group's pixels; in CTAs of up to 256 threads, four
-    // per thread at a time while four remain, then one: each op of the program
-    // is dispatched once for the four, and their loads and arithmetic overlap
+    // prologue over the row group's pixels, one per thread at a time (CTAs of
+    // more than 256 threads: the four-pixel form below ran slower in them)
+    if constexpr (F::THREADS > 256) {
+      int last = -1;
+      float Y = 0.f, z2 = 0.f;
+      for (int idx = tid; idx < C::G * nx; idx += F::THREADS) {
+        const int g2 = C::G == 1 ? 0 : idx / nx, n = idx - g2 * nx, r = r0 + g2;
+        if (r >= ny) break;
+        const long long pix = (long long)r * nx + n;
+        float2 e[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int c = 0; c < CIN; ++c) {
+          const int fo = st.fld[c];
+          e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
+        }
+        if (p.pre.nops) {
+          PixelCtx px{r, n, pix, b};
+          apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
+        }
+        if constexpr (MODE == 2) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
+          if (g2 != last) {
+            last = g2;
+            Y = (float)p.y[r];
+            const float zb = (float)p.z[b];
+            z2 = Y * Y + zb * zb;
+          }
+          const float X = xf[n];
+          const float inv = rsqrtf(X * X + z2);
+          e[2] = cadd(cscale(e[0], X * inv), cscale(e[1], Y * inv));
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) post[(c * C::G + g2) * nx + n] = e[c];
+      }
+    } else
+    // CTAs of up to 256 threads: four pixels per thread at a time while four
+    // remain, then one; each op of the program is dispatched once for the
+    // four, and their loads and arithmetic overlap
     {
       const int lim = min(C::G, ny - r0) * nx;
       const float zb = MODE == 2 ? (float)p.z[b] : 0.f;
+      // one row per group (every 2048-point line and longer): its y and
+      // y^2 + z^2 once for the group instead of once per pixel
+      const float Y0 = MODE == 2 && C::G == 1 ? (float)p.y[r0] : 0.f;
+      const float z20 = Y0 * Y0 + zb * zb;
       auto chunk = [&](auto npx, int base) {
         constexpr int NPX = decltype(npx)::value;
         float2 e[NPX][3];
@@ -261,8 +298,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
         for (int q = 0; q < NPX; ++q) {
           const int r = px[q].row, n = px[q].col;
           if constexpr (MODE == 2) {  // vectorized_optics.py:258-261, Ez = Ex X/r + Ey Y/r
-            const float Y = (float)p.y[r];
-            const float z2 = Y * Y + zb * zb;
+            const float Y = C::G == 1 ? Y0 : (float)p.y[r];
+            const float z2 = C::G == 1 ? z20 : Y * Y + zb * zb;
             const float X = xf[n];
             const float inv = rsqrtf(X * X + z2);
             e[q][2] = cadd(cscale(e[q][0], X * inv), cscale(e[q][1], Y * inv));
@@ -272,9 +309,7 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
         }
       };
       int base = tid;
-      if constexpr (F::THREADS <= 256) {   // CTAs of 768 threads ran slower with it
-        for (; base + 3 * F::THREADS < lim; base += 4 * F::THREADS) chunk(std::integral_constant<int, 4>{}, base);
-      }
+      for (; base + 3 * F::THREADS < lim; base += 4 * F::THREADS) chunk(std::integral_constant<int, 4>{}, base);
       for (; base < lim; base += F::THREADS) chunk(std::integral_constant<int, 1>{}, base);
     }
     // every thread has read the stage and written its pixels; every thread
@@ -287,8 +322,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
       return;
     }
     phase ^= 1u;
-    if (tid == 0 && grp + gridDim.x < total) {
-      if (staged) fence_proxy_async();
+    if (tid == 0 && staged && grp + gridDim.x < total) {
+      fence_proxy_async();
       issue(grp + gridDim.x);
     }
     const int r = r0 + gi;
