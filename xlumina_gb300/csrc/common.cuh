@@ -344,6 +344,50 @@ __device__ __forceinline__ void apply_prog_vec(const XlProg& prog, float2 (&e)[N
   for (int i = 0; i < prog.nops; ++i) apply_op_vec<NPX>(prog.ops[i], i, e, px, pr);
 }
 
+// A program's op kinds as a compile-time list, for kernels specialised to
+// the programs the tables run (FixedKinds<> : none, read them from the
+// program).  at(k) folds to a constant once the caller's loop over k unrolls.
+template <int... KS> struct FixedKinds {
+  static constexpr int n = 0;
+  __host__ __device__ static constexpr int at(int) { return XL_OP_NONE; }
+  static bool matches(const XlProg&) { return false; }
+};
+template <int K0, int... KR> struct FixedKinds<K0, KR...> {
+  static constexpr int n = 1 + sizeof...(KR);
+  __host__ __device__ static constexpr int at(int k) { return k == 0 ? K0 : FixedKinds<KR...>::at(k - 1); }
+  // the program has exactly these kinds, in this order
+  static bool matches(const XlProg& p) {
+    const int ks[] = {K0, KR...};
+    if (p.nops != n) return false;
+    for (int k = 0; k < n; ++k)
+      if (p.ops[k].kind != ks[k]) return false;
+    return true;
+  }
+};
+
+// apply_prog_vec for a program whose kinds FK fixes (no switches): ops K..
+template <class FK, int K = 0, int NPX, class PR>
+__device__ __forceinline__ void apply_prog_fixed(const XlProg& prog, float2 (&e)[NPX][3],
+                                                 const PixelCtx (&px)[NPX], const PR (&pr)[NPX]) {
+  static_assert(FK::n > 0 && FK::n <= XL_MAX_OPS, "a fixed program");
+  if constexpr (K < FK::n) {
+#pragma unroll
+    for (int q = 0; q < NPX; ++q) apply_kind<FK::at(K)>(prog.ops[K], K, e[q], px[q], pr[q]);
+    apply_prog_fixed<FK, K + 1>(prog, e, px, pr);
+  }
+}
+
+// The same for one pixel.
+template <class FK, int K = 0, class PR>
+__device__ __forceinline__ void apply_prog_fixed1(const XlProg& prog, float2 (&e)[3], const PixelCtx& px,
+                                                  const PR& pr) {
+  static_assert(FK::n > 0 && FK::n <= XL_MAX_OPS, "a fixed program");
+  if constexpr (K < FK::n) {
+    apply_kind<FK::at(K)>(prog.ops[K], K, e, px, pr);
+    apply_prog_fixed1<FK, K + 1>(prog, e, px, pr);
+  }
+}
+
 template <class PR>
 __device__ __forceinline__ void apply_prog_r(const XlProg& prog, float2 (&e)[3], const PixelCtx& px, const PR& pr) {
   for (int i = 0; i < prog.nops; ++i) apply_op_r(prog.ops[i], i, e, px, pr);

@@ -70,8 +70,10 @@ __device__ __forceinline__ long long tiled_rt(int r, int col, int rows, int lw) 
 // x transform.  NC: components per row (1, or 3 for VCZT and the high-NA
 // focus; a plain transform of 2 components runs as 3 with the third idle).
 // ZU: the input window lies in the first half of the line.  MB: resident
-// CTAs per SM the registers are sized for (0: CztRowCfg's MINB).
-template <int LOGL, int NC, bool ZU, int MB = 0>
+// CTAs per SM the registers are sized for (0: CztRowCfg's MINB).  FK: the
+// fused program's op kinds fixed at compile time (FixedKinds<...>, for the
+// tables' programs), or FixedKinds<>.
+template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>>
 __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRowCfg<LOGL, NC>::MINB)
     czt_rows(const __grid_constant__ CztLaunch p, const __grid_constant__ RowStage st) {
   using C = CztCfg<LOGL>;
@@ -142,7 +144,8 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRow
         px[q] = PixelCtx{r, n, pix, b};
         pr[q] = StagedParams{stage, &st, g2, nx, n};
       }
-      if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
+      if constexpr (FK::n > 0) apply_prog_fixed<FK>(p.pre, e, px, pr);
+      else if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
 #pragma unroll
       for (int q = 0; q < NPX; ++q) {
         const int r = px[q].row, n = px[q].col;
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
 // ---------------------------------------------------------------------------
 // Launch code.
 
-template <int LOGL, int NC, bool ZU, int MB = 0>
+template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>>
 static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   using C = CztCfg<LOGL>;
   using F = CztRowCfg<LOGL, NC>;
@@ -323,7 +326,7 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   const int var = kernel_variant(XL_PASS_CZT_ROWS, LOGL);
   constexpr int MB2 = 512 / F::THREADS;   // two CTAs of 256 threads
   if constexpr (NC == 1 && MB == 0 && MB2 >= 1 && MB2 < F::MINB) {
-    if (var == 3) return launch_czt_rows<LOGL, NC, ZU, MB2>(s, p);
+    if (var == 3) return launch_czt_rows<LOGL, NC, ZU, MB2, FK>(s, p);
   }
   const size_t one_cta = (size_t)226 * 1024, two_cta = (size_t)(227 * 1024) / 2 - 1024;
   const size_t cap = (var == 0 || var == 3) ? (NC == 1 ? two_cta : one_cta) : var == 1 ? one_cta : 0;
@@ -334,11 +337,11 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
     set_error("czt: input row of %d columns too long for shared memory", p.nx);
     return XL_EUNSUPPORTED;
   }
-  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU, MB>, sm);
+  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU, MB, FK>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "czt_rows smem");
   const int total = p.B * ((p.ny + C::G - 1) / C::G);
-  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU, MB>, F::THREADS, sm, total);
-  czt_rows<LOGL, NC, ZU, MB><<<grid, F::THREADS, sm, s>>>(p, st);
+  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU, MB, FK>, F::THREADS, sm, total);
+  czt_rows<LOGL, NC, ZU, MB, FK><<<grid, F::THREADS, sm, s>>>(p, st);
   XL_CHECK_LAUNCH("czt_rows");
   return XL_OK;
 }
@@ -346,6 +349,17 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
 template <int LOGL>
 int czt_rows_launch(cudaStream_t s, const CztLaunch& p) {
   const bool zu = p.ioff_x >= 0 && p.ioff_x + p.nx <= (1 << LOGL) / 2;
+  // the tables' forward programs get a kernel with their op kinds fixed: the
+  // high-NA table's LCD, sSLM and lens Ez row (4096-point lines), the 4f
+  // table's phase SLM (2048-point lines)
+  if constexpr (LOGL == 12) {
+    using HighNaEz = FixedKinds<XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA_EZ>;
+    if (p.cout == 1 && zu && HighNaEz::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, HighNaEz>(s, p);
+  }
+  if constexpr (LOGL == 11) {
+    using SlmOnly = FixedKinds<XL_OP_PHASE>;
+    if (p.cout == 1 && zu && SlmOnly::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, SlmOnly>(s, p);
+  }
   if (p.cout == 1) return zu ? launch_czt_rows<LOGL, 1, true>(s, p) : launch_czt_rows<LOGL, 1, false>(s, p);
   return zu ? launch_czt_rows<LOGL, 3, true>(s, p) : launch_czt_rows<LOGL, 3, false>(s, p);
 }

@@ -59,14 +59,6 @@ struct OpsBwdLaunch {
 // FK: the program's op kinds fixed at compile time (FixedKinds<...>, for the
 // programs the tables run), so that the per-op switches fold and the trig
 // stays in registers; FixedKinds<> reads them from the program.
-template <int... KS> struct FixedKinds {
-  static constexpr int n = 0;
-  __device__ static constexpr int at(int) { return XL_OP_NONE; }
-};
-template <int K0, int... KR> struct FixedKinds<K0, KR...> {
-  static constexpr int n = 1 + sizeof...(KR);
-  __device__ static constexpr int at(int k) { return k == 0 ? K0 : FixedKinds<KR...>::at(k - 1); }
-};
 
 template <int KMAX, class FK = FixedKinds<>>
 __global__ void __launch_bounds__(128) ops_backward_kernel(const OpsBwdLaunch p, int scalar_acc, int plane_acc) {

@@ -181,7 +181,9 @@ template <int LOGQ, int NC> struct RowCfg {
 // prologue runs the fused program over every pixel and writes the components
 // to a shared buffer; the stage is then free, so the bulk copies of the next
 // row group start while the component groups transform this one.
-template <int LOGQ, int MODE>
+// FK: the fused program's op kinds fixed at compile time (FixedKinds<...>,
+// for the programs the benchmarks and tables run), or FixedKinds<>.
+template <int LOGQ, int MODE, class FK = FixedKinds<>>
 __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowCfg<LOGQ, MODE == 1 ? 1 : 3>::MINB)
     rs_rows_fwd(const __grid_constant__ RsLaunch p, const __grid_constant__ RowStage st) {
   using C = RsCfg<LOGQ>;
@@ -243,7 +245,9 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
           const int fo = st.fld[c];
           e[c] = fo >= 0 ? ((const float2*)(stage + fo))[g2 * nx + n] : p.in[c][(long long)b * p.ibs + pix];
         }
-        if (p.pre.nops) {
+        if constexpr (FK::n > 0) {
+          apply_prog_fixed1<FK>(p.pre, e, PixelCtx{r, n, pix, b}, StagedParams{stage, &st, g2, nx, n});
+        } else if (p.pre.nops) {
           PixelCtx px{r, n, pix, b};
           apply_prog_r(p.pre, e, px, StagedParams{stage, &st, g2, nx, n});
         }
@@ -293,7 +297,8 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
           px[q] = PixelCtx{r, n, pix, b};
           pr[q] = StagedParams{stage, &st, g2, nx, n};
         }
-        if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
+        if constexpr (FK::n > 0) apply_prog_fixed<FK>(p.pre, e, px, pr);
+        else if (p.pre.nops) apply_prog_vec<NPX>(p.pre, e, px, pr);
 #pragma unroll
         for (int q = 0; q < NPX; ++q) {
           const int r = px[q].row, n = px[q].col;
@@ -828,7 +833,7 @@ int rs_spectrum(cudaStream_t st, int ny, int nx, const double* offx, const doubl
   return XL_OK;
 }
 
-template <int LOGQ, int MODE>
+template <int LOGQ, int MODE, class FK = FixedKinds<>>
 static int launch_rows_fwd(cudaStream_t s, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
   constexpr int NC = MODE == 1 ? 1 : 3;
@@ -842,11 +847,11 @@ static int launch_rows_fwd(cudaStream_t s, const RsLaunch& p) {
     set_error("rs: row of %d columns too long for shared memory", p.nx);
     return XL_EUNSUPPORTED;
   }
-  cudaError_t e = allow_smem(rs_rows_fwd<LOGQ, MODE>, sm);
+  cudaError_t e = allow_smem(rs_rows_fwd<LOGQ, MODE, FK>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "rs_rows_fwd smem");
   const int total = p.B * ((p.ny + C::G - 1) / C::G);
-  const int grid = persistent_grid(rs_rows_fwd<LOGQ, MODE>, F::THREADS, sm, total);
-  rs_rows_fwd<LOGQ, MODE><<<grid, F::THREADS, sm, s>>>(p, st);
+  const int grid = persistent_grid(rs_rows_fwd<LOGQ, MODE, FK>, F::THREADS, sm, total);
+  rs_rows_fwd<LOGQ, MODE, FK><<<grid, F::THREADS, sm, s>>>(p, st);
   XL_CHECK_LAUNCH("rs_rows_fwd");
   return XL_OK;
 }
@@ -919,8 +924,21 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   using C = RsCfg<LOGQ>;
   cudaError_t e;
   if (stage == 0) {
-    if (p.cout == 1) return launch_rows_fwd<LOGQ, 1>(st, p);
-    if (p.cin == 2) return launch_rows_fwd<LOGQ, 2>(st, p);
+    // the programs of the benchmarks' fields (1024^2 and larger) get a kernel
+    // with their op kinds fixed: a phase SLM before scalar RS, an LCD and a
+    // polarizer before VRS
+    using SlmOnly = FixedKinds<XL_OP_PHASE>;
+    using LcdLp = FixedKinds<XL_OP_LCD, XL_OP_LP>;
+    if (p.cout == 1) {
+      if constexpr (LOGQ >= 10)
+        if (SlmOnly::matches(p.pre)) return launch_rows_fwd<LOGQ, 1, SlmOnly>(st, p);
+      return launch_rows_fwd<LOGQ, 1>(st, p);
+    }
+    if (p.cin == 2) {
+      if constexpr (LOGQ >= 10)
+        if (LcdLp::matches(p.pre)) return launch_rows_fwd<LOGQ, 2, LcdLp>(st, p);
+      return launch_rows_fwd<LOGQ, 2>(st, p);
+    }
     return launch_rows_fwd<LOGQ, 3>(st, p);
   } else if (stage == 1) {
     const int var = kernel_variant(XL_PASS_RS_COLS, C::LOGP);
