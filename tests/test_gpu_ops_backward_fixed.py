@@ -1,6 +1,6 @@
 """The Jones-program backward specialised for the programs the tables run
-(LCD-sSLM-lens, LCD-polarizer, phase SLM: kernels with the op kinds fixed at
-compile time) gives the generic kernel's gradients.  The generic kernel is
+(LCD-sSLM-lens, LCD-polarizer, phase SLM, thin lens: kernels with the op
+kinds fixed at compile time) gives the generic kernel's gradients.  The generic kernel is
 reached by adding an exact identity op (a complex multiply by 1 + 0i) after
 the first op, which changes the program's signature and not its values."""
 import numpy as np
@@ -68,3 +68,16 @@ def test_phase_slm():
     ops = [engine.op_phase(P[0])]
     gen = [ops[0], engine.op_cmul(one)]
     _compare(ops, gen, [E[0]], [G[0]], n)
+
+
+def test_thin_lens():
+    """The 4f table's lens (a separable mask with a float64 pupil test, no
+    parameters): only the input gradient."""
+    from oracle import xlumina_ref as ref
+    from xlumina_gb300 import engine
+    n = 96
+    E, G, P, one = _setup(n)
+    x, y = ref.space(900.0, n)
+    lens = engine.op_lens(x, y, 0.532, (300.0, 300.0), (2.0e4, 2.0e4), False)
+    gen = [lens, engine.op_cmul(one)]
+    _compare([lens], gen, [E[0]], [G[0]], n)

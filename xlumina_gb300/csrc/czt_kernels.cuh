@@ -351,12 +351,16 @@ int czt_rows_launch(cudaStream_t s, const CztLaunch& p) {
   const bool zu = p.ioff_x >= 0 && p.ioff_x + p.nx <= (1 << LOGL) / 2;
   // the tables' forward programs get a kernel with their op kinds fixed: the
   // high-NA table's LCD, sSLM and lens Ez row (4096-point lines), the 4f
-  // table's phase SLM (2048-point lines)
+  // table's thin lens (2048-point lines) and second phase SLM (1024-point)
   if constexpr (LOGL == 12) {
     using HighNaEz = FixedKinds<XL_OP_LCD, XL_OP_SSLM, XL_OP_HIGHNA_EZ>;
     if (p.cout == 1 && zu && HighNaEz::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, HighNaEz>(s, p);
   }
   if constexpr (LOGL == 11) {
+    using LensOnly = FixedKinds<XL_OP_SEPMASK>;
+    if (p.cout == 1 && zu && LensOnly::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, LensOnly>(s, p);
+  }
+  if constexpr (LOGL == 10) {
     using SlmOnly = FixedKinds<XL_OP_PHASE>;
     if (p.cout == 1 && zu && SlmOnly::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, SlmOnly>(s, p);
   }

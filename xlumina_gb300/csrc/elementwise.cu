@@ -480,7 +480,9 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
     return dim3((unsigned)bx, gy);
   };
   // programs the tables and the benchmarks run get a kernel with their op
-  // kinds fixed; any other program takes the generic one
+  // kinds fixed (the high-NA table's LCD-sSLM-lens, the VRS benchmark's
+  // LCD-polarizer, the 4f table's phase SLM and thin lens); any other
+  // program takes the generic one
   auto is = [&](std::initializer_list<int> ks) {
     if ((int)ks.size() != prog->nops) return false;
     int k = 0;
@@ -498,6 +500,8 @@ extern "C" int xl_ops_backward(void* stream, int batch, int comps, int ny, int n
     run(ops_backward_kernel<2, FixedKinds<XL_OP_LCD, XL_OP_LP>>);
   else if (is({XL_OP_PHASE}))
     run(ops_backward_kernel<1, FixedKinds<XL_OP_PHASE>>);
+  else if (is({XL_OP_SEPMASK}))
+    run(ops_backward_kernel<1, FixedKinds<XL_OP_SEPMASK>>);
   else if (prog->nops <= 4)
     run(ops_backward_kernel<4>);
   else
