@@ -365,6 +365,8 @@ int czt_rows_launch(cudaStream_t s, const CztLaunch& p) {
     if (p.cout == 1 && zu && SlmOnly::matches(p.pre)) return launch_czt_rows<LOGL, 1, true, 0, SlmOnly>(s, p);
   }
   if (p.cout == 1) return zu ? launch_czt_rows<LOGL, 1, true>(s, p) : launch_czt_rows<LOGL, 1, false>(s, p);
+  // (a fixed LCD-sSLM-lens program in the three-component kernel ran slower:
+  // 1.96 against 1.90 ms per 8 x 2048^2 high-NA focuses)
   return zu ? launch_czt_rows<LOGL, 3, true>(s, p) : launch_czt_rows<LOGL, 3, false>(s, p);
 }
 
