@@ -902,7 +902,9 @@ def run_serving(n_req=10000, seed=4000):
         capacity = n_sat / (time.perf_counter() - t0)
         srv.reset_stats()
         offered = 0.8 * capacity if rate is None else min(rate, 0.8 * capacity)
-        gaps = rng.exponential(1.0 / offered, n_req)
+        # the same arrival pattern for every run (scaled to its rate), so that
+        # runs at the same offered rate see the same bursts
+        gaps = np.random.default_rng(seed + 1).exponential(1.0, n_req) / offered
         futs = [None] * n_req
 
         def client():
@@ -960,7 +962,7 @@ def main():
                     help="tables per step for --only highna_step / fourf_step (default: the workload's)")
     ap.add_argument("--czt-rows-variant", type=int, default=None,
                     help="use this chirp-z row-pass kernel variant (all transform lengths)")
-    ap.add_argument("--only", choices=["czt", "hybrid", "rs1024", "highna_step", "fourf_step"], default=None,
+    ap.add_argument("--only", choices=["czt", "hybrid", "rs1024", "highna_step", "fourf_step", "serving"], default=None,
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
@@ -987,6 +989,9 @@ def main():
         return
     if args.only == "rs1024":
         print(json.dumps({"rs_plain_1024": run_rs_plain_config(steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only == "serving":
+        print(json.dumps({"serving": run_serving()}))
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -21,15 +21,6 @@
 
 #include "fft_core.cuh"
 
-// A compiler-only ordering point: keeps the loads of one chunk of a long
-// unrolled loop from being hoisted above the previous chunk's stores (which
-// would hold every loaded value in registers at once).
-#if defined(__CUDA_ARCH__)
-#define XL_ORDER() asm volatile("" ::: "memory")
-#else
-#define XL_ORDER() ((void)0)
-#endif
-
 namespace xl {
 
 constexpr int F64_ROW = 69;                 // slots per 64 elements (5 pad slots)
@@ -147,18 +138,11 @@ template <int DIR, bool ZIN> XL_HD void f64_pass0(float2 (&v)[64]) { dft64<DIR, 
 // write it to slot 69 j + k of the line's exchange buffer xb.
 template <int DIR> XL_HD void f64_write(const float2 (&v)[64], int j, float2* xb, const float2* tw) {
   float2* d = xb + F64_ROW * j;
+  d[0] = v[0];
 #pragma unroll
-  for (int k0 = 0; k0 < 64; k0 += 16) {
-#pragma unroll
-    for (int k = k0; k < k0 + 16; ++k) {
-      if (k == 0) {
-        d[0] = v[0];
-        continue;
-      }
-      const float2 w = tw[k * 64 + j];
-      d[k] = DIR < 0 ? cmul(v[k], w) : cmulc(v[k], w);
-    }
-    XL_ORDER();
+  for (int k = 1; k < 64; ++k) {
+    const float2 w = tw[k * 64 + j];
+    d[k] = DIR < 0 ? cmul(v[k], w) : cmulc(v[k], w);
   }
 }
 

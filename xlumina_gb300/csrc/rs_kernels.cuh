@@ -477,16 +477,10 @@ __global__ void __launch_bounds__(256, 1) rs_cols_conv64(const __grid_constant__
       asm volatile("" : "+l"(sp));
       if (p.adjoint) {
 #pragma unroll
-        for (int m = 0; m < 64; ++m) {
-          v[m] = cmulc(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
-          if (m % 16 == 15) XL_ORDER();
-        }
+        for (int m = 0; m < 64; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
       } else {
 #pragma unroll
-        for (int m = 0; m < 64; ++m) {
-          v[m] = cmul(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
-          if (m % 16 == 15) XL_ORDER();
-        }
+        for (int m = 0; m < 64; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + 64 * m) * C::SW));
       }
       f64_pass0<1, false>(v);
       __syncthreads();
