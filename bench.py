@@ -150,9 +150,11 @@ NCU_TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
                        "--no-cpu-baseline --no-fwd-bwd --no-serving")
 
 
-def host_link_rates(dev, nbytes=256 << 20, reps=4):
+def host_link_rates(dev, nbytes=256 << 20, reps=2, trials=5):
     """Copy rates (GB/s) between pinned host memory and the device: each
-    direction alone and both at once on two streams."""
+    direction alone and both at once on two streams; the best of ``trials``
+    timings of ``reps`` copies each (the link is shared with the rest of the
+    machine, so a single timing can catch a slow spell)."""
     import torch
     d = torch.empty(nbytes // 8, dtype=torch.complex64, device=dev)
     d2 = torch.empty_like(d)
@@ -163,11 +165,14 @@ def host_link_rates(dev, nbytes=256 << 20, reps=4):
     def rate(fn, moved):
         fn()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            fn()
-        torch.cuda.synchronize()
-        return moved * reps / (time.perf_counter() - t0) / 1e9
+        best = 0.0
+        for _ in range(trials):
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            torch.cuda.synchronize()
+            best = max(best, moved * reps / (time.perf_counter() - t0) / 1e9)
+        return best
 
     def both():
         with torch.cuda.stream(s1):
@@ -492,8 +497,8 @@ def run_gpu(args):
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "segments": segments, "steps_per_segment": ke,
                 "host_link": dict(link, how="pinned-memory copies of 256 MiB, one stream per direction, "
-                                            "timed outside the timed region; bound = B / the longest of "
-                                            "the step's copies at these rates")},
+                                            "timed outside the timed region, best of 5 timings; bound = B / "
+                                            "the longest of the step's copies at these rates")},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
         "spectrum_builds": engine.SPECTRA.builds,
