@@ -145,3 +145,37 @@ def test_czt_row_variants_match(v):
             lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, s)
     for got, exp in zip(res[v], res[0]):
         assert rel_l2(got, exp) < 1e-6
+
+
+@pytest.mark.parametrize("v", [0, 1, 2])
+def test_czt_row_variants_with_the_fixed_high_na_program(v):
+    """The high-NA table's program (LCD, sSLM, the lens's Ez row) at 4096-point
+    lines runs a kernel with its op kinds fixed; every stage / register
+    variant of it gives the default variant's (3) focal Ez."""
+    import torch
+
+    import xlumina_gb300.optical_elements as oe
+    import xlumina_gb300.vectorized_optics as vo
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    n, m = 1500, 600           # Bluestein length 4096 on both axes
+    x, y = ref.space(1800.0, n)
+    xo, yo = ref.space(3.0, m)
+    rng = np.random.default_rng(7 + v)
+    E = torch.as_tensor((rng.standard_normal((2, 2, n, n)) + 1j * rng.standard_normal((2, 2, n, n)))
+                        .astype(np.complex64), device="cuda")
+    P = [torch.as_tensor(rng.uniform(0, 2 * np.pi, (2, n, n)).astype(np.float32), device="cuda") for _ in range(4)]
+    saved = lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12)
+    assert saved == 3
+    res = {}
+    try:
+        for var in (3, v):
+            _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12, var))
+            light = vo.VectorizedLight(x, y, 0.65)
+            light.Ex, light.Ey = E[0], E[1]
+            lit = oe.sSLM(oe.LCD(light, P[0], P[1]), P[2], P[3])
+            res[var] = _np(oe.VCZT_objective_lens_ez(lit, 900.0, 1000.0, xo, yo))
+    finally:
+        lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12, saved)
+    assert np.all(np.isfinite(res[3]))
+    assert rel_l2(res[v], res[3]) < 1e-6
