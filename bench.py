@@ -891,7 +891,14 @@ def run_serving(n_req=10000, seed=4000):
         Poisson stream at ``rate`` (default 80 % of that capacity).  Each run
         serves fresh copies of the requests (a request's future completes once)."""
         import dataclasses
+        import gc
         from concurrent.futures import Future
+        # start from a settled process: collect and freeze the objects the
+        # earlier sections left (so that garbage collections during the run
+        # do not walk them), and return the allocator's unused blocks
+        gc.collect()
+        gc.freeze()
+        torch.cuda.empty_cache()
         stream = [dataclasses.replace(r, future=Future()) for r in reqs]
         srv = Server(hbm_budget_bytes=150e9, max_batch=16, streams=2,
                      tuner=BatchTuner(candidates=(1, 2, 4, 8, 16), repeats=2), max_launch_ms=max_launch_ms)
@@ -929,6 +936,7 @@ def run_serving(n_req=10000, seed=4000):
             f.result(timeout=600)
         wall = time.perf_counter() - t0
         srv.close()
+        gc.unfreeze()
         st = srv.stats()
         return {"capacity_req_per_s": capacity, "offered_req_per_s": offered, "served_req_per_s": n_req / wall,
                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_batch": st["mean_batch"],
