@@ -74,7 +74,9 @@ struct RowStage {
   int fld[3];                  // stage offset of input component c, -1: read from global memory
   int prm[XL_MAX_OPS][4];      // stage offset of parameter plane i of op k, -1: global memory
   // planes the prologue reads from global memory (not staged, or the lens
-  // coefficient planes), prefetched into L2 one row group ahead
+  // coefficient planes); the chirp-z x transform prefetches them into L2 one
+  // row group ahead (in the RS forward row pass, whose planes are all staged
+  // in the benchmarked cases, the prefetch code cost 1.5 % and is left out)
   int npf;
   RowStream pf[XL_ROW_PREFETCH];   // soff unused
 };
