@@ -490,8 +490,10 @@ def run_gpu(args):
                                             "3 one line per thread with L2 prefetch; 4 packed interleaved "
                                             "with L2 and register prefetch; 5 one line per thread, two "
                                             "barrier groups; 6 one line per thread, two CTAs per SM; 7 as 5 with "
-                                            "the groups started half a component apart; 8 (4096 points) "
-                                            "radix-64, 64 elements per thread, one exchange per transform"},
+                                            "the groups started half a component apart; 8 one line per thread, "
+                                            "persistent (the library's default at 4096 points); 9 (4096 "
+                                            "points) radix-64, 64 elements per thread, one exchange per "
+                                            "transform"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -971,6 +973,8 @@ def main():
     ap.add_argument("--col-variant", type=int, default=None,
                     help="use this column-pass kernel variant instead of measuring them all")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the timed outputs")
+    ap.add_argument("--czt-cols-variant", type=int, default=None,
+                    help="use this chirp-z column-pass kernel variant (all transform lengths)")
     ap.add_argument("--step-batch", type=int, default=None,
                     help="tables per step for --only highna_step / fourf_step (default: the workload's)")
     ap.add_argument("--czt-rows-variant", type=int, default=None,
@@ -990,6 +994,10 @@ def main():
         from xlumina_gb300 import _lib, engine
         for lg in range(5, 14):
             _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, args.czt_rows_variant))
+    if args.czt_cols_variant is not None:
+        from xlumina_gb300 import _lib, engine
+        for lg in range(5, 14):
+            _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_CZT_COLS, lg, args.czt_cols_variant))
     if args.only in ("highna_step", "fourf_step"):
         import torch
 

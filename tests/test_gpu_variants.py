@@ -1,8 +1,9 @@
 """Every kernel variant of a pass gives the oracle's result: the packed
 two-line column pass (interleaved, in barrier groups, with prefetching), the
-prefetching one-line kernel and, at 4096 points, the radix-64 kernel against
-the one-line kernel and the FP64 oracle, for the transform lengths that have
-them (1024, 2048 and 4096 points: fields of 257..2048 per side).
+prefetching and the persistent one-line kernels and, at 4096 points, the
+radix-64 kernel, against the one-line kernel and the FP64 oracle, for the
+transform lengths that have them (1024, 2048 and 4096 points: fields of
+257..2048 per side).
 
 Tolerance: relative L2 <= 1e-5 against the oracle (the path's bar); the
 variants agree with each other to float32 rounding (<= 1e-6).
@@ -39,13 +40,14 @@ def variants():
 def test_variant_table_bounds():
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 9
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 8
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 10
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 9
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 4
     assert lib.xl_kernel_variant_count(99, 12) == 0
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 9) == _lib.XL_EINVAL
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 8) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 10) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 9) == _lib.XL_EINVAL
+    assert lib.xl_get_kernel_variant(_lib.XL_PASS_RS_COLS, 12) == 8   # the default at 4096 points
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
     assert lib.xl_get_kernel_variant(-1, 12) == _lib.XL_EINVAL
 
@@ -58,7 +60,7 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     select, count = variants
     logp = engine.rs_logq(n, n) + 1
     nv = count(logp)
-    assert nv == (9 if logp == 12 else 8)
+    assert nv == (10 if logp == 12 else 9)
     x, y = ref.space(1000.0, n)
     rng = np.random.default_rng(n + vector)
     Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
@@ -83,16 +85,16 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
             assert rel_l2(g, g0) < 1e-6, v
 
 
-@pytest.mark.parametrize("v", [1, 2, 3, 4, 5, 6, 7, 8])
-def test_rs_column_variants_adjoint_and_batch(variants, v):
+@pytest.mark.parametrize("v,n", [(1, 700), (2, 700), (3, 700), (4, 700), (5, 700), (6, 700), (7, 700), (8, 700),
+                                 (8, 1100), (9, 1100)])
+def test_rs_column_variants_adjoint_and_batch(variants, v, n):
     """The adjoint (conjugate spectrum) and a batch with a distance per entry
     through a variant equal the one-line kernel's results (the radix-64
-    variant 8 exists for 4096-point transforms only: fields of 1025..2048)."""
+    variant 9 exists for 4096-point transforms only: fields of 1025..2048)."""
     import torch
 
     from xlumina_gb300 import engine
     select, _ = variants
-    n = 1100 if v == 8 else 700
     x, y = ref.space(600.0, n)
     rng = np.random.default_rng(77)
     E = torch.as_tensor((rng.standard_normal((3, 2, n, n)) + 1j * rng.standard_normal((3, 2, n, n)))
@@ -179,3 +181,43 @@ def test_czt_row_variants_with_the_fixed_high_na_program(v):
         lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12, saved)
     assert np.all(np.isfinite(res[3]))
     assert rel_l2(res[v], res[3]) < 1e-6
+
+
+def test_czt_column_variants_match():
+    """The persistent chirp-z y transform (variant 1) gives the per-tile
+    kernel's (0) results: a VCZT behind an LCD, forward and adjoint (the Ez
+    fold), and a batch with a distance per entry."""
+    import torch
+
+    import xlumina_gb300.optical_elements as oe
+    import xlumina_gb300.vectorized_optics as vo
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    n, m = 400, 160
+    x, y = ref.space(1200.0, n)
+    xo, yo = ref.space(300.0, m)
+    rng = np.random.default_rng(123)
+    E = torch.as_tensor((rng.standard_normal((2, 3, n, n)) + 1j * rng.standard_normal((2, 3, n, n)))
+                        .astype(np.complex64), device="cuda")
+    G = torch.as_tensor((rng.standard_normal((3, 3, m, m)) + 1j * rng.standard_normal((3, 3, m, m)))
+                        .astype(np.complex64), device="cuda")
+    eta = torch.as_tensor(rng.uniform(0, 6, (3, n, n)).astype(np.float32), device="cuda")
+    logl = list(range(5, 14))
+    saved = {lg: lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_COLS, lg) for lg in logl}
+    res = {}
+    try:
+        for var in (0, 1):
+            for lg in logl:
+                _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_COLS, lg, var))
+            light = vo.VectorizedLight(x, y, 0.6)
+            light.Ex, light.Ey = E[0], E[1]
+            fwd = oe.LCD(light, eta, 0.3).VCZT([1.5e4, 2.0e4, 3.0e4], xo, yo)
+            adj = engine.CztCall([G[0], G[1], G[2]], x, y, 0.6, 2.0e4, xo, yo, "vczt", adjoint=True).run()
+            torch.cuda.synchronize()
+            res[var] = [_np(fwd.Ex), _np(fwd.Ey), _np(fwd.Ez)] + [_np(a) for a in adj]
+    finally:
+        for lg, s in saved.items():
+            lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_COLS, lg, s)
+    for got, exp in zip(res[1], res[0]):
+        assert np.all(np.isfinite(exp))
+        assert rel_l2(got, exp) < 1e-6

@@ -137,25 +137,31 @@ int read_status(unsigned int* flag, int clear) {
 // interleaved packed one with L2 and register prefetch (4), and the one-line
 // kernel with prefetch in two barrier groups (5) or in CTAs of half the
 // columns, two per SM (6), and the two groups of (5) started half a
-// component apart (7); for 4096-point transforms also the radix-64 column
-// pass (8: two passes of 64 elements per thread, one exchange per
+// component apart (7), the one-line kernel persistent (8: the pass twiddle
+// table loaded once per CTA); for 4096-point transforms also the radix-64
+// column pass (9: two passes of 64 elements per thread, one exchange per
 // transform).  The chirp-z x transform: the stage capped for two
 // CTAs per SM (0), every plane staged that fits one CTA per SM (1), no
 // staging (2), as 0 with registers for two CTAs per SM (3).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
-  if (pass == XL_PASS_RS_COLS && log2_len == 12) return 9;
-  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 11) return 8;
+  if (pass == XL_PASS_RS_COLS && log2_len == 12) return 10;
+  if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 11) return 9;
   if (pass == XL_PASS_CZT_ROWS && log2_len >= 5) return 4;
+  if (pass == XL_PASS_CZT_COLS && log2_len >= 5) return 2;
   return 1;
 }
 static std::atomic<int> g_variant[XL_NUM_PASSES][14];
 
 // Defaults that differ from variant 0, by measurement: the 4096-point chirp-z
 // x transform (the 2048^2 high-NA focus) with registers for two CTAs per SM,
-// 1451 against 1400 tables/s on the high-NA optimisation step.
+// 1451 against 1400 tables/s on the high-NA optimisation step; the
+// persistent one-line RS column pass at 4096 points, 1.929 against 1.971 ms
+// per 8 x 2048^2 VRS fields (the same at 2048 points: 5549-5564 against
+// 5524-5566 4f tables/s, so variant 0 stays the default there).
 static const bool g_variant_defaults = [] {
   g_variant[XL_PASS_CZT_ROWS][12].store(3, std::memory_order_relaxed);
+  g_variant[XL_PASS_RS_COLS][12].store(8, std::memory_order_relaxed);
   return true;
 }();
 

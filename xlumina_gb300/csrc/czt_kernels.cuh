@@ -236,7 +236,10 @@ __global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRow
 // y transform over tiles of W columns, with the epilogue.  Lanes interleave
 // the W columns of a tile, so every warp load of the intermediate is one
 // contiguous run.
-template <int LOGL, bool ZU>
+// PERSIST: one CTA per resident slot walks the (column tile, batch entry)
+// units in the grid's order; the pass twiddle table is loaded once per CTA
+// instead of once per tile.
+template <int LOGL, bool ZU, bool PERSIST = false>
 __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_MINB)
     czt_cols(const __grid_constant__ CztLaunch p) {
   using C = CztCfg<LOGL>;
@@ -246,10 +249,6 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
   float2* stw = smem + W * C::CXS;     // NTW
   const int tid = threadIdx.x, lane = tid & 31;
   const int w = lane % W, j = (tid >> 5) * LPW + lane / W;
-  const int t = blockIdx.x, b = blockIdx.y;
-  const int col = t * W + w;
-  const bool live = col < p.mx;
-  const int ny = p.ny;
   {
     const float2* g = pass_tw<LOGL>();
     for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
@@ -257,56 +256,66 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
   __syncthreads();
   float2* xb = xch + w * C::CXS;
   const bool fold = p.adjoint && p.mode == XL_CZT_VECTOR;
-  const double zd = p.zb ? p.zb[b] : p.z;
-  const float zf = (float)zd;
-  const float2* pre_y = czt_entry(p.pre_y, p, b, ny);
-  const float2* g_y = czt_entry(p.g_y, p, b, C::L);
-  const float2* post_y = czt_entry(p.post_y, p, b, p.my);
-  float2 cte = p.cte;
-  if (p.cteb) {
-    cte = p.cteb[b];
-    if (p.adjoint) cte.y = -cte.y;
-  }
+  const int ny = p.ny;
+  const int ntiles = (p.mx + W - 1) / W;
+  const int units = PERSIST ? ntiles * p.B : 1;
 #pragma unroll 1
-  for (int c = 0; c < p.cout; ++c) {
-    const float2* tileT = p.work + ((long long)b * p.cout + c) * ny * p.mxp + (long long)t * ny * W + w;
-    float2 v[16];
-    constexpr int MN = ZU ? C::H : 16;
-#pragma unroll
-    for (int m = 0; m < MN; ++m) {
-      const int n = j + m * C::T - p.ioff_y;
-      v[m] = (live && n >= 0 && n < ny) ? cmul(tileT[(long long)n * W], __ldg(pre_y + n)) : make_float2(0.f, 0.f);
+  for (int u = PERSIST ? (int)blockIdx.x : 0; u < units; u += PERSIST ? (int)gridDim.x : 1) {
+    const int t = PERSIST ? u % ntiles : (int)blockIdx.x;
+    const int b = PERSIST ? u / ntiles : (int)blockIdx.y;
+    const int col = t * W + w;
+    const bool live = col < p.mx;
+    const double zd = p.zb ? p.zb[b] : p.z;
+    const float zf = (float)zd;
+    const float2* pre_y = czt_entry(p.pre_y, p, b, ny);
+    const float2* g_y = czt_entry(p.g_y, p, b, C::L);
+    const float2* post_y = czt_entry(p.post_y, p, b, p.my);
+    float2 cte = p.cte;
+    if (p.cteb) {
+      cte = p.cteb[b];
+      if (p.adjoint) cte.y = -cte.y;
     }
+#pragma unroll 1
+    for (int c = 0; c < p.cout; ++c) {
+      const float2* tileT = p.work + ((long long)b * p.cout + c) * ny * p.mxp + (long long)t * ny * W + w;
+      float2 v[16];
+      constexpr int MN = ZU ? C::H : 16;
 #pragma unroll
-    for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
-    block_fft_x<LOGL, 16, -1, ZU, false>(v, j, xb, stw);
-    {
-      const float2* g = g_y;
-      asm volatile("" : "+l"(g));
-#pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
-    }
-    block_fft_x<LOGL, 16, 1, false, false>(v, j, xb, stw);
-    if (!live) continue;
-#pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      const int o = j + m * C::T - p.ooff_y;
-      if (o < 0 || o >= p.my) continue;
-      float2 val = cmul(v[m], __ldg(post_y + o));
-      if (p.mode != XL_CZT_PLAIN) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
-        const float2 Fv = p.fout ? p.fout[(long long)o * p.mx + col]
-                                 : rs_kernel_value(p.xo[col], p.yo[o], zd, p.inv_lambda, p.k);
-        val = p.adjoint ? cmulc(val, Fv) : cmul(val, Fv);
+      for (int m = 0; m < MN; ++m) {
+        const int n = j + m * C::T - p.ioff_y;
+        v[m] = (live && n >= 0 && n < ny) ? cmul(tileT[(long long)n * W], __ldg(pre_y + n)) : make_float2(0.f, 0.f);
       }
-      val = cmul(val, cte);
-      const long long pix = (long long)b * p.obs + (long long)o * p.mx + col;
-      if (fold && c == 2) {  // adjoint of Ez = (Ex X/r + Ey Y/r) z/r, vectorized_optics.py:341-344
-        const float X = (float)p.xo[col], Y = (float)p.yo[o];
-        const float r2 = X * X + Y * Y + zf * zf;
-        p.out[0][pix] = cadd(p.out[0][pix], cscale(val, X * zf / r2));
-        p.out[1][pix] = cadd(p.out[1][pix], cscale(val, Y * zf / r2));
-      } else {
-        p.out[c][pix] = val;
+#pragma unroll
+      for (int m = MN; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+      block_fft_x<LOGL, 16, -1, ZU, false>(v, j, xb, stw);
+      {
+        const float2* g = g_y;
+        asm volatile("" : "+l"(g));
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(g + j + m * C::T));
+      }
+      block_fft_x<LOGL, 16, 1, false, false>(v, j, xb, stw);
+      if (!live) continue;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int o = j + m * C::T - p.ooff_y;
+        if (o < 0 || o >= p.my) continue;
+        float2 val = cmul(v[m], __ldg(post_y + o));
+        if (p.mode != XL_CZT_PLAIN) {  // wave_optics.py:340, 355: F0 * U (adjoint: conj F)
+          const float2 Fv = p.fout ? p.fout[(long long)o * p.mx + col]
+                                   : rs_kernel_value(p.xo[col], p.yo[o], zd, p.inv_lambda, p.k);
+          val = p.adjoint ? cmulc(val, Fv) : cmul(val, Fv);
+        }
+        val = cmul(val, cte);
+        const long long pix = (long long)b * p.obs + (long long)o * p.mx + col;
+        if (fold && c == 2) {  // adjoint of Ez = (Ex X/r + Ey Y/r) z/r, vectorized_optics.py:341-344
+          const float X = (float)p.xo[col], Y = (float)p.yo[o];
+          const float r2 = X * X + Y * Y + zf * zf;
+          p.out[0][pix] = cadd(p.out[0][pix], cscale(val, X * zf / r2));
+          p.out[1][pix] = cadd(p.out[1][pix], cscale(val, Y * zf / r2));
+        } else {
+          p.out[c][pix] = val;
+        }
       }
     }
   }
@@ -379,9 +388,18 @@ template <int LOGL, bool ZU>
 static int launch_czt_cols(cudaStream_t s, const CztLaunch& p) {
   using C = CztCfg<LOGL>;
   const size_t sm = (size_t)(C::W * C::CXS + C::NTW) * sizeof(float2);
-  cudaError_t e = allow_smem(czt_cols<LOGL, ZU>, sm);
-  if (e != cudaSuccess) return cuda_fail(e, "czt_cols smem");
-  czt_cols<LOGL, ZU><<<dim3((p.mx + C::W - 1) / C::W, p.B), C::COL_THREADS, sm, s>>>(p);
+  // kernel variant: 0 one CTA per column tile and entry; 1 persistent
+  if (kernel_variant(XL_PASS_CZT_COLS, LOGL) == 1) {
+    cudaError_t e = allow_smem(czt_cols<LOGL, ZU, true>, sm);
+    if (e != cudaSuccess) return cuda_fail(e, "czt_cols smem");
+    const int grid = persistent_grid(czt_cols<LOGL, ZU, true>, C::COL_THREADS, sm,
+                                     ((p.mx + C::W - 1) / C::W) * p.B);
+    czt_cols<LOGL, ZU, true><<<grid, C::COL_THREADS, sm, s>>>(p);
+  } else {
+    cudaError_t e = allow_smem(czt_cols<LOGL, ZU>, sm);
+    if (e != cudaSuccess) return cuda_fail(e, "czt_cols smem");
+    czt_cols<LOGL, ZU><<<dim3((p.mx + C::W - 1) / C::W, p.B), C::COL_THREADS, sm, s>>>(p);
+  }
   XL_CHECK_LAUNCH("czt_cols");
   return XL_OK;
 }

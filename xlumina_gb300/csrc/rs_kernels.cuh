@@ -367,7 +367,10 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 // L2 prefetch (PF): the CTA's spectrum columns at the start, and the next
 // component's column tile while this one is transformed, so that their loads
 // meet L2 rather than DRAM latency.
-template <int LOGQ, bool PF>
+// PERSIST: one CTA per resident slot walks the (batch entry, column group)
+// units batch entries fastest, as the grid does otherwise; the pass twiddle
+// table is then loaded once per CTA instead of once per unit.
+template <int LOGQ, bool PF, bool PERSIST = false>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
     rs_cols_conv(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
@@ -377,53 +380,58 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
   float2* stw = smem + CW * C::CXS;    // NTW
   const int tid = threadIdx.x, lane = tid & 31;
   const int wc = lane % CW, j = (tid >> 5) * LPW + lane / CW;
-  // batch entries fastest: the CTAs of one column tile run together and share
-  // its transfer-spectrum columns in L2
-  const int t = blockIdx.y / (W / CW);                      // column tile
-  const int w = (blockIdx.y % (W / CW)) * CW + wc;          // column within the tile
-  const int b = blockIdx.x;
-  const int ny = p.ny;
   {
     const float2* g = pass_tw<C::LOGP>();
     for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
   }
   __syncthreads();
-  const int kx = t * W + w;
-  const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
-  const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
   float2* xb = xch + wc * C::CXS;
-  if (PF && tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
+  const int ny = p.ny;
+  const int units = PERSIST ? p.B * (C::P / CW) : 1;
 #pragma unroll 1
-  for (int c = 0; c < p.cout; ++c) {
-    float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
-    if (PF && tid == 0 && c + 1 < p.cout)
-      l2_prefetch(p.work + ((long long)b * p.cout + c + 1) * ny * C::P + (long long)t * ny * W,
-                  (unsigned)(ny * W * 8));
-    float2 v[16];
+  for (int u = PERSIST ? (int)blockIdx.x : 0; u < units; u += PERSIST ? (int)gridDim.x : 1) {
+    // batch entries fastest: the CTAs of one column tile run together and share
+    // its transfer-spectrum columns in L2
+    const int b = PERSIST ? u % p.B : (int)blockIdx.x;
+    const int g = PERSIST ? u / p.B : (int)blockIdx.y;
+    const int t = g / (W / CW);                      // column tile
+    const int w = (g % (W / CW)) * CW + wc;          // column within the tile
+    const int kx = t * W + w;
+    const float2* sbase = p.specs ? p.specs[b] : p.spec + (long long)(p.sidx ? p.sidx[b] : 0) * p.sstride;
+    const float2* spec = sbase + (long long)(kx / C::SW) * C::P * C::SW + kx % C::SW;
+    if (PF && tid == 0) l2_prefetch(sbase + (long long)(kx / C::SW) * C::P * C::SW, (unsigned)(C::P * C::SW * 8));
+#pragma unroll 1
+    for (int c = 0; c < p.cout; ++c) {
+      float2* tile = p.work + ((long long)b * p.cout + c) * ny * C::P + (long long)t * ny * W + w;
+      if (PF && tid == 0 && c + 1 < p.cout)
+        l2_prefetch(p.work + ((long long)b * p.cout + c + 1) * ny * C::P + (long long)t * ny * W,
+                    (unsigned)(ny * W * 8));
+      float2 v[16];
 #pragma unroll
-    for (int m = 0; m < C::H; ++m) {
-      const int n = j + m * C::T;
-      v[m] = n < ny ? tile[(long long)n * W] : make_float2(0.f, 0.f);
-    }
+      for (int m = 0; m < C::H; ++m) {
+        const int n = j + m * C::T;
+        v[m] = n < ny ? tile[(long long)n * W] : make_float2(0.f, 0.f);
+      }
 #pragma unroll
-    for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
-    block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
-    // the spectrum loads stay here rather than ahead of the transform, where
-    // they would hold 32 registers through it
-    const float2* sp = spec;
-    asm volatile("" : "+l"(sp));
-    if (p.adjoint) {
+      for (int m = C::H; m < 16; ++m) v[m] = make_float2(0.f, 0.f);
+      block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
+      // the spectrum loads stay here rather than ahead of the transform, where
+      // they would hold 32 registers through it
+      const float2* sp = spec;
+      asm volatile("" : "+l"(sp));
+      if (p.adjoint) {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
-    } else {
+        for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+      } else {
 #pragma unroll
-      for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
-    }
-    block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
+        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+      }
+      block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
 #pragma unroll
-    for (int m = 0; m < C::H; ++m) {
-      const int n = j + m * C::T;
-      if (n < ny) tile[(long long)n * W] = v[m];
+      for (int m = 0; m < C::H; ++m) {
+        const int n = j + m * C::T;
+        if (n < ny) tile[(long long)n * W] = v[m];
+      }
     }
   }
 }
@@ -902,13 +910,18 @@ static int launch_cols64(cudaStream_t st, const RsLaunch& p) {
   return XL_OK;
 }
 
-template <int LOGQ, bool PF>
+template <int LOGQ, bool PF, bool PERSIST = false>
 static int launch_cols(cudaStream_t st, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
   const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
-  cudaError_t e = allow_smem(rs_cols_conv<LOGQ, PF>, sm);
+  cudaError_t e = allow_smem(rs_cols_conv<LOGQ, PF, PERSIST>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
-  rs_cols_conv<LOGQ, PF><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
+  if constexpr (PERSIST) {
+    const int grid = persistent_grid(rs_cols_conv<LOGQ, PF, true>, C::COL_THREADS, sm, p.B * (C::P / C::CW));
+    rs_cols_conv<LOGQ, PF, true><<<grid, C::COL_THREADS, sm, st>>>(p);
+  } else {
+    rs_cols_conv<LOGQ, PF><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
+  }
   XL_CHECK_LAUNCH("rs_cols_conv");
   return XL_OK;
 }
@@ -945,8 +958,11 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
       if (var == 6) return launch_cols_g<LOGQ, C::CW / 2, 1>(st, p);
       if (var == 7) return launch_cols_g<LOGQ, C::CW, 2, true>(st, p);
     }
+    if constexpr (LOGQ >= 9 && LOGQ <= 11) {
+      if (var == 8) return launch_cols<LOGQ, false, true>(st, p);
+    }
     if constexpr (LOGQ == 11) {
-      if (var == 8) return launch_cols64<LOGQ>(st, p);
+      if (var == 9) return launch_cols64<LOGQ>(st, p);
     }
     return launch_cols<LOGQ, false>(st, p);
   } else {
