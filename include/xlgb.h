@@ -135,13 +135,15 @@ enum {
 /* Variants available for `pass` at transform length 2^log2_len (>= 1; 0 if
  * the pass or length is unknown).  Variant 0 is the default kernel shape
  * except at 4096 points: the RS column pass defaults to variant 8 (the
- * one-line kernel, persistent) and the chirp-z x transform to variant 3
- * (registers sized for two CTAs per SM).  The others are the alternatives
- * the autotuner measures against the default.  RS column pass: 0 one line
- * per thread, 1-2 two lines per thread (packed FP32), 3-7 prefetching,
- * barrier groups, CTA shapes, 8 persistent one line, 9 (4096 points)
- * radix 64.  Chirp-z x transform: 0 the stage capped for two CTAs per SM,
- * 1 for one, 2 no stage, 3 as 0 with registers for two CTAs. */
+ * one-line kernel, persistent), the chirp-z x transform to variant 3
+ * (registers sized for two CTAs per SM) and the chirp-z y transform to
+ * variant 1 (persistent).  The others are the alternatives the autotuner
+ * measures against the default.  RS column pass: 0 one line per thread,
+ * 1-2 two lines per thread (packed FP32), 3-7 prefetching, barrier groups,
+ * CTA shapes, 8 persistent one line, 9 (4096 points) radix 64.  Chirp-z x
+ * transform: 0 the stage capped for two CTAs per SM, 1 for one, 2 no
+ * stage, 3 as 0 with registers for two CTAs.  Chirp-z y transform: 0 one
+ * CTA per column tile and entry, 1 persistent. */
 int xl_kernel_variant_count(int pass, int log2_len);
 /* Select variant `variant` (< the count) for later launches. */
 int xl_set_kernel_variant(int pass, int log2_len, int variant);

@@ -44,6 +44,8 @@ def test_variant_table_bounds():
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 9
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 4
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_COLS, 12) == 2
+    assert lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_COLS, 12) == 1   # the default at 4096 points
     assert lib.xl_kernel_variant_count(99, 12) == 0
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 10) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 9) == _lib.XL_EINVAL

@@ -142,7 +142,8 @@ int read_status(unsigned int* flag, int clear) {
 // column pass (9: two passes of 64 elements per thread, one exchange per
 // transform).  The chirp-z x transform: the stage capped for two
 // CTAs per SM (0), every plane staged that fits one CTA per SM (1), no
-// staging (2), as 0 with registers for two CTAs per SM (3).
+// staging (2), as 0 with registers for two CTAs per SM (3).  The chirp-z y
+// transform: one CTA per column tile and entry (0), persistent (1).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
   if (pass == XL_PASS_RS_COLS && log2_len == 12) return 10;
@@ -159,9 +160,13 @@ static std::atomic<int> g_variant[XL_NUM_PASSES][14];
 // persistent one-line RS column pass at 4096 points, 1.929 against 1.971 ms
 // per 8 x 2048^2 VRS fields (the same at 2048 points: 5549-5564 against
 // 5524-5566 4f tables/s, so variant 0 stays the default there).
+// The persistent chirp-z y transform at 4096 points: 1945 against 1925
+// tables/s on the high-NA step (on the 4f step's 2048- and 1024-point
+// transforms it measured 0.3 % slower, so variant 0 stays there).
 static const bool g_variant_defaults = [] {
   g_variant[XL_PASS_CZT_ROWS][12].store(3, std::memory_order_relaxed);
   g_variant[XL_PASS_RS_COLS][12].store(8, std::memory_order_relaxed);
+  g_variant[XL_PASS_CZT_COLS][12].store(1, std::memory_order_relaxed);
   return true;
 }();
 
