@@ -983,6 +983,14 @@ def main():
                     help="run one section alone (for profiling): czt = the high-NA focus, "
                          "hybrid = the sharp-focus discovery step")
     args = ap.parse_args()
+    for pass_name, v in (("XL_PASS_CZT_ROWS", args.czt_rows_variant), ("XL_PASS_CZT_COLS", args.czt_cols_variant)):
+        if v is None:
+            continue
+        from xlumina_gb300 import _lib, engine
+        pid = getattr(_lib, pass_name)
+        for lg in range(5, 14):   # every transform length that has the variant
+            if v < engine.lib().xl_kernel_variant_count(pid, lg):
+                _lib.check(engine.lib().xl_set_kernel_variant(pid, lg, v))
     if args.only == "czt":
         print(json.dumps({"czt_high_na": run_czt(batch=args.batch, steps=args.steps, warmup=args.warmup,
                                                   check=False)}))
@@ -990,14 +998,6 @@ def main():
     if args.only == "hybrid":
         print(json.dumps({"hybrid_sharp_focus": run_hybrid(steps=args.steps, warmup=args.warmup)}))
         return
-    if args.czt_rows_variant is not None:
-        from xlumina_gb300 import _lib, engine
-        for lg in range(5, 14):
-            _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, lg, args.czt_rows_variant))
-    if args.czt_cols_variant is not None:
-        from xlumina_gb300 import _lib, engine
-        for lg in range(5, 14):
-            _lib.check(engine.lib().xl_set_kernel_variant(_lib.XL_PASS_CZT_COLS, lg, args.czt_cols_variant))
     if args.only in ("highna_step", "fourf_step"):
         import torch
 

@@ -142,8 +142,9 @@ enum {
  * 1-2 two lines per thread (packed FP32), 3-7 prefetching, barrier groups,
  * CTA shapes, 8 persistent one line, 9 (4096 points) radix 64.  Chirp-z x
  * transform: 0 the stage capped for two CTAs per SM, 1 for one, 2 no
- * stage, 3 as 0 with registers for two CTAs.  Chirp-z y transform: 0 one
- * CTA per column tile and entry, 1 persistent. */
+ * stage, 3 as 0 with registers for two CTAs, 4 (4096 points, three
+ * components) one component group, two CTAs per SM.  Chirp-z y transform:
+ * 0 one CTA per column tile and entry, 1 persistent. */
 int xl_kernel_variant_count(int pass, int log2_len);
 /* Select variant `variant` (< the count) for later launches. */
 int xl_set_kernel_variant(int pass, int log2_len, int variant);

@@ -43,7 +43,8 @@ def test_variant_table_bounds():
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 10
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 9
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 4
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 5
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 11) == 4
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_COLS, 12) == 2
     assert lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_COLS, 12) == 1   # the default at 4096 points
     assert lib.xl_kernel_variant_count(99, 12) == 0
@@ -221,5 +222,41 @@ def test_czt_column_variants_match():
         for lg, s in saved.items():
             lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_COLS, lg, s)
     for got, exp in zip(res[1], res[0]):
+        assert np.all(np.isfinite(exp))
+        assert rel_l2(got, exp) < 1e-6
+
+
+def test_czt_row_one_group_variant_matches():
+    """Variant 4 of the 4096-point chirp-z x transform (one component group
+    transforming Ex, Ey, Ez one after the other, two CTAs per SM) gives the
+    default kernel's VCZT behind an LCD, and the full high-NA focus."""
+    import torch
+
+    import xlumina_gb300.optical_elements as oe
+    import xlumina_gb300.vectorized_optics as vo
+    from xlumina_gb300 import _lib, engine
+    lib = engine.lib()
+    n, m = 1500, 600           # Bluestein length 4096 on both axes
+    x, y = ref.space(1800.0, n)
+    xo, yo = ref.space(300.0, m)
+    rng = np.random.default_rng(44)
+    E = torch.as_tensor((rng.standard_normal((2, 2, n, n)) + 1j * rng.standard_normal((2, 2, n, n)))
+                        .astype(np.complex64), device="cuda")
+    eta = torch.as_tensor(rng.uniform(0, 6, (2, n, n)).astype(np.float32), device="cuda")
+    saved = lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12)
+    res = {}
+    try:
+        for var in (saved, 4):
+            _lib.check(lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12, var))
+            light = vo.VectorizedLight(x, y, 0.65)
+            light.Ex, light.Ey = E[0], E[1]
+            a = oe.LCD(light, eta, 0.3).VCZT(2.0e4, xo, yo)
+            xf, yf = ref.space(3.0, m)
+            b = oe.VCZT_objective_lens(oe.sSLM(light, eta, eta), 900.0, 1000.0, xf, yf)
+            torch.cuda.synchronize()
+            res[var] = [_np(a.Ex), _np(a.Ey), _np(a.Ez), _np(b.Ex), _np(b.Ey), _np(b.Ez)]
+    finally:
+        lib.xl_set_kernel_variant(_lib.XL_PASS_CZT_ROWS, 12, saved)
+    for got, exp in zip(res[4], res[saved]):
         assert np.all(np.isfinite(exp))
         assert rel_l2(got, exp) < 1e-6

@@ -54,9 +54,10 @@ template <int LOGL> struct CztCfg {
 // x transform organisation for NC line components: CG component groups of G
 // rows of T threads; CG = NC (every component of a row at once) when the CTA
 // can hold them, else 1.
-template <int LOGL, int NC> struct CztRowCfg {
+template <int LOGL, int NC, bool OG = false> struct CztRowCfg {
   using C = CztCfg<LOGL>;
-  static constexpr int CG = (NC * C::G * C::T <= 1024) ? NC : 1;
+  // OG: one component group whatever NC (the components one after the other)
+  static constexpr int CG = (!OG && NC * C::G * C::T <= 1024) ? NC : 1;
   static constexpr int ITER = (NC + CG - 1) / CG;              // transforms per group and row
   static constexpr int LINES = CG * C::G;
   static constexpr int THREADS = LINES * C::T;
@@ -73,11 +74,11 @@ __device__ __forceinline__ long long tiled_rt(int r, int col, int rows, int lw) 
 // CTAs per SM the registers are sized for (0: CztRowCfg's MINB).  FK: the
 // fused program's op kinds fixed at compile time (FixedKinds<...>, for the
 // tables' programs), or FixedKinds<>.
-template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>>
-__global__ void __launch_bounds__(CztRowCfg<LOGL, NC>::THREADS, MB ? MB : CztRowCfg<LOGL, NC>::MINB)
+template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>, bool OG = false>
+__global__ void __launch_bounds__(CztRowCfg<LOGL, NC, OG>::THREADS, MB ? MB : CztRowCfg<LOGL, NC, OG>::MINB)
     czt_rows(const __grid_constant__ CztLaunch p, const __grid_constant__ RowStage st) {
   using C = CztCfg<LOGL>;
-  using F = CztRowCfg<LOGL, NC>;
+  using F = CztRowCfg<LOGL, NC, OG>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = p.nx, ny = p.ny;
   float2* xch = (float2*)smraw;                                    // LINES x XS
@@ -324,10 +325,10 @@ __global__ void __launch_bounds__(CztCfg<LOGL>::COL_THREADS, CztCfg<LOGL>::COL_M
 // ---------------------------------------------------------------------------
 // Launch code.
 
-template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>>
+template <int LOGL, int NC, bool ZU, int MB = 0, class FK = FixedKinds<>, bool OG = false>
 static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   using C = CztCfg<LOGL>;
-  using F = CztRowCfg<LOGL, NC>;
+  using F = CztRowCfg<LOGL, NC, OG>;
   const size_t fixed = ((size_t)(F::LINES * C::XS + NC * C::G * p.nx) * 8 + 15) / 16 * 16;
   // kernel variant: 0 cap the stage so that two CTAs fit per SM where the
   // registers allow two (the one-component transforms; three components keep
@@ -337,13 +338,20 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
   // sized for two CTAs per SM instead of three (MB = 2: no spills).
   // Measured on the Ez-only high-NA step (32 x 2048^2): 1354 (0), 1138 (1),
   // 1348 (2) tables/s.
-  const int var = kernel_variant(XL_PASS_CZT_ROWS, LOGL);
+  // 4 (three components, 4096 points): one component group transforming
+  // the components one after the other, two CTAs per SM as in 3.
+  int var = kernel_variant(XL_PASS_CZT_ROWS, LOGL);
+  if (var == 4 && NC == 1) var = 3;   // a single component is one group already
+  if constexpr (NC == 3 && LOGL == 12 && !OG) {
+    if (var == 4) return launch_czt_rows<LOGL, NC, ZU, 2, FK, true>(s, p);
+  }
   constexpr int MB2 = 512 / F::THREADS;   // two CTAs of 256 threads
   if constexpr (NC == 1 && MB == 0 && MB2 >= 1 && MB2 < F::MINB) {
     if (var == 3) return launch_czt_rows<LOGL, NC, ZU, MB2, FK>(s, p);
   }
   const size_t one_cta = (size_t)226 * 1024, two_cta = (size_t)(227 * 1024) / 2 - 1024;
-  const size_t cap = (var == 0 || var == 3) ? (NC == 1 ? two_cta : one_cta) : var == 1 ? one_cta : 0;
+  const size_t cap = (var == 0 || var == 3 || var == 4) ? ((NC == 1 || OG) ? two_cta : one_cta)
+                     : var == 1 ? one_cta : 0;
   RowStage st;
   plan_row_stage(p.cin, p.in, p.ibs, p.nx, p.pre, C::G, fixed, st, cap);
   const size_t sm = fixed + (size_t)C::G * st.row_bytes + 16;
@@ -351,11 +359,11 @@ static int launch_czt_rows(cudaStream_t s, const CztLaunch& p) {
     set_error("czt: input row of %d columns too long for shared memory", p.nx);
     return XL_EUNSUPPORTED;
   }
-  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU, MB, FK>, sm);
+  cudaError_t e = allow_smem(czt_rows<LOGL, NC, ZU, MB, FK, OG>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "czt_rows smem");
   const int total = p.B * ((p.ny + C::G - 1) / C::G);
-  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU, MB, FK>, F::THREADS, sm, total);
-  czt_rows<LOGL, NC, ZU, MB, FK><<<grid, F::THREADS, sm, s>>>(p, st);
+  const int grid = persistent_grid(czt_rows<LOGL, NC, ZU, MB, FK, OG>, F::THREADS, sm, total);
+  czt_rows<LOGL, NC, ZU, MB, FK, OG><<<grid, F::THREADS, sm, s>>>(p, st);
   XL_CHECK_LAUNCH("czt_rows");
   return XL_OK;
 }
