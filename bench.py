@@ -194,10 +194,12 @@ def cpu_vrs_field(ref, x, Ex, Ey, eta, theta, alpha, z):
     return ref.vrs_propagate(ax, ay, x, x, WAVELENGTH, z)
 
 
-def run_reference(args, budget_s=90.0):
+def run_reference(args, budget_s=150.0):
     """The reference algorithm on the host cores, one field per step.  A CPU
     field takes over a second, so the timed steps are capped at about
-    `budget_s` of work (at least 3); the line reports how many were timed."""
+    `budget_s` of work (at least 5; about 100 fields at 1.4 s each, the
+    sample size planned for the 2048^2 propagators); the line reports how
+    many were timed."""
     from oracle import xlumina_ref as ref
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:      # under torchrun rank 0 alone runs the CPU reference
