@@ -495,7 +495,8 @@ def run_gpu(args):
                                             "the groups started half a component apart; 8 one line per thread, "
                                             "persistent (the library's default at 4096 points); 9 (4096 "
                                             "points) radix-64, 64 elements per thread, one exchange per "
-                                            "transform"},
+                                            "transform; 10 (4096 points) as 8, each unit's spectrum values "
+                                            "kept in Tensor Memory for its second and third components"},
         "pipeline_roofline": {"alg_bytes_per_field": 272 * n2, "achieved": pipe_gbs, "frac": pipe_gbs / peak},
         "plain_path": {"value": plain, "unit": "fields/s", "how": "one VRS_propagation call per field"},
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -140,7 +140,8 @@ enum {
  * variant 1 (persistent).  The others are the alternatives the autotuner
  * measures against the default.  RS column pass: 0 one line per thread,
  * 1-2 two lines per thread (packed FP32), 3-7 prefetching, barrier groups,
- * CTA shapes, 8 persistent one line, 9 (4096 points) radix 64.  Chirp-z x
+ * CTA shapes, 8 persistent one line, 9 (4096 points) radix 64, 10 (4096
+ * points) as 8 with each unit's spectrum values kept in Tensor Memory.  Chirp-z x
  * transform: 0 the stage capped for two CTAs per SM, 1 for one, 2 no
  * stage, 3 as 0 with registers for two CTAs, 4 (4096 points, three
  * components) one component group, two CTAs per SM.  Chirp-z y transform:

@@ -1,7 +1,8 @@
 """Every kernel variant of a pass gives the oracle's result: the packed
 two-line column pass (interleaved, in barrier groups, with prefetching), the
 prefetching and the persistent one-line kernels and, at 4096 points, the
-radix-64 kernel, against the one-line kernel and the FP64 oracle, for the
+radix-64 kernel and the persistent kernel that keeps each unit's spectrum
+values in Tensor Memory (variant 10), against the one-line kernel and the FP64 oracle, for the
 transform lengths that have them (1024, 2048 and 4096 points: fields of
 257..2048 per side).
 
@@ -40,7 +41,7 @@ def variants():
 def test_variant_table_bounds():
     from xlumina_gb300 import _lib, engine
     lib = engine.lib()
-    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 10
+    assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 12) == 11
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 11) == 9
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_RS_COLS, 6) == 1
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_ROWS, 12) == 5
@@ -48,7 +49,7 @@ def test_variant_table_bounds():
     assert lib.xl_kernel_variant_count(_lib.XL_PASS_CZT_COLS, 12) == 2
     assert lib.xl_get_kernel_variant(_lib.XL_PASS_CZT_COLS, 12) == 1   # the default at 4096 points
     assert lib.xl_kernel_variant_count(99, 12) == 0
-    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 10) == _lib.XL_EINVAL
+    assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 12, 11) == _lib.XL_EINVAL
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 11, 9) == _lib.XL_EINVAL
     assert lib.xl_get_kernel_variant(_lib.XL_PASS_RS_COLS, 12) == 8   # the default at 4096 points
     assert lib.xl_set_kernel_variant(_lib.XL_PASS_RS_COLS, 6, 1) == _lib.XL_EINVAL
@@ -63,7 +64,7 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
     select, count = variants
     logp = engine.rs_logq(n, n) + 1
     nv = count(logp)
-    assert nv == (10 if logp == 12 else 9)
+    assert nv == (11 if logp == 12 else 9)
     x, y = ref.space(1000.0, n)
     rng = np.random.default_rng(n + vector)
     Ex = ref.gaussian_beam(x, y, 0.633, (300.0, 300.0)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (n, n)))
@@ -89,11 +90,12 @@ def test_rs_column_variants_match_oracle(variants, n, vector):
 
 
 @pytest.mark.parametrize("v,n", [(1, 700), (2, 700), (3, 700), (4, 700), (5, 700), (6, 700), (7, 700), (8, 700),
-                                 (8, 1100), (9, 1100)])
+                                 (8, 1100), (9, 1100), (10, 1100)])
 def test_rs_column_variants_adjoint_and_batch(variants, v, n):
     """The adjoint (conjugate spectrum) and a batch with a distance per entry
     through a variant equal the one-line kernel's results (the radix-64
-    variant 9 exists for 4096-point transforms only: fields of 1025..2048)."""
+    variant 9 and the Tensor Memory variant 10 exist for 4096-point
+    transforms only: fields of 1025..2048)."""
     import torch
 
     from xlumina_gb300 import engine

@@ -140,7 +140,8 @@ int read_status(unsigned int* flag, int clear) {
 // component apart (7), the one-line kernel persistent (8: the pass twiddle
 // table loaded once per CTA); for 4096-point transforms also the radix-64
 // column pass (9: two passes of 64 elements per thread, one exchange per
-// transform).  The chirp-z x transform: the stage capped for two
+// transform) and the persistent one-line kernel that keeps each unit's
+// spectrum values in Tensor Memory for its later components (10).  The chirp-z x transform: the stage capped for two
 // CTAs per SM (0), every plane staged that fits one CTA per SM (1), no
 // staging (2), as 0 with registers for two CTAs per SM (3), and at 4096
 // points for three components one group transforming them one after the
@@ -148,7 +149,7 @@ int read_status(unsigned int* flag, int clear) {
 // tile and entry (0), persistent (1).
 static int variant_count(int pass, int log2_len) {
   if (pass < 0 || pass >= XL_NUM_PASSES || log2_len < 1 || log2_len > 13) return 0;
-  if (pass == XL_PASS_RS_COLS && log2_len == 12) return 10;
+  if (pass == XL_PASS_RS_COLS && log2_len == 12) return 11;
   if (pass == XL_PASS_RS_COLS && log2_len >= 10 && log2_len <= 11) return 9;
   if (pass == XL_PASS_CZT_ROWS && log2_len == 12) return 5;
   if (pass == XL_PASS_CZT_ROWS && log2_len >= 5) return 4;

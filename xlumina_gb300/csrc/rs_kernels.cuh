@@ -359,6 +359,51 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
   }
 }
 
+// ---- Tensor Memory (tcgen05) as per-thread storage ----
+// TMEM is 128 lanes x 512 columns of 32-bit cells per SM.  With the 32x32b
+// access shape, thread i of warp w reads and writes lane 32 (w mod 4) + i, so
+// each thread owns its own cells; the kernels below give a thread 32
+// consecutive columns of its lane (16 complex values).  One warp allocates
+// the CTA's columns and hands the base address out through shared memory;
+// the same warp frees them before the CTA exits.
+__device__ __forceinline__ void tmem_alloc(unsigned* dst_smem, unsigned ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// four complex values into this thread's cells [col, col + 8)
+__device__ __forceinline__ void tmem_st4(unsigned taddr, float2 a, float2 b, float2 c, float2 d) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y), "f"(d.x), "f"(d.y)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// four complex values back; the values pass through the wait so that no use
+// is scheduled before the load has completed
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float2 (&o)[4]) {
+  float r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+f"(r[0]), "+f"(r[1]), "+f"(r[2]), "+f"(r[3]), "+f"(r[4]), "+f"(r[5]), "+f"(r[6]), "+f"(r[7])
+               :
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = make_float2(r[2 * i], r[2 * i + 1]);
+}
+
 // Column pass, in place on one tile of W spectrum columns: FFT along y of the
 // ny nonzero rows (pruned first pass), multiply by the transfer spectrum
 // (conjugate for the adjoint), inverse FFT, keep the ny surviving rows.
@@ -370,21 +415,40 @@ __global__ void __launch_bounds__(RowCfg<LOGQ, MODE == 1 ? 1 : 3>::THREADS, RowC
 // PERSIST: one CTA per resident slot walks the (batch entry, column group)
 // units batch entries fastest, as the grid does otherwise; the pass twiddle
 // table is then loaded once per CTA instead of once per unit.
-template <int LOGQ, bool PF, bool PERSIST = false>
+// TM (with PERSIST): the unit's spectrum values are read from global memory
+// for its first component only and kept in Tensor Memory for the others
+// (each thread's 16 values in its own TMEM cells), so the three components of
+// a VRS field read the spectrum tile from L2 once instead of three times.
+template <int LOGQ, bool PF, bool PERSIST = false, bool TM = false>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
     rs_cols_conv(const __grid_constant__ RsLaunch p) {
   using C = RsCfg<LOGQ>;
   constexpr int W = C::W, CW = C::CW, LPW = 32 / CW;
+  // TMEM columns: 32 per thread, the warps of a lane quarter side by side
+  constexpr unsigned TM_COLS = (unsigned)(C::COL_THREADS / 128) * 32u;
+  static_assert(!TM || (PERSIST && C::COL_THREADS % 128 == 0 && TM_COLS >= 32 && TM_COLS <= 256 &&
+                        (TM_COLS & (TM_COLS - 1)) == 0),
+                "TMEM spectrum cache: persistent CTAs of whole warp quarters, a power-of-two column count");
   extern __shared__ __align__(16) float2 smem[];
+  __shared__ unsigned s_tmem;
   float2* xch = smem;                  // CW x CXS
   float2* stw = smem + CW * C::CXS;    // NTW
   const int tid = threadIdx.x, lane = tid & 31;
   const int wc = lane % CW, j = (tid >> 5) * LPW + lane / CW;
+  if constexpr (TM) {
+    if (tid < 32) tmem_alloc(&s_tmem, TM_COLS);
+  }
   {
     const float2* g = pass_tw<C::LOGP>();
     for (int i = tid; i < C::NTW; i += blockDim.x) stw[i] = g[i];
   }
+  if constexpr (TM) tmem_fence_before_sync();
   __syncthreads();
+  unsigned tcell = 0;   // this thread's first TMEM cell: lane 32 (warp mod 4) + lane, 32 columns per warp
+  if constexpr (TM) {
+    tmem_fence_after_sync();
+    tcell = s_tmem + ((32u * ((unsigned)(tid >> 5) & 3u)) << 16) + (unsigned)(tid >> 7) * 32u;
+  }
   float2* xb = xch + wc * C::CXS;
   const int ny = p.ny;
   const int units = PERSIST ? p.B * (C::P / CW) : 1;
@@ -417,14 +481,37 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
       block_fft_x<C::LOGP, 16, -1, true, false>(v, j, xb, stw);
       // the spectrum loads stay here rather than ahead of the transform, where
       // they would hold 32 registers through it
-      const float2* sp = spec;
-      asm volatile("" : "+l"(sp));
-      if (p.adjoint) {
+      if (TM && c > 0) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+        for (int q = 0; q < 4; ++q) {
+          float2 s[4];
+          tmem_ld4(tcell + 8u * q, s);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) v[4 * q + i] = p.adjoint ? cmulc(v[4 * q + i], s[i]) : cmul(v[4 * q + i], s[i]);
+        }
+      } else if (TM) {
+        const float2* sp = spec;
+        asm volatile("" : "+l"(sp));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float2 s[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) s[i] = __ldg(sp + (long long)(j + (4 * q + i) * C::T) * C::SW);
+          tmem_st4(tcell + 8u * q, s[0], s[1], s[2], s[3]);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) v[4 * q + i] = p.adjoint ? cmulc(v[4 * q + i], s[i]) : cmul(v[4 * q + i], s[i]);
+        }
+        tmem_wait_st();   // the stores are complete before the next component's loads
       } else {
+        const float2* sp = spec;
+        asm volatile("" : "+l"(sp));
+        if (p.adjoint) {
 #pragma unroll
-        for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+          for (int m = 0; m < 16; ++m) v[m] = cmulc(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+        } else {
+#pragma unroll
+          for (int m = 0; m < 16; ++m) v[m] = cmul(v[m], __ldg(sp + (long long)(j + m * C::T) * C::SW));
+        }
       }
       block_fft_x<C::LOGP, 16, 1, false, false>(v, j, xb, stw);
 #pragma unroll
@@ -432,6 +519,15 @@ __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MIN
         const int n = j + m * C::T;
         if (n < ny) tile[(long long)n * W] = v[m];
       }
+    }
+  }
+  if constexpr (TM) {
+    // every thread is done with its cells before the allocating warp frees them
+    tmem_fence_before_sync();
+    __syncthreads();
+    if (tid < 32) {
+      tmem_fence_after_sync();
+      tmem_dealloc(s_tmem, TM_COLS);
     }
   }
 }
@@ -910,15 +1006,15 @@ static int launch_cols64(cudaStream_t st, const RsLaunch& p) {
   return XL_OK;
 }
 
-template <int LOGQ, bool PF, bool PERSIST = false>
+template <int LOGQ, bool PF, bool PERSIST = false, bool TM = false>
 static int launch_cols(cudaStream_t st, const RsLaunch& p) {
   using C = RsCfg<LOGQ>;
   const size_t sm = (size_t)(C::CW * C::CXS + C::NTW) * sizeof(float2);
-  cudaError_t e = allow_smem(rs_cols_conv<LOGQ, PF, PERSIST>, sm);
+  cudaError_t e = allow_smem(rs_cols_conv<LOGQ, PF, PERSIST, TM>, sm);
   if (e != cudaSuccess) return cuda_fail(e, "rs_cols_conv smem");
   if constexpr (PERSIST) {
-    const int grid = persistent_grid(rs_cols_conv<LOGQ, PF, true>, C::COL_THREADS, sm, p.B * (C::P / C::CW));
-    rs_cols_conv<LOGQ, PF, true><<<grid, C::COL_THREADS, sm, st>>>(p);
+    const int grid = persistent_grid(rs_cols_conv<LOGQ, PF, true, TM>, C::COL_THREADS, sm, p.B * (C::P / C::CW));
+    rs_cols_conv<LOGQ, PF, true, TM><<<grid, C::COL_THREADS, sm, st>>>(p);
   } else {
     rs_cols_conv<LOGQ, PF><<<dim3(p.B, C::P / C::CW), C::COL_THREADS, sm, st>>>(p);
   }
@@ -963,6 +1059,7 @@ static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
     }
     if constexpr (LOGQ == 11) {
       if (var == 9) return launch_cols64<LOGQ>(st, p);
+      if (var == 10) return launch_cols<LOGQ, false, true, true>(st, p);
     }
     return launch_cols<LOGQ, false>(st, p);
   } else {
