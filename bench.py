@@ -145,6 +145,15 @@ class ClockSampler:
 # scaled per field (every field is an independent slice of those launches).
 # The column-pass variants move the same bytes (within 2 % at batch 2).
 NCU_TRAFFIC_PER_FIELD = {"rs_rows_fwd": 276.15e6, "rs_cols_conv": 478.88e6, "rs_rows_inv": 283.60e6}
+# Warp instructions per 2048^2 VRS field of the column pass, by kernel variant
+# (ncu smsp__inst_executed.sum of one launch of the batch-2 case, halved; the
+# instruction stream does not depend on the batch): NCU_INST_COMMAND below
+# with V = 8 and 10.  The pass's issue ceiling is 4 warp instructions per
+# cycle per SM (one per scheduler).
+NCU_COL_INST_PER_FIELD = {8: 303.87e6 / 2, 10: 314.38e6 / 2}
+NCU_INST_COMMAND = ("ncu --metrics smsp__inst_executed.sum --clock-control none -k regex:rs_cols -s 4 -c 1 "
+                    "python bench.py --steps 2 --warmup 3 --batch 2 --no-cpu-baseline --no-fwd-bwd --no-serving "
+                    "--no-parity --col-variant V")
 NCU_TRAFFIC_COMMAND = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum "
                        "--clock-control none -k regex:rs_cols -s 1 -c 1 python bench.py --steps 10 --warmup 3 "
                        "--no-cpu-baseline --no-fwd-bwd --no-serving")
@@ -462,6 +471,22 @@ def run_gpu(args):
                  (d2h + h2d) / (link["duplex_gbs"] * 1e9))
     link["bound_fields_per_s"] = B / link_s
 
+    # the column pass against its instruction-issue ceiling: warp instructions
+    # per launch (ncu, per variant) over the SMs' issue rate at the SM clock
+    # sampled while the timed region ran
+    clocks = clk.summary()
+    inst = NCU_COL_INST_PER_FIELD.get(int(tuned["variant"]))
+    issue_roofline = None
+    if inst is not None and clocks.get("sm_mhz"):
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        ipeak = n_sm * 4 * float(clocks["sm_mhz"]) * 1e6
+        iach = inst * B / (stage_ms[1] / 1e3)
+        issue_roofline = {"bound": "instruction issue", "kernel": "rs_cols_conv", "variant": int(tuned["variant"]),
+                          "achieved": iach, "peak": ipeak, "unit": "warp instructions/s", "frac": iach / ipeak,
+                          "instructions_per_launch": inst * B,
+                          "source": "ncu smsp__inst_executed.sum per field x fields per launch: " + NCU_INST_COMMAND,
+                          "peak_how": "%d SMs x 4 schedulers x the median SM clock of the timed region" % n_sm}
+
     line = {
         "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -478,6 +503,7 @@ def run_gpu(args):
                                        "dram__bytes_read.sum + dram__bytes_write.sum: " + NCU_TRAFFIC_COMMAND,
                      "peak_source": peak_src,
                      "alg_bytes_per_launch": alg[dom], "ms_per_launch": stage_ms[dom]},
+        "issue_roofline": issue_roofline,
         "rel_l2": parity,
         "latency": {"step_ms_p50": float(np.percentile(step_ms, 50)),
                     "step_ms_p99": float(np.percentile(step_ms, 99)),
@@ -505,7 +531,7 @@ def run_gpu(args):
                                             "timed outside the timed region, best of 5 timings; bound = B / "
                                             "the longest of the step's copies at these rates")},
         "gpu_launches": 3 * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "spectrum_builds": engine.SPECTRA.builds,
     }
     if world > 1:   # the single-GPU sections below are not replicated
