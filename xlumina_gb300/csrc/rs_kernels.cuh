@@ -419,6 +419,9 @@ __device__ __forceinline__ void tmem_ld4(unsigned taddr, float2 (&o)[4]) {
 // for its first component only and kept in Tensor Memory for the others
 // (each thread's 16 values in its own TMEM cells), so the three components of
 // a VRS field read the spectrum tile from L2 once instead of three times.
+// The CTA allocates 256 of an SM's 512 TMEM columns; its shared memory allows
+// one such CTA per SM and no other kernel of the library allocates Tensor
+// Memory, so the allocation never has to wait for columns to be freed.
 template <int LOGQ, bool PF, bool PERSIST = false, bool TM = false>
 __global__ void __launch_bounds__(RsCfg<LOGQ>::COL_THREADS, RsCfg<LOGQ>::COL_MINB)
     rs_cols_conv(const __grid_constant__ RsLaunch p) {
