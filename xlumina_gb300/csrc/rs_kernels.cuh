@@ -1028,7 +1028,6 @@ static int launch_cols(cudaStream_t st, const RsLaunch& p) {
 template <int LOGQ>
 static int launch_stage(cudaStream_t st, const RsLaunch& p, int stage) {
   using C = RsCfg<LOGQ>;
-  cudaError_t e;
   if (stage == 0) {
     // the programs of the benchmarks' fields (1024^2 and larger) get a kernel
     // with their op kinds fixed: a phase SLM before scalar RS, an LCD and a
